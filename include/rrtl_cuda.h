@@ -1,0 +1,216 @@
+/*
+ * rrtl_cuda.h — C ABI of the GB300 batched cycle-simulation engine.
+ *
+ * This is the drop-in boundary for RRTL's batch simulator. The reference
+ * exposes the same capability as the Rust type `GpuBatchSimulator`
+ * (crates/rrtl-gpu-sim/src/lib.rs:458-1512) and the design-as-data
+ * `InterpGpuSimulator` (crates/rrtl-gpu-sim/src/interp.rs:1772-2069), selected
+ * through `RuntimeBackend::Gpu` (crates/rrtl-runtime/src/lib.rs:29-40). Each
+ * entry point below names the method it replaces.
+ *
+ * Conventions
+ *  - Every function returns rrtl_status (0 = OK). rrtl_last_error() returns
+ *    the message of the calling thread's last failure, prefixed by a stable
+ *    code mirroring the reference diagnostics (E_GPU_LANES, E_GPU_SIGNAL, ...).
+ *  - Handles are opaque. The library owns all device memory; caller buffers
+ *    are only read or written during the call.
+ *  - Host lane arrays are signal-major [limb][lane], the reference's
+ *    `(offset + limb) * lanes + lane` order (crates/rrtl-gpu-sim/src/lib.rs:1637-1639).
+ *    The top limb is masked to the signal width on set and on get.
+ *  - Memories are exchanged as [addr][limb][lane].
+ *  - Signals are addressed by packed signal index (position in the packed
+ *    program, crates/rrtl-sim-ir/src/lib.rs:12340-12414); look it up by name
+ *    with rrtl_design_signal().
+ *  - One thread drives a batch at a time (the Rust API is `&mut self`).
+ */
+#ifndef RRTL_CUDA_H
+#define RRTL_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t rrtl_status;
+
+enum {
+  RRTL_OK = 0,
+  RRTL_E_ARG = 1,        /* bad argument (E_GPU_LANE_VALUES, E_GPU_MEMORY_VALUES, ...) */
+  RRTL_E_DESIGN = 2,     /* design rejected by the compiler / lowering (E_SIM_IR_*, E_EXPR_TYPE, ...) */
+  RRTL_E_SIGNAL = 3,     /* unknown signal or memory (E_GPU_SIGNAL, E_GPU_MEMORY) */
+  RRTL_E_DEVICE = 4,     /* CUDA error */
+  RRTL_E_OOM = 5,        /* device allocation failed */
+  RRTL_E_TIMEOUT = 6,    /* a bounded device wait gave up */
+  RRTL_E_UNSUPPORTED = 7,/* feature outside this engine's scope */
+  RRTL_E_LANES = 8       /* lanes == 0 or lanes beyond the limit (E_GPU_LANES) */
+};
+
+typedef struct rrtl_ctx rrtl_ctx;
+typedef struct rrtl_design rrtl_design;
+typedef struct rrtl_batch rrtl_batch;
+
+/* Message of the calling thread's last failure ("" when none). */
+const char* rrtl_last_error(void);
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Device context with its own CUDA stream. Replaces the wgpu adapter/device/
+ * queue setup in GpuBatchSimulator::new_async (crates/rrtl-gpu-sim/src/lib.rs:612-642). */
+rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out);
+rrtl_status rrtl_ctx_destroy(rrtl_ctx* ctx);
+/* Number of streaming multiprocessors of the context's device. */
+rrtl_status rrtl_ctx_sm_count(rrtl_ctx* ctx, uint32_t* out);
+
+/* ---- compiled design ---------------------------------------------------- */
+
+/* Compile once: parse the serde-JSON of `rrtl_ir::Design`, flatten and lower
+ * it (lower_to_packed_program / lower_to_machine_program,
+ * crates/rrtl-sim-ir/src/lib.rs:592-672) and upload the device program.
+ * Replaces GpuBatchSimulator::new / new_from_compiled (crates/rrtl-gpu-sim/src/lib.rs:497-530). */
+rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out);
+rrtl_status rrtl_design_destroy(rrtl_design* design);
+
+typedef struct {
+  uint32_t n_signals;          /* packed signals */
+  uint32_t n_memories;
+  uint64_t total_signal_words; /* PackedProgram::total_signal_words */
+  uint64_t total_memory_words_per_lane;
+  uint32_t engine;             /* RRTL_ENGINE_GATE (bit-sliced) or RRTL_ENGINE_WORD */
+  uint32_t n_gates;            /* gate engine: LUT3 cells after mapping; word engine: instructions */
+  uint32_t n_levels;           /* gate engine: logic levels; word engine: comb packets */
+  uint32_t n_nets;             /* gate engine: materialised nets */
+  uint32_t n_slots;            /* gate engine: on-chip net slots after liveness allocation */
+  uint32_t n_regs;             /* registers (flip-flops for the gate engine) */
+  uint64_t source_instrs;      /* machine-program instructions, all streams */
+} rrtl_design_info;
+
+enum { RRTL_ENGINE_GATE = 1, RRTL_ENGINE_WORD = 2 };
+
+rrtl_status rrtl_design_info_get(rrtl_design* design, rrtl_design_info* out);
+/* Look up a packed signal by name: either "<top>.<name>" or "<name>" for a
+ * top-level signal. Writes its index, width and kind (0 in, 1 out, 2 wire, 3 reg). */
+rrtl_status rrtl_design_signal(rrtl_design* design, const char* name, uint32_t* index, uint32_t* width, uint32_t* kind);
+rrtl_status rrtl_design_memory(rrtl_design* design, const char* name, uint32_t* index, uint64_t* depth, uint32_t* width);
+
+/* ---- lane batch ---------------------------------------------------------- */
+
+/* Device lane state for `lanes` independent instances, zero-initialised and
+ * settled (PackedSimulator::new evaluates comb once, crates/rrtl-sim-ir/src/lib.rs:3033-3060).
+ * lanes == 0 fails with RRTL_E_LANES (E_GPU_LANES, crates/rrtl-gpu-sim/src/lib.rs:525-529). */
+rrtl_status rrtl_batch_create(rrtl_design* design, uint32_t lanes, rrtl_batch** out);
+rrtl_status rrtl_batch_destroy(rrtl_batch* b);
+rrtl_status rrtl_batch_lanes(rrtl_batch* b, uint32_t* out);
+
+/* GpuBatchSimulator::set_input_limbs (crates/rrtl-gpu-sim/src/lib.rs:836-843).
+ * `lane_limbs` is [limbs][lanes]; n must equal limbs*lanes. Like the reference
+ * it does not re-settle (crates/rrtl-gpu-sim/src/lib.rs:1514-1555). */
+rrtl_status rrtl_batch_set_input_limbs(rrtl_batch* b, uint32_t signal, const uint32_t* lane_limbs, size_t n);
+/* GpuBatchSimulator::get_signal_limbs (crates/rrtl-gpu-sim/src/lib.rs:860-876). Synchronises. */
+rrtl_status rrtl_batch_get_signal_limbs(rrtl_batch* b, uint32_t signal, uint32_t* out, size_t n);
+/* Bit-packed forms for 1-bit signals: word w bit k is lane 32*w+k. n = ceil(lanes/32). */
+rrtl_status rrtl_batch_set_input_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words, size_t n);
+rrtl_status rrtl_batch_get_signal_bits(rrtl_batch* b, uint32_t signal, uint32_t* out, size_t n);
+
+/* GpuBatchSimulator::set_memory_limbs / get_memory_limbs
+ * (crates/rrtl-gpu-sim/src/lib.rs:903-951). Layout [addr][limb][lane]. */
+rrtl_status rrtl_batch_set_memory_limbs(rrtl_batch* b, uint32_t memory, const uint32_t* data, size_t n);
+rrtl_status rrtl_batch_get_memory_limbs(rrtl_batch* b, uint32_t memory, uint32_t* out, size_t n);
+
+/* GpuBatchSimulator::eval_combinational (crates/rrtl-gpu-sim/src/lib.rs:953-957). */
+rrtl_status rrtl_batch_eval(rrtl_batch* b);
+/* GpuBatchSimulator::tick: settle, capture, commit, settle (crates/rrtl-gpu-sim/src/lib.rs:966-971). */
+rrtl_status rrtl_batch_tick(rrtl_batch* b);
+/* GpuBatchSimulator::tick_many with inputs held (crates/rrtl-gpu-sim/src/lib.rs:973-987).
+ * Asynchronous on the context stream like InterpGpuSimulator::tick_many
+ * (crates/rrtl-gpu-sim/src/interp.rs:2020-2042); getters synchronise. */
+rrtl_status rrtl_batch_tick_many(rrtl_batch* b, uint64_t steps);
+rrtl_status rrtl_batch_synchronize(rrtl_batch* b);
+
+/* ---- per-cycle stimulus and recording (trace replay) ----------------------
+ * One run advances `cycles` clock cycles. Per cycle c, in order:
+ *   1. every stimulated input takes its value for cycle c;
+ *   2. the design settles (comb, then async resets);
+ *   3. recorded signals are sampled (trace / hash / fault detection);
+ *   4. registers capture, memories write, registers commit (then stuck-at
+ *      forces on registers are re-applied).
+ * This is the reference's replay step order: inputs, settle, check, tick
+ * (crates/rrtl-sim-ir/src/lib.rs:9540-9568; crates/rrtl-gpu-sim/src/lib.rs:2892-3078).
+ * After the last cycle the design is settled again, so getters see the state
+ * a final tick would leave. */
+enum {
+  RRTL_STIM_HOLD = 0,   /* keep the current value */
+  RRTL_STIM_RANDOM = 1, /* uniform bits from the counter hash (param = stream id) */
+  RRTL_STIM_PULSE = 2,  /* 1 for cycles < param, then 0 (a reset pulse) */
+  RRTL_STIM_CONST = 3,  /* constant param on every lane */
+  RRTL_STIM_TRACE = 4   /* from input_trace column `param` */
+};
+
+typedef struct {
+  uint32_t signal;
+  uint32_t kind;
+  uint64_t param;
+} rrtl_stim;
+
+enum { RRTL_REC_TRACE = 1, RRTL_REC_HASH = 2, RRTL_REC_DETECT = 4 };
+
+typedef struct {
+  uint64_t cycles;
+  uint64_t seed;
+  uint32_t n_stim;
+  const rrtl_stim* stim;
+  uint32_t n_record;
+  const uint32_t* record;      /* recorded signals (1-bit for the gate engine) */
+  uint32_t record_mode;        /* RRTL_REC_* bitmask */
+  uint32_t n_trace_cols;       /* columns of input_trace */
+  const uint32_t* input_trace; /* gate engine: [cycle][col][word]; word engine: [cycle][col][lane] (one limb) */
+  uint32_t* out_trace;         /* gate engine: [cycle][rec][word]; word engine: [cycle][rec][limb][lane] */
+  uint64_t* out_hash;          /* [cycle] per-cycle output hash */
+  uint32_t* detect;            /* [lanes] first cycle a lane's recorded signals differ from lane 0 of its
+                                  32-lane word; 0xFFFFFFFF if never (gate engine only) */
+} rrtl_run;
+
+/* Runs on the device. Host pointers in `run` are copied in and out inside the
+ * call (use rrtl_batch_run_device for device-resident buffers). */
+rrtl_status rrtl_batch_run(rrtl_batch* b, const rrtl_run* run);
+
+/* Same, with every buffer pointer in `run` a device pointer of the batch's
+ * device; returns without synchronising. */
+rrtl_status rrtl_batch_run_device(rrtl_batch* b, const rrtl_run* run);
+
+/* ---- fault injection (BitParallelSimulator::set_force, crates/rrtl-sim-ir/src/bitparallel.rs:96-126) */
+typedef struct {
+  uint32_t lane;
+  uint32_t signal;  /* packed signal index of a wire, output or register net */
+  uint32_t value;   /* stuck-at value, 0 or 1 */
+} rrtl_fault;
+
+/* Replace the batch's fault list. Gate engine only. Lane 0 of every 32-lane
+ * word is the fault-free reference for RRTL_REC_DETECT, so faults on those
+ * lanes are rejected. */
+rrtl_status rrtl_batch_set_faults(rrtl_batch* b, const rrtl_fault* faults, size_t n);
+
+/* ---- snapshots (GpuBatchSimulator::snapshot_storage / restore_storage,
+ * crates/rrtl-gpu-sim/src/lib.rs:1363-1408) ------------------------------- */
+/* values: total_signal_words*lanes words in [(offset+limb)][lane] order (the
+ * PackedSimulatorStorage::values layout); memories: total_memory_words_per_lane*lanes
+ * words in [lane][word] order (PackedSimulatorStorage::memories). */
+rrtl_status rrtl_batch_snapshot(rrtl_batch* b, uint32_t* values, size_t nv, uint32_t* memories, size_t nm);
+rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv, const uint32_t* memories, size_t nm);
+
+/* ---- execution path selection -------------------------------------------
+ * RRTL_PATH_FUSED: persistent multi-cycle kernel with on-chip net slots (default).
+ * RRTL_PATH_PLAIN: one kernel launch per cycle, nets in HBM (the baseline). */
+enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1 };
+rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
+
+/* Device time of the last run/tick_many in milliseconds (CUDA events on the
+ * context stream around the kernels of that call). */
+rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RRTL_CUDA_H */

@@ -1,0 +1,371 @@
+"""ctypes binding of the CPU oracle (test infrastructure only).
+
+Only the tests, the smoke check and the benchmark's CPU-baseline leg import
+this module; the product path never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, c_char_p, c_int, c_size_t, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+class Stim(ctypes.Structure):
+    _fields_ = [("signal", c_uint32), ("kind", c_uint32), ("param", c_uint64)]
+
+
+class Run(ctypes.Structure):
+    _fields_ = [
+        ("cycles", c_uint64),
+        ("seed", c_uint64),
+        ("n_stim", c_uint32),
+        ("stim", POINTER(Stim)),
+        ("n_record", c_uint32),
+        ("record", POINTER(c_uint32)),
+        ("record_mode", c_uint32),
+        ("n_trace_cols", c_uint32),
+        ("input_trace", POINTER(c_uint32)),
+        ("out_trace", POINTER(c_uint32)),
+        ("out_hash", POINTER(c_uint64)),
+        ("detect", POINTER(c_uint32)),
+    ]
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        L.orc_last_error.restype = c_char_p
+        L.orc_design_load.restype = c_void_p
+        L.orc_design_load.argtypes = [c_char_p, c_size_t, c_char_p]
+        L.orc_design_free.argtypes = [c_void_p]
+        for n in ("orc_signal_index", "orc_memory_index"):
+            getattr(L, n).argtypes = [c_void_p, c_char_p]
+            getattr(L, n).restype = c_int
+        for n in ("orc_signal_width", "orc_signal_kind"):
+            getattr(L, n).argtypes = [c_void_p, c_uint32]
+            getattr(L, n).restype = c_uint32
+        L.orc_signal_top_id.argtypes = [c_void_p, c_uint32]
+        L.orc_signal_top_id.restype = c_int
+        for n in ("orc_num_signals", "orc_num_comb_packets", "orc_num_levels"):
+            getattr(L, n).argtypes = [c_void_p]
+            getattr(L, n).restype = c_uint32
+        for n in ("orc_total_signal_words", "orc_total_memory_words", "orc_num_instrs"):
+            getattr(L, n).argtypes = [c_void_p]
+            getattr(L, n).restype = c_uint64
+        L.orc_stim_word.argtypes = [c_uint64, c_uint64, c_uint64, c_uint64]
+        L.orc_stim_word.restype = c_uint32
+        L.orc_hash_term.argtypes = [c_uint64, c_uint32, c_uint64, c_uint32]
+        L.orc_hash_term.restype = c_uint64
+        L.orc_packed_new.argtypes = [c_void_p, c_uint32]
+        L.orc_packed_new.restype = c_void_p
+        L.orc_packed_free.argtypes = [c_void_p]
+        L.orc_packed_set_signal.argtypes = [c_void_p, c_uint32, POINTER(c_uint32), c_int]
+        L.orc_packed_get_signal.argtypes = [c_void_p, c_uint32, POINTER(c_uint32)]
+        L.orc_packed_set_memory.argtypes = [c_void_p, c_uint32, POINTER(c_uint32), c_int]
+        L.orc_packed_get_memory.argtypes = [c_void_p, c_uint32, POINTER(c_uint32)]
+        for n in ("orc_packed_eval", "orc_packed_tick", "orc_packed_tick_from_evaluated"):
+            getattr(L, n).argtypes = [c_void_p]
+        L.orc_packed_tick_many.argtypes = [c_void_p, c_uint64]
+        L.orc_packed_snapshot.argtypes = [c_void_p, POINTER(c_uint32), POINTER(c_uint32)]
+        L.orc_packed_run.argtypes = [c_void_p, POINTER(Run)]
+        L.orc_packed_run.restype = c_int
+        L.orc_bp_new.argtypes = [c_void_p, c_uint32]
+        L.orc_bp_new.restype = c_void_p
+        L.orc_bp_free.argtypes = [c_void_p]
+        L.orc_bp_set_force.argtypes = [c_void_p, c_uint32, c_uint32, c_int]
+        L.orc_bp_set.argtypes = [c_void_p, c_uint32, c_uint32, c_int]
+        L.orc_bp_set_all.argtypes = [c_void_p, c_uint32, c_int]
+        L.orc_bp_get.argtypes = [c_void_p, c_uint32, c_uint32]
+        L.orc_bp_get.restype = c_int
+        L.orc_bp_tick.argtypes = [c_void_p]
+        L.orc_bp_settle.argtypes = [c_void_p]
+        L.orc_bp_get_bits.argtypes = [c_void_p, c_uint32, POINTER(c_uint32)]
+        L.orc_bp_set_bits.argtypes = [c_void_p, c_uint32, POINTER(c_uint32)]
+        L.orc_bp_run.argtypes = [c_void_p, POINTER(Run)]
+        L.orc_bp_run.restype = c_int
+        L.orc_bp_run_parallel.argtypes = [c_void_p, c_uint32, POINTER(Run), c_uint32]
+        L.orc_bp_run_parallel.restype = c_int
+        L.orc_scalar_new.argtypes = [c_void_p]
+        L.orc_scalar_new.restype = c_void_p
+        L.orc_scalar_free.argtypes = [c_void_p]
+        L.orc_scalar_id.argtypes = [c_void_p, c_char_p]
+        L.orc_scalar_id.restype = c_int
+        L.orc_scalar_set.argtypes = [c_void_p, c_uint32, c_uint64, c_uint64, c_int]
+        L.orc_scalar_get.argtypes = [c_void_p, c_uint32, POINTER(c_uint64)]
+        L.orc_scalar_get.restype = c_uint64
+        L.orc_scalar_tick.argtypes = [c_void_p]
+        L.orc_scalar_eval.argtypes = [c_void_p]
+        L.orc_scalar_peek_mem.argtypes = [c_void_p, c_uint32, c_uint64]
+        L.orc_scalar_peek_mem.restype = c_uint64
+        L.orc_scalar_poke_mem.argtypes = [c_void_p, c_uint32, c_uint64, c_uint64]
+        _lib = L
+    return _lib
+
+
+def _u32p(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_uint32))
+
+
+def _u64p(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_uint64))
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+class OracleDesign:
+    def __init__(self, design_json: str, top: str):
+        L = lib()
+        raw = design_json.encode()
+        self.h = L.orc_design_load(raw, len(raw), top.encode())
+        if not self.h:
+            raise OracleError(L.orc_last_error().decode())
+        self.top = top
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_design_free(self.h)
+            self.h = None
+
+    def signal(self, name: str) -> int:
+        i = lib().orc_signal_index(self.h, name.encode())
+        if i < 0:
+            raise KeyError(name)
+        return i
+
+    def memory(self, name: str) -> int:
+        i = lib().orc_memory_index(self.h, name.encode())
+        if i < 0:
+            raise KeyError(name)
+        return i
+
+    def width(self, sig: int) -> int:
+        return lib().orc_signal_width(self.h, sig)
+
+    def kind(self, sig: int) -> int:
+        return lib().orc_signal_kind(self.h, sig)
+
+    @property
+    def num_signals(self) -> int:
+        return lib().orc_num_signals(self.h)
+
+    @property
+    def total_signal_words(self) -> int:
+        return lib().orc_total_signal_words(self.h)
+
+    @property
+    def total_memory_words(self) -> int:
+        return lib().orc_total_memory_words(self.h)
+
+    @property
+    def num_instrs(self) -> int:
+        return lib().orc_num_instrs(self.h)
+
+    @property
+    def num_levels(self) -> int:
+        return lib().orc_num_levels(self.h)
+
+
+def make_run(cycles, seed, stim, record, mode, input_trace=None, n_trace_cols=0, out_trace=None, out_hash=None,
+             detect=None):
+    """Build an rrtl_run structure; keeps the numpy buffers alive on the object."""
+    st = (Stim * max(1, len(stim)))(*[Stim(s, k, p) for (s, k, p) in stim])
+    rec = np.asarray(record, dtype=np.uint32)
+    r = Run()
+    r.cycles = cycles
+    r.seed = seed
+    r.n_stim = len(stim)
+    r.stim = ctypes.cast(st, POINTER(Stim))
+    r.n_record = len(rec)
+    r.record = _u32p(rec)
+    r.record_mode = mode
+    r.n_trace_cols = n_trace_cols
+    r.input_trace = _u32p(input_trace) if input_trace is not None else None
+    r.out_trace = _u32p(out_trace) if out_trace is not None else None
+    r.out_hash = _u64p(out_hash) if out_hash is not None else None
+    r.detect = _u32p(detect) if detect is not None else None
+    r._keep = (st, rec, input_trace, out_trace, out_hash, detect)
+    return r
+
+
+class PackedSim:
+    """Restated `PackedSimulator` (word-level, any width)."""
+
+    def __init__(self, design: OracleDesign, lanes: int):
+        self.d = design
+        self.lanes = lanes
+        self.h = lib().orc_packed_new(design.h, lanes)
+        if not self.h:
+            raise OracleError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_packed_free(self.h)
+            self.h = None
+
+    def _limbs(self, sig):
+        return (self.d.width(sig) + 31) // 32
+
+    def set_signal(self, sig: int, values, settle: bool = True):
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.uint32).reshape(self._limbs(sig), self.lanes))
+        lib().orc_packed_set_signal(self.h, sig, _u32p(a), 1 if settle else 0)
+
+    def get_signal(self, sig: int) -> np.ndarray:
+        out = np.zeros((self._limbs(sig), self.lanes), dtype=np.uint32)
+        lib().orc_packed_get_signal(self.h, sig, _u32p(out))
+        return out
+
+    def set_memory(self, mem: int, data: np.ndarray, settle: bool = True):
+        a = np.ascontiguousarray(data, dtype=np.uint32)
+        lib().orc_packed_set_memory(self.h, mem, _u32p(a), 1 if settle else 0)
+
+    def get_memory(self, mem: int, depth: int, limbs: int) -> np.ndarray:
+        out = np.zeros((depth, limbs, self.lanes), dtype=np.uint32)
+        lib().orc_packed_get_memory(self.h, mem, _u32p(out))
+        return out
+
+    def eval(self):
+        lib().orc_packed_eval(self.h)
+
+    def tick(self):
+        lib().orc_packed_tick(self.h)
+
+    def tick_many(self, n: int):
+        lib().orc_packed_tick_many(self.h, n)
+
+    def tick_from_evaluated(self):
+        lib().orc_packed_tick_from_evaluated(self.h)
+
+    def snapshot(self):
+        v = np.zeros(self.d.total_signal_words * self.lanes, dtype=np.uint32)
+        m = np.zeros(max(1, self.d.total_memory_words * self.lanes), dtype=np.uint32)
+        lib().orc_packed_snapshot(self.h, _u32p(v), _u32p(m))
+        return v, m[: self.d.total_memory_words * self.lanes]
+
+    def run(self, run: Run):
+        rc = lib().orc_packed_run(self.h, ctypes.byref(run))
+        if rc:
+            raise OracleError(lib().orc_last_error().decode())
+
+
+class BitParallel:
+    """Restated `BitParallelSimulator` (1-bit gate-level, per-lane stuck-at forces)."""
+
+    def __init__(self, design: OracleDesign, lanes: int):
+        self.d = design
+        self.lanes = lanes
+        self.h = lib().orc_bp_new(design.h, lanes)
+        if not self.h:
+            raise OracleError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_bp_free(self.h)
+            self.h = None
+
+    def set_force(self, sig, lane, value):
+        lib().orc_bp_set_force(self.h, sig, lane, int(value))
+
+    def set(self, sig, lane, v):
+        lib().orc_bp_set(self.h, sig, lane, int(v))
+
+    def set_all(self, sig, v):
+        lib().orc_bp_set_all(self.h, sig, int(v))
+
+    def get(self, sig, lane) -> int:
+        return lib().orc_bp_get(self.h, sig, lane)
+
+    def tick(self):
+        lib().orc_bp_tick(self.h)
+
+    def settle(self):
+        lib().orc_bp_settle(self.h)
+
+    def get_bits(self, sig) -> np.ndarray:
+        out = np.zeros((self.lanes + 31) // 32, dtype=np.uint32)
+        lib().orc_bp_get_bits(self.h, sig, _u32p(out))
+        return out
+
+    def set_bits(self, sig, words):
+        a = np.ascontiguousarray(words, dtype=np.uint32)
+        lib().orc_bp_set_bits(self.h, sig, _u32p(a))
+
+    def run(self, run: Run):
+        rc = lib().orc_bp_run(self.h, ctypes.byref(run))
+        if rc:
+            raise OracleError(lib().orc_last_error().decode())
+
+
+def bp_run_parallel(design: OracleDesign, lanes: int, run: Run, threads: int):
+    rc = lib().orc_bp_run_parallel(design.h, lanes, ctypes.byref(run), threads)
+    if rc:
+        raise OracleError(lib().orc_last_error().decode())
+
+
+class ScalarSim:
+    """Restated `rrtl_core::Simulator` (single instance, top-module signal names)."""
+
+    def __init__(self, design: OracleDesign):
+        self.h = lib().orc_scalar_new(design.h)
+        if not self.h:
+            raise OracleError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_scalar_free(self.h)
+            self.h = None
+
+    def id(self, name: str) -> int:
+        i = lib().orc_scalar_id(self.h, name.encode())
+        if i < 0:
+            raise KeyError(name)
+        return i
+
+    def set(self, name_or_id, value: int, settle: bool = True):
+        i = self.id(name_or_id) if isinstance(name_or_id, str) else name_or_id
+        lib().orc_scalar_set(self.h, i, value & (2**64 - 1), (value >> 64) & (2**64 - 1), 1 if settle else 0)
+
+    def get(self, name_or_id) -> int:
+        i = self.id(name_or_id) if isinstance(name_or_id, str) else name_or_id
+        hi = c_uint64(0)
+        lo = lib().orc_scalar_get(self.h, i, ctypes.byref(hi))
+        return (hi.value << 64) | lo
+
+    def tick(self):
+        lib().orc_scalar_tick(self.h)
+
+    def eval(self):
+        lib().orc_scalar_eval(self.h)
+
+    def peek_mem(self, name_or_id, addr) -> int:
+        i = self.id(name_or_id) if isinstance(name_or_id, str) else name_or_id
+        return lib().orc_scalar_peek_mem(self.h, i, addr)
+
+    def poke_mem(self, name_or_id, addr, value):
+        i = self.id(name_or_id) if isinstance(name_or_id, str) else name_or_id
+        lib().orc_scalar_poke_mem(self.h, i, addr, value)
+
+
+def crc_step(c: int, din: int) -> int:
+    """CRC-32 byte step, MSB-first, polynomial 0x04C11DB7
+    (crates/rrtl-sim-ir/examples/netlist_crc32.rs:26-33)."""
+    for i in range(8):
+        bit = ((c >> 31) & 1) ^ ((din >> i) & 1)
+        c = ((c << 1) & 0xFFFFFFFF) ^ (0x04C11DB7 if bit else 0)
+    return c

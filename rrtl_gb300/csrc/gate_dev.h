@@ -1,0 +1,76 @@
+// Device-side descriptors of a gate program and of one run over a batch.
+// Shared by the CUDA kernels and the host runtime.
+#pragma once
+
+#include <stdint.h>
+
+namespace rrtl {
+
+struct GateStimDev {
+  uint32_t slot;  // on-chip slot (fused path)
+  uint32_t net;   // global net row (plain path)
+  uint32_t kind;  // RRTL_STIM_*
+  uint32_t pad;
+  uint64_t param;
+};
+
+struct GateRecDev {
+  uint32_t slot;
+  uint32_t net;
+};
+
+// One stuck-at force on one 32-lane word: v = (v & ~mask) | (val & mask).
+struct GateForceDev {
+  uint32_t slot;
+  uint32_t net;
+  uint32_t word;  // 0..7 inside the tile
+  uint32_t mask;
+  uint32_t val;
+  uint32_t pad;
+};
+
+// Register commit entry. flags: 1 has reset, 2 active-low reset, 4 reset value 1.
+struct GateRegDev {
+  uint32_t q, d, rst, flags;
+};
+
+struct GateProgDev {
+  // fused path (slots in shared memory)
+  const uint2* srecs;          // [groups*4] packed slot records (pack_smem_record)
+  const uint4* pieces;         // {group_begin, n_groups, level, last_of_level}
+  uint32_t n_pieces, n_slots, n_levels, piece_groups;
+  const uint32_t* src_net;     // sources loaded per tile and written back
+  const uint32_t* src_slot;
+  uint32_t n_src;
+  const GateRegDev* sregs;     // slot-based commit list
+  const uint32_t* wb_net;      // [groups*4] global net of each cell's signal output, or ~0
+  // plain path (nets in HBM)
+  const uint4* grecs;          // [groups*4] {a, b, c, out | lut << 24}
+  const uint32_t* level_group_begin;  // [n_levels+1]
+  const GateRegDev* gregs;     // net-based commit list
+  uint32_t n_regs;
+  uint32_t const0_slot, const1_slot;
+};
+
+struct GateRunDev {
+  unsigned long long cycles, seed;
+  uint32_t n_stim;
+  const GateStimDev* stim;
+  uint32_t n_rec;
+  const GateRecDev* rec;
+  uint32_t mode;
+  uint32_t n_trace_cols;
+  const uint32_t* in_trace;   // [cycle][col][words]
+  uint32_t* out_trace;        // [cycle][rec][words]
+  unsigned long long* out_hash;
+  uint32_t* detect;           // [lanes]
+  uint32_t lanes, words, words_pad, n_tiles;
+  const uint32_t* force_off;  // [n_tiles*(n_levels+2)]: per tile, per stage (0 = after commit, L+1 = after level L)
+  const GateForceDev* forces;
+  uint32_t has_forces;
+  uint32_t final_settle;
+  uint32_t* nets;             // [rows][words_pad]
+  uint32_t* err;              // device status word
+};
+
+}  // namespace rrtl

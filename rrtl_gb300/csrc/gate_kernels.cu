@@ -1,0 +1,475 @@
+// Bit-sliced gate kernels for sm_103a.
+//
+// Evaluates a GateProgram (see gateprog.h) over many 32-lane words. Each
+// cycle follows the run order documented in include/rrtl_cuda.h: stimulus,
+// settle (levels), record, register commit, register forces.
+//
+//  gate_fused_kernel  persistent: one CTA per SM walks 8-word tiles; a tile's
+//                     nets live in shared memory for all cycles, and the cell
+//                     records are streamed level piece by level piece from
+//                     HBM/L2 into a shared-memory ring by cp.async.bulk (TMA
+//                     bulk copy) with mbarrier completion.
+//  gate_plain_kernel  one launch per cycle; nets live in HBM, read and written
+//                     once per cell per cycle (the baseline path).
+//
+// Warp layout: lane = 8*gsub + w; w is the word inside the tile and gsub picks
+// one of the four cells of a group. All cells of a group share one truth
+// table, so the table is warp-uniform and evaluates as one LOP3.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rrtl_cuda.h"
+#include "gate_dev.h"
+#include "stim.h"
+
+namespace rrtl {
+
+constexpr int kFusedThreads = 1024;
+constexpr int kFusedWarps = kFusedThreads / 32;
+constexpr int kPlainThreads = 256;
+constexpr int kRing = 4;                 // record ring buffers
+constexpr uint32_t kSpinLimit = 1u << 22; // bounded mbarrier wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t addr = smem_u32(bar);
+  for (uint32_t it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <int L>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(L));
+  return d;
+}
+
+// Runtime truth table (plain path): Shannon expansion on a, then b, then c.
+__device__ __forceinline__ uint32_t lut_eval(uint32_t t, uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t m0 = 0u - (t & 1u), m1 = 0u - ((t >> 1) & 1u), m2 = 0u - ((t >> 2) & 1u), m3 = 0u - ((t >> 3) & 1u);
+  uint32_t m4 = 0u - ((t >> 4) & 1u), m5 = 0u - ((t >> 5) & 1u), m6 = 0u - ((t >> 6) & 1u), m7 = 0u - ((t >> 7) & 1u);
+  uint32_t u0 = (c & m1) | (~c & m0), u1 = (c & m3) | (~c & m2);
+  uint32_t u2 = (c & m5) | (~c & m4), u3 = (c & m7) | (~c & m6);
+  uint32_t f0 = (b & u1) | (~b & u0), f1 = (b & u3) | (~b & u2);
+  return (a & f1) | (~a & f0);
+}
+
+__device__ __forceinline__ uint32_t rec_lut(uint2 r) {
+  return ((r.x >> 14) & 3u) | ((r.x >> 28) & 0xCu) | ((r.y >> 10) & 0x30u) | ((r.y >> 24) & 0xC0u);
+}
+
+__device__ __forceinline__ uint32_t valid_mask(uint32_t gw, uint32_t lanes) {
+  uint32_t base = gw * 32u;
+  if (base >= lanes) return 0u;
+  uint32_t n = lanes - base;
+  return n >= 32u ? 0xFFFFFFFFu : ((1u << n) - 1u);
+}
+
+__device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateRunDev& R, uint64_t c, uint32_t gw,
+                                               uint32_t cur) {
+  switch (s.kind) {
+    case RRTL_STIM_RANDOM: return stim_word(R.seed, s.param, c, gw);
+    case RRTL_STIM_PULSE: return c < s.param ? 0xFFFFFFFFu : 0u;
+    case RRTL_STIM_CONST: return (s.param & 1u) ? 0xFFFFFFFFu : 0u;
+    case RRTL_STIM_TRACE:
+      return gw < R.words ? R.in_trace[((size_t)c * R.n_trace_cols + s.param) * R.words + gw] : 0u;
+    default: return cur;
+  }
+}
+
+// ------------------------------------------------------------ fused path --
+
+struct FusedCtx {
+  uint32_t* S;         // slots [n_slots][8]
+  const uint32_t* wb;  // writeback nets for the current piece (final settle) or null
+  uint32_t* nets;
+  uint32_t words_pad, col;  // col = tile*8 + w
+  uint32_t w, gsub;
+};
+
+// Evaluate consecutive groups with truth table L; stop at the first group with another table.
+template <int L>
+__device__ __noinline__ int run_groups(const uint2* __restrict__ rb, int g, int g1, FusedCtx& X) {
+  constexpr bool kUseA = (L & 0x0F) != ((L >> 4) & 0x0F);
+  constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
+  constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
+  uint32_t* S = X.S;
+  for (; g < g1; ++g) {
+    uint2 r = rb[g * 4 + X.gsub];
+    if (rec_lut(r) != (uint32_t)L) break;
+    uint32_t a = r.x & 0x3FFFu, b = (r.x >> 16) & 0x3FFFu, c = r.y & 0x3FFFu, o = (r.y >> 16) & 0x3FFFu;
+    uint32_t va = kUseA ? S[a * 8 + X.w] : 0u;
+    uint32_t vb = kUseB ? S[b * 8 + X.w] : 0u;
+    uint32_t vc = kUseC ? S[c * 8 + X.w] : 0u;
+    uint32_t v = lop3<L>(va, vb, vc);
+    S[o * 8 + X.w] = v;
+    if (X.wb) {
+      uint32_t net = __ldg(X.wb + g * 4 + X.gsub);
+      if (net != 0xFFFFFFFFu) X.nets[(size_t)net * X.words_pad + X.col] = v;
+    }
+  }
+  return g;
+}
+
+#define RRTL_CASE(n) \
+  case n: g = run_groups<n>(rb, g, g1, X); break;
+#define RRTL_CASE4(n) RRTL_CASE(n) RRTL_CASE(n + 1) RRTL_CASE(n + 2) RRTL_CASE(n + 3)
+#define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
+#define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
+
+__device__ __forceinline__ void eval_groups(const uint2* __restrict__ rb, int g, int g1, FusedCtx& X) {
+  while (g < g1) {
+    uint32_t lut = rec_lut(rb[g * 4 + X.gsub]);
+    switch (lut) {
+      RRTL_CASE64(0)
+      RRTL_CASE64(64)
+      RRTL_CASE64(128)
+      RRTL_CASE64(192)
+      default: g = g1; break;
+    }
+  }
+}
+
+__device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, uint32_t tile, uint32_t stage,
+                                             uint32_t stages) {
+  const uint32_t* off = R.force_off + (size_t)tile * (stages + 1);
+  uint32_t b = __ldg(off + stage), e = __ldg(off + stage + 1);
+  for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    GateForceDev f = R.forces[i];
+    uint32_t& v = S[f.slot * 8 + f.word];
+    v = (v & ~f.mask) | (f.val & f.mask);
+  }
+}
+
+__global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDev P, GateRunDev R) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  const uint32_t piece_bytes = P.piece_groups * 32u;
+  uint2* ring = reinterpret_cast<uint2*>(smem);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kRing * piece_bytes);
+  unsigned long long* hacc = reinterpret_cast<unsigned long long*>(bars + kRing);
+  uint32_t* dstate = reinterpret_cast<uint32_t*>(hacc + 1);  // diff[8], detected[8]
+  uint32_t* S = dstate + 16;
+  __shared__ int s_abort;
+
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t w = lane & 7u, gsub = lane >> 3;
+  const bool resident = P.n_pieces <= (uint32_t)kRing;
+  const uint32_t stages = P.n_levels + 1;
+
+  uint32_t my_tiles = 0;
+  for (uint32_t t = blockIdx.x; t < R.n_tiles; t += gridDim.x) ++my_tiles;
+  const uint64_t passes = R.cycles + (R.final_settle ? 1u : 0u);
+  const uint64_t total_q = resident ? P.n_pieces : (uint64_t)my_tiles * passes * P.n_pieces;
+
+  if (tid == 0) {
+    s_abort = 0;
+    *hacc = 0ull;
+    for (int i = 0; i < kRing; ++i) mbar_init(&bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (tid == 0) {
+    uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
+    for (uint64_t q = 0; q < n0; ++q) {
+      uint4 pc = P.pieces[q % P.n_pieces];
+      bulk_load(ring + (size_t)(q % kRing) * P.piece_groups * 4, P.srecs + (size_t)pc.x * 4, pc.y * 32u, &bars[q % kRing]);
+    }
+  }
+
+  uint64_t q = 0;
+  FusedCtx X;
+  X.S = S;
+  X.nets = R.nets;
+  X.words_pad = R.words_pad;
+  X.w = w;
+  X.gsub = gsub;
+  // Thread 0 waits for a piece's records; the CTA barrier that follows
+  // publishes them to every thread. The wait for piece q+1 is folded into the
+  // barrier that closes piece q, so each piece costs one barrier.
+  auto wait_piece = [&](uint64_t qq) {
+    if (qq >= total_q && resident) return;
+    if (!resident && qq >= total_q) return;
+    if (resident && qq >= P.n_pieces) return;
+    uint32_t buf = resident ? (uint32_t)qq : (uint32_t)(qq % kRing);
+    uint32_t par = resident ? 0u : (uint32_t)((qq / kRing) & 1u);
+    if (!mbar_wait(&bars[buf], par)) {
+      s_abort = 1;
+      atomicExch(R.err, (uint32_t)RRTL_E_TIMEOUT);
+    }
+  };
+  if (tid == 0) wait_piece(0);
+  __syncthreads();
+
+  for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !s_abort; tile += gridDim.x) {
+    const uint32_t col0 = tile * 8u;
+    X.col = col0 + w;
+    // constants, scratch, sources
+    for (uint32_t i = tid; i < 8u; i += blockDim.x) {
+      S[0 * 8 + i] = 0u;
+      S[P.const0_slot * 8 + i] = 0u;
+      S[P.const1_slot * 8 + i] = 0xFFFFFFFFu;
+      dstate[i] = 0u;
+      dstate[8 + i] = 0u;
+    }
+    for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
+      uint32_t k = i >> 3, ww = i & 7u;
+      S[__ldg(P.src_slot + k) * 8 + ww] = R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww];
+    }
+    __syncthreads();
+
+    for (uint64_t pass = 0; pass < passes; ++pass) {
+      const bool final_pass = pass == R.cycles;
+      const uint64_t c = pass;
+      if (final_pass) {
+        // register slots may host other nets during a settle: write the
+        // sources back before the final settle recomputes every signal
+        for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
+          uint32_t k = i >> 3, ww = i & 7u;
+          R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * 8 + ww];
+        }
+      } else {
+        for (uint32_t i = tid; i < R.n_stim * 8u; i += blockDim.x) {
+          const GateStimDev& s = R.stim[i >> 3];
+          if (s.kind == RRTL_STIM_HOLD) continue;
+          uint32_t ww = i & 7u;
+          uint32_t& slot = S[s.slot * 8 + ww];
+          slot = stim_value(s, R, c, col0 + ww, slot);
+        }
+      }
+      __syncthreads();
+      for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
+        const uint4 pc = P.pieces[p];
+        const uint32_t buf = resident ? p : (uint32_t)(q % kRing);
+        const uint2* rb = ring + (size_t)buf * P.piece_groups * 4;
+        X.wb = final_pass ? (P.wb_net + (size_t)pc.x * 4) : nullptr;
+        int g0 = (int)((pc.y * warp) / kFusedWarps), g1 = (int)((pc.y * (warp + 1)) / kFusedWarps);
+        eval_groups(rb, g0, g1, X);
+        if (pc.w && R.has_forces) {
+          __syncthreads();
+          apply_forces(R, S, tile, pc.z + 1, stages);
+        }
+        if (tid == 0) wait_piece(q + 1);
+        __syncthreads();
+        if (s_abort) break;
+        if (!resident && tid == 0 && q + kRing < total_q) {
+          uint64_t nq = q + kRing;
+          uint4 npc = P.pieces[nq % P.n_pieces];
+          bulk_load(ring + (size_t)buf * P.piece_groups * 4, P.srecs + (size_t)npc.x * 4, npc.y * 32u, &bars[buf]);
+        }
+      }
+      if (s_abort) break;
+      if (final_pass) break;
+      // record
+      if (R.n_rec) {
+        unsigned long long h = 0ull;
+        for (uint32_t i = tid; i < R.n_rec * 8u; i += blockDim.x) {
+          uint32_t k = i >> 3, ww = i & 7u, gw = col0 + ww;
+          uint32_t v = S[R.rec[k].slot * 8 + ww] & valid_mask(gw, R.lanes);
+          if (gw < R.words) {
+            if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
+            if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
+            if (R.mode & RRTL_REC_DETECT) atomicOr(&dstate[ww], v ^ (0u - (v & 1u)));
+          }
+        }
+        if (R.mode & RRTL_REC_HASH) {
+          for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
+          if (lane == 0 && h) atomicAdd(hacc, h);
+        }
+        __syncthreads();
+        if (tid == 0 && (R.mode & RRTL_REC_HASH)) {
+          unsigned long long t = *hacc;
+          if (t) atomicAdd(R.out_hash + c, t);
+          *hacc = 0ull;
+        }
+        if ((R.mode & RRTL_REC_DETECT) && tid < 8u) {
+          uint32_t gw = col0 + tid;
+          uint32_t nb = dstate[tid] & ~dstate[8 + tid] & valid_mask(gw, R.lanes);
+          dstate[8 + tid] |= nb;
+          dstate[tid] = 0u;
+          while (nb) {
+            uint32_t b = __ffs(nb) - 1u;
+            R.detect[gw * 32u + b] = (uint32_t)c;
+            nb &= nb - 1u;
+          }
+        }
+      }
+      // commit (D and reset nets are never register nets, so one pass is safe)
+      for (uint32_t i = tid; i < P.n_regs * 8u; i += blockDim.x) {
+        GateRegDev r = P.sregs[i >> 3];
+        uint32_t ww = i & 7u;
+        uint32_t d = S[r.d * 8 + ww];
+        if (r.flags & 1u) {
+          uint32_t m = S[r.rst * 8 + ww];
+          if (r.flags & 2u) m = ~m;
+          uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
+          d = (m & rv) | (~m & d);
+        }
+        S[r.q * 8 + ww] = d;
+      }
+      __syncthreads();
+      if (R.has_forces) {
+        apply_forces(R, S, tile, 0, stages);
+        __syncthreads();
+      }
+    }
+    if (s_abort) break;
+    if (!R.final_settle) {
+      for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
+        uint32_t k = i >> 3, ww = i & 7u;
+        R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * 8 + ww];
+      }
+    }
+    __syncthreads();
+  }
+  if (s_abort && tid == 0) {
+    // let any copy still in flight land before the CTA's shared memory is released
+    for (int i = 0; i < kRing; ++i) {
+      uint64_t last = q + i;
+      if (last < total_q) (void)mbar_wait(&bars[last % kRing], (uint32_t)((last / kRing) & 1u));
+    }
+  }
+}
+
+// ------------------------------------------------------------ plain path --
+
+// One launch = one cycle (phase 0) or one settle with no stimulus/commit (phase 1).
+__global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P, GateRunDev R, uint64_t c,
+                                                                    int phase) {
+  __shared__ unsigned long long hacc;
+  __shared__ uint32_t diff[8];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t w = lane & 7u, gsub = lane >> 3;
+  const uint32_t tile = blockIdx.x, col0 = tile * 8u, col = col0 + w;
+  uint32_t* G = R.nets;
+  const size_t wp = R.words_pad;
+  const uint32_t stages = P.n_levels + 1;
+  if (tid == 0) hacc = 0ull;
+  if (tid < 8) diff[tid] = 0u;
+  if (phase == 0) {
+    for (uint32_t i = tid; i < R.n_stim * 8u; i += blockDim.x) {
+      const GateStimDev& s = R.stim[i >> 3];
+      if (s.kind == RRTL_STIM_HOLD) continue;
+      uint32_t ww = i & 7u;
+      uint32_t* p = G + (size_t)s.net * wp + col0 + ww;
+      *p = stim_value(s, R, c, col0 + ww, *p);
+    }
+  }
+  __syncthreads();
+  for (uint32_t L = 0; L < P.n_levels; ++L) {
+    uint32_t g0 = P.level_group_begin[L], g1 = P.level_group_begin[L + 1];
+    for (uint32_t g = g0 + warp; g < g1; g += nwarps) {
+      uint4 r = P.grecs[(size_t)g * 4 + gsub];
+      uint32_t va = G[(size_t)r.x * wp + col], vb = G[(size_t)r.y * wp + col], vc = G[(size_t)r.z * wp + col];
+      G[(size_t)(r.w & 0xFFFFFFu) * wp + col] = lut_eval(r.w >> 24, va, vb, vc);
+    }
+    __syncthreads();
+    if (R.has_forces) {
+      const uint32_t* off = R.force_off + (size_t)tile * (stages + 1);
+      for (uint32_t i = off[L + 1] + tid; i < off[L + 2]; i += blockDim.x) {
+        GateForceDev f = R.forces[i];
+        uint32_t& v = G[(size_t)f.net * wp + col0 + f.word];
+        v = (v & ~f.mask) | (f.val & f.mask);
+      }
+      __syncthreads();
+    }
+  }
+  if (phase != 0) return;
+  if (R.n_rec) {
+    unsigned long long h = 0ull;
+    for (uint32_t i = tid; i < R.n_rec * 8u; i += blockDim.x) {
+      uint32_t k = i >> 3, ww = i & 7u, gw = col0 + ww;
+      uint32_t v = G[(size_t)R.rec[k].net * wp + gw] & valid_mask(gw, R.lanes);
+      if (gw < R.words) {
+        if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
+        if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
+        if (R.mode & RRTL_REC_DETECT) atomicOr(&diff[ww], v ^ (0u - (v & 1u)));
+      }
+    }
+    if (R.mode & RRTL_REC_HASH) {
+      for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
+      if (lane == 0 && h) atomicAdd(&hacc, h);
+    }
+    __syncthreads();
+    if (tid == 0 && (R.mode & RRTL_REC_HASH) && hacc) atomicAdd(R.out_hash + c, hacc);
+    if ((R.mode & RRTL_REC_DETECT) && tid < 8u) {
+      uint32_t gw = col0 + tid;
+      uint32_t nb = diff[tid] & valid_mask(gw, R.lanes);
+      while (nb) {
+        uint32_t b = __ffs(nb) - 1u;
+        uint32_t* d = R.detect + gw * 32u + b;
+        if (*d == 0xFFFFFFFFu) *d = (uint32_t)c;
+        nb &= nb - 1u;
+      }
+    }
+    __syncthreads();
+  }
+  for (uint32_t i = tid; i < P.n_regs * 8u; i += blockDim.x) {
+    GateRegDev r = P.gregs[i >> 3];
+    uint32_t ww = i & 7u;
+    uint32_t d = G[(size_t)r.d * wp + col0 + ww];
+    if (r.flags & 1u) {
+      uint32_t m = G[(size_t)r.rst * wp + col0 + ww];
+      if (r.flags & 2u) m = ~m;
+      uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
+      d = (m & rv) | (~m & d);
+    }
+    G[(size_t)r.q * wp + col0 + ww] = d;
+  }
+  if (R.has_forces) {
+    __syncthreads();
+    const uint32_t* off = R.force_off + (size_t)tile * (stages + 1);
+    for (uint32_t i = off[0] + tid; i < off[1]; i += blockDim.x) {
+      GateForceDev f = R.forces[i];
+      uint32_t& v = G[(size_t)f.net * wp + col0 + f.word];
+      v = (v & ~f.mask) | (f.val & f.mask);
+    }
+  }
+}
+
+// ------------------------------------------------------------- launchers --
+
+size_t gate_fused_smem_bytes(const GateProgDev& P) {
+  return (size_t)kRing * P.piece_groups * 32u + kRing * 8u + 8u + 16u * 4u + (size_t)P.n_slots * 8u * 4u;
+}
+
+cudaError_t gate_fused_prepare(size_t smem) {
+  return cudaFuncSetAttribute(gate_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem,
+                              cudaStream_t st) {
+  gate_fused_kernel<<<grid, kFusedThreads, smem, st>>>(P, R);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st) {
+  gate_plain_kernel<<<R.n_tiles, kPlainThreads, 0, st>>>(P, R, c, phase);
+  return cudaGetLastError();
+}
+
+}  // namespace rrtl

@@ -1,0 +1,437 @@
+// Gate-program lowering (see gateprog.h).
+#include "gateprog.h"
+
+#include <algorithm>
+#include <map>
+#include <tuple>
+#include <unordered_map>
+
+namespace rrtl {
+
+namespace {
+
+const uint8_t kVarMask[3] = {0xF0, 0xCC, 0xAA};
+
+// Evaluate an 8-bit LOP3 table on three 8-bit variable masks.
+uint8_t apply_tt(uint8_t tt, uint8_t x, uint8_t y, uint8_t z) {
+  uint8_t r = 0;
+  for (int p = 0; p < 8; ++p) {
+    int idx = (((x >> p) & 1) << 2) | (((y >> p) & 1) << 1) | ((z >> p) & 1);
+    if ((tt >> idx) & 1) r |= (uint8_t)(1u << p);
+  }
+  return r;
+}
+
+// A boolean function over at most three leaf nets.
+struct Fn {
+  uint8_t n = 0;
+  uint32_t leaf[3] = {0, 0, 0};
+  uint8_t tt = 0;
+};
+
+Fn fn_const(bool b) {
+  Fn f;
+  f.tt = b ? 0xFF : 0x00;
+  return f;
+}
+
+Fn fn_leaf(uint32_t net) {
+  if (net == kNetConst0) return fn_const(false);
+  if (net == kNetConst1) return fn_const(true);
+  Fn f;
+  f.n = 1;
+  f.leaf[0] = net;
+  f.tt = kVarMask[0];
+  return f;
+}
+
+// Re-express f over the leaf list `u` (which contains all of f's leaves).
+uint8_t remap(const Fn& f, const uint32_t* u, int un) {
+  uint8_t m[3] = {0, 0, 0};
+  for (int i = 0; i < f.n; ++i)
+    for (int j = 0; j < un; ++j)
+      if (u[j] == f.leaf[i]) m[i] = kVarMask[j];
+  return apply_tt(f.tt, m[0], m[1], m[2]);
+}
+
+// Drop leaves the table does not depend on and renumber.
+Fn simplify(Fn f) {
+  for (int i = 0; i < f.n;) {
+    uint8_t v = kVarMask[i];
+    // f depends on var i iff cofactors differ
+    uint8_t hi = f.tt & v, lo = f.tt & (uint8_t)~v;
+    int sh = i == 0 ? 4 : i == 1 ? 2 : 1;
+    bool depends = (uint8_t)(hi >> sh) != lo;
+    if (depends) {
+      ++i;
+      continue;
+    }
+    // remove leaf i: rebuild the table over the remaining leaves
+    Fn g;
+    g.n = f.n - 1;
+    int k = 0;
+    for (int j = 0; j < f.n; ++j)
+      if (j != i) g.leaf[k++] = f.leaf[j];
+    // evaluate f with var i fixed to 0 over the new variable positions
+    uint8_t m[3] = {0, 0, 0};
+    k = 0;
+    for (int j = 0; j < f.n; ++j) m[j] = (j == i) ? 0 : kVarMask[k++];
+    g.tt = apply_tt(f.tt, m[0], m[1], m[2]);
+    f = g;
+  }
+  if (f.n == 0) f.tt = (f.tt & 1) ? 0xFF : 0x00;
+  return f;
+}
+
+bool merge(const Fn* parts, int np, uint32_t* u, int* un) {
+  *un = 0;
+  for (int p = 0; p < np; ++p)
+    for (int i = 0; i < parts[p].n; ++i) {
+      bool seen = false;
+      for (int j = 0; j < *un; ++j) seen |= u[j] == parts[p].leaf[i];
+      if (!seen) {
+        if (*un == 3) return false;
+        u[(*un)++] = parts[p].leaf[i];
+      }
+    }
+  return true;
+}
+
+struct Builder {
+  const MachineProgram& mp;
+  GateProgram& gp;
+  // per-block state
+  const Block* blk = nullptr;
+  std::unordered_map<uint32_t, const Instr*> instr_of;
+  std::unordered_map<uint32_t, Fn> fn_memo;
+  std::unordered_map<uint32_t, uint32_t> net_memo;
+  std::vector<uint32_t> sig_cur_net;  // current net holding each signal's value
+  std::map<std::tuple<uint8_t, uint8_t, uint32_t, uint32_t, uint32_t>, uint32_t> cell_cse;  // internal-cell dedup
+  int cur_packet = 0;
+  std::vector<int> store_packet;  // comb packet storing each signal, -1 if none
+
+  Builder(const MachineProgram& m, GateProgram& g) : mp(m), gp(g) {}
+
+  uint32_t new_net() {
+    gp.net_signal.push_back(-1);
+    gp.net_is_source.push_back(0);
+    return gp.n_nets++;
+  }
+
+  void add_cell(const Fn& f0, uint32_t out) {
+    Fn f = simplify(f0);
+    GateCell c;
+    c.lut = f.tt;
+    for (int i = 0; i < 3; ++i) c.in[i] = i < f.n ? f.leaf[i] : kNetConst0;
+    c.out = out;
+    gp.cells.push_back(c);
+  }
+
+  uint32_t signal_net_for_read(uint32_t s) {
+    if (blk == &mp.comb && store_packet[s] >= 0 && store_packet[s] >= cur_packet)
+      throw RrtlError("E_GATE_SCOPE", "signal read before its combinational store (combinational loop)");
+    return sig_cur_net[s];
+  }
+
+  Fn fn_of(uint32_t v) {
+    auto it = fn_memo.find(v);
+    if (it != fn_memo.end()) return it->second;
+    const Instr& in = *instr_of.at(v);
+    Fn r;
+    switch (in.kind) {
+      case IK::Signal: r = fn_leaf(signal_net_for_read(in.index)); break;
+      case IK::Lit: r = fn_const(!in.lit.empty() && (in.lit[0] & 1)); break;
+      case IK::Not: r = fn_of(in.ops[0]); r.tt = (uint8_t)~r.tt; break;
+      case IK::And: case IK::Or: case IK::Xor: case IK::Mux: {
+        int np = in.kind == IK::Mux ? 3 : 2;
+        Fn parts[3];
+        for (int i = 0; i < np; ++i) parts[i] = simplify(fn_of(in.ops[i]));
+        uint32_t u[3];
+        int un;
+        while (!merge(parts, np, u, &un)) {
+          // materialise the operand with the widest support
+          int best = -1;
+          for (int i = 0; i < np; ++i)
+            if (parts[i].n >= 2 && (best < 0 || parts[i].n > parts[best].n)) best = i;
+          if (best < 0) throw RrtlError("E_GATE_SCOPE", "internal: cannot cover expression");
+          parts[best] = fn_leaf(realize(in.ops[best]));
+        }
+        uint8_t t[3];
+        for (int i = 0; i < np; ++i) t[i] = remap(parts[i], u, un);
+        r.n = (uint8_t)un;
+        for (int i = 0; i < un; ++i) r.leaf[i] = u[i];
+        if (in.kind == IK::And) r.tt = t[0] & t[1];
+        else if (in.kind == IK::Or) r.tt = t[0] | t[1];
+        else if (in.kind == IK::Xor) r.tt = t[0] ^ t[1];
+        else r.tt = (uint8_t)((t[0] & t[1]) | (~t[0] & t[2]));
+        r = simplify(r);
+        break;
+      }
+      default:
+        throw RrtlError("E_GATE_SCOPE", "op is not a gate-level bitwise op");
+    }
+    fn_memo[v] = r;
+    return r;
+  }
+
+  // A net holding value v (creates an internal cell if needed).
+  uint32_t realize(uint32_t v) {
+    auto it = net_memo.find(v);
+    if (it != net_memo.end()) return it->second;
+    Fn f = simplify(fn_of(v));
+    uint32_t net;
+    if (f.n == 0) net = (f.tt & 1) ? kNetConst1 : kNetConst0;
+    else if (f.n == 1 && f.tt == kVarMask[0]) net = f.leaf[0];
+    else {
+      auto key = std::make_tuple(f.tt, f.n, f.leaf[0], f.leaf[1], f.leaf[2]);
+      auto c = cell_cse.find(key);
+      if (c != cell_cse.end()) {
+        net = c->second;
+      } else {
+        net = new_net();
+        add_cell(f, net);
+        cell_cse[key] = net;
+      }
+    }
+    net_memo[v] = net;
+    fn_memo[v] = fn_leaf(net);
+    return net;
+  }
+
+  void start_block(const Block& b) {
+    blk = &b;
+    instr_of.clear();
+    fn_memo.clear();
+    net_memo.clear();
+    for (auto& p : b.packets)
+      for (auto& in : p.instrs) instr_of[in.dst] = &in;
+  }
+};
+
+}  // namespace
+
+GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups) {
+  const PackedProgram& P = mp.source;
+  GateProgram gp;
+  gp.piece_groups = piece_groups;
+  for (auto& s : P.signals)
+    if (s.layout.width != 1) throw RrtlError("E_GATE_SCOPE", "signal `" + s.name + "` is wider than 1 bit");
+  if (!P.memories.empty()) throw RrtlError("E_GATE_SCOPE", "memories are outside the gate engine");
+  if (!mp.async_reset_comb.packets.empty()) throw RrtlError("E_GATE_SCOPE", "asynchronous resets are outside the gate engine");
+  for (const Block* b : {&mp.comb, &mp.tick_next, &mp.tick_commit})
+    for (auto& p : b->packets) {
+      gp.source_instrs += p.instrs.size();
+      for (auto& e : p.effects)
+        if (e.kind == EffK::MemoryWrite) throw RrtlError("E_GATE_SCOPE", "memory writes are outside the gate engine");
+    }
+
+  uint32_t ns = (uint32_t)P.signals.size();
+  gp.n_signals = ns;
+  gp.n_nets = 2 + ns;
+  gp.net_signal.assign(gp.n_nets, -1);
+  gp.net_is_source.assign(gp.n_nets, 0);
+  gp.net_is_source[kNetConst0] = gp.net_is_source[kNetConst1] = 1;
+  gp.signal_net.resize(ns);
+  for (uint32_t s = 0; s < ns; ++s) {
+    gp.signal_net[s] = 2 + s;
+    gp.net_signal[2 + s] = (int32_t)s;
+  }
+
+  Builder B(mp, gp);
+  B.store_packet.assign(ns, -1);
+  for (size_t p = 0; p < mp.comb.packets.size(); ++p)
+    for (auto& e : mp.comb.packets[p].effects)
+      if (e.kind == EffK::StoreSignal) {
+        if (B.store_packet[e.dst] >= 0) throw RrtlError("E_GATE_SCOPE", "signal assigned more than once");
+        B.store_packet[e.dst] = (int)p;
+      }
+  for (uint32_t s = 0; s < ns; ++s)
+    if (B.store_packet[s] < 0) gp.net_is_source[2 + s] = 1;
+  B.sig_cur_net.resize(ns);
+  for (uint32_t s = 0; s < ns; ++s) B.sig_cur_net[s] = 2 + s;
+
+  // comb block: one cell per stored signal
+  B.start_block(mp.comb);
+  for (size_t p = 0; p < mp.comb.packets.size(); ++p) {
+    B.cur_packet = (int)p;
+    for (auto& e : mp.comb.packets[p].effects) {
+      if (e.kind != EffK::StoreSignal) continue;
+      Fn f = B.fn_of(e.value);
+      B.add_cell(f, 2 + e.dst);
+    }
+  }
+  // tick_next block: D nets
+  B.start_block(mp.tick_next);
+  B.cur_packet = 1 << 30;
+  for (auto& p : mp.tick_next.packets)
+    for (auto& e : p.effects) {
+      if (e.kind != EffK::CaptureReg) continue;
+      if (gp.net_is_source[2 + e.dst] == 0)
+        throw RrtlError("E_GATE_SCOPE", "captured signal is also combinationally assigned");
+      GateReg r;
+      r.signal = e.dst;
+      r.q_net = 2 + e.dst;
+      uint32_t d = B.realize(e.value);
+      bool d_is_reg = d >= 2 && d < 2 + ns && P.signals[d - 2].kind == PSK::Reg;
+      if (d_is_reg) {  // keep D distinct from every Q so the commit is one pass
+        uint32_t nd = B.new_net();
+        B.add_cell(fn_leaf(d), nd);
+        d = nd;
+      }
+      r.d_net = d;
+      r.has_reset = e.has_reset;
+      r.rst_net = e.has_reset ? 2 + e.reset.signal : kNetConst0;
+      if (e.has_reset && P.signals[e.reset.signal].kind == PSK::Reg) {  // same one-pass rule for resets
+        uint32_t nr = B.new_net();
+        B.add_cell(fn_leaf(r.rst_net), nr);
+        r.rst_net = nr;
+      }
+      r.active_low = e.has_reset && e.reset.active_low;
+      r.reset_value = e.has_reset && !e.reset.value.empty() && (e.reset.value[0] & 1);
+      gp.regs.push_back(r);
+    }
+  gp.n_real_cells = (uint32_t)gp.cells.size();
+
+  // ---- levelize
+  gp.net_level.assign(gp.n_nets, -1);
+  std::vector<int32_t> cell_of_net(gp.n_nets, -1);
+  for (size_t i = 0; i < gp.cells.size(); ++i) cell_of_net[gp.cells[i].out] = (int32_t)i;
+  std::vector<int32_t> memo(gp.cells.size(), -2);
+  // cells were created in dependency order except for signal reads of later
+  // stores (rejected above), so one forward pass suffices; iterate to a fixpoint
+  // to be robust to creation order.
+  bool changed = true;
+  for (auto& c : gp.cells) c.level = 0;
+  while (changed) {
+    changed = false;
+    for (auto& c : gp.cells) {
+      int32_t lv = 0;
+      for (int k = 0; k < 3; ++k) {
+        int32_t pc = cell_of_net[c.in[k]];
+        if (pc >= 0) lv = std::max(lv, gp.cells[pc].level + 1);
+      }
+      if (lv != c.level) {
+        if (lv > (int32_t)gp.cells.size()) throw RrtlError("E_GATE_SCOPE", "combinational cycle between cells");
+        c.level = lv;
+        changed = true;
+      }
+    }
+  }
+  int32_t max_level = -1;
+  for (auto& c : gp.cells) {
+    max_level = std::max(max_level, c.level);
+    gp.net_level[c.out] = c.level;
+  }
+  gp.n_levels = (uint32_t)(max_level + 1);
+
+  // ---- group by level and truth table, pad to kGroup
+  std::vector<GateCell> sorted(gp.cells);
+  std::stable_sort(sorted.begin(), sorted.end(), [](const GateCell& x, const GateCell& y) {
+    if (x.level != y.level) return x.level < y.level;
+    return x.lut < y.lut;
+  });
+  std::vector<GateCell> grouped;
+  gp.level_group_begin.assign(gp.n_levels + 1, 0);
+  size_t i = 0;
+  for (uint32_t L = 0; L < gp.n_levels; ++L) {
+    gp.level_group_begin[L] = (uint32_t)(grouped.size() / kGroup);
+    while (i < sorted.size() && sorted[i].level == (int32_t)L) {
+      size_t j = i;
+      while (j < sorted.size() && sorted[j].level == (int32_t)L && sorted[j].lut == sorted[i].lut) ++j;
+      for (size_t k = i; k < j; ++k) grouped.push_back(sorted[k]);
+      while (grouped.size() % kGroup) {
+        GateCell pad;
+        pad.lut = sorted[i].lut;
+        pad.level = (int32_t)L;
+        pad.pad = true;
+        pad.out = kNetConst0;  // redirected to the scratch slot / row
+        grouped.push_back(pad);
+      }
+      i = j;
+    }
+  }
+  gp.level_group_begin[gp.n_levels] = (uint32_t)(grouped.size() / kGroup);
+  gp.cells = std::move(grouped);
+
+  // ---- pieces
+  for (uint32_t L = 0; L < gp.n_levels; ++L) {
+    uint32_t g0 = gp.level_group_begin[L], g1 = gp.level_group_begin[L + 1];
+    for (uint32_t g = g0; g < g1; g += piece_groups) {
+      GatePiece pc;
+      pc.level = L;
+      pc.group_begin = g;
+      pc.n_groups = std::min(piece_groups, g1 - g);
+      pc.last_of_level = g + pc.n_groups >= g1;
+      gp.pieces.push_back(pc);
+    }
+  }
+
+  // ---- on-chip slots by liveness
+  // last use: consumer level; D nets and output-port nets live to the end.
+  const int32_t kEnd = (int32_t)gp.n_levels;
+  std::vector<int32_t> last_use(gp.n_nets, -1);
+  for (auto& c : gp.cells) {
+    if (c.pad) continue;
+    for (int k = 0; k < 3; ++k) last_use[c.in[k]] = std::max(last_use[c.in[k]], c.level);
+  }
+  for (auto& r : gp.regs) {
+    last_use[r.d_net] = kEnd;
+    last_use[r.rst_net] = kEnd;
+  }
+  for (uint32_t s = 0; s < ns; ++s)
+    if (P.signals[s].kind == PSK::Output) last_use[2 + s] = kEnd;
+  // Registers are rewritten by every commit, so between a register's last
+  // read in the settle and the commit its slot can host nets that die before
+  // the end of the cycle. End-live nets (D, reset, outputs) never take such a
+  // slot, so every register slot is free again when the commit writes it.
+  gp.net_slot.assign(gp.n_nets, -1);
+  std::vector<uint8_t> is_reg_q(gp.n_nets, 0);
+  for (auto& r : gp.regs) is_reg_q[r.q_net] = 1;
+  uint32_t next_slot = 1;  // slot 0 is the scratch slot for padding cells
+  std::vector<std::vector<uint32_t>> q_free_after(gp.n_levels + 1);  // register slots released after level L
+  for (uint32_t n = 0; n < gp.n_nets; ++n)
+    if (gp.net_is_source[n]) {
+      gp.net_slot[n] = (int32_t)next_slot++;
+      if (n != kNetConst0 && n != kNetConst1) gp.source_nets.push_back(n);
+      if (is_reg_q[n] && last_use[n] < kEnd) q_free_after[std::max<int32_t>(last_use[n], -1) + 1].push_back((uint32_t)gp.net_slot[n]);
+    }
+  std::vector<std::vector<uint32_t>> produced(gp.n_levels), dying(gp.n_levels + 1);
+  for (uint32_t n = 0; n < gp.n_nets; ++n) {
+    if (gp.net_is_source[n] || gp.net_level[n] < 0) continue;
+    produced[gp.net_level[n]].push_back(n);
+    int32_t lu = std::max(last_use[n], gp.net_level[n]);
+    if (lu < kEnd) dying[lu].push_back(n);
+  }
+  std::vector<uint32_t> free_general, free_q;
+  std::vector<uint8_t> slot_is_q(next_slot + 1, 0);
+  for (uint32_t n = 0; n < gp.n_nets; ++n)
+    if (is_reg_q[n] && gp.net_slot[n] >= 0) slot_is_q[gp.net_slot[n]] = 1;
+  for (uint32_t L = 0; L < gp.n_levels; ++L) {
+    // register slots whose last read was before level L (index L in q_free_after)
+    for (uint32_t s : q_free_after[L]) free_q.push_back(s);
+    if (L > 0)
+      for (uint32_t n : dying[L - 1]) {
+        uint32_t s = (uint32_t)gp.net_slot[n];
+        (s < slot_is_q.size() && slot_is_q[s] ? free_q : free_general).push_back(s);
+      }
+    for (uint32_t n : produced[L]) {
+      bool end_live = std::max(last_use[n], gp.net_level[n]) >= kEnd;
+      if (!end_live && !free_q.empty()) {
+        gp.net_slot[n] = (int32_t)free_q.back();
+        free_q.pop_back();
+      } else if (!free_general.empty()) {
+        gp.net_slot[n] = (int32_t)free_general.back();
+        free_general.pop_back();
+      } else {
+        gp.net_slot[n] = (int32_t)next_slot++;
+      }
+    }
+  }
+  for (uint32_t n = 0; n < gp.n_nets; ++n) gp.net_end_live.push_back(std::max(last_use[n], gp.net_level[n]) >= kEnd ? 1 : 0);
+  for (uint32_t n = 0; n < gp.n_nets; ++n)
+    if (gp.net_is_source[n] && !is_reg_q[n]) gp.net_end_live[n] = 1;
+  gp.n_slots = next_slot;
+  return gp;
+}
+
+}  // namespace rrtl

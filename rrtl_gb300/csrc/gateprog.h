@@ -1,0 +1,95 @@
+// Bit-sliced gate program: the GPU lowering of a gate-level machine program.
+//
+// Scope is the reference's bit-parallel engine (crates/rrtl-sim-ir/src/bitparallel.rs:1-17):
+// every signal 1 bit, ops Signal/Lit/Not/And/Or/Xor/Mux, registers with
+// optional synchronous reset, no memories. Each 32-lane word of a net is one
+// u32 (bit k = lane 32*w + k).
+//
+// Lowering steps:
+//  1. Every comb-assigned signal becomes a net produced by one LUT3 cell whose
+//     truth table is the assignment's expression over at most three leaf nets
+//     (other signals, internal nets, constants). Sub-expressions whose support
+//     exceeds three leaves become internal nets. Cells never look through
+//     another signal's net, so a stuck-at force on any signal net behaves as
+//     in BitParallelSimulator::settle (bitparallel.rs:256-300).
+//  2. Register next-state expressions (tick_next) become cells too; their
+//     outputs are the D nets read by the commit.
+//  3. Cells are levelized (level = 1 + deepest input producer) and, within a
+//     level, sorted by truth table and padded to groups of kGroup cells that
+//     share one table, so a warp evaluates one table per group.
+//  4. Nets get on-chip slots by liveness over the level order; sources
+//     (inputs, registers, constants) keep permanent slots.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "lower.h"
+
+namespace rrtl {
+
+constexpr uint32_t kGroup = 4;        // cells per warp group (32 lanes / 8 words)
+constexpr uint32_t kTileWords = 8;    // 32-lane words per CTA tile in the fused kernel
+constexpr uint32_t kNetConst0 = 0;    // all-zero net
+constexpr uint32_t kNetConst1 = 1;    // all-ones net
+constexpr uint32_t kMaxSlots = 16383; // 14-bit slot fields in packed records
+
+struct GateCell {
+  uint8_t lut = 0;      // LOP3 table: input a <-> 0xF0, b <-> 0xCC, c <-> 0xAA
+  uint32_t in[3] = {kNetConst0, kNetConst0, kNetConst0};
+  uint32_t out = 0;     // net
+  int32_t level = 0;
+  bool pad = false;     // padding cell (writes the scratch slot)
+};
+
+struct GateReg {
+  uint32_t signal;   // packed signal index
+  uint32_t q_net;
+  uint32_t d_net;
+  uint32_t rst_net;  // kNetConst0 when no reset
+  bool has_reset, active_low, reset_value;
+};
+
+// Bounded piece of one level's cells: the unit staged into shared memory.
+struct GatePiece {
+  uint32_t level;
+  uint32_t group_begin;  // index of the first group in the level-ordered group array
+  uint32_t n_groups;
+  bool last_of_level;
+};
+
+struct GateProgram {
+  uint32_t n_signals = 0;
+  uint32_t n_nets = 0;                  // global net array rows
+  std::vector<uint32_t> signal_net;     // packed signal -> net
+  std::vector<int32_t> net_signal;      // net -> packed signal or -1
+  std::vector<uint8_t> net_is_source;   // constants, inputs, registers, undriven signals
+  std::vector<int32_t> net_level;       // producing cell level, -1 for sources
+  std::vector<GateCell> cells;          // level-ordered, grouped, padded
+  uint32_t n_real_cells = 0;
+  uint32_t n_levels = 0;
+  std::vector<uint32_t> level_group_begin;  // per level, first group; size n_levels+1
+  std::vector<GateReg> regs;
+  // on-chip slots
+  std::vector<int32_t> net_slot;  // -1: not resident
+  std::vector<uint8_t> net_end_live;  // holds its value in its slot when the cycle's settle ends
+  uint32_t n_slots = 0;           // including the scratch slot (slot 0)
+  std::vector<uint32_t> source_nets;  // nets loaded into slots at tile start (and written back)
+  std::vector<GatePiece> pieces;
+  uint32_t piece_groups = 0;      // max groups per piece
+  uint64_t source_instrs = 0;
+};
+
+// Throws RrtlError("E_GATE_SCOPE", ...) when the program is outside the gate engine's scope.
+GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups);
+
+// Packed 8-byte record for one cell in shared memory: four 14-bit slot fields
+// (a, b, c, out) with the 8-bit truth table spread over their top two bits.
+inline uint64_t pack_smem_record(uint32_t a, uint32_t b, uint32_t c, uint32_t out, uint8_t lut) {
+  uint64_t x = (uint64_t)(a | ((lut & 3u) << 14)) | ((uint64_t)(b | (((lut >> 2) & 3u) << 14)) << 16) |
+               ((uint64_t)(c | (((lut >> 4) & 3u) << 14)) << 32) | ((uint64_t)(out | (((lut >> 6) & 3u) << 14)) << 48);
+  return x;
+}
+
+}  // namespace rrtl

@@ -1,0 +1,1013 @@
+// C ABI implementation (include/rrtl_cuda.h): contexts, compiled designs,
+// lane batches and runs. All device memory is owned here; caller buffers are
+// only touched during a call.
+#include "runtime.h"
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+namespace rrtl {
+
+// kernels (gate_kernels.cu, word_kernels.cu)
+size_t gate_fused_smem_bytes(const GateProgDev& P);
+cudaError_t gate_fused_prepare(size_t smem);
+cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
+cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st);
+cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st);
+cudaError_t word_prepare(size_t smem);
+
+constexpr uint32_t kPieceGroups = 256;
+constexpr uint32_t kWordThreads = 128;
+constexpr size_t kWordSmemBudget = 96 * 1024;
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) fail(RRTL_E_OOM, std::string("E_OOM: ") + what + ": " + cudaGetErrorString(e));
+  if (e != cudaSuccess) fail(RRTL_E_DEVICE, std::string("E_DEVICE: ") + what + ": " + cudaGetErrorString(e));
+}
+
+DevBuf::~DevBuf() {
+  if (p) cudaFree(p);
+}
+
+void DevBuf::reserve(size_t n) {
+  if (n <= bytes) return;
+  if (p) cudaFree(p);
+  p = nullptr;
+  bytes = 0;
+  cuda_check(cudaMalloc(&p, n), "cudaMalloc");
+  bytes = n;
+}
+
+}  // namespace rrtl
+
+using namespace rrtl;
+
+static thread_local std::string g_last_error;
+
+template <class F>
+static rrtl_status guard(F&& f) {
+  try {
+    f();
+    g_last_error.clear();
+    return RRTL_OK;
+  } catch (const ApiError& e) {
+    g_last_error = e.msg;
+    return e.status;
+  } catch (const RrtlError& e) {
+    g_last_error = e.what();
+    return e.code.rfind("E_GATE_SCOPE", 0) == 0 || e.code.rfind("E_WORD_SCOPE", 0) == 0 ? RRTL_E_UNSUPPORTED
+                                                                                         : RRTL_E_DESIGN;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "E_OOM: host allocation failed";
+    return RRTL_E_OOM;
+  } catch (const std::exception& e) {
+    g_last_error = std::string("E_INTERNAL: ") + e.what();
+    return RRTL_E_ARG;
+  }
+}
+
+#define REQUIRE(cond, st, msg) \
+  do {                         \
+    if (!(cond)) fail(st, msg); \
+  } while (0)
+
+// ------------------------------------------------------------------ helpers --
+
+namespace {
+
+uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
+
+void set_device(rrtl_ctx* c) { cuda_check(cudaSetDevice(c->device), "cudaSetDevice"); }
+
+const PackedSignal& signal_of(rrtl_design* d, uint32_t s) {
+  REQUIRE(s < d->mp.source.signals.size(), RRTL_E_SIGNAL, "E_GPU_SIGNAL: signal index out of range");
+  return d->mp.source.signals[s];
+}
+
+void upload_gate_program(rrtl_design* d) {
+  const GateProgram& gp = d->gp;
+  uint32_t n_groups = (uint32_t)(gp.cells.size() / kGroup);
+  REQUIRE(gp.n_nets + 1 < (1u << 24), RRTL_E_UNSUPPORTED, "E_GATE_SCOPE: more than 16M nets");
+  const uint32_t scratch_net = gp.n_nets;  // extra row for padding cells
+  std::vector<uint4> grecs(gp.cells.size());
+  std::vector<uint32_t> wb(gp.cells.size(), 0xFFFFFFFFu);
+  for (size_t i = 0; i < gp.cells.size(); ++i) {
+    const GateCell& c = gp.cells[i];
+    uint32_t out = c.pad ? scratch_net : c.out;
+    grecs[i] = make_uint4(c.in[0], c.in[1], c.in[2], out | ((uint32_t)c.lut << 24));
+    if (!c.pad && gp.net_signal[c.out] >= 0) wb[i] = c.out;
+  }
+  std::vector<GateRegDev> gregs, sregs;
+  for (auto& r : gp.regs) {
+    uint32_t fl = (r.has_reset ? 1u : 0u) | (r.active_low ? 2u : 0u) | (r.reset_value ? 4u : 0u);
+    gregs.push_back(GateRegDev{r.q_net, r.d_net, r.rst_net, fl});
+  }
+  upload(d->d_grecs, grecs);
+  upload(d->d_wb, wb);
+  upload(d->d_lgb, gp.level_group_begin);
+  upload(d->d_gregs, gregs);
+
+  // fused program: only when every slot index fits the packed record
+  d->fused_ok = gp.n_slots <= kMaxSlots;
+  if (d->fused_ok) {
+    std::vector<uint2> srecs(gp.cells.size());
+    int32_t c0 = gp.net_slot[kNetConst0];
+    for (size_t i = 0; i < gp.cells.size(); ++i) {
+      const GateCell& c = gp.cells[i];
+      uint32_t a = c.pad ? c0 : gp.net_slot[c.in[0]], b = c.pad ? c0 : gp.net_slot[c.in[1]];
+      uint32_t cc = c.pad ? c0 : gp.net_slot[c.in[2]], o = c.pad ? 0 : gp.net_slot[c.out];
+      uint64_t x = pack_smem_record(a, b, cc, o, c.lut);
+      srecs[i] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
+    }
+    std::vector<uint4> pieces;
+    for (auto& p : gp.pieces) pieces.push_back(make_uint4(p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u));
+    std::vector<uint32_t> src_slot;
+    for (uint32_t n : gp.source_nets) src_slot.push_back((uint32_t)gp.net_slot[n]);
+    for (auto& r : gp.regs) {
+      uint32_t fl = (r.has_reset ? 1u : 0u) | (r.active_low ? 2u : 0u) | (r.reset_value ? 4u : 0u);
+      sregs.push_back(GateRegDev{(uint32_t)gp.net_slot[r.q_net], (uint32_t)gp.net_slot[r.d_net],
+                                 (uint32_t)gp.net_slot[r.rst_net], fl});
+    }
+    upload(d->d_srecs, srecs);
+    upload(d->d_pieces, pieces);
+    upload(d->d_src_net, gp.source_nets);
+    upload(d->d_src_slot, src_slot);
+    upload(d->d_sregs, sregs);
+  }
+  GateProgDev& G = d->gdev;
+  G = GateProgDev{};
+  G.srecs = d->d_srecs.as<uint2>();
+  G.pieces = d->d_pieces.as<uint4>();
+  G.n_pieces = (uint32_t)gp.pieces.size();
+  G.n_slots = gp.n_slots;
+  G.n_levels = gp.n_levels;
+  G.piece_groups = kPieceGroups;
+  G.src_net = d->d_src_net.as<uint32_t>();
+  G.src_slot = d->d_src_slot.as<uint32_t>();
+  G.n_src = (uint32_t)gp.source_nets.size();
+  G.sregs = d->d_sregs.as<GateRegDev>();
+  G.wb_net = d->d_wb.as<uint32_t>();
+  G.grecs = d->d_grecs.as<uint4>();
+  G.level_group_begin = d->d_lgb.as<uint32_t>();
+  G.gregs = d->d_gregs.as<GateRegDev>();
+  G.n_regs = (uint32_t)gp.regs.size();
+  G.const0_slot = d->fused_ok ? (uint32_t)gp.net_slot[kNetConst0] : 0;
+  G.const1_slot = d->fused_ok ? (uint32_t)gp.net_slot[kNetConst1] : 0;
+  (void)n_groups;
+  if (d->fused_ok) {
+    d->fused_smem = gate_fused_smem_bytes(G);
+    if (d->fused_smem > d->ctx->max_smem) {
+      d->fused_ok = false;
+    } else {
+      cuda_check(gate_fused_prepare(d->fused_smem), "gate_fused_prepare");
+    }
+  }
+  // nets that hold their end-of-cycle value in a slot (recordable on the fused path)
+  d->end_live = gp.net_end_live;
+}
+
+void upload_word_program(rrtl_design* d) {
+  const WordProgram& wp = d->wp;
+  upload(d->d_wcode, wp.code);
+  upload(d->d_wlit, wp.lits);
+  // memories and commits share one buffer
+  std::vector<uint8_t> blob(wp.mems.size() * sizeof(WMemDev) + wp.commits.size() * sizeof(WCommitDev) + 16);
+  if (!wp.mems.empty()) memcpy(blob.data(), wp.mems.data(), wp.mems.size() * sizeof(WMemDev));
+  if (!wp.commits.empty())
+    memcpy(blob.data() + wp.mems.size() * sizeof(WMemDev), wp.commits.data(), wp.commits.size() * sizeof(WCommitDev));
+  upload(d->d_wcap, blob);
+  WordProgDev& W = d->wdev;
+  W = WordProgDev{};
+  W.code = d->d_wcode.as<WInstr>();
+  W.comb_b = wp.comb_b; W.comb_e = wp.comb_e;
+  W.async_b = wp.async_b; W.async_e = wp.async_e;
+  W.next_b = wp.next_b; W.next_e = wp.next_e;
+  W.commit_b = wp.commit_b; W.commit_e = wp.commit_e;
+  W.lits = d->d_wlit.as<unsigned long long>();
+  W.mems = d->d_wcap.as<WMemDev>();
+  W.commits = reinterpret_cast<const WCommitDev*>(d->d_wcap.as<uint8_t>() + wp.mems.size() * sizeof(WMemDev));
+  W.n_commits = (uint32_t)wp.commits.size();
+  W.n_vslots = std::max<uint32_t>(wp.n_vslots, 1);
+  size_t smem = (size_t)W.n_vslots * kWordThreads * 8u;
+  if (smem <= kWordSmemBudget) cuda_check(word_prepare(smem), "word_prepare");
+}
+
+bool word_smem_slots(rrtl_design* d) { return (size_t)d->wdev.n_vslots * kWordThreads * 8u <= kWordSmemBudget; }
+
+struct Timer {
+  rrtl_batch* b;
+  explicit Timer(rrtl_batch* bb) : b(bb) { cuda_check(cudaEventRecord(b->ev0, b->d->ctx->stream), "event"); }
+  void stop() { cuda_check(cudaEventRecord(b->ev1, b->d->ctx->stream), "event"); }
+};
+
+void check_err_word(rrtl_batch* b) {
+  uint32_t e = 0;
+  cuda_check(cudaMemcpyAsync(&e, b->d_err.p, 4, cudaMemcpyDeviceToHost, b->d->ctx->stream), "err");
+  cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+  if (e) {
+    cudaMemsetAsync(b->d_err.p, 0, 4, b->d->ctx->stream);
+    fail((rrtl_status)e, "E_TIMEOUT: a bounded device wait gave up");
+  }
+}
+
+// Forces grouped per 8-word tile and per stage (stage 0 after commit, L+1 after level L).
+void build_forces(rrtl_batch* b) {
+  rrtl_design* d = b->d;
+  const GateProgram& gp = d->gp;
+  uint32_t stages = gp.n_levels + 1;
+  std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, std::pair<uint32_t, uint32_t>> merged;  // (tile, stage, net, word)
+  for (auto& f : b->faults) {
+    uint32_t net = gp.signal_net[f.signal];
+    int32_t lv = gp.net_level[net];
+    uint32_t stage = lv < 0 ? 0u : (uint32_t)lv + 1u;
+    uint32_t gw = f.lane / 32, bit = f.lane % 32;
+    auto& mv = merged[std::make_tuple(gw / 8, stage, net, gw % 8)];
+    mv.first |= 1u << bit;
+    if (f.value) mv.second |= 1u << bit;
+    else mv.second &= ~(1u << bit);
+  }
+  std::vector<GateForceDev> fs;
+  std::vector<uint32_t> off((size_t)b->n_tiles * (stages + 1), 0);
+  size_t k = 0;
+  auto it = merged.begin();
+  for (uint32_t t = 0; t < b->n_tiles; ++t)
+    for (uint32_t s = 0; s <= stages; ++s) {
+      off[(size_t)t * (stages + 1) + s] = (uint32_t)k;
+      if (s == stages) continue;
+      while (it != merged.end() && std::get<0>(it->first) == t && std::get<1>(it->first) == s) {
+        uint32_t net = std::get<2>(it->first);
+        int32_t slot = gp.net_slot.empty() ? 0 : gp.net_slot[net];
+        fs.push_back(GateForceDev{(uint32_t)std::max(slot, 0), net, std::get<3>(it->first), it->second.first,
+                                  it->second.second, 0});
+        ++k;
+        ++it;
+      }
+    }
+  // the per-tile table stores stages+1 boundaries; the last boundary of tile t is the first of tile t+1
+  for (uint32_t t = 0; t < b->n_tiles; ++t) off[(size_t)t * (stages + 1) + stages] = t + 1 < b->n_tiles ? off[(size_t)(t + 1) * (stages + 1)] : (uint32_t)k;
+  upload(b->d_forces, fs);
+  upload(b->d_force_off, off);
+  b->has_forces = !fs.empty();
+}
+
+// ---- gate engine run
+void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
+  rrtl_design* d = b->d;
+  const GateProgram& gp = d->gp;
+  cudaStream_t st = d->ctx->stream;
+  bool fused = b->path == RRTL_PATH_FUSED && d->fused_ok;
+  std::vector<GateStimDev> stim;
+  for (uint32_t i = 0; i < run.n_stim; ++i) {
+    const rrtl_stim& s = run.stim[i];
+    signal_of(d, s.signal);
+    uint32_t net = gp.signal_net[s.signal];
+    REQUIRE(gp.net_is_source[net], RRTL_E_ARG, "E_GPU_STIM: stimulus targets a combinationally driven signal");
+    REQUIRE(s.kind <= RRTL_STIM_TRACE, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
+    if (s.kind == RRTL_STIM_TRACE)
+      REQUIRE(s.param < run.n_trace_cols && run.input_trace, RRTL_E_ARG, "E_GPU_STIM: trace column out of range");
+    stim.push_back(GateStimDev{fused ? (uint32_t)gp.net_slot[net] : 0u, net, s.kind, 0, s.param});
+  }
+  std::vector<GateRecDev> rec;
+  for (uint32_t i = 0; i < run.n_record; ++i) {
+    signal_of(d, run.record[i]);
+    uint32_t net = gp.signal_net[run.record[i]];
+    if (fused && !d->end_live[net]) fused = false;  // value not held to the end of the cycle: use the plain path
+    rec.push_back(GateRecDev{0u, net});
+  }
+  if (fused)
+    for (auto& r : rec) r.slot = (uint32_t)gp.net_slot[r.net];
+  if (fused)
+    for (auto& s : stim) s.slot = (uint32_t)gp.net_slot[s.net];
+  REQUIRE(!(run.record_mode & (RRTL_REC_TRACE | RRTL_REC_HASH | RRTL_REC_DETECT)) || run.n_record > 0, RRTL_E_ARG,
+          "E_GPU_RECORD: recording needs at least one signal");
+  REQUIRE(run.cycles < (1ull << 32), RRTL_E_ARG, "E_GPU_STEPS: cycle count exceeds 2^32");
+  upload(b->d_stim, stim);
+  upload(b->d_rec, rec);
+
+  GateRunDev R{};
+  R.cycles = run.cycles;
+  R.seed = run.seed;
+  R.n_stim = (uint32_t)stim.size();
+  R.stim = b->d_stim.as<GateStimDev>();
+  R.n_rec = (uint32_t)rec.size();
+  R.rec = b->d_rec.as<GateRecDev>();
+  R.mode = run.record_mode;
+  R.n_trace_cols = run.n_trace_cols;
+  R.lanes = b->lanes;
+  R.words = b->words;
+  R.words_pad = b->words_pad;
+  R.n_tiles = b->n_tiles;
+  R.force_off = b->d_force_off.as<uint32_t>();
+  R.forces = b->d_forces.as<GateForceDev>();
+  R.has_forces = b->has_forces ? 1u : 0u;
+  R.final_settle = 1;
+  R.nets = b->d_nets.as<uint32_t>();
+  R.err = b->d_err.as<uint32_t>();
+
+  size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->words * 4;
+  size_t trace_out_bytes = (size_t)run.cycles * run.n_record * b->words * 4;
+  size_t hash_bytes = (size_t)run.cycles * 8;
+  size_t det_bytes = (size_t)b->lanes * 4;
+  bool want_trace = run.record_mode & RRTL_REC_TRACE, want_hash = run.record_mode & RRTL_REC_HASH,
+       want_det = run.record_mode & RRTL_REC_DETECT;
+  REQUIRE(!want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
+  REQUIRE(!want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
+  REQUIRE(!want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
+  if (device_ptrs) {
+    R.in_trace = run.input_trace;
+    R.out_trace = run.out_trace;
+    R.out_hash = reinterpret_cast<unsigned long long*>(run.out_hash);
+    R.detect = run.detect;
+  } else {
+    if (trace_in_bytes) {
+      b->d_in_trace.reserve(trace_in_bytes);
+      cuda_check(cudaMemcpyAsync(b->d_in_trace.p, run.input_trace, trace_in_bytes, cudaMemcpyHostToDevice, st), "h2d trace");
+      R.in_trace = b->d_in_trace.as<uint32_t>();
+    }
+    if (want_trace) {
+      b->d_out_trace.reserve(std::max<size_t>(trace_out_bytes, 16));
+      R.out_trace = b->d_out_trace.as<uint32_t>();
+    }
+    if (want_hash) {
+      b->d_hash.reserve(std::max<size_t>(hash_bytes, 16));
+      R.out_hash = b->d_hash.as<unsigned long long>();
+    }
+    if (want_det) {
+      b->d_detect.reserve(std::max<size_t>(det_bytes, 16));
+      R.detect = b->d_detect.as<uint32_t>();
+    }
+  }
+  if (want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, hash_bytes, st), "memset hash");
+  if (want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, det_bytes, st), "memset detect");
+
+  Timer tm(b);
+  if (fused) {
+    uint32_t grid = std::min<uint32_t>(b->n_tiles, d->ctx->sm_count);
+    cuda_check(launch_gate_fused(d->gdev, R, grid, d->fused_smem, st), "gate_fused_kernel");
+  } else {
+    for (uint64_t c = 0; c < run.cycles; ++c) cuda_check(launch_gate_plain(d->gdev, R, c, 0, st), "gate_plain_kernel");
+    cuda_check(launch_gate_plain(d->gdev, R, 0, 1, st), "gate_plain_kernel");
+  }
+  tm.stop();
+  if (!device_ptrs) {
+    if (want_trace) cuda_check(cudaMemcpyAsync(run.out_trace, R.out_trace, trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
+    if (want_hash) cuda_check(cudaMemcpyAsync(run.out_hash, R.out_hash, hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
+    if (want_det) cuda_check(cudaMemcpyAsync(run.detect, R.detect, det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+    check_err_word(b);
+    cuda_check(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "elapsed");
+  }
+}
+
+// ---- word engine run
+void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle) {
+  rrtl_design* d = b->d;
+  cudaStream_t st = d->ctx->stream;
+  const PackedProgram& P = d->mp.source;
+  std::vector<WordStimDev> stim;
+  for (uint32_t i = 0; i < run.n_stim; ++i) {
+    const rrtl_stim& s = run.stim[i];
+    const PackedSignal& ps = signal_of(d, s.signal);
+    REQUIRE(s.kind <= RRTL_STIM_TRACE, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
+    if (s.kind == RRTL_STIM_TRACE)
+      REQUIRE(s.param < run.n_trace_cols && run.input_trace, RRTL_E_ARG, "E_GPU_STIM: trace column out of range");
+    stim.push_back(WordStimDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, s.kind, s.param});
+  }
+  std::vector<WordRecDev> rec;
+  uint32_t rec_limbs = 0;
+  for (uint32_t i = 0; i < run.n_record; ++i) {
+    const PackedSignal& ps = signal_of(d, run.record[i]);
+    rec.push_back(WordRecDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, rec_limbs});
+    rec_limbs += ps.layout.limbs;
+  }
+  REQUIRE(!(run.record_mode & (RRTL_REC_TRACE | RRTL_REC_HASH | RRTL_REC_DETECT)) || run.n_record > 0, RRTL_E_ARG,
+          "E_GPU_RECORD: recording needs at least one signal");
+  upload(b->d_stim, stim);
+  upload(b->d_rec, rec);
+  WordRunDev R{};
+  R.cycles = run.cycles;
+  R.seed = run.seed;
+  R.n_stim = (uint32_t)stim.size();
+  R.stim = b->d_stim.as<WordStimDev>();
+  R.n_rec = (uint32_t)rec.size();
+  R.rec = b->d_rec.as<WordRecDev>();
+  R.rec_limbs = rec_limbs;
+  R.mode = run.record_mode;
+  R.n_trace_cols = run.n_trace_cols;
+  R.lanes = b->lanes;
+  R.lanes_pad = b->lanes_pad;
+  R.values = b->d_values.as<uint32_t>();
+  R.mems = b->d_mem.as<uint32_t>();
+  R.caps = b->d_caps.as<uint32_t>();
+  R.final_settle = final_settle;
+  R.start_settle = start_settle;
+  R.err = b->d_err.as<uint32_t>();
+  bool smem_slots = word_smem_slots(d);
+  REQUIRE(smem_slots, RRTL_E_UNSUPPORTED,
+          "E_WORD_SCOPE: design needs " + std::to_string(d->wdev.n_vslots) + " live value slots, more than shared memory holds");
+  size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->lanes * 4;
+  size_t trace_out_bytes = (size_t)run.cycles * rec_limbs * b->lanes * 4;
+  size_t hash_bytes = (size_t)run.cycles * 8;
+  size_t det_bytes = (size_t)b->lanes * 4;
+  bool want_trace = run.record_mode & RRTL_REC_TRACE, want_hash = run.record_mode & RRTL_REC_HASH,
+       want_det = run.record_mode & RRTL_REC_DETECT;
+  REQUIRE(!want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
+  REQUIRE(!want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
+  REQUIRE(!want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
+  if (device_ptrs) {
+    R.in_trace = run.input_trace;
+    R.out_trace = run.out_trace;
+    R.out_hash = reinterpret_cast<unsigned long long*>(run.out_hash);
+    R.detect = run.detect;
+  } else {
+    if (trace_in_bytes) {
+      b->d_in_trace.reserve(trace_in_bytes);
+      cuda_check(cudaMemcpyAsync(b->d_in_trace.p, run.input_trace, trace_in_bytes, cudaMemcpyHostToDevice, st), "h2d trace");
+      R.in_trace = b->d_in_trace.as<uint32_t>();
+    }
+    if (want_trace) {
+      b->d_out_trace.reserve(std::max<size_t>(trace_out_bytes, 16));
+      R.out_trace = b->d_out_trace.as<uint32_t>();
+    }
+    if (want_hash) {
+      b->d_hash.reserve(std::max<size_t>(hash_bytes, 16));
+      R.out_hash = b->d_hash.as<unsigned long long>();
+    }
+    if (want_det) {
+      b->d_detect.reserve(std::max<size_t>(det_bytes, 16));
+      R.detect = b->d_detect.as<uint32_t>();
+    }
+  }
+  if (want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, hash_bytes, st), "memset hash");
+  if (want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, det_bytes, st), "memset detect");
+  R.vspill = nullptr;
+  Timer tm(b);
+  if (b->path == RRTL_PATH_PLAIN && run.cycles > 1) {
+    // one launch per cycle: the baseline path
+    WordRunDev R1 = R;
+    for (uint64_t c = 0; c < run.cycles; ++c) {
+      R1.cycles = 1;
+      R1.start_settle = (c == 0) ? R.start_settle : 0;
+      R1.final_settle = (c + 1 == run.cycles) ? R.final_settle : 0;
+      // per-cycle pointers shift so cycle c of this launch is cycle 0 of its buffers
+      R1.in_trace = R.in_trace ? R.in_trace + (size_t)c * run.n_trace_cols * b->lanes : nullptr;
+      R1.out_trace = R.out_trace ? R.out_trace + (size_t)c * rec_limbs * b->lanes : nullptr;
+      R1.out_hash = R.out_hash ? R.out_hash + c : nullptr;
+      R1.cycle_base = c;
+      cuda_check(launch_word(d->wdev, R1, smem_slots, st), "word_kernel");
+    }
+  } else {
+    cuda_check(launch_word(d->wdev, R, smem_slots, st), "word_kernel");
+  }
+  tm.stop();
+  if (!device_ptrs) {
+    if (want_trace) cuda_check(cudaMemcpyAsync(run.out_trace, R.out_trace, trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
+    if (want_hash) cuda_check(cudaMemcpyAsync(run.out_hash, R.out_hash, hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
+    if (want_det) cuda_check(cudaMemcpyAsync(run.detect, R.detect, det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+    check_err_word(b);
+    cuda_check(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "elapsed");
+  }
+}
+
+void batch_eval(rrtl_batch* b) {
+  rrtl_run r{};
+  if (b->d->engine == RRTL_ENGINE_GATE) gate_run(b, r, false);
+  else word_run(b, r, false, true, false);
+}
+
+void batch_tick_many(rrtl_batch* b, uint64_t steps, bool sync) {
+  rrtl_run r{};
+  r.cycles = steps;
+  if (b->d->engine == RRTL_ENGINE_GATE) gate_run(b, r, !sync);
+  else word_run(b, r, !sync, true, true);
+  if (sync) check_err_word(b);
+}
+
+}  // namespace
+
+// -------------------------------------------------------------------- C ABI --
+
+extern "C" {
+
+const char* rrtl_last_error(void) { return g_last_error.c_str(); }
+
+rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out) {
+  return guard([&] {
+    REQUIRE(out, RRTL_E_ARG, "E_ARG: out is null");
+    int n = 0;
+    cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+    REQUIRE(device >= 0 && device < n, RRTL_E_ARG, "E_ARG: no such device");
+    auto* c = new rrtl_ctx;
+    c->device = device;
+    try {
+      set_device(c);
+      cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
+      int sms = 0, smem = 0;
+      cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
+      cuda_check(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
+      c->sm_count = (uint32_t)sms;
+      c->max_smem = (size_t)smem;
+    } catch (...) {
+      delete c;
+      throw;
+    }
+    *out = c;
+  });
+}
+
+rrtl_status rrtl_ctx_destroy(rrtl_ctx* ctx) {
+  return guard([&] {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+  });
+}
+
+rrtl_status rrtl_ctx_sm_count(rrtl_ctx* ctx, uint32_t* out) {
+  return guard([&] {
+    REQUIRE(ctx && out, RRTL_E_ARG, "E_ARG: null argument");
+    *out = ctx->sm_count;
+  });
+}
+
+rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out) {
+  return guard([&] {
+    REQUIRE(ctx && json && top && out, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    auto d = std::make_unique<rrtl_design>();
+    d->ctx = ctx;
+    d->design = design_from_json(json, len);
+    d->top = top;
+    PackedProgram pp = lower_to_packed_program(d->design, top);
+    d->mp = lower_to_machine_program(pp);
+    bool gate = true;
+    try {
+      d->gp = build_gate_program(d->mp, kPieceGroups);
+    } catch (const RrtlError& e) {
+      if (e.code != "E_GATE_SCOPE") throw;
+      gate = false;
+    }
+    if (gate) {
+      d->engine = RRTL_ENGINE_GATE;
+      upload_gate_program(d.get());
+    } else {
+      d->engine = RRTL_ENGINE_WORD;
+      d->wp = build_word_program(d->mp);
+      upload_word_program(d.get());
+    }
+    *out = d.release();
+  });
+}
+
+rrtl_status rrtl_design_destroy(rrtl_design* d) {
+  return guard([&] {
+    if (!d) return;
+    cudaSetDevice(d->ctx->device);
+    delete d;
+  });
+}
+
+rrtl_status rrtl_design_info_get(rrtl_design* d, rrtl_design_info* out) {
+  return guard([&] {
+    REQUIRE(d && out, RRTL_E_ARG, "E_ARG: null argument");
+    rrtl_design_info i{};
+    const PackedProgram& P = d->mp.source;
+    i.n_signals = (uint32_t)P.signals.size();
+    i.n_memories = (uint32_t)P.memories.size();
+    i.total_signal_words = P.total_signal_words;
+    i.total_memory_words_per_lane = P.total_memory_words_per_lane;
+    i.engine = d->engine;
+    if (d->engine == RRTL_ENGINE_GATE) {
+      i.n_gates = d->gp.n_real_cells;
+      i.n_levels = d->gp.n_levels;
+      i.n_nets = d->gp.n_nets;
+      i.n_slots = d->fused_ok ? d->gp.n_slots : 0;
+      i.n_regs = (uint32_t)d->gp.regs.size();
+      i.source_instrs = d->gp.source_instrs;
+    } else {
+      i.n_gates = (uint32_t)d->wp.code.size();
+      i.n_levels = (uint32_t)d->mp.comb.packets.size();
+      i.n_slots = d->wp.n_vslots;
+      i.n_regs = (uint32_t)d->wp.commits.size();
+      i.source_instrs = d->wp.source_instrs;
+    }
+    *out = i;
+  });
+}
+
+rrtl_status rrtl_design_signal(rrtl_design* d, const char* name, uint32_t* index, uint32_t* width, uint32_t* kind) {
+  return guard([&] {
+    REQUIRE(d && name, RRTL_E_ARG, "E_ARG: null argument");
+    std::string full = d->top + "." + name;
+    const auto& S = d->mp.source.signals;
+    for (size_t i = 0; i < S.size(); ++i)
+      if (S[i].name == name || S[i].name == full) {
+        if (index) *index = (uint32_t)i;
+        if (width) *width = S[i].layout.width;
+        if (kind) *kind = (uint32_t)S[i].kind;
+        return;
+      }
+    fail(RRTL_E_SIGNAL, std::string("E_GPU_SIGNAL: no signal `") + name + "`");
+  });
+}
+
+rrtl_status rrtl_design_memory(rrtl_design* d, const char* name, uint32_t* index, uint64_t* depth, uint32_t* width) {
+  return guard([&] {
+    REQUIRE(d && name, RRTL_E_ARG, "E_ARG: null argument");
+    std::string full = d->top + "." + name;
+    const auto& M = d->mp.source.memories;
+    for (size_t i = 0; i < M.size(); ++i)
+      if (M[i].name == name || M[i].name == full) {
+        if (index) *index = (uint32_t)i;
+        if (depth) *depth = M[i].depth;
+        if (width) *width = M[i].data_layout.width;
+        return;
+      }
+    fail(RRTL_E_SIGNAL, std::string("E_GPU_MEMORY: no memory `") + name + "`");
+  });
+}
+
+rrtl_status rrtl_batch_create(rrtl_design* d, uint32_t lanes, rrtl_batch** out) {
+  return guard([&] {
+    REQUIRE(d && out, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(lanes > 0, RRTL_E_LANES, "E_GPU_LANES: GPU simulator requires at least one lane");
+    REQUIRE(lanes <= (1u << 30), RRTL_E_LANES, "E_GPU_LANES: too many lanes");
+    set_device(d->ctx);
+    auto b = std::make_unique<rrtl_batch>();
+    b->d = d;
+    b->lanes = lanes;
+    cuda_check(cudaEventCreate(&b->ev0), "event");
+    cuda_check(cudaEventCreate(&b->ev1), "event");
+    b->d_err.reserve(16);
+    cuda_check(cudaMemset(b->d_err.p, 0, 16), "memset");
+    if (d->engine == RRTL_ENGINE_GATE) {
+      b->words = (lanes + 31) / 32;
+      b->words_pad = round_up(b->words, kTileWords);
+      b->n_tiles = b->words_pad / kTileWords;
+      b->rows = d->gp.n_nets + 1;
+      size_t bytes = (size_t)b->rows * b->words_pad * 4;
+      b->d_nets.reserve(bytes);
+      cuda_check(cudaMemset(b->d_nets.p, 0, bytes), "memset nets");
+      cuda_check(cudaMemset(b->d_nets.as<uint8_t>() + (size_t)kNetConst1 * b->words_pad * 4, 0xFF, (size_t)b->words_pad * 4),
+                 "memset const1");
+      build_forces(b.get());
+    } else {
+      b->lanes_pad = round_up(lanes, kWordThreads);
+      const PackedProgram& P = d->mp.source;
+      size_t vb = std::max<size_t>((size_t)P.total_signal_words * b->lanes_pad * 4, 16);
+      size_t mb = std::max<size_t>((size_t)P.total_memory_words_per_lane * b->lanes_pad * 4, 16);
+      size_t cb = std::max<size_t>((size_t)d->wp.total_capture_words * b->lanes_pad * 4, 16);
+      b->d_values.reserve(vb);
+      b->d_mem.reserve(mb);
+      b->d_caps.reserve(cb);
+      cuda_check(cudaMemset(b->d_values.p, 0, vb), "memset");
+      cuda_check(cudaMemset(b->d_mem.p, 0, mb), "memset");
+    }
+    batch_eval(b.get());
+    *out = b.release();
+  });
+}
+
+rrtl_status rrtl_batch_destroy(rrtl_batch* b) {
+  return guard([&] {
+    if (!b) return;
+    cudaSetDevice(b->d->ctx->device);
+    cudaStreamSynchronize(b->d->ctx->stream);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    delete b;
+  });
+}
+
+rrtl_status rrtl_batch_lanes(rrtl_batch* b, uint32_t* out) {
+  return guard([&] {
+    REQUIRE(b && out, RRTL_E_ARG, "E_ARG: null argument");
+    *out = b->lanes;
+  });
+}
+
+static void gate_set_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words) {
+  uint32_t net = b->d->gp.signal_net[signal];
+  std::vector<uint32_t> row(b->words_pad, 0);
+  for (uint32_t w = 0; w < b->words; ++w) {
+    uint32_t valid = b->lanes - w * 32;
+    row[w] = valid >= 32 ? words[w] : (words[w] & ((1u << valid) - 1u));
+  }
+  cuda_check(cudaMemcpyAsync(b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad, row.data(), (size_t)b->words_pad * 4,
+                             cudaMemcpyHostToDevice, b->d->ctx->stream),
+             "h2d signal");
+  cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+}
+
+static void gate_get_bits(rrtl_batch* b, uint32_t signal, uint32_t* words) {
+  uint32_t net = b->d->gp.signal_net[signal];
+  cuda_check(cudaMemcpyAsync(words, b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad, (size_t)b->words * 4,
+                             cudaMemcpyDeviceToHost, b->d->ctx->stream),
+             "d2h signal");
+  cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+  uint32_t valid = b->lanes - (b->words - 1) * 32;
+  if (valid < 32) words[b->words - 1] &= (1u << valid) - 1u;
+}
+
+rrtl_status rrtl_batch_set_input_limbs(rrtl_batch* b, uint32_t signal, const uint32_t* data, size_t n) {
+  return guard([&] {
+    REQUIRE(b && data, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedSignal& ps = signal_of(b->d, signal);
+    REQUIRE(n == (size_t)ps.layout.limbs * b->lanes, RRTL_E_ARG,
+            "E_GPU_LANE_VALUES: expected " + std::to_string((size_t)ps.layout.limbs * b->lanes) + " values, got " + std::to_string(n));
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      std::vector<uint32_t> words(b->words, 0);
+      for (uint32_t l = 0; l < b->lanes; ++l)
+        if (data[l] & 1u) words[l / 32] |= 1u << (l % 32);
+      gate_set_bits(b, signal, words.data());
+    } else {
+      uint32_t limbs = ps.layout.limbs;
+      std::vector<uint32_t> rows((size_t)limbs * b->lanes_pad, 0);
+      for (uint32_t k = 0; k < limbs; ++k)
+        for (uint32_t l = 0; l < b->lanes; ++l) {
+          uint32_t v = data[(size_t)k * b->lanes + l];
+          if (k + 1 == limbs) v &= final_limb_mask(ps.layout.width);
+          rows[(size_t)k * b->lanes_pad + l] = v;
+        }
+      cuda_check(cudaMemcpyAsync(b->d_values.as<uint32_t>() + (size_t)ps.layout.offset * b->lanes_pad, rows.data(),
+                                 rows.size() * 4, cudaMemcpyHostToDevice, b->d->ctx->stream),
+                 "h2d signal");
+      cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+    }
+  });
+}
+
+rrtl_status rrtl_batch_get_signal_limbs(rrtl_batch* b, uint32_t signal, uint32_t* out, size_t n) {
+  return guard([&] {
+    REQUIRE(b && out, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedSignal& ps = signal_of(b->d, signal);
+    REQUIRE(n == (size_t)ps.layout.limbs * b->lanes, RRTL_E_ARG, "E_GPU_LANE_VALUES: output size mismatch");
+    check_err_word(b);
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      std::vector<uint32_t> words(b->words);
+      gate_get_bits(b, signal, words.data());
+      for (uint32_t l = 0; l < b->lanes; ++l) out[l] = (words[l / 32] >> (l % 32)) & 1u;
+    } else {
+      uint32_t limbs = ps.layout.limbs;
+      std::vector<uint32_t> rows((size_t)limbs * b->lanes_pad);
+      cuda_check(cudaMemcpyAsync(rows.data(), b->d_values.as<uint32_t>() + (size_t)ps.layout.offset * b->lanes_pad,
+                                 rows.size() * 4, cudaMemcpyDeviceToHost, b->d->ctx->stream),
+                 "d2h signal");
+      cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+      for (uint32_t k = 0; k < limbs; ++k)
+        for (uint32_t l = 0; l < b->lanes; ++l) {
+          uint32_t v = rows[(size_t)k * b->lanes_pad + l];
+          if (k + 1 == limbs) v &= final_limb_mask(ps.layout.width);
+          out[(size_t)k * b->lanes + l] = v;
+        }
+    }
+  });
+}
+
+rrtl_status rrtl_batch_set_input_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words, size_t n) {
+  return guard([&] {
+    REQUIRE(b && words, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedSignal& ps = signal_of(b->d, signal);
+    REQUIRE(ps.layout.width == 1, RRTL_E_ARG, "E_GPU_WIDE_SIGNAL: bit-packed access needs a 1-bit signal");
+    REQUIRE(n == (b->lanes + 31) / 32, RRTL_E_ARG, "E_GPU_LANE_VALUES: expected ceil(lanes/32) words");
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      gate_set_bits(b, signal, words);
+    } else {
+      std::vector<uint32_t> v(b->lanes);
+      for (uint32_t l = 0; l < b->lanes; ++l) v[l] = (words[l / 32] >> (l % 32)) & 1u;
+      rrtl_status st = rrtl_batch_set_input_limbs(b, signal, v.data(), v.size());
+      if (st) fail(st, g_last_error);
+    }
+  });
+}
+
+rrtl_status rrtl_batch_get_signal_bits(rrtl_batch* b, uint32_t signal, uint32_t* out, size_t n) {
+  return guard([&] {
+    REQUIRE(b && out, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedSignal& ps = signal_of(b->d, signal);
+    REQUIRE(ps.layout.width == 1, RRTL_E_ARG, "E_GPU_WIDE_SIGNAL: bit-packed access needs a 1-bit signal");
+    REQUIRE(n == (b->lanes + 31) / 32, RRTL_E_ARG, "E_GPU_LANE_VALUES: expected ceil(lanes/32) words");
+    check_err_word(b);
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      gate_get_bits(b, signal, out);
+    } else {
+      std::vector<uint32_t> v(b->lanes);
+      rrtl_status st = rrtl_batch_get_signal_limbs(b, signal, v.data(), v.size());
+      if (st) fail(st, g_last_error);
+      memset(out, 0, n * 4);
+      for (uint32_t l = 0; l < b->lanes; ++l) out[l / 32] |= (v[l] & 1u) << (l % 32);
+    }
+  });
+}
+
+rrtl_status rrtl_batch_set_memory_limbs(rrtl_batch* b, uint32_t memory, const uint32_t* data, size_t n) {
+  return guard([&] {
+    REQUIRE(b && data, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const auto& M = b->d->mp.source.memories;
+    REQUIRE(memory < M.size(), RRTL_E_SIGNAL, "E_GPU_MEMORY: memory index out of range");
+    REQUIRE(b->d->engine == RRTL_ENGINE_WORD, RRTL_E_UNSUPPORTED, "E_GPU_MEMORY: engine has no memories");
+    const PackedMemory& m = M[memory];
+    uint32_t limbs = m.data_layout.limbs;
+    size_t words = (size_t)m.depth * limbs;
+    REQUIRE(n == words * b->lanes, RRTL_E_ARG, "E_GPU_MEMORY_VALUES: expected depth*limbs*lanes values");
+    std::vector<uint32_t> rows(words * b->lanes_pad, 0);
+    for (size_t wv = 0; wv < words; ++wv)
+      for (uint32_t l = 0; l < b->lanes; ++l) {
+        uint32_t v = data[wv * b->lanes + l];
+        if (wv % limbs == limbs - 1) v &= final_limb_mask(m.data_layout.width);
+        rows[wv * b->lanes_pad + l] = v;
+      }
+    cuda_check(cudaMemcpyAsync(b->d_mem.as<uint32_t>() + (size_t)m.offset * b->lanes_pad, rows.data(), rows.size() * 4,
+                               cudaMemcpyHostToDevice, b->d->ctx->stream),
+               "h2d memory");
+    cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+  });
+}
+
+rrtl_status rrtl_batch_get_memory_limbs(rrtl_batch* b, uint32_t memory, uint32_t* out, size_t n) {
+  return guard([&] {
+    REQUIRE(b && out, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const auto& M = b->d->mp.source.memories;
+    REQUIRE(memory < M.size(), RRTL_E_SIGNAL, "E_GPU_MEMORY: memory index out of range");
+    REQUIRE(b->d->engine == RRTL_ENGINE_WORD, RRTL_E_UNSUPPORTED, "E_GPU_MEMORY: engine has no memories");
+    const PackedMemory& m = M[memory];
+    uint32_t limbs = m.data_layout.limbs;
+    size_t words = (size_t)m.depth * limbs;
+    REQUIRE(n == words * b->lanes, RRTL_E_ARG, "E_GPU_MEMORY_VALUES: expected depth*limbs*lanes values");
+    check_err_word(b);
+    std::vector<uint32_t> rows(words * b->lanes_pad);
+    cuda_check(cudaMemcpyAsync(rows.data(), b->d_mem.as<uint32_t>() + (size_t)m.offset * b->lanes_pad, rows.size() * 4,
+                               cudaMemcpyDeviceToHost, b->d->ctx->stream),
+               "d2h memory");
+    cuda_check(cudaStreamSynchronize(b->d->ctx->stream), "sync");
+    for (size_t wv = 0; wv < words; ++wv)
+      for (uint32_t l = 0; l < b->lanes; ++l) {
+        uint32_t v = rows[wv * b->lanes_pad + l];
+        if (wv % limbs == limbs - 1) v &= final_limb_mask(m.data_layout.width);
+        out[wv * b->lanes + l] = v;
+      }
+  });
+}
+
+rrtl_status rrtl_batch_eval(rrtl_batch* b) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    batch_eval(b);
+  });
+}
+
+rrtl_status rrtl_batch_tick(rrtl_batch* b) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    batch_tick_many(b, 1, true);
+  });
+}
+
+rrtl_status rrtl_batch_tick_many(rrtl_batch* b, uint64_t steps) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    REQUIRE(steps < (1ull << 32), RRTL_E_ARG, "E_GPU_STEPS: tick_many step count exceeds 2^32");
+    if (steps == 0) return;
+    batch_tick_many(b, steps, false);
+  });
+}
+
+rrtl_status rrtl_batch_synchronize(rrtl_batch* b) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    check_err_word(b);
+    cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  });
+}
+
+rrtl_status rrtl_batch_run(rrtl_batch* b, const rrtl_run* run) {
+  return guard([&] {
+    REQUIRE(b && run, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    REQUIRE(run->n_stim == 0 || run->stim, RRTL_E_ARG, "E_ARG: stim is null");
+    REQUIRE(run->n_record == 0 || run->record, RRTL_E_ARG, "E_ARG: record is null");
+    if (b->d->engine == RRTL_ENGINE_GATE) gate_run(b, *run, false);
+    else word_run(b, *run, false, false, true);
+  });
+}
+
+rrtl_status rrtl_batch_run_device(rrtl_batch* b, const rrtl_run* run) {
+  return guard([&] {
+    REQUIRE(b && run, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    REQUIRE(run->n_stim == 0 || run->stim, RRTL_E_ARG, "E_ARG: stim is null");
+    REQUIRE(run->n_record == 0 || run->record, RRTL_E_ARG, "E_ARG: record is null");
+    if (b->d->engine == RRTL_ENGINE_GATE) gate_run(b, *run, true);
+    else word_run(b, *run, true, false, true);
+  });
+}
+
+rrtl_status rrtl_batch_set_faults(rrtl_batch* b, const rrtl_fault* faults, size_t n) {
+  return guard([&] {
+    REQUIRE(b && (faults || n == 0), RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    REQUIRE(b->d->engine == RRTL_ENGINE_GATE, RRTL_E_UNSUPPORTED, "E_FAULT: fault injection needs the gate engine");
+    const GateProgram& gp = b->d->gp;
+    for (size_t i = 0; i < n; ++i) {
+      const rrtl_fault& f = faults[i];
+      REQUIRE(f.lane < b->lanes, RRTL_E_ARG, "E_FAULT_LANE: lane out of range");
+      REQUIRE(f.lane % 32 != 0, RRTL_E_ARG, "E_FAULT_LANE: lane 0 of each 32-lane word is the fault-free reference");
+      const PackedSignal& ps = signal_of(b->d, f.signal);
+      REQUIRE(ps.kind != PSK::Input, RRTL_E_ARG, "E_FAULT_NET: stuck-at faults go on wires, outputs or registers");
+      uint32_t net = gp.signal_net[f.signal];
+      REQUIRE(!gp.net_is_source[net] || ps.kind == PSK::Reg, RRTL_E_ARG, "E_FAULT_NET: undriven signal");
+      REQUIRE(f.value <= 1, RRTL_E_ARG, "E_FAULT: stuck-at value must be 0 or 1");
+    }
+    b->faults.assign(faults, faults + n);
+    build_forces(b);
+  });
+}
+
+rrtl_status rrtl_batch_snapshot(rrtl_batch* b, uint32_t* values, size_t nv, uint32_t* memories, size_t nm) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedProgram& P = b->d->mp.source;
+    REQUIRE(nv == (size_t)P.total_signal_words * b->lanes, RRTL_E_ARG, "E_SIM_IR_STORAGE_VALUES: size mismatch");
+    REQUIRE(nm == (size_t)P.total_memory_words_per_lane * b->lanes, RRTL_E_ARG, "E_SIM_IR_STORAGE_MEMORIES: size mismatch");
+    check_err_word(b);
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      std::vector<uint32_t> words(b->words);
+      for (uint32_t s = 0; s < P.signals.size(); ++s) {
+        gate_get_bits(b, s, words.data());
+        for (uint32_t l = 0; l < b->lanes; ++l) values[(size_t)P.signals[s].layout.offset * b->lanes + l] = (words[l / 32] >> (l % 32)) & 1u;
+      }
+    } else {
+      std::vector<uint32_t> rows((size_t)P.total_signal_words * b->lanes_pad);
+      cuda_check(cudaMemcpy(rows.data(), b->d_values.p, rows.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+      for (size_t wv = 0; wv < P.total_signal_words; ++wv)
+        for (uint32_t l = 0; l < b->lanes; ++l) values[wv * b->lanes + l] = rows[wv * b->lanes_pad + l];
+      if (nm) {
+        std::vector<uint32_t> mrows((size_t)P.total_memory_words_per_lane * b->lanes_pad);
+        cuda_check(cudaMemcpy(mrows.data(), b->d_mem.p, mrows.size() * 4, cudaMemcpyDeviceToHost), "d2h");
+        for (size_t wv = 0; wv < P.total_memory_words_per_lane; ++wv)
+          for (uint32_t l = 0; l < b->lanes; ++l)
+            memories[(size_t)l * P.total_memory_words_per_lane + wv] = mrows[wv * b->lanes_pad + l];
+      }
+    }
+  });
+}
+
+rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv, const uint32_t* memories, size_t nm) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const PackedProgram& P = b->d->mp.source;
+    REQUIRE(nv == (size_t)P.total_signal_words * b->lanes, RRTL_E_ARG, "E_SIM_IR_STORAGE_VALUES: size mismatch");
+    REQUIRE(nm == (size_t)P.total_memory_words_per_lane * b->lanes, RRTL_E_ARG, "E_SIM_IR_STORAGE_MEMORIES: size mismatch");
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      std::vector<uint32_t> words(b->words);
+      for (uint32_t s = 0; s < P.signals.size(); ++s) {
+        std::fill(words.begin(), words.end(), 0u);
+        for (uint32_t l = 0; l < b->lanes; ++l)
+          if (values[(size_t)P.signals[s].layout.offset * b->lanes + l] & 1u) words[l / 32] |= 1u << (l % 32);
+        gate_set_bits(b, s, words.data());
+      }
+    } else {
+      std::vector<uint32_t> rows((size_t)P.total_signal_words * b->lanes_pad, 0);
+      for (size_t wv = 0; wv < P.total_signal_words; ++wv)
+        for (uint32_t l = 0; l < b->lanes; ++l) rows[wv * b->lanes_pad + l] = values[wv * b->lanes + l];
+      cuda_check(cudaMemcpy(b->d_values.p, rows.data(), rows.size() * 4, cudaMemcpyHostToDevice), "h2d");
+      if (nm) {
+        std::vector<uint32_t> mrows((size_t)P.total_memory_words_per_lane * b->lanes_pad, 0);
+        for (size_t wv = 0; wv < P.total_memory_words_per_lane; ++wv)
+          for (uint32_t l = 0; l < b->lanes; ++l)
+            mrows[wv * b->lanes_pad + l] = memories[(size_t)l * P.total_memory_words_per_lane + wv];
+        cuda_check(cudaMemcpy(b->d_mem.p, mrows.data(), mrows.size() * 4, cudaMemcpyHostToDevice), "h2d");
+      }
+    }
+  });
+}
+
+rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(path == RRTL_PATH_FUSED || path == RRTL_PATH_PLAIN, RRTL_E_ARG, "E_ARG: unknown path");
+    b->path = path;
+  });
+}
+
+rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms) {
+  return guard([&] {
+    REQUIRE(b && ms, RRTL_E_ARG, "E_ARG: null argument");
+    *ms = b->last_ms;
+  });
+}
+
+}  // extern "C"

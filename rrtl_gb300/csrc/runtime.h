@@ -1,0 +1,94 @@
+// Host runtime objects behind the C ABI (include/rrtl_cuda.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/rrtl_cuda.h"
+#include "gate_dev.h"
+#include "gateprog.h"
+#include "lower.h"
+#include "word_dev.h"
+#include "wordprog.h"
+
+namespace rrtl {
+
+struct ApiError {
+  rrtl_status status;
+  std::string msg;
+};
+
+[[noreturn]] inline void fail(rrtl_status st, const std::string& msg) { throw ApiError{st, msg}; }
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Device buffer owned by the library (grow-only when used as scratch).
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf();
+  void reserve(size_t n);
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <class T>
+void upload(DevBuf& b, const std::vector<T>& v) {
+  b.reserve(std::max<size_t>(v.size() * sizeof(T), 16));
+  if (!v.empty()) cuda_check(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+}
+
+}  // namespace rrtl
+
+struct rrtl_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t sm_count = 0;
+  size_t max_smem = 0;
+};
+
+struct rrtl_design {
+  rrtl_ctx* ctx = nullptr;
+  rrtl::Design design;
+  std::string top;
+  rrtl::MachineProgram mp;
+  uint32_t engine = 0;
+  // gate engine
+  rrtl::GateProgram gp;
+  std::vector<uint8_t> end_live;  // net is resident at the end of a cycle (recordable on the fused path)
+  rrtl::GateProgDev gdev{};
+  bool fused_ok = false;
+  size_t fused_smem = 0;
+  rrtl::DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
+  // word engine
+  rrtl::WordProgram wp;
+  rrtl::WordProgDev wdev{};
+  rrtl::DevBuf d_wcode, d_wcap, d_wlit;
+};
+
+struct rrtl_batch {
+  rrtl_design* d = nullptr;
+  uint32_t lanes = 0;
+  uint32_t path = RRTL_PATH_FUSED;
+  float last_ms = 0.f;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  rrtl::DevBuf d_err;
+  // gate engine state
+  uint32_t words = 0, words_pad = 0, n_tiles = 0, rows = 0;
+  rrtl::DevBuf d_nets;
+  std::vector<rrtl_fault> faults;
+  rrtl::DevBuf d_force_off, d_forces;
+  bool has_forces = false;
+  // word engine state
+  uint32_t lanes_pad = 0;
+  rrtl::DevBuf d_values, d_mem, d_caps;
+  // per-run scratch
+  rrtl::DevBuf d_stim, d_rec, d_in_trace, d_out_trace, d_hash, d_detect;
+};

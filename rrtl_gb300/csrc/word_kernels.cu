@@ -1,0 +1,215 @@
+// Lane-per-thread word kernel for sm_103a (general designs: multi-bit values,
+// memories, asynchronous resets). One thread simulates one lane through the
+// whole run; lanes never communicate, so the kernel has no barriers. Signals
+// and memories are word-major [word][lane] in HBM, so the 32 lanes of a warp
+// touch one contiguous 128-byte line per access. Value slots of the current
+// block live in shared memory ([slot][thread], conflict-free) or, when a
+// design needs more slots than fit, in a spill array in HBM.
+//
+// Operation semantics follow eval_machine_instr_lane and its limb helpers
+// (crates/rrtl-sim-ir/src/lib.rs:9796-9907, 12942-13196) specialised to
+// values of at most 64 bits: every result is masked to its width.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rrtl_cuda.h"
+#include "stim.h"
+#include "word_dev.h"
+
+namespace rrtl {
+
+__device__ __forceinline__ unsigned long long wmask(uint32_t w) { return w >= 64u ? ~0ull : ((1ull << w) - 1ull); }
+
+struct WordLane {
+  const WordProgDev& P;
+  const WordRunDev& R;
+  unsigned long long* vbase;
+  uint32_t vstride;
+  uint32_t lane;
+  size_t LP;
+
+  __device__ unsigned long long& V(uint32_t s) const { return vbase[(size_t)s * vstride]; }
+
+  __device__ unsigned long long load_sig(uint32_t off, bool two) const {
+    unsigned long long v = R.values[(size_t)off * LP + lane];
+    if (two) v |= (unsigned long long)R.values[(size_t)(off + 1) * LP + lane] << 32;
+    return v;
+  }
+  __device__ void store_sig(uint32_t off, bool two, unsigned long long v) const {
+    R.values[(size_t)off * LP + lane] = (uint32_t)v;
+    if (two) R.values[(size_t)(off + 1) * LP + lane] = (uint32_t)(v >> 32);
+  }
+  __device__ bool reset_asserted(uint32_t off, bool active_low) const {
+    bool b = R.values[(size_t)off * LP + lane] & 1u;
+    return active_low ? !b : b;
+  }
+
+  __device__ void run(uint32_t b, uint32_t e) const {
+    for (uint32_t pc = b; pc < e; ++pc) {
+      const WInstr I = P.code[pc];
+      const unsigned long long m = wmask(I.width);
+      unsigned long long r = 0;
+      switch (I.op) {
+        case W_LIT: r = __ldg(P.lits + I.aux) & m; break;
+        case W_SIG: r = load_sig(I.aux, I.flags & 1) & m; break;
+        case W_NOT: r = ~V(I.a) & m; break;
+        case W_AND: r = (V(I.a) & V(I.b)) & m; break;
+        case W_OR: r = (V(I.a) | V(I.b)) & m; break;
+        case W_XOR: r = (V(I.a) ^ V(I.b)) & m; break;
+        case W_ADD: r = (V(I.a) + V(I.b)) & m; break;
+        case W_SUB: r = (V(I.a) - V(I.b)) & m; break;
+        case W_MUL: r = (V(I.a) * V(I.b)) & m; break;
+        case W_EQ: r = V(I.a) == V(I.b); break;
+        case W_NE: r = V(I.a) != V(I.b); break;
+        case W_LT: {
+          unsigned long long om = wmask(I.aux);
+          r = (V(I.a) & om) < (V(I.b) & om);
+          break;
+        }
+        case W_LTS: {
+          unsigned long long om = wmask(I.aux);
+          unsigned long long x = V(I.a) & om, y = V(I.b) & om;
+          unsigned long long sb = 1ull << (I.aux - 1u);
+          bool xs = x & sb, ys = y & sb;
+          r = (xs != ys) ? (unsigned long long)xs : (unsigned long long)(x < y);
+          break;
+        }
+        case W_MUX: r = ((V(I.a) & 1ull) ? V(I.b) : V(I.c)) & m; break;
+        case W_SLICE: r = I.aux >= 64u ? 0ull : ((V(I.a) >> I.aux) & m); break;
+        case W_MASK: r = V(I.a) & m; break;
+        case W_SEXT: {
+          unsigned long long x = V(I.a) & wmask(I.aux);
+          bool s = (x >> (I.aux - 1u)) & 1ull;
+          r = (s ? (x | ~wmask(I.aux)) : x) & m;
+          break;
+        }
+        case W_CAT: r = ((I.aux >= 64u ? 0ull : (V(I.a) << I.aux)) | V(I.b)) & m; break;
+        case W_MEMRD: {
+          const WMemDev M = P.mems[I.aux];
+          unsigned long long addr = V(I.a);
+          if (addr < M.depth) {
+            size_t w0 = (size_t)M.offset + (size_t)addr * M.limbs;
+            r = R.mems[w0 * LP + lane];
+            if (M.limbs == 2) r |= (unsigned long long)R.mems[(w0 + 1) * LP + lane] << 32;
+            r &= wmask(M.width) & m;
+          }
+          break;
+        }
+        case W_STORE: store_sig(I.aux, I.flags & 1, V(I.a) & m); continue;
+        case W_ASTORE:
+          if (reset_asserted(I.aux2, I.flags & 4)) store_sig(I.aux, I.flags & 1, V(I.a) & m);
+          continue;
+        case W_CAPTURE: {
+          unsigned long long v = ((I.flags & 2) && reset_asserted(I.aux2, I.flags & 4)) ? __ldg(P.lits + I.aux3) : V(I.a);
+          v &= m;
+          R.caps[(size_t)I.aux * LP + lane] = (uint32_t)v;
+          if (I.flags & 1) R.caps[(size_t)(I.aux + 1) * LP + lane] = (uint32_t)(v >> 32);
+          continue;
+        }
+        case W_MEMWR: {
+          if (V(I.a) & 1ull) {
+            const WMemDev M = P.mems[I.aux];
+            unsigned long long addr = V(I.b);
+            if (addr < M.depth) {
+              unsigned long long v = V(I.c) & wmask(M.width);
+              size_t w0 = (size_t)M.offset + (size_t)addr * M.limbs;
+              R.mems[w0 * LP + lane] = (uint32_t)v;
+              if (M.limbs == 2) R.mems[(w0 + 1) * LP + lane] = (uint32_t)(v >> 32);
+            }
+          }
+          continue;
+        }
+        default: continue;
+      }
+      V(I.dst) = r;
+    }
+  }
+
+  __device__ void commit() const {
+    for (uint32_t k = 0; k < P.n_commits; ++k) {
+      const WCommitDev cm = P.commits[k];
+      for (uint32_t l = 0; l < cm.limbs; ++l)
+        R.values[(size_t)(cm.sig_off + l) * LP + lane] = R.caps[(size_t)(cm.cap_off + l) * LP + lane];
+    }
+  }
+};
+
+template <bool kSmem>
+__global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) {
+  extern __shared__ unsigned long long vsm[];
+  const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
+  WordLane W{P, R, kSmem ? vsm + threadIdx.x : R.vspill + lane, kSmem ? blockDim.x : R.lanes_pad, lane, R.lanes_pad};
+  const bool live = lane < R.lanes;
+  bool detected = false;
+  if (R.start_settle) {
+    W.run(P.comb_b, P.comb_e);
+    W.run(P.async_b, P.async_e);
+  }
+  for (unsigned long long c = 0; c < R.cycles; ++c) {
+    const unsigned long long ca = R.cycle_base + c;
+    for (uint32_t k = 0; k < R.n_stim; ++k) {
+      const WordStimDev s = R.stim[k];
+      if (s.kind == RRTL_STIM_HOLD) continue;
+      for (uint32_t l = 0; l < s.limbs; ++l) {
+        uint32_t v = 0;
+        if (s.kind == RRTL_STIM_RANDOM) v = stim_lane_limb(R.seed, s.param, ca, lane, s.width, l);
+        else if (s.kind == RRTL_STIM_PULSE) v = (l == 0 && ca < s.param) ? 1u : 0u;
+        else if (s.kind == RRTL_STIM_CONST) v = l < 2 ? (uint32_t)(s.param >> (32 * l)) : 0u;
+        else if (s.kind == RRTL_STIM_TRACE)
+          v = (l == 0 && live) ? R.in_trace[((size_t)c * R.n_trace_cols + s.param) * R.lanes + lane] : 0u;
+        if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
+        R.values[(size_t)(s.sig_off + l) * R.lanes_pad + lane] = v;
+      }
+    }
+    W.run(P.comb_b, P.comb_e);
+    W.run(P.async_b, P.async_e);
+    if (R.n_rec) {
+      unsigned long long h = 0ull;
+      bool diff = false;
+      for (uint32_t k = 0; k < R.n_rec; ++k) {
+        const WordRecDev rc = R.rec[k];
+        for (uint32_t l = 0; l < rc.limbs; ++l) {
+          uint32_t v = R.values[(size_t)(rc.sig_off + l) * R.lanes_pad + lane];
+          if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
+          if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
+          if (!live) continue;
+          if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
+          if (R.mode & RRTL_REC_HASH) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
+        }
+      }
+      if (R.mode & RRTL_REC_HASH) {
+        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
+        if ((threadIdx.x & 31u) == 0 && h) atomicAdd(R.out_hash + c, h);
+      }
+      if ((R.mode & RRTL_REC_DETECT) && live && diff && !detected) {
+        detected = true;
+        R.detect[lane] = (uint32_t)ca;
+      }
+    }
+    W.run(P.next_b, P.next_e);
+    W.run(P.commit_b, P.commit_e);
+    W.commit();
+  }
+  if (R.final_settle) {
+    W.run(P.comb_b, P.comb_e);
+    W.run(P.async_b, P.async_e);
+  }
+}
+
+cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st) {
+  const uint32_t threads = 128;
+  uint32_t grid = R.lanes_pad / threads;
+  if (smem_slots) {
+    size_t smem = (size_t)P.n_vslots * threads * 8u;
+    word_kernel<true><<<grid, threads, smem, st>>>(P, R);
+  } else {
+    word_kernel<false><<<grid, threads, 0, st>>>(P, R);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t word_prepare(size_t smem) {
+  return cudaFuncSetAttribute(word_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+}  // namespace rrtl

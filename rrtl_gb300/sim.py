@@ -1,0 +1,458 @@
+"""Python mirror of the reference's batch simulator API over the C ABI.
+
+`GpuBatchSimulator` follows `rrtl_gpu_sim::GpuBatchSimulator`
+(crates/rrtl-gpu-sim/src/lib.rs:458-1512): compile once, set inputs per lane,
+tick / tick_many, read signals, memories and snapshots. Every call goes
+through librrtl_gb300.so (include/rrtl_cuda.h); there is no CPU fallback, and
+loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, byref, c_char_p, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
+from typing import Iterable, Optional, Sequence, Union
+
+import numpy as np
+
+from . import builder as _b
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "librrtl_gb300.so")
+
+STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE = 0, 1, 2, 3, 4
+REC_TRACE, REC_HASH, REC_DETECT = 1, 2, 4
+PATH_FUSED, PATH_PLAIN = 0, 1
+ENGINE_GATE, ENGINE_WORD = 1, 2
+
+_STATUS = {
+    1: "RRTL_E_ARG",
+    2: "RRTL_E_DESIGN",
+    3: "RRTL_E_SIGNAL",
+    4: "RRTL_E_DEVICE",
+    5: "RRTL_E_OOM",
+    6: "RRTL_E_TIMEOUT",
+    7: "RRTL_E_UNSUPPORTED",
+    8: "RRTL_E_LANES",
+}
+
+
+class RrtlError(RuntimeError):
+    """A failed C-ABI call: `status` is the rrtl_status, `code` the diagnostic code."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        self.code = message.split(":", 1)[0] if ":" in message else message
+        super().__init__(f"{_STATUS.get(status, status)}: {message}")
+
+
+class Stim(ctypes.Structure):
+    _fields_ = [("signal", c_uint32), ("kind", c_uint32), ("param", c_uint64)]
+
+
+class Run(ctypes.Structure):
+    _fields_ = [
+        ("cycles", c_uint64),
+        ("seed", c_uint64),
+        ("n_stim", c_uint32),
+        ("stim", POINTER(Stim)),
+        ("n_record", c_uint32),
+        ("record", POINTER(c_uint32)),
+        ("record_mode", c_uint32),
+        ("n_trace_cols", c_uint32),
+        ("input_trace", POINTER(c_uint32)),
+        ("out_trace", POINTER(c_uint32)),
+        ("out_hash", POINTER(c_uint64)),
+        ("detect", POINTER(c_uint32)),
+    ]
+
+
+class Fault(ctypes.Structure):
+    _fields_ = [("lane", c_uint32), ("signal", c_uint32), ("value", c_uint32)]
+
+
+class DesignInfo(ctypes.Structure):
+    _fields_ = [
+        ("n_signals", c_uint32),
+        ("n_memories", c_uint32),
+        ("total_signal_words", c_uint64),
+        ("total_memory_words_per_lane", c_uint64),
+        ("engine", c_uint32),
+        ("n_gates", c_uint32),
+        ("n_levels", c_uint32),
+        ("n_nets", c_uint32),
+        ("n_slots", c_uint32),
+        ("n_regs", c_uint32),
+        ("source_instrs", c_uint64),
+    ]
+
+
+# Exported C-ABI symbols, as declared in include/rrtl_cuda.h.
+EXPORTS = (
+    "rrtl_last_error",
+    "rrtl_ctx_create",
+    "rrtl_ctx_destroy",
+    "rrtl_ctx_sm_count",
+    "rrtl_design_load_json",
+    "rrtl_design_destroy",
+    "rrtl_design_info_get",
+    "rrtl_design_signal",
+    "rrtl_design_memory",
+    "rrtl_batch_create",
+    "rrtl_batch_destroy",
+    "rrtl_batch_lanes",
+    "rrtl_batch_set_input_limbs",
+    "rrtl_batch_get_signal_limbs",
+    "rrtl_batch_set_input_bits",
+    "rrtl_batch_get_signal_bits",
+    "rrtl_batch_set_memory_limbs",
+    "rrtl_batch_get_memory_limbs",
+    "rrtl_batch_eval",
+    "rrtl_batch_tick",
+    "rrtl_batch_tick_many",
+    "rrtl_batch_synchronize",
+    "rrtl_batch_run",
+    "rrtl_batch_run_device",
+    "rrtl_batch_set_faults",
+    "rrtl_batch_snapshot",
+    "rrtl_batch_restore",
+    "rrtl_batch_set_path",
+    "rrtl_batch_last_kernel_ms",
+)
+
+_lib = None
+
+
+def lib():
+    """Load librrtl_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run rrtl_gb300.build.build() first")
+    L = ctypes.CDLL(LIB_PATH)
+    L.rrtl_last_error.restype = c_char_p
+    P = POINTER
+    sigs = {
+        "rrtl_ctx_create": [c_int32, P(c_void_p)],
+        "rrtl_ctx_destroy": [c_void_p],
+        "rrtl_ctx_sm_count": [c_void_p, P(c_uint32)],
+        "rrtl_design_load_json": [c_void_p, c_char_p, c_size_t, c_char_p, P(c_void_p)],
+        "rrtl_design_destroy": [c_void_p],
+        "rrtl_design_info_get": [c_void_p, P(DesignInfo)],
+        "rrtl_design_signal": [c_void_p, c_char_p, P(c_uint32), P(c_uint32), P(c_uint32)],
+        "rrtl_design_memory": [c_void_p, c_char_p, P(c_uint32), P(c_uint64), P(c_uint32)],
+        "rrtl_batch_create": [c_void_p, c_uint32, P(c_void_p)],
+        "rrtl_batch_destroy": [c_void_p],
+        "rrtl_batch_lanes": [c_void_p, P(c_uint32)],
+        "rrtl_batch_set_input_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_get_signal_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_set_input_bits": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_get_signal_bits": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_set_memory_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_get_memory_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_eval": [c_void_p],
+        "rrtl_batch_tick": [c_void_p],
+        "rrtl_batch_tick_many": [c_void_p, c_uint64],
+        "rrtl_batch_synchronize": [c_void_p],
+        "rrtl_batch_run": [c_void_p, P(Run)],
+        "rrtl_batch_run_device": [c_void_p, P(Run)],
+        "rrtl_batch_set_faults": [c_void_p, P(Fault), c_size_t],
+        "rrtl_batch_snapshot": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
+        "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
+        "rrtl_batch_set_path": [c_void_p, c_uint32],
+        "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
+    }
+    for name, args in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = c_int32
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        raise RrtlError(status, lib().rrtl_last_error().decode())
+
+
+def _u32p(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_uint32))
+
+
+class Context:
+    """One device plus its stream (rrtl_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.h = c_void_p()
+        check(lib().rrtl_ctx_create(device, byref(self.h)))
+
+    @property
+    def sm_count(self) -> int:
+        n = c_uint32()
+        check(lib().rrtl_ctx_sm_count(self.h, byref(n)))
+        return n.value
+
+    def close(self):
+        if self.h:
+            lib().rrtl_ctx_destroy(self.h)
+            self.h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Optional[Context] = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class CompiledDesign:
+    """A design compiled and uploaded once (rrtl_design)."""
+
+    def __init__(self, design: Union[_b.Design, str], top: str, ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        text = design.to_json() if isinstance(design, _b.Design) else design
+        raw = text.encode()
+        self.h = c_void_p()
+        check(lib().rrtl_design_load_json(self.ctx.h, raw, len(raw), top.encode(), byref(self.h)))
+        self.top = top
+        self._cache = {}
+
+    @property
+    def info(self) -> DesignInfo:
+        i = DesignInfo()
+        check(lib().rrtl_design_info_get(self.h, byref(i)))
+        return i
+
+    def signal(self, name: str):
+        """(index, width, kind) of a signal by name."""
+        if name in self._cache:
+            return self._cache[name]
+        idx, w, k = c_uint32(), c_uint32(), c_uint32()
+        check(lib().rrtl_design_signal(self.h, name.encode(), byref(idx), byref(w), byref(k)))
+        self._cache[name] = (idx.value, w.value, k.value)
+        return self._cache[name]
+
+    def memory(self, name: str):
+        idx, depth, w = c_uint32(), c_uint64(), c_uint32()
+        check(lib().rrtl_design_memory(self.h, name.encode(), byref(idx), byref(depth), byref(w)))
+        return idx.value, depth.value, w.value
+
+    def close(self):
+        if self.h:
+            lib().rrtl_design_destroy(self.h)
+            self.h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+SignalRef = Union[str, int, "_b.Signal"]
+
+
+class GpuBatchSimulator:
+    """`lanes` independent instances of one compiled design on the GPU."""
+
+    def __init__(self, design: Union[CompiledDesign, _b.Design, str], top: Optional[str] = None, lanes: int = 1,
+                 ctx: Optional[Context] = None):
+        if not isinstance(design, CompiledDesign):
+            design = CompiledDesign(design, top, ctx)
+        self.design = design
+        self._names = design._builder_names if hasattr(design, "_builder_names") else None
+        self.h = c_void_p()
+        check(lib().rrtl_batch_create(design.h, lanes, byref(self.h)))
+        self.lanes = lanes
+        self._keep = None
+
+    # -- signal addressing
+    def _sig(self, s: SignalRef):
+        if isinstance(s, int):
+            return s
+        if isinstance(s, str):
+            return self.design.signal(s)[0]
+        raise TypeError("signals are addressed by name or packed index")
+
+    def _limbs(self, idx: int) -> int:
+        return None
+
+    def signal_width(self, s: SignalRef) -> int:
+        if isinstance(s, str):
+            return self.design.signal(s)[1]
+        raise TypeError("use a name")
+
+    # -- I/O (crates/rrtl-gpu-sim/src/lib.rs:820-951)
+    def set_input(self, s: SignalRef, lane_values: Sequence[int]):
+        name = s
+        w = self.design.signal(name)[1] if isinstance(name, str) else 32
+        if w > 32:
+            raise RrtlError(1, "E_GPU_WIDE_SIGNAL: use set_input_limbs for signals wider than 32 bits")
+        a = np.ascontiguousarray(np.asarray(lane_values, dtype=np.uint64).astype(np.uint32))
+        check(lib().rrtl_batch_set_input_limbs(self.h, self._sig(s), _u32p(a), a.size))
+
+    def set_input_limbs(self, s: SignalRef, limbs_by_lane: np.ndarray):
+        """limbs_by_lane: [limbs][lanes] uint32."""
+        a = np.ascontiguousarray(limbs_by_lane, dtype=np.uint32)
+        check(lib().rrtl_batch_set_input_limbs(self.h, self._sig(s), _u32p(a), a.size))
+
+    def get_signal_limbs(self, s: SignalRef) -> np.ndarray:
+        name = s
+        w = self.design.signal(name)[1] if isinstance(name, str) else None
+        if w is None:
+            raise TypeError("use a name")
+        limbs = max(1, (w + 31) // 32)
+        out = np.zeros((limbs, self.lanes), dtype=np.uint32)
+        check(lib().rrtl_batch_get_signal_limbs(self.h, self._sig(s), _u32p(out), out.size))
+        return out
+
+    def get_signal(self, s: SignalRef) -> np.ndarray:
+        if isinstance(s, str) and self.design.signal(s)[1] > 32:
+            raise RrtlError(1, "E_GPU_WIDE_SIGNAL: use get_signal_limbs for signals wider than 32 bits")
+        return self.get_signal_limbs(s)[0]
+
+    def set_input_bits(self, s: SignalRef, words: np.ndarray):
+        a = np.ascontiguousarray(words, dtype=np.uint32)
+        check(lib().rrtl_batch_set_input_bits(self.h, self._sig(s), _u32p(a), a.size))
+
+    def get_signal_bits(self, s: SignalRef) -> np.ndarray:
+        out = np.zeros((self.lanes + 31) // 32, dtype=np.uint32)
+        check(lib().rrtl_batch_get_signal_bits(self.h, self._sig(s), _u32p(out), out.size))
+        return out
+
+    def set_memory_limbs(self, mem: str, data: np.ndarray):
+        """data: [depth][limbs][lanes] uint32."""
+        idx = self.design.memory(mem)[0]
+        a = np.ascontiguousarray(data, dtype=np.uint32)
+        check(lib().rrtl_batch_set_memory_limbs(self.h, idx, _u32p(a), a.size))
+
+    def get_memory_limbs(self, mem: str) -> np.ndarray:
+        idx, depth, w = self.design.memory(mem)
+        limbs = max(1, (w + 31) // 32)
+        out = np.zeros((depth, limbs, self.lanes), dtype=np.uint32)
+        check(lib().rrtl_batch_get_memory_limbs(self.h, idx, _u32p(out), out.size))
+        return out
+
+    def set_memory(self, mem: str, lane_words: np.ndarray):
+        """lane_words: [lanes][depth] values (<= 32 bits)."""
+        a = np.asarray(lane_words, dtype=np.uint64)
+        data = np.ascontiguousarray(a.T.astype(np.uint32)[:, None, :])
+        self.set_memory_limbs(mem, data)
+
+    def get_memory(self, mem: str) -> np.ndarray:
+        return self.get_memory_limbs(mem)[:, 0, :].T.copy()
+
+    # -- stepping (crates/rrtl-gpu-sim/src/lib.rs:953-987)
+    def eval_combinational(self):
+        check(lib().rrtl_batch_eval(self.h))
+
+    def tick(self):
+        check(lib().rrtl_batch_tick(self.h))
+
+    def tick_many(self, steps: int):
+        check(lib().rrtl_batch_tick_many(self.h, steps))
+        self.synchronize()
+
+    def tick_many_async(self, steps: int):
+        check(lib().rrtl_batch_tick_many(self.h, steps))
+
+    def synchronize(self):
+        check(lib().rrtl_batch_synchronize(self.h))
+
+    def set_path(self, path: int):
+        check(lib().rrtl_batch_set_path(self.h, path))
+
+    @property
+    def last_kernel_ms(self) -> float:
+        f = c_float()
+        check(lib().rrtl_batch_last_kernel_ms(self.h, byref(f)))
+        return f.value
+
+    # -- per-cycle runs
+    def make_run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
+                 input_trace: Optional[np.ndarray] = None, out_trace=None, out_hash=None, detect=None) -> Run:
+        st = [(self._sig(s), k, p) for (s, k, p) in stim]
+        arr = (Stim * max(1, len(st)))(*[Stim(a, b, c) for a, b, c in st])
+        rec = np.asarray([self._sig(r) for r in record], dtype=np.uint32)
+        r = Run()
+        r.cycles = cycles
+        r.seed = seed
+        r.n_stim = len(st)
+        r.stim = ctypes.cast(arr, POINTER(Stim))
+        r.n_record = len(rec)
+        r.record = _u32p(rec) if len(rec) else None
+        r.record_mode = mode
+        if input_trace is not None:
+            input_trace = np.ascontiguousarray(input_trace, dtype=np.uint32)
+            r.n_trace_cols = input_trace.shape[1]
+            r.input_trace = _u32p(input_trace)
+        r.out_trace = _u32p(out_trace) if out_trace is not None else None
+        r.out_hash = out_hash.ctypes.data_as(POINTER(c_uint64)) if out_hash is not None else None
+        r.detect = _u32p(detect) if detect is not None else None
+        r._keep = (arr, rec, input_trace, out_trace, out_hash, detect)
+        return r
+
+    def run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
+            input_trace: Optional[np.ndarray] = None):
+        """Run `cycles` cycles; returns dict(trace=..., hash=..., detect=...) for the requested records."""
+        record = list(record)
+        engine = self.design.info.engine
+        words = (self.lanes + 31) // 32
+        out_trace = out_hash = detect = None
+        if mode & REC_TRACE:
+            if engine == ENGINE_GATE:
+                out_trace = np.zeros((cycles, len(record), words), dtype=np.uint32)
+            else:
+                limbs = sum(max(1, (self.design.signal(r)[1] + 31) // 32) for r in record)
+                out_trace = np.zeros((cycles, limbs, self.lanes), dtype=np.uint32)
+        if mode & REC_HASH:
+            out_hash = np.zeros(cycles, dtype=np.uint64)
+        if mode & REC_DETECT:
+            detect = np.zeros(self.lanes, dtype=np.uint32)
+        r = self.make_run(cycles, seed, stim, record, mode, input_trace, out_trace, out_hash, detect)
+        check(lib().rrtl_batch_run(self.h, byref(r)))
+        return {"trace": out_trace, "hash": out_hash, "detect": detect}
+
+    def set_faults(self, faults: Sequence[tuple]):
+        """faults: (lane, signal, value) triples; signal by name or index."""
+        arr = (Fault * max(1, len(faults)))(*[Fault(l, self._sig(s), v) for l, s, v in faults])
+        check(lib().rrtl_batch_set_faults(self.h, arr, len(faults)))
+
+    # -- snapshots (crates/rrtl-gpu-sim/src/lib.rs:1363-1408)
+    def snapshot_storage(self):
+        info = self.design.info
+        v = np.zeros(info.total_signal_words * self.lanes, dtype=np.uint32)
+        m = np.zeros(max(1, info.total_memory_words_per_lane * self.lanes), dtype=np.uint32)
+        check(lib().rrtl_batch_snapshot(self.h, _u32p(v), v.size, _u32p(m), info.total_memory_words_per_lane * self.lanes))
+        return v, m[: info.total_memory_words_per_lane * self.lanes]
+
+    def restore_storage(self, values: np.ndarray, memories: np.ndarray):
+        v = np.ascontiguousarray(values, dtype=np.uint32)
+        m = np.ascontiguousarray(memories, dtype=np.uint32)
+        if m.size == 0:
+            m = np.zeros(1, dtype=np.uint32)
+            nm = 0
+        else:
+            nm = m.size
+        check(lib().rrtl_batch_restore(self.h, _u32p(v), v.size, _u32p(m), nm))
+
+    def close(self):
+        if self.h:
+            lib().rrtl_batch_destroy(self.h)
+            self.h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,251 @@
+"""GPU parity of the bit-sliced gate engine against the bit-parallel oracle.
+
+Every comparison is bit-exact: per-cycle traces, per-cycle hashes, final
+register and wire state, first-detection cycles.
+"""
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from rrtl_gb300 import sim
+from rrtl_gb300.workloads import Rng, gate_netlist, netlist_run_spec
+
+from .helpers import crc32_netlist_json, oracle_bp_run
+
+pytestmark = pytest.mark.gpu
+
+
+def _crc_ref_states(din_fn, rst_fn, lanes, cycles):
+    """state[c] = crc register value seen before the clock edge of cycle c."""
+    st = np.zeros((cycles + 1, lanes), dtype=np.uint64)
+    for c in range(cycles):
+        for l in range(lanes):
+            if rst_fn(c):
+                st[c + 1, l] = 0xFFFFFFFF
+            else:
+                st[c + 1, l] = ob.crc_step(int(st[c, l]), din_fn(c, l))
+    return st
+
+
+@pytest.fixture(scope="module")
+def crc(engine):
+    d = crc32_netlist_json()
+    cd = sim.CompiledDesign(d, "crc32")
+    od = ob.OracleDesign(d.to_json(), "crc32")
+    return d, cd, od
+
+
+def _pack_lane_bits(bits_by_lane):
+    lanes = len(bits_by_lane)
+    words = np.zeros((lanes + 31) // 32, dtype=np.uint32)
+    for l, b in enumerate(bits_by_lane):
+        if b:
+            words[l // 32] |= np.uint32(1 << (l % 32))
+    return words
+
+
+@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN])
+def test_crc32_netlist_per_lane_din_matches_crc_step(crc, path):
+    """crates/rrtl-sim-ir/examples/netlist_crc32.rs:63-83: din = ((cyc + l) * 2654435761 >> 13) & 0xff."""
+    d, cd, od = crc
+    lanes, cycles = 256, 64
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g.set_path(path)
+    cols = ["rst"] + [f"din_{i}" for i in range(8)]
+    trace = np.zeros((cycles, len(cols), (lanes + 31) // 32), dtype=np.uint32)
+    for c in range(cycles):
+        trace[c, 0] = _pack_lane_bits([c < 1] * lanes)
+        for i in range(8):
+            trace[c, 1 + i] = _pack_lane_bits([(((c + l) * 2654435761 >> 13) & 0xFF) >> i & 1 for l in range(lanes)])
+    stim = [("clk", sim.STIM_CONST, 1)] + [(n, sim.STIM_TRACE, k) for k, n in enumerate(cols)]
+    rec = [f"crc_{i}" for i in range(32)]
+    out = g.run(cycles, stim=stim, record=rec, mode=sim.REC_TRACE, input_trace=trace)["trace"]
+    ref = _crc_ref_states(lambda c, l: ((c + l) * 2654435761 >> 13) & 0xFF, lambda c: c < 1, lanes, cycles)
+    got = np.zeros((cycles, lanes), dtype=np.uint64)
+    for i in range(32):
+        bits = (out[:, i, :, None] >> np.arange(32, dtype=np.uint32)) & 1
+        got |= bits.reshape(cycles, -1)[:, :lanes].astype(np.uint64) << np.uint64(i)
+    assert np.array_equal(got, ref[:cycles])
+    # the final settled state equals the state after the last edge
+    final = np.zeros(lanes, dtype=np.uint64)
+    for i in range(32):
+        final |= g.get_signal(f"crc_{i}").astype(np.uint64) << np.uint64(i)
+    assert np.array_equal(final, ref[cycles])
+
+
+def test_crc32_constant_din_200_cycles(crc):
+    """1,024 lanes, din = 0xAB, crc0 = 0xFFFFFFFF, 200 steps (crates/rrtl-sim-ir/examples/opencl_run.rs:54-74 shape)."""
+    d, cd, od = crc
+    g = sim.GpuBatchSimulator(cd, lanes=1024)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
+    stim += [(f"din_{i}", sim.STIM_CONST, (0xAB >> i) & 1) for i in range(8)]
+    g.run(201, stim=stim)
+    x = 0xFFFFFFFF
+    for _ in range(200):
+        x = ob.crc_step(x, 0xAB)
+    assert x == 0x53535102
+    vals = np.zeros(1024, dtype=np.uint64)
+    for i in range(32):
+        vals |= g.get_signal(f"crc_{i}").astype(np.uint64) << np.uint64(i)
+    assert np.all(vals == x)
+
+
+@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN])
+def test_crc32_fault_sim_coverage_and_latency(crc, path):
+    """Stuck-at-0/1 on every flop: 64/64 detected, latency min 1 / max 6 / mean 2.1
+    (crates/rrtl-sim-ir/examples/fault_sim.rs; docs/rrtl-optimizations.md:1411-1416)."""
+    d, cd, od = crc
+    regs = [i for i in range(od.num_signals) if od.kind(i) == 3]
+    faults = [(r, v) for r in regs for v in (0, 1)]
+    lanes_for = [l for l in range(96) if l % 32]  # lane 0 of each word stays fault-free
+    placed = [(lanes_for[f], sig, v) for f, (sig, v) in enumerate(faults)]
+    cycles = 96
+    trace = np.zeros((cycles, 9, 3), dtype=np.uint32)
+    for c in range(cycles):
+        din = (c * 2654435761 >> 13) & 0xFF
+        trace[c, 0] = 0xFFFFFFFF if c < 1 else 0
+        for i in range(8):
+            trace[c, 1 + i] = 0xFFFFFFFF if (din >> i) & 1 else 0
+    names = ["rst"] + [f"din_{i}" for i in range(8)]
+    g = sim.GpuBatchSimulator(cd, lanes=96)
+    g.set_path(path)
+    g.set_faults(placed)
+    stim = [("clk", sim.STIM_CONST, 1)] + [(n, sim.STIM_TRACE, k) for k, n in enumerate(names)]
+    rec = [f"crc_{i}" for i in range(32)]
+    res = g.run(cycles, stim=stim, record=rec, mode=sim.REC_DETECT | sim.REC_HASH, input_trace=trace)
+    det = res["detect"][[l for l, _, _ in placed]]
+    assert np.all(det != 0xFFFFFFFF)
+    # detection at cycle c means c edges have passed: the reference's latency
+    lat = det.astype(np.int64)
+    assert (lat.min(), lat.max()) == (1, 6)
+    assert round(lat.mean(), 1) == 2.1
+    # bit-exact against the oracle on the same protocol
+    stim_i = [(od.signal(n), k, p) for n, k, p in stim]
+    ref = oracle_bp_run(od, 96, cycles, 0, stim_i, [od.signal(r) for r in rec], 6,
+                        faults=[(l, s, v) for l, s, v in placed], input_trace=trace)
+    assert np.array_equal(res["detect"], ref["detect"])
+    assert np.array_equal(res["hash"], ref["hash"])
+
+
+@pytest.fixture(scope="module")
+def small_netlist(engine):
+    d, meta = gate_netlist(n_gates=3000, n_ff=160, n_pi=16, n_po=24, depth=12, seed=9)
+    js = d.to_json()
+    return d, meta, sim.CompiledDesign(js, meta.top), ob.OracleDesign(js, meta.top)
+
+
+@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN])
+@pytest.mark.parametrize("lanes", [1, 33, 300, 2048])
+def test_netlist_trace_and_hash_match_oracle(small_netlist, path, lanes):
+    d, meta, cd, od = small_netlist
+    cycles = 25
+    stim, rec = netlist_run_spec(meta)
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g.set_path(path)
+    res = g.run(cycles, seed=123, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
+    ref = oracle_bp_run(od, lanes, cycles, 123, [(od.signal(n), k, p) for n, k, p in stim],
+                        [od.signal(r) for r in rec], 3)
+    assert np.array_equal(res["trace"], ref["trace"])
+    assert np.array_equal(res["hash"], ref["hash"])
+    # final state of every register and every wire after the closing settle
+    ref["sim"].settle()
+    for name in meta.regs[:40] + meta.gate_names[::97] + meta.outputs:
+        assert np.array_equal(g.get_signal_bits(name), ref["sim"].get_bits(od.signal(name))), name
+
+
+def test_netlist_faults_match_oracle(small_netlist):
+    d, meta, cd, od = small_netlist
+    lanes, cycles = 500, 30
+    rng = Rng(77)
+    sites = meta.gate_names + meta.regs + meta.outputs
+    faults = [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]
+    stim, rec = netlist_run_spec(meta)
+    # lane-uniform stimulus: constant words per input, drawn per cycle
+    cols = [meta.rst] + meta.inputs
+    trace = np.zeros((cycles, len(cols), (lanes + 31) // 32), dtype=np.uint32)
+    for c in range(cycles):
+        for k in range(len(cols)):
+            bit = (c < 1) if k == 0 else rng.below(2)
+            trace[c, k] = 0xFFFFFFFF if bit else 0
+    stim = [(meta.clk, sim.STIM_CONST, 1)] + [(n, sim.STIM_TRACE, k) for k, n in enumerate(cols)]
+    for path in (sim.PATH_FUSED, sim.PATH_PLAIN):
+        g = sim.GpuBatchSimulator(cd, lanes=lanes)
+        g.set_path(path)
+        g.set_faults(faults)
+        res = g.run(cycles, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH | sim.REC_DETECT,
+                    input_trace=trace)
+        ref = oracle_bp_run(od, lanes, cycles, 0, [(od.signal(n), k, p) for n, k, p in stim],
+                            [od.signal(r) for r in rec], 7,
+                            faults=[(l, od.signal(s), v) for l, s, v in faults], input_trace=trace)
+        assert np.array_equal(res["trace"], ref["trace"])
+        assert np.array_equal(res["detect"], ref["detect"])
+        assert (res["detect"] != 0xFFFFFFFF).sum() > 0
+
+
+def test_tick_many_and_snapshot_match_oracle(small_netlist):
+    d, meta, cd, od = small_netlist
+    lanes = 200
+    rng = Rng(5)
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    bp = ob.BitParallel(od, lanes)
+    for name in [meta.clk] + meta.inputs:
+        bits = [rng.below(2) for _ in range(lanes)]
+        g.set_input(name, bits)
+        for l, b in enumerate(bits):
+            bp.set(od.signal(name), l, b)
+    g.set_input(meta.rst, [0] * lanes)
+    for _ in range(13):
+        bp.tick()
+    g.tick_many(13)
+    v, m = g.snapshot_storage()
+    for s in range(od.num_signals):
+        assert np.array_equal(v[s * lanes:(s + 1) * lanes], [bp.get(s, l) for l in range(lanes)]), s
+    # restore round trip
+    g2 = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g2.restore_storage(v, m)
+    v2, _ = g2.snapshot_storage()
+    assert np.array_equal(v, v2)
+
+
+def test_full_size_netlist_fused_equals_plain(engine):
+    """50k gates, 2,048 flops, depth 40: fused and plain paths agree on every
+    per-cycle hash and the final flop state (a size-independent check), and a
+    256-lane slice matches the oracle."""
+    d, meta = gate_netlist()
+    js = d.to_json()
+    cd = sim.CompiledDesign(js, meta.top)
+    info = cd.info
+    assert info.engine == sim.ENGINE_GATE and info.n_levels >= 40
+    stim, rec = netlist_run_spec(meta)
+    lanes, cycles = 8192, 20
+    out = {}
+    for path in (sim.PATH_FUSED, sim.PATH_PLAIN):
+        g = sim.GpuBatchSimulator(cd, lanes=lanes)
+        g.set_path(path)
+        res = g.run(cycles, seed=4, stim=stim, record=rec, mode=sim.REC_HASH)
+        out[path] = (res["hash"], [g.get_signal_bits(q) for q in meta.regs[::64]])
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+    od = ob.OracleDesign(js, meta.top)
+    g = sim.GpuBatchSimulator(cd, lanes=256)
+    res = g.run(cycles, seed=4, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
+    ref = oracle_bp_run(od, 256, cycles, 4, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec], 3)
+    assert np.array_equal(res["trace"], ref["trace"])
+    assert np.array_equal(res["hash"], ref["hash"])
+
+
+def test_error_codes(small_netlist):
+    d, meta, cd, od = small_netlist
+    with pytest.raises(sim.RrtlError) as e:
+        sim.GpuBatchSimulator(cd, lanes=0)
+    assert e.value.code == "E_GPU_LANES"
+    g = sim.GpuBatchSimulator(cd, lanes=64)
+    with pytest.raises(sim.RrtlError) as e:
+        g.set_faults([(32, meta.regs[0], 1)])
+    assert e.value.code == "E_FAULT_LANE"
+    with pytest.raises(sim.RrtlError) as e:
+        g.set_input(meta.inputs[0], [0] * 63)
+    assert e.value.code == "E_GPU_LANE_VALUES"
+    with pytest.raises(sim.RrtlError):
+        g.get_signal("no_such_signal")
