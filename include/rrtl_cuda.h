@@ -62,6 +62,13 @@ rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out);
 rrtl_status rrtl_ctx_destroy(rrtl_ctx* ctx);
 /* Number of streaming multiprocessors of the context's device. */
 rrtl_status rrtl_ctx_sm_count(rrtl_ctx* ctx, uint32_t* out);
+/* Device timing on the context stream (no reference counterpart; the Rust
+ * API times with wall clocks, crates/rrtl-gpu-sim/src/lib.rs:305-322).
+ * Records CUDA event `slot` (0..7) on the stream; elapsed_ms synchronises on
+ * event `b` and returns the time from event `a` to event `b`. */
+rrtl_status rrtl_ctx_event_record(rrtl_ctx* ctx, uint32_t slot);
+rrtl_status rrtl_ctx_event_elapsed(rrtl_ctx* ctx, uint32_t a, uint32_t b, float* ms);
+rrtl_status rrtl_ctx_synchronize(rrtl_ctx* ctx);
 
 /* ---- compiled design ---------------------------------------------------- */
 
@@ -112,6 +119,9 @@ rrtl_status rrtl_batch_get_signal_limbs(rrtl_batch* b, uint32_t signal, uint32_t
 /* Bit-packed forms for 1-bit signals: word w bit k is lane 32*w+k. n = ceil(lanes/32). */
 rrtl_status rrtl_batch_set_input_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words, size_t n);
 rrtl_status rrtl_batch_get_signal_bits(rrtl_batch* b, uint32_t signal, uint32_t* out, size_t n);
+
+/* Bit-packed values of several 1-bit signals at once: out is [n][ceil(lanes/32)]. */
+rrtl_status rrtl_batch_get_signals_bits(rrtl_batch* b, const uint32_t* signals, size_t n, uint32_t* out, size_t n_out);
 
 /* GpuBatchSimulator::set_memory_limbs / get_memory_limbs
  * (crates/rrtl-gpu-sim/src/lib.rs:903-951). Layout [addr][limb][lane]. */

@@ -507,6 +507,7 @@ rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out) {
       cuda_check(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
       c->sm_count = (uint32_t)sms;
       c->max_smem = (size_t)smem;
+      for (auto& e : c->events) cuda_check(cudaEventCreate(&e), "event");
     } catch (...) {
       delete c;
       throw;
@@ -519,6 +520,8 @@ rrtl_status rrtl_ctx_destroy(rrtl_ctx* ctx) {
   return guard([&] {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    for (auto& e : ctx->events)
+      if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
   });
@@ -528,6 +531,31 @@ rrtl_status rrtl_ctx_sm_count(rrtl_ctx* ctx, uint32_t* out) {
   return guard([&] {
     REQUIRE(ctx && out, RRTL_E_ARG, "E_ARG: null argument");
     *out = ctx->sm_count;
+  });
+}
+
+rrtl_status rrtl_ctx_event_record(rrtl_ctx* ctx, uint32_t slot) {
+  return guard([&] {
+    REQUIRE(ctx && slot < 8, RRTL_E_ARG, "E_ARG: bad event slot");
+    set_device(ctx);
+    cuda_check(cudaEventRecord(ctx->events[slot], ctx->stream), "cudaEventRecord");
+  });
+}
+
+rrtl_status rrtl_ctx_event_elapsed(rrtl_ctx* ctx, uint32_t a, uint32_t b, float* ms) {
+  return guard([&] {
+    REQUIRE(ctx && a < 8 && b < 8 && ms, RRTL_E_ARG, "E_ARG: bad event slot");
+    set_device(ctx);
+    cuda_check(cudaEventSynchronize(ctx->events[b]), "cudaEventSynchronize");
+    cuda_check(cudaEventElapsedTime(ms, ctx->events[a], ctx->events[b]), "cudaEventElapsedTime");
+  });
+}
+
+rrtl_status rrtl_ctx_synchronize(rrtl_ctx* ctx) {
+  return guard([&] {
+    REQUIRE(ctx, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    cuda_check(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   });
 }
 
@@ -801,6 +829,40 @@ rrtl_status rrtl_batch_get_signal_bits(rrtl_batch* b, uint32_t signal, uint32_t*
       if (st) fail(st, g_last_error);
       memset(out, 0, n * 4);
       for (uint32_t l = 0; l < b->lanes; ++l) out[l / 32] |= (v[l] & 1u) << (l % 32);
+    }
+  });
+}
+
+rrtl_status rrtl_batch_get_signals_bits(rrtl_batch* b, const uint32_t* signals, size_t n, uint32_t* out, size_t n_out) {
+  return guard([&] {
+    REQUIRE(b && (signals || n == 0) && (out || n == 0), RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    uint32_t words = (b->lanes + 31) / 32;
+    REQUIRE(n_out == n * words, RRTL_E_ARG, "E_GPU_LANE_VALUES: expected n*ceil(lanes/32) words");
+    for (size_t i = 0; i < n; ++i)
+      REQUIRE(signal_of(b->d, signals[i]).layout.width == 1, RRTL_E_ARG, "E_GPU_WIDE_SIGNAL: bit-packed access needs 1-bit signals");
+    check_err_word(b);
+    if (b->d->engine == RRTL_ENGINE_GATE) {
+      cudaStream_t st = b->d->ctx->stream;
+      // one 2-D copy per run of consecutive net rows
+      for (size_t i = 0; i < n;) {
+        uint32_t net = b->d->gp.signal_net[signals[i]];
+        size_t j = i + 1;
+        while (j < n && b->d->gp.signal_net[signals[j]] == net + (j - i)) ++j;
+        cuda_check(cudaMemcpy2DAsync(out + i * words, (size_t)words * 4, b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad,
+                                     (size_t)b->words_pad * 4, (size_t)words * 4, j - i, cudaMemcpyDeviceToHost, st),
+                   "d2h signals");
+        i = j;
+      }
+      cuda_check(cudaStreamSynchronize(st), "sync");
+      uint32_t valid = b->lanes - (words - 1) * 32;
+      if (valid < 32)
+        for (size_t i = 0; i < n; ++i) out[i * words + words - 1] &= (1u << valid) - 1u;
+    } else {
+      for (size_t i = 0; i < n; ++i) {
+        rrtl_status stt = rrtl_batch_get_signal_bits(b, signals[i], out + i * words, words);
+        if (stt) fail(stt, g_last_error);
+      }
     }
   });
 }

@@ -52,6 +52,7 @@ struct rrtl_ctx {
   cudaStream_t stream = nullptr;
   uint32_t sm_count = 0;
   size_t max_smem = 0;
+  cudaEvent_t events[8] = {};
 };
 
 struct rrtl_design {

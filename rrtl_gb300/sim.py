@@ -93,6 +93,9 @@ EXPORTS = (
     "rrtl_ctx_create",
     "rrtl_ctx_destroy",
     "rrtl_ctx_sm_count",
+    "rrtl_ctx_event_record",
+    "rrtl_ctx_event_elapsed",
+    "rrtl_ctx_synchronize",
     "rrtl_design_load_json",
     "rrtl_design_destroy",
     "rrtl_design_info_get",
@@ -105,6 +108,7 @@ EXPORTS = (
     "rrtl_batch_get_signal_limbs",
     "rrtl_batch_set_input_bits",
     "rrtl_batch_get_signal_bits",
+    "rrtl_batch_get_signals_bits",
     "rrtl_batch_set_memory_limbs",
     "rrtl_batch_get_memory_limbs",
     "rrtl_batch_eval",
@@ -137,6 +141,9 @@ def lib():
         "rrtl_ctx_create": [c_int32, P(c_void_p)],
         "rrtl_ctx_destroy": [c_void_p],
         "rrtl_ctx_sm_count": [c_void_p, P(c_uint32)],
+        "rrtl_ctx_event_record": [c_void_p, c_uint32],
+        "rrtl_ctx_event_elapsed": [c_void_p, c_uint32, c_uint32, P(c_float)],
+        "rrtl_ctx_synchronize": [c_void_p],
         "rrtl_design_load_json": [c_void_p, c_char_p, c_size_t, c_char_p, P(c_void_p)],
         "rrtl_design_destroy": [c_void_p],
         "rrtl_design_info_get": [c_void_p, P(DesignInfo)],
@@ -149,6 +156,7 @@ def lib():
         "rrtl_batch_get_signal_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
         "rrtl_batch_set_input_bits": [c_void_p, c_uint32, P(c_uint32), c_size_t],
         "rrtl_batch_get_signal_bits": [c_void_p, c_uint32, P(c_uint32), c_size_t],
+        "rrtl_batch_get_signals_bits": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_memory_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
         "rrtl_batch_get_memory_limbs": [c_void_p, c_uint32, P(c_uint32), c_size_t],
         "rrtl_batch_eval": [c_void_p],
@@ -192,6 +200,17 @@ class Context:
         n = c_uint32()
         check(lib().rrtl_ctx_sm_count(self.h, byref(n)))
         return n.value
+
+    def record(self, slot: int):
+        check(lib().rrtl_ctx_event_record(self.h, slot))
+
+    def elapsed_ms(self, a: int, b: int) -> float:
+        f = c_float()
+        check(lib().rrtl_ctx_event_elapsed(self.h, a, b, byref(f)))
+        return f.value
+
+    def synchronize(self):
+        check(lib().rrtl_ctx_synchronize(self.h))
 
     def close(self):
         if self.h:
@@ -328,6 +347,14 @@ class GpuBatchSimulator:
     def get_signal_bits(self, s: SignalRef) -> np.ndarray:
         out = np.zeros((self.lanes + 31) // 32, dtype=np.uint32)
         check(lib().rrtl_batch_get_signal_bits(self.h, self._sig(s), _u32p(out), out.size))
+        return out
+
+    def get_signals_bits(self, signals) -> np.ndarray:
+        """[n][ceil(lanes/32)] bit-packed values of several 1-bit signals."""
+        idx = np.asarray([self._sig(s) for s in signals], dtype=np.uint32)
+        words = (self.lanes + 31) // 32
+        out = np.zeros((len(idx), words), dtype=np.uint32)
+        check(lib().rrtl_batch_get_signals_bits(self.h, _u32p(idx), len(idx), _u32p(out), out.size))
         return out
 
     def set_memory_limbs(self, mem: str, data: np.ndarray):
