@@ -22,6 +22,8 @@
  *    program, crates/rrtl-sim-ir/src/lib.rs:12340-12414); look it up by name
  *    with rrtl_design_signal().
  *  - One thread drives a batch at a time (the Rust API is `&mut self`).
+ *  - Destroy calls may come in any order: a design keeps its context and a
+ *    batch its design alive until the last of them is destroyed.
  */
 #ifndef RRTL_CUDA_H
 #define RRTL_CUDA_H

@@ -34,11 +34,18 @@ struct GateRegDev {
   uint32_t q, d, rst, flags;
 };
 
+struct GatePieceDev {
+  uint32_t group_begin, n_groups, level, last_of_level;
+  uint32_t seg_begin, seg_end, pad0, pad1;
+};
+
 struct GateProgDev {
   // fused path (slots in shared memory)
   const uint2* srecs;          // [groups*4] packed slot records (pack_smem_record)
-  const uint4* pieces;         // {group_begin, n_groups, level, last_of_level}
+  const GatePieceDev* pieces;
+  const uint4* segs;           // {lut, begin, end, 0}: truth-table runs, group indices relative to the piece
   uint32_t n_pieces, n_slots, n_levels, piece_groups;
+  uint32_t n_segs;
   const uint32_t* src_net;     // sources loaded per tile and written back
   const uint32_t* src_slot;
   uint32_t n_src;

@@ -29,6 +29,14 @@ constexpr int kFusedWarps = kFusedThreads / 32;
 constexpr int kPlainThreads = 256;
 constexpr int kRing = 4;                 // record ring buffers
 constexpr uint32_t kSpinLimit = 1u << 22; // bounded mbarrier wait
+constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slot array
+#ifndef RRTL_FUSED_UNROLL
+#define RRTL_FUSED_UNROLL 2                // groups per unrolled step of a truth-table run
+#endif
+#ifndef RRTL_WARP_SPLIT
+#define RRTL_WARP_SPLIT 0                  // 0: contiguous group ranges per warp, 1: round robin
+#endif
+static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -78,10 +86,6 @@ __device__ __forceinline__ uint32_t lut_eval(uint32_t t, uint32_t a, uint32_t b,
   return (a & f1) | (~a & f0);
 }
 
-__device__ __forceinline__ uint32_t rec_lut(uint2 r) {
-  return ((r.x >> 14) & 3u) | ((r.x >> 28) & 0xCu) | ((r.y >> 10) & 0x30u) | ((r.y >> 24) & 0xC0u);
-}
-
 __device__ __forceinline__ uint32_t valid_mask(uint32_t gw, uint32_t lanes) {
   uint32_t base = gw * 32u;
   if (base >= lanes) return 0u;
@@ -103,53 +107,75 @@ __device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateR
 
 // ------------------------------------------------------------ fused path --
 
-struct FusedCtx {
-  uint32_t* S;         // slots [n_slots][8]
-  const uint32_t* wb;  // writeback nets for the current piece (final settle) or null
-  uint32_t* nets;
-  uint32_t words_pad, col;  // col = tile*8 + w
-  uint32_t w, gsub;
-};
+// Evaluate groups [g, e) of one truth-table run. `rb` is this thread's record
+// in group 0 of the staged piece and `Sw` this thread's word column of the
+// slot array; both are shared memory, so every access below is an LDS/STS.
+constexpr int kStride = RRTL_WARP_SPLIT ? kFusedWarps : 1;
+constexpr int kUnroll = RRTL_FUSED_UNROLL;
 
-// Evaluate consecutive groups with truth table L; stop at the first group with another table.
 template <int L>
-__device__ __noinline__ int run_groups(const uint2* __restrict__ rb, int g, int g1, FusedCtx& X) {
+__device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw, int g, int e) {
   constexpr bool kUseA = (L & 0x0F) != ((L >> 4) & 0x0F);
   constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
   constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
-  uint32_t* S = X.S;
-  for (; g < g1; ++g) {
-    uint2 r = rb[g * 4 + X.gsub];
-    if (rec_lut(r) != (uint32_t)L) break;
-    uint32_t a = r.x & 0x3FFFu, b = (r.x >> 16) & 0x3FFFu, c = r.y & 0x3FFFu, o = (r.y >> 16) & 0x3FFFu;
-    uint32_t va = kUseA ? S[a * 8 + X.w] : 0u;
-    uint32_t vb = kUseB ? S[b * 8 + X.w] : 0u;
-    uint32_t vc = kUseC ? S[c * 8 + X.w] : 0u;
-    uint32_t v = lop3<L>(va, vb, vc);
-    S[o * 8 + X.w] = v;
-    if (X.wb) {
-      uint32_t net = __ldg(X.wb + g * 4 + X.gsub);
-      if (net != 0xFFFFFFFFu) X.nets[(size_t)net * X.words_pad + X.col] = v;
-    }
+#pragma unroll kUnroll
+  for (; g < e; g += kStride) {
+    const uint2 r = rb[g * 4];
+    const uint32_t va = kUseA ? Sw[(r.x & 0xFFFFu) * 8u] : 0u;
+    const uint32_t vb = kUseB ? Sw[(r.x >> 16) * 8u] : 0u;
+    const uint32_t vc = kUseC ? Sw[(r.y & 0xFFFFu) * 8u] : 0u;
+    Sw[(r.y >> 16) * 8u] = lop3<L>(va, vb, vc);
   }
-  return g;
 }
 
 #define RRTL_CASE(n) \
-  case n: g = run_groups<n>(rb, g, g1, X); break;
+  case n: run_seg<n>(rb, Sw, b, e); break;
 #define RRTL_CASE4(n) RRTL_CASE(n) RRTL_CASE(n + 1) RRTL_CASE(n + 2) RRTL_CASE(n + 3)
 #define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
 #define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
 
-__device__ __forceinline__ void eval_groups(const uint2* __restrict__ rb, int g, int g1, FusedCtx& X) {
-  while (g < g1) {
-    uint32_t lut = rec_lut(rb[g * 4 + X.gsub]);
-    switch (lut) {
+// This warp's share [g0, g1) of a piece, dispatched once per truth-table run.
+__device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
+                                           const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0, int g1) {
+  for (uint32_t s = s0; s < s1; ++s) {
+    const uint4 sg = segs[s];
+#if RRTL_WARP_SPLIT
+    // round robin: this warp takes groups g0, g0+32, ... (g1 = group count of the piece)
+    const int first = (int)sg.y + (((g0 - (int)sg.y) % kFusedWarps) + kFusedWarps) % kFusedWarps;
+    const int b = first, e = (int)sg.z;
+#else
+    const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
+#endif
+    if (b >= e) continue;
+    switch (sg.x) {
       RRTL_CASE64(0)
       RRTL_CASE64(64)
       RRTL_CASE64(128)
       RRTL_CASE64(192)
-      default: g = g1; break;
+      default: break;
+    }
+  }
+}
+
+// Final settle: same evaluation with a runtime truth table, plus a copy of
+// every signal net to the global state.
+__device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
+                                                     const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0,
+                                                     int g1, const uint32_t* __restrict__ wb, uint32_t* nets,
+                                                     size_t words_pad, uint32_t col) {
+  for (uint32_t s = s0; s < s1; ++s) {
+    const uint4 sg = segs[s];
+#if RRTL_WARP_SPLIT
+    const int b = (int)sg.y + (((g0 - (int)sg.y) % kFusedWarps) + kFusedWarps) % kFusedWarps, e = (int)sg.z;
+#else
+    const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
+#endif
+    for (int g = b; g < e; g += kStride) {
+      const uint2 r = rb[g * 4];
+      const uint32_t v = lut_eval(sg.x, Sw[(r.x & 0xFFFFu) * 8u], Sw[(r.x >> 16) * 8u], Sw[(r.y & 0xFFFFu) * 8u]);
+      Sw[(r.y >> 16) * 8u] = v;
+      const uint32_t net = __ldg(wb + g * 4);
+      if (net != 0xFFFFFFFFu) nets[(size_t)net * words_pad + col] = v;
     }
   }
 }
@@ -168,11 +194,18 @@ __device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, u
 __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDev P, GateRunDev R) {
   extern __shared__ __align__(128) uint8_t smem[];
   const uint32_t piece_bytes = P.piece_groups * 32u;
+  // layout: [record ring][128-byte header: 4 mbarriers, hash accumulator,
+  // detect state][slots][piece table][segment table]; every region after the
+  // ring starts on a 16-byte boundary (the segment table is read as uint4)
   uint2* ring = reinterpret_cast<uint2*>(smem);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kRing * piece_bytes);
-  unsigned long long* hacc = reinterpret_cast<unsigned long long*>(bars + kRing);
-  uint32_t* dstate = reinterpret_cast<uint32_t*>(hacc + 1);  // diff[8], detected[8]
-  uint32_t* S = dstate + 16;
+  uint8_t* hdr = smem + (size_t)kRing * piece_bytes;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(hdr);
+  unsigned long long* hacc = reinterpret_cast<unsigned long long*>(hdr + kRing * 8);
+  uint32_t* dstate = reinterpret_cast<uint32_t*>(hdr + kRing * 8 + 8);  // diff[8], detected[8]
+  uint32_t* S = reinterpret_cast<uint32_t*>(hdr + kFusedHeader);
+  // piece and segment tables, staged once per launch
+  GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(S + (size_t)P.n_slots * 8);
+  uint4* segs = reinterpret_cast<uint4*>(pieces + P.n_pieces);
   __shared__ int s_abort;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
@@ -185,6 +218,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   const uint64_t passes = R.cycles + (R.final_settle ? 1u : 0u);
   const uint64_t total_q = resident ? P.n_pieces : (uint64_t)my_tiles * passes * P.n_pieces;
 
+  for (uint32_t i = tid; i < P.n_pieces; i += blockDim.x) pieces[i] = P.pieces[i];
+  for (uint32_t i = tid; i < P.n_segs; i += blockDim.x) segs[i] = P.segs[i];
   if (tid == 0) {
     s_abort = 0;
     *hacc = 0ull;
@@ -196,18 +231,14 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   if (tid == 0) {
     uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
     for (uint64_t q = 0; q < n0; ++q) {
-      uint4 pc = P.pieces[q % P.n_pieces];
-      bulk_load(ring + (size_t)(q % kRing) * P.piece_groups * 4, P.srecs + (size_t)pc.x * 4, pc.y * 32u, &bars[q % kRing]);
+      const GatePieceDev pc = P.pieces[q % P.n_pieces];
+      bulk_load(ring + (size_t)(q % kRing) * P.piece_groups * 4, P.srecs + (size_t)pc.group_begin * 4, pc.n_groups * 32u,
+                &bars[q % kRing]);
     }
   }
 
   uint64_t q = 0;
-  FusedCtx X;
-  X.S = S;
-  X.nets = R.nets;
-  X.words_pad = R.words_pad;
-  X.w = w;
-  X.gsub = gsub;
+  uint32_t* const Sw = S + w;
   // Thread 0 waits for a piece's records; the CTA barrier that follows
   // publishes them to every thread. The wait for piece q+1 is folded into the
   // barrier that closes piece q, so each piece costs one barrier.
@@ -227,7 +258,6 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
 
   for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !s_abort; tile += gridDim.x) {
     const uint32_t col0 = tile * 8u;
-    X.col = col0 + w;
     // constants, scratch, sources
     for (uint32_t i = tid; i < 8u; i += blockDim.x) {
       S[0 * 8 + i] = 0u;
@@ -263,23 +293,31 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       }
       __syncthreads();
       for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
-        const uint4 pc = P.pieces[p];
+        const GatePieceDev pc = pieces[p];
         const uint32_t buf = resident ? p : (uint32_t)(q % kRing);
-        const uint2* rb = ring + (size_t)buf * P.piece_groups * 4;
-        X.wb = final_pass ? (P.wb_net + (size_t)pc.x * 4) : nullptr;
-        int g0 = (int)((pc.y * warp) / kFusedWarps), g1 = (int)((pc.y * (warp + 1)) / kFusedWarps);
-        eval_groups(rb, g0, g1, X);
-        if (pc.w && R.has_forces) {
+        const uint2* rb = ring + (size_t)buf * P.piece_groups * 4 + gsub;
+#if RRTL_WARP_SPLIT
+        const int g0 = (int)warp, g1 = (int)pc.n_groups;
+#else
+        const int g0 = (int)((pc.n_groups * warp) / kFusedWarps), g1 = (int)((pc.n_groups * (warp + 1)) / kFusedWarps);
+#endif
+        if (final_pass)
+          eval_piece_writeback(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1, P.wb_net + (size_t)pc.group_begin * 4 + gsub,
+                               R.nets, R.words_pad, col0 + w);
+        else
+          eval_piece(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1);
+        if (pc.last_of_level && R.has_forces) {
           __syncthreads();
-          apply_forces(R, S, tile, pc.z + 1, stages);
+          apply_forces(R, S, tile, pc.level + 1, stages);
         }
         if (tid == 0) wait_piece(q + 1);
         __syncthreads();
         if (s_abort) break;
         if (!resident && tid == 0 && q + kRing < total_q) {
           uint64_t nq = q + kRing;
-          uint4 npc = P.pieces[nq % P.n_pieces];
-          bulk_load(ring + (size_t)buf * P.piece_groups * 4, P.srecs + (size_t)npc.x * 4, npc.y * 32u, &bars[buf]);
+          const GatePieceDev npc = pieces[nq % P.n_pieces];
+          bulk_load(ring + (size_t)buf * P.piece_groups * 4, P.srecs + (size_t)npc.group_begin * 4, npc.n_groups * 32u,
+                    &bars[buf]);
         }
       }
       if (s_abort) break;
@@ -454,8 +492,10 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
 // ------------------------------------------------------------- launchers --
 
 size_t gate_fused_smem_bytes(const GateProgDev& P) {
-  return (size_t)kRing * P.piece_groups * 32u + kRing * 8u + 8u + 16u * 4u + (size_t)P.n_slots * 8u * 4u;
+  return (size_t)kRing * P.piece_groups * 32u + kFusedHeader + (size_t)P.n_slots * 8u * 4u +
+         (size_t)P.n_pieces * sizeof(GatePieceDev) + (size_t)P.n_segs * 16u;
 }
+static_assert(sizeof(GatePieceDev) == 32, "piece descriptor layout");
 
 cudaError_t gate_fused_prepare(size_t smem) {
   return cudaFuncSetAttribute(gate_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -210,10 +210,9 @@ struct Builder {
 
 }  // namespace
 
-GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups) {
+GateProgram build_gate_program(const MachineProgram& mp) {
   const PackedProgram& P = mp.source;
   GateProgram gp;
-  gp.piece_groups = piece_groups;
   for (auto& s : P.signals)
     if (s.layout.width != 1) throw RrtlError("E_GATE_SCOPE", "signal `" + s.name + "` is wider than 1 bit");
   if (!P.memories.empty()) throw RrtlError("E_GATE_SCOPE", "memories are outside the gate engine");
@@ -324,62 +323,25 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups) 
   }
   gp.n_levels = (uint32_t)(max_level + 1);
 
-  // ---- group by level and truth table, pad to kGroup
-  std::vector<GateCell> sorted(gp.cells);
-  std::stable_sort(sorted.begin(), sorted.end(), [](const GateCell& x, const GateCell& y) {
-    if (x.level != y.level) return x.level < y.level;
-    return x.lut < y.lut;
-  });
-  std::vector<GateCell> grouped;
-  gp.level_group_begin.assign(gp.n_levels + 1, 0);
-  size_t i = 0;
-  for (uint32_t L = 0; L < gp.n_levels; ++L) {
-    gp.level_group_begin[L] = (uint32_t)(grouped.size() / kGroup);
-    while (i < sorted.size() && sorted[i].level == (int32_t)L) {
-      size_t j = i;
-      while (j < sorted.size() && sorted[j].level == (int32_t)L && sorted[j].lut == sorted[i].lut) ++j;
-      for (size_t k = i; k < j; ++k) grouped.push_back(sorted[k]);
-      while (grouped.size() % kGroup) {
-        GateCell pad;
-        pad.lut = sorted[i].lut;
-        pad.level = (int32_t)L;
-        pad.pad = true;
-        pad.out = kNetConst0;  // redirected to the scratch slot / row
-        grouped.push_back(pad);
-      }
-      i = j;
-    }
-  }
-  gp.level_group_begin[gp.n_levels] = (uint32_t)(grouped.size() / kGroup);
-  gp.cells = std::move(grouped);
-
-  // ---- pieces
-  for (uint32_t L = 0; L < gp.n_levels; ++L) {
-    uint32_t g0 = gp.level_group_begin[L], g1 = gp.level_group_begin[L + 1];
-    for (uint32_t g = g0; g < g1; g += piece_groups) {
-      GatePiece pc;
-      pc.level = L;
-      pc.group_begin = g;
-      pc.n_groups = std::min(piece_groups, g1 - g);
-      pc.last_of_level = g + pc.n_groups >= g1;
-      gp.pieces.push_back(pc);
-    }
-  }
-
-  // ---- on-chip slots by liveness
-  // last use: consumer level; D nets and output-port nets live to the end.
+  // ---- liveness: consumer level; D nets, reset nets and output-port nets live to the end
   const int32_t kEnd = (int32_t)gp.n_levels;
   std::vector<int32_t> last_use(gp.n_nets, -1);
-  for (auto& c : gp.cells) {
-    if (c.pad) continue;
+  for (auto& c : gp.cells)
     for (int k = 0; k < 3; ++k) last_use[c.in[k]] = std::max(last_use[c.in[k]], c.level);
-  }
   for (auto& r : gp.regs) {
     last_use[r.d_net] = kEnd;
     last_use[r.rst_net] = kEnd;
   }
   for (uint32_t s = 0; s < ns; ++s)
     if (P.signals[s].kind == PSK::Output) last_use[2 + s] = kEnd;
+  auto end_live = [&](uint32_t n) { return std::max(last_use[n], gp.net_level[n]) >= kEnd; };
+
+  // ---- on-chip slots
+  // Slot s occupies banks 8*(s%4)..8*(s%4)+7 of every 32-bank row pair (8
+  // words per slot), so the four cells of a group conflict only when two of
+  // their operand rows share s%4. Cells are grouped to spread operand rows
+  // over the four residues and each group's outputs get distinct residues.
+  //
   // Registers are rewritten by every commit, so between a register's last
   // read in the settle and the commit its slot can host nets that die before
   // the end of the cycle. End-live nets (D, reset, outputs) never take such a
@@ -388,50 +350,158 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups) 
   std::vector<uint8_t> is_reg_q(gp.n_nets, 0);
   for (auto& r : gp.regs) is_reg_q[r.q_net] = 1;
   uint32_t next_slot = 1;  // slot 0 is the scratch slot for padding cells
-  std::vector<std::vector<uint32_t>> q_free_after(gp.n_levels + 1);  // register slots released after level L
+  std::vector<std::vector<uint32_t>> q_free_after(gp.n_levels + 1);  // register slots released before level L
+  std::vector<uint8_t> slot_is_q;
   for (uint32_t n = 0; n < gp.n_nets; ++n)
     if (gp.net_is_source[n]) {
       gp.net_slot[n] = (int32_t)next_slot++;
       if (n != kNetConst0 && n != kNetConst1) gp.source_nets.push_back(n);
-      if (is_reg_q[n] && last_use[n] < kEnd) q_free_after[std::max<int32_t>(last_use[n], -1) + 1].push_back((uint32_t)gp.net_slot[n]);
+      slot_is_q.resize(next_slot, 0);
+      if (is_reg_q[n]) {
+        slot_is_q[gp.net_slot[n]] = 1;
+        if (last_use[n] < kEnd) q_free_after[std::max<int32_t>(last_use[n], -1) + 1].push_back((uint32_t)gp.net_slot[n]);
+      }
     }
-  std::vector<std::vector<uint32_t>> produced(gp.n_levels), dying(gp.n_levels + 1);
+  std::vector<std::vector<uint32_t>> dying(gp.n_levels + 1);
   for (uint32_t n = 0; n < gp.n_nets; ++n) {
     if (gp.net_is_source[n] || gp.net_level[n] < 0) continue;
-    produced[gp.net_level[n]].push_back(n);
     int32_t lu = std::max(last_use[n], gp.net_level[n]);
     if (lu < kEnd) dying[lu].push_back(n);
   }
-  std::vector<uint32_t> free_general, free_q;
-  std::vector<uint8_t> slot_is_q(next_slot + 1, 0);
-  for (uint32_t n = 0; n < gp.n_nets; ++n)
-    if (is_reg_q[n] && gp.net_slot[n] >= 0) slot_is_q[gp.net_slot[n]] = 1;
+  std::vector<uint32_t> free_general[4], free_q[4];
+  auto release = [&](uint32_t s) {
+    bool q = s < slot_is_q.size() && slot_is_q[s];
+    (q ? free_q : free_general)[s & 3].push_back(s);
+  };
+  auto take = [&](bool live_to_end, uint32_t res) -> uint32_t {
+    if (!live_to_end && !free_q[res].empty()) {
+      uint32_t s = free_q[res].back();
+      free_q[res].pop_back();
+      return s;
+    }
+    if (!free_general[res].empty()) {
+      uint32_t s = free_general[res].back();
+      free_general[res].pop_back();
+      return s;
+    }
+    while ((next_slot & 3) != res) free_general[next_slot & 3].push_back(next_slot++);
+    return next_slot++;
+  };
+
+  std::vector<std::vector<uint32_t>> cells_at(gp.n_levels);
+  for (uint32_t i = 0; i < gp.cells.size(); ++i) cells_at[gp.cells[i].level].push_back(i);
+  std::vector<GateCell> grouped;
+  gp.level_group_begin.assign(gp.n_levels + 1, 0);
+  const int kLook = 48;
   for (uint32_t L = 0; L < gp.n_levels; ++L) {
-    // register slots whose last read was before level L (index L in q_free_after)
-    for (uint32_t s : q_free_after[L]) free_q.push_back(s);
+    for (uint32_t s : q_free_after[L]) release(s);
     if (L > 0)
-      for (uint32_t n : dying[L - 1]) {
-        uint32_t s = (uint32_t)gp.net_slot[n];
-        (s < slot_is_q.size() && slot_is_q[s] ? free_q : free_general).push_back(s);
+      for (uint32_t n : dying[L - 1]) release((uint32_t)gp.net_slot[n]);
+    gp.level_group_begin[L] = (uint32_t)(grouped.size() / kGroup);
+    std::vector<uint32_t>& cs = cells_at[L];
+    std::stable_sort(cs.begin(), cs.end(), [&](uint32_t x, uint32_t y) { return gp.cells[x].lut < gp.cells[y].lut; });
+    for (size_t i = 0; i < cs.size();) {
+      size_t j = i;
+      const uint8_t lut = gp.cells[cs[i]].lut;
+      while (j < cs.size() && gp.cells[cs[j]].lut == lut) ++j;
+      const bool use[3] = {(lut & 0x0F) != ((lut >> 4) & 0x0F), (lut & 0x33) != ((lut >> 2) & 0x33),
+                           (lut & 0x55) != ((lut >> 1) & 0x55)};
+      std::vector<uint32_t> rem(cs.begin() + i, cs.begin() + j);
+      size_t head = 0;
+      std::vector<uint8_t> taken(rem.size(), 0);
+      while (head < rem.size()) {
+        while (head < rem.size() && taken[head]) ++head;
+        if (head == rem.size()) break;
+        std::vector<uint32_t> grp{rem[head]};
+        taken[head] = 1;
+        // greedy: add the candidate that adds the fewest operand-row conflicts
+        for (uint32_t pick = 1; pick < kGroup; ++pick) {
+          int best = -1, best_cost = 1 << 30;
+          int seen = 0;
+          for (size_t k = head + 1; k < rem.size() && seen < kLook; ++k) {
+            if (taken[k]) continue;
+            ++seen;
+            int cost = 0;
+            for (int p = 0; p < 3; ++p) {
+              if (!use[p]) continue;
+              uint32_t cand = (uint32_t)gp.net_slot[gp.cells[rem[k]].in[p]];
+              int same = 0;
+              bool dup = false;
+              for (uint32_t m : grp) {
+                uint32_t sl = (uint32_t)gp.net_slot[gp.cells[m].in[p]];
+                if (sl == cand) dup = true;
+                else if ((sl & 3) == (cand & 3)) ++same;
+              }
+              if (!dup) cost += same;
+            }
+            if (cost < best_cost) {
+              best_cost = cost;
+              best = (int)k;
+              if (cost == 0) break;
+            }
+          }
+          if (best < 0) break;
+          grp.push_back(rem[best]);
+          taken[best] = 1;
+        }
+        // outputs: distinct residues; residue 0 last when padding (scratch slot 0) shares the group
+        const bool padded = grp.size() < kGroup;
+        const uint32_t order[4] = {padded ? 1u : 0u, padded ? 2u : 1u, padded ? 3u : 2u, padded ? 0u : 3u};
+        for (size_t k = 0; k < grp.size(); ++k) {
+          GateCell c = gp.cells[grp[k]];
+          gp.net_slot[c.out] = (int32_t)take(end_live(c.out), order[k]);
+          if (slot_is_q.size() <= (size_t)gp.net_slot[c.out]) slot_is_q.resize(gp.net_slot[c.out] + 1, 0);
+          grouped.push_back(c);
+        }
+        while (grouped.size() % kGroup) {
+          GateCell pad;
+          pad.lut = lut;
+          pad.level = (int32_t)L;
+          pad.pad = true;
+          pad.out = kNetConst0;  // redirected to the scratch slot / row
+          grouped.push_back(pad);
+        }
       }
-    for (uint32_t n : produced[L]) {
-      bool end_live = std::max(last_use[n], gp.net_level[n]) >= kEnd;
-      if (!end_live && !free_q.empty()) {
-        gp.net_slot[n] = (int32_t)free_q.back();
-        free_q.pop_back();
-      } else if (!free_general.empty()) {
-        gp.net_slot[n] = (int32_t)free_general.back();
-        free_general.pop_back();
-      } else {
-        gp.net_slot[n] = (int32_t)next_slot++;
-      }
+      i = j;
     }
   }
-  for (uint32_t n = 0; n < gp.n_nets; ++n) gp.net_end_live.push_back(std::max(last_use[n], gp.net_level[n]) >= kEnd ? 1 : 0);
+  gp.level_group_begin[gp.n_levels] = (uint32_t)(grouped.size() / kGroup);
+  gp.cells = std::move(grouped);
+  for (uint32_t n = 0; n < gp.n_nets; ++n) gp.net_end_live.push_back(end_live(n) ? 1 : 0);
   for (uint32_t n = 0; n < gp.n_nets; ++n)
     if (gp.net_is_source[n] && !is_reg_q[n]) gp.net_end_live[n] = 1;
   gp.n_slots = next_slot;
   return gp;
+}
+
+void build_pieces(GateProgram& gp, uint32_t piece_groups) {
+  gp.piece_groups = piece_groups;
+  gp.pieces.clear();
+  gp.segments.clear();
+  for (uint32_t L = 0; L < gp.n_levels; ++L) {
+    uint32_t g0 = gp.level_group_begin[L], g1 = gp.level_group_begin[L + 1];
+    uint32_t n = g1 - g0;
+    if (n == 0) continue;
+    uint32_t np = (n + piece_groups - 1) / piece_groups;
+    for (uint32_t k = 0; k < np; ++k) {
+      GatePiece pc;
+      pc.level = L;
+      pc.group_begin = g0 + (uint32_t)((uint64_t)n * k / np);
+      uint32_t end = g0 + (uint32_t)((uint64_t)n * (k + 1) / np);
+      pc.n_groups = end - pc.group_begin;
+      pc.last_of_level = k + 1 == np;
+      pc.seg_begin = (uint32_t)gp.segments.size();
+      for (uint32_t g = pc.group_begin; g < end;) {
+        uint32_t h = g;
+        uint8_t lut = gp.cells[(size_t)g * kGroup].lut;
+        while (h < end && gp.cells[(size_t)h * kGroup].lut == lut) ++h;
+        gp.segments.push_back(GateSegment{lut, g - pc.group_begin, h - pc.group_begin});
+        g = h;
+      }
+      pc.seg_end = (uint32_t)gp.segments.size();
+      gp.pieces.push_back(pc);
+    }
+  }
 }
 
 }  // namespace rrtl

@@ -33,7 +33,7 @@ constexpr uint32_t kGroup = 4;        // cells per warp group (32 lanes / 8 word
 constexpr uint32_t kTileWords = 8;    // 32-lane words per CTA tile in the fused kernel
 constexpr uint32_t kNetConst0 = 0;    // all-zero net
 constexpr uint32_t kNetConst1 = 1;    // all-ones net
-constexpr uint32_t kMaxSlots = 16383; // 14-bit slot fields in packed records
+constexpr uint32_t kMaxSlots = 65535; // 16-bit slot fields in packed records
 
 struct GateCell {
   uint8_t lut = 0;      // LOP3 table: input a <-> 0xF0, b <-> 0xCC, c <-> 0xAA
@@ -57,6 +57,13 @@ struct GatePiece {
   uint32_t group_begin;  // index of the first group in the level-ordered group array
   uint32_t n_groups;
   bool last_of_level;
+  uint32_t seg_begin, seg_end;  // runs of one truth table inside the piece
+};
+
+// A run of groups inside a piece that share one truth table (group indices
+// relative to the piece).
+struct GateSegment {
+  uint32_t lut, begin, end;
 };
 
 struct GateProgram {
@@ -77,19 +84,22 @@ struct GateProgram {
   uint32_t n_slots = 0;           // including the scratch slot (slot 0)
   std::vector<uint32_t> source_nets;  // nets loaded into slots at tile start (and written back)
   std::vector<GatePiece> pieces;
+  std::vector<GateSegment> segments;
   uint32_t piece_groups = 0;      // max groups per piece
   uint64_t source_instrs = 0;
 };
 
 // Throws RrtlError("E_GATE_SCOPE", ...) when the program is outside the gate engine's scope.
-GateProgram build_gate_program(const MachineProgram& mp, uint32_t piece_groups);
+GateProgram build_gate_program(const MachineProgram& mp);
 
-// Packed 8-byte record for one cell in shared memory: four 14-bit slot fields
-// (a, b, c, out) with the 8-bit truth table spread over their top two bits.
-inline uint64_t pack_smem_record(uint32_t a, uint32_t b, uint32_t c, uint32_t out, uint8_t lut) {
-  uint64_t x = (uint64_t)(a | ((lut & 3u) << 14)) | ((uint64_t)(b | (((lut >> 2) & 3u) << 14)) << 16) |
-               ((uint64_t)(c | (((lut >> 4) & 3u) << 14)) << 32) | ((uint64_t)(out | (((lut >> 6) & 3u) << 14)) << 48);
-  return x;
+// Split every level into nearly equal pieces of at most `piece_groups` groups
+// and record the truth-table runs of each piece.
+void build_pieces(GateProgram& gp, uint32_t piece_groups);
+
+// Packed 8-byte record for one cell in shared memory: four 16-bit slot
+// fields a, b, c, out (the truth table comes from the piece's segments).
+inline uint64_t pack_smem_record(uint32_t a, uint32_t b, uint32_t c, uint32_t out) {
+  return (uint64_t)a | ((uint64_t)b << 16) | ((uint64_t)c << 32) | ((uint64_t)out << 48);
 }
 
 }  // namespace rrtl

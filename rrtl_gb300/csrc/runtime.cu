@@ -17,7 +17,6 @@ cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_
 cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st);
 cudaError_t word_prepare(size_t smem);
 
-constexpr uint32_t kPieceGroups = 256;
 constexpr uint32_t kWordThreads = 128;
 constexpr size_t kWordSmemBudget = 96 * 1024;
 
@@ -108,8 +107,29 @@ void upload_gate_program(rrtl_design* d) {
   upload(d->d_lgb, gp.level_group_begin);
   upload(d->d_gregs, gregs);
 
-  // fused program: only when every slot index fits the packed record
-  d->fused_ok = gp.n_slots <= kMaxSlots;
+  // fused program: slots and a 4-deep record ring must fit shared memory;
+  // pieces take whatever the slots leave (up to 1024 groups per piece)
+  // the piece/segment tables (staged in shared memory too) depend on the piece
+  // size, so shrink pieces until everything fits
+  size_t slot_bytes = (size_t)gp.n_slots * kTileWords * 4 + 256;
+  d->fused_ok = gp.n_slots <= kMaxSlots && slot_bytes + 4 * 32 * 32 <= d->ctx->max_smem;
+  uint32_t piece_groups = 32;
+  if (d->fused_ok) {
+    size_t per_buf = (d->ctx->max_smem - slot_bytes) / 4;
+    piece_groups = (uint32_t)std::min<size_t>(512, per_buf / 32) & ~7u;
+    for (;;) {
+      build_pieces(d->gp, piece_groups);
+      size_t tables = gp.pieces.size() * sizeof(GatePieceDev) + gp.segments.size() * 16;
+      if (slot_bytes + tables + (size_t)4 * piece_groups * 32 <= d->ctx->max_smem) break;
+      if (piece_groups <= 32) {
+        d->fused_ok = false;
+        break;
+      }
+      piece_groups -= 32;
+    }
+  } else {
+    build_pieces(d->gp, 256);
+  }
   if (d->fused_ok) {
     std::vector<uint2> srecs(gp.cells.size());
     int32_t c0 = gp.net_slot[kNetConst0];
@@ -117,11 +137,14 @@ void upload_gate_program(rrtl_design* d) {
       const GateCell& c = gp.cells[i];
       uint32_t a = c.pad ? c0 : gp.net_slot[c.in[0]], b = c.pad ? c0 : gp.net_slot[c.in[1]];
       uint32_t cc = c.pad ? c0 : gp.net_slot[c.in[2]], o = c.pad ? 0 : gp.net_slot[c.out];
-      uint64_t x = pack_smem_record(a, b, cc, o, c.lut);
+      uint64_t x = pack_smem_record(a, b, cc, o);
       srecs[i] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
     }
-    std::vector<uint4> pieces;
-    for (auto& p : gp.pieces) pieces.push_back(make_uint4(p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u));
+    std::vector<GatePieceDev> pieces;
+    for (auto& p : gp.pieces)
+      pieces.push_back(GatePieceDev{p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u, p.seg_begin, p.seg_end, 0, 0});
+    std::vector<uint4> segs;
+    for (auto& sg : gp.segments) segs.push_back(make_uint4(sg.lut, sg.begin, sg.end, 0));
     std::vector<uint32_t> src_slot;
     for (uint32_t n : gp.source_nets) src_slot.push_back((uint32_t)gp.net_slot[n]);
     for (auto& r : gp.regs) {
@@ -131,6 +154,7 @@ void upload_gate_program(rrtl_design* d) {
     }
     upload(d->d_srecs, srecs);
     upload(d->d_pieces, pieces);
+    upload(d->d_segs, segs);
     upload(d->d_src_net, gp.source_nets);
     upload(d->d_src_slot, src_slot);
     upload(d->d_sregs, sregs);
@@ -138,11 +162,13 @@ void upload_gate_program(rrtl_design* d) {
   GateProgDev& G = d->gdev;
   G = GateProgDev{};
   G.srecs = d->d_srecs.as<uint2>();
-  G.pieces = d->d_pieces.as<uint4>();
+  G.pieces = d->d_pieces.as<GatePieceDev>();
+  G.segs = d->d_segs.as<uint4>();
+  G.n_segs = (uint32_t)gp.segments.size();
   G.n_pieces = (uint32_t)gp.pieces.size();
   G.n_slots = gp.n_slots;
   G.n_levels = gp.n_levels;
-  G.piece_groups = kPieceGroups;
+  G.piece_groups = piece_groups;
   G.src_net = d->d_src_net.as<uint32_t>();
   G.src_slot = d->d_src_slot.as<uint32_t>();
   G.n_src = (uint32_t)gp.source_nets.size();
@@ -363,7 +389,6 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
 void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
-  const PackedProgram& P = d->mp.source;
   std::vector<WordStimDev> stim;
   for (uint32_t i = 0; i < run.n_stim; ++i) {
     const rrtl_stim& s = run.stim[i];
@@ -516,14 +541,29 @@ rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out) {
   });
 }
 
+static void ctx_release(rrtl_ctx* ctx) {
+  if (--ctx->refs > 0) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->events)
+    if (e) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+static void design_release(rrtl_design* d) {
+  if (--d->refs > 0) return;
+  rrtl_ctx* ctx = d->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  delete d;  // frees the device program while the context is still alive
+  ctx_release(ctx);
+}
+
 rrtl_status rrtl_ctx_destroy(rrtl_ctx* ctx) {
   return guard([&] {
     if (!ctx) return;
-    cudaSetDevice(ctx->device);
-    for (auto& e : ctx->events)
-      if (e) cudaEventDestroy(e);
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    ctx_release(ctx);
   });
 }
 
@@ -571,7 +611,7 @@ rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, c
     d->mp = lower_to_machine_program(pp);
     bool gate = true;
     try {
-      d->gp = build_gate_program(d->mp, kPieceGroups);
+      d->gp = build_gate_program(d->mp);
     } catch (const RrtlError& e) {
       if (e.code != "E_GATE_SCOPE") throw;
       gate = false;
@@ -584,6 +624,7 @@ rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, c
       d->wp = build_word_program(d->mp);
       upload_word_program(d.get());
     }
+    ctx->refs++;
     *out = d.release();
   });
 }
@@ -591,8 +632,7 @@ rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, c
 rrtl_status rrtl_design_destroy(rrtl_design* d) {
   return guard([&] {
     if (!d) return;
-    cudaSetDevice(d->ctx->device);
-    delete d;
+    design_release(d);
   });
 }
 
@@ -693,6 +733,7 @@ rrtl_status rrtl_batch_create(rrtl_design* d, uint32_t lanes, rrtl_batch** out) 
       cuda_check(cudaMemset(b->d_mem.p, 0, mb), "memset");
     }
     batch_eval(b.get());
+    d->refs++;
     *out = b.release();
   });
 }
@@ -700,11 +741,13 @@ rrtl_status rrtl_batch_create(rrtl_design* d, uint32_t lanes, rrtl_batch** out) 
 rrtl_status rrtl_batch_destroy(rrtl_batch* b) {
   return guard([&] {
     if (!b) return;
-    cudaSetDevice(b->d->ctx->device);
-    cudaStreamSynchronize(b->d->ctx->stream);
+    rrtl_design* d = b->d;
+    cudaSetDevice(d->ctx->device);
+    cudaStreamSynchronize(d->ctx->stream);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     delete b;
+    design_release(d);
   });
 }
 

@@ -47,7 +47,11 @@ void upload(DevBuf& b, const std::vector<T>& v) {
 
 }  // namespace rrtl
 
+// Handles are reference counted: a design holds its context and a batch its
+// design, so destroying a parent first only drops the caller's reference and
+// the parent is released with its last child.
 struct rrtl_ctx {
+  int refs = 1;
   int device = 0;
   cudaStream_t stream = nullptr;
   uint32_t sm_count = 0;
@@ -56,6 +60,7 @@ struct rrtl_ctx {
 };
 
 struct rrtl_design {
+  int refs = 1;
   rrtl_ctx* ctx = nullptr;
   rrtl::Design design;
   std::string top;
@@ -67,7 +72,7 @@ struct rrtl_design {
   rrtl::GateProgDev gdev{};
   bool fused_ok = false;
   size_t fused_smem = 0;
-  rrtl::DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
+  rrtl::DevBuf d_srecs, d_pieces, d_segs, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
   // word engine
   rrtl::WordProgram wp;
   rrtl::WordProgDev wdev{};
