@@ -183,3 +183,163 @@ def netlist_run_spec(meta: NetlistMeta, reset_cycles: int = 1):
     stim = [(meta.clk, STIM_CONST, 1), (meta.rst, STIM_PULSE, reset_cycles)]
     stim += [(p, STIM_RANDOM, i) for i, p in enumerate(meta.inputs)]
     return stim, list(meta.outputs)
+
+
+# --------------------------------------------------------- pipelined CPU --
+CPU_OPS = ("add", "sub", "and", "or", "xor", "sll", "srl", "sra", "slt", "sltu",
+           "addi", "lw", "sw", "beq", "bne", "jal")
+
+
+def _shift_barrel(x, amt, kind):
+    """32-bit shift by a 5-bit amount as a mux barrel over the amount bits:
+    `<<k` = concat(slice, 0_k), `>>k` = zext(slice), `>>>k` = sext(slice)."""
+    for i in range(5):
+        k = 1 << i
+        if kind == "sll":
+            sh = concat([x.slice(0, 32 - k), lit_u(0, k)])
+        elif kind == "srl":
+            sh = x.slice(k, 32 - k).zext(32)
+        else:
+            sh = x.slice(k, 32 - k).sext(32).as_uint()
+        x = mux(amt.slice(i, 1), sh, x)
+    return x
+
+
+def pipelined_cpu(top: str = "Cpu8"):
+    """8-stage pipelined 32-bit accumulator CPU (IF1 IF2 ID RR EX1 EX2 MEM WB).
+
+    Per lane: 16 x 32-bit register file, 1,024 x 32-bit data memory and a
+    256 x 32-bit instruction ROM (all memories), an 8-bit PC and a 64-bit
+    accumulator that sums every written-back result. Instruction word:
+    op[3:0] rd[7:4] rs1[11:8] rs2[15:12] imm[31:16]; ops are
+    add sub and or xor sll srl sra slt sltu (register-register), addi, lw, sw,
+    beq, bne (target = imm[7:0]) and jal (rd = pc + 1, jump to imm[7:0]).
+    Branches resolve in EX1 and squash the three younger instructions; there
+    is no forwarding, so a register read sees the register file as of the read.
+    """
+    d = Design()
+    m = d.module(top)
+    clk = m.input("clk", uint(1))
+    rst = m.input("rst", uint(1))
+    rom = m.mem("rom", 8, uint(32), 256)
+    dmem = m.mem("dmem", 10, uint(32), 1024)
+    rf = m.mem("rf", 4, uint(32), 16)
+
+    def reg(name, w, reset=True):
+        r = m.reg(name, uint(w))
+        m.clock(r, clk)
+        if reset:
+            m.reset(r, rst, 0)
+        return r
+
+    def wire(name, w, e):
+        x = m.wire(name, uint(w))
+        m.assign(x, e)
+        return x
+
+    pc = reg("pc", 8)
+    v1, pc1 = reg("v1", 1), reg("pc1", 8)
+    v2, pc2, ins2 = reg("v2", 1), reg("pc2", 8), reg("ins2", 32)
+    v3, pc3, op3, rd3, rs13, rs23, imm3 = (reg("v3", 1), reg("pc3", 8), reg("op3", 4), reg("rd3", 4),
+                                          reg("rs1_3", 4), reg("rs2_3", 4), reg("imm3", 16))
+    v4, pc4, op4, rd4, a4, b4, imm4 = (reg("v4", 1), reg("pc4", 8), reg("op4", 4), reg("rd4", 4),
+                                      reg("a4", 32), reg("b4", 32), reg("imm4", 16))
+    v5, op5, rd5, res5, addr5, sd5 = (reg("v5", 1), reg("op5", 4), reg("rd5", 4), reg("res5", 32),
+                                      reg("addr5", 10), reg("sd5", 32))
+    v6, op6, rd6, res6, addr6, sd6 = (reg("v6", 1), reg("op6", 4), reg("rd6", 4), reg("res6", 32),
+                                      reg("addr6", 10), reg("sd6", 32))
+    v7, op7, rd7, res7 = reg("v7", 1), reg("op7", 4), reg("rd7", 4), reg("res7", 32)
+    acc = reg("acc", 64)
+
+    def is_op(o, name):
+        return o.eq_expr(lit_u(CPU_OPS.index(name), 4))
+
+    # EX1: ALU and branch resolution from the RR stage registers
+    simm4 = wire("simm4", 32, imm4.sext(32).as_uint())
+    amt = wire("amt", 5, b4.slice(0, 5))
+    alu = {
+        "add": a4 + b4,
+        "sub": a4 - b4,
+        "and": a4 & b4,
+        "or": a4 | b4,
+        "xor": a4 ^ b4,
+        "sll": _shift_barrel(a4.value(), amt, "sll"),
+        "srl": _shift_barrel(a4.value(), amt, "srl"),
+        "sra": _shift_barrel(a4.value(), amt, "sra"),
+        "slt": a4.as_sint().lt_expr(b4.as_sint()).zext(32),
+        "sltu": a4.lt_expr(b4).zext(32),
+        "addi": a4 + simm4,
+        "jal": pc4.zext(32) + lit_u(1, 32),
+    }
+    res = lit_u(0, 32)
+    for name, e in alu.items():
+        res = mux(is_op(op4, name), wire(f"alu_{name}", 32, e), res)
+    res_w = wire("alu_res", 32, res)
+    eq = wire("eq4", 1, a4.eq_expr(b4))
+    taken = wire("taken", 1, v4 & ((is_op(op4, "beq") & eq) | (is_op(op4, "bne") & ~eq.value()) | is_op(op4, "jal")))
+    flush = taken
+    nflush = wire("nflush", 1, ~flush.value())
+
+    # IF1 / IF2 / ID / RR
+    m.next(pc, mux(flush, imm4.slice(0, 8), pc + lit_u(1, 8)))
+    m.next(v1, nflush)
+    m.next(pc1, pc)
+    m.next(v2, v1 & nflush)
+    m.next(pc2, pc1)
+    m.next(ins2, mem_read(rom, pc1))
+    m.next(v3, v2 & nflush)
+    m.next(pc3, pc2)
+    m.next(op3, ins2.slice(0, 4))
+    m.next(rd3, ins2.slice(4, 4))
+    m.next(rs13, ins2.slice(8, 4))
+    m.next(rs23, ins2.slice(12, 4))
+    m.next(imm3, ins2.slice(16, 16))
+    m.next(v4, v3 & nflush)
+    m.next(pc4, pc3)
+    m.next(op4, op3)
+    m.next(rd4, rd3)
+    m.next(a4, mem_read(rf, rs13))
+    m.next(b4, mem_read(rf, rs23))
+    m.next(imm4, imm3)
+    # EX1 -> EX2 -> MEM -> WB
+    m.next(v5, v4)
+    m.next(op5, op4)
+    m.next(rd5, rd4)
+    m.next(res5, res_w)
+    m.next(addr5, (a4 + simm4).slice(0, 10))
+    m.next(sd5, b4)
+    m.next(v6, v5)
+    m.next(op6, op5)
+    m.next(rd6, rd5)
+    m.next(res6, res5)
+    m.next(addr6, addr5)
+    m.next(sd6, sd5)
+    m.next(v7, v6)
+    m.next(op7, op6)
+    m.next(rd7, rd6)
+    m.next(res7, mux(is_op(op6, "lw"), mem_read(dmem, addr6), res6))
+    m.mem_write(dmem, clk, v6 & is_op(op6, "sw"), addr6, sd6)
+    writes = wire("wb_en", 1, v7 & ~(is_op(op7, "sw") | is_op(op7, "beq") | is_op(op7, "bne")))
+    m.mem_write(rf, clk, writes, rd7, res7)
+    m.next(acc, mux(writes, acc + res7.zext(64), acc))
+    out_pc = m.output("out_pc", uint(8))
+    m.assign(out_pc, pc)
+    out_acc = m.output("out_acc", uint(64))
+    m.assign(out_acc, acc)
+    return d
+
+
+def cpu_rom(lanes: int, seed: int = 3):
+    """[256][1][lanes] instruction words: random valid instructions per lane,
+    branch and jump targets uniform over the ROM."""
+    import numpy as np
+
+    rng = Rng(seed)
+    rom = np.zeros((256, 1, lanes), dtype=np.uint32)
+    for lane in range(lanes):
+        for a in range(256):
+            op = rng.below(16)
+            rd, rs1, rs2 = rng.below(16), rng.below(16), rng.below(16)
+            imm = rng.below(256) if op in (13, 14, 15) else rng.below(1 << 16)
+            rom[a, 0, lane] = op | (rd << 4) | (rs1 << 8) | (rs2 << 12) | (imm << 16)
+    return rom

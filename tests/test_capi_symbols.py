@@ -1,0 +1,37 @@
+"""The C-ABI library loads on a host without a GPU and exports every entry
+point include/rrtl_cuda.h declares (no compute calls)."""
+import ctypes
+import os
+import re
+
+from rrtl_gb300 import build, sim
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "rrtl_cuda.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"^(?:rrtl_status|const char\*)\s+(rrtl_[a-z_0-9]+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    names = declared_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+    assert set(names) == set(sim.EXPORTS)
+
+
+def test_last_error_is_empty_before_any_call():
+    build.build()
+    assert sim.lib().rrtl_last_error() == b""
+
+
+def test_null_arguments_fail_with_codes_not_crashes():
+    build.build()
+    L = sim.lib()
+    assert L.rrtl_ctx_create(0, None) == 1  # RRTL_E_ARG: out is null
+    assert b"E_ARG" in L.rrtl_last_error()
+    assert L.rrtl_batch_eval(None) == 1
