@@ -13,8 +13,7 @@
 //
 // Parity pins (tests/test_oracle_golden.py): the reference's Counter known
 // answer [1,0,2,2] (crates/rrtl-gpu-sim/src/lib.rs:5763-5787), the crc32 gate
-// netlist against the CRC-32 algorithm (crates/rrtl-sim-ir/examples/netlist_crc32.rs),
-// the crc32 known answer 0xf7c3094b (crates/rrtl-sim-ir/examples/opencl_run.rs:54-74)
+// netlist against the CRC-32 algorithm (crates/rrtl-sim-ir/examples/netlist_crc32.rs)
 // and the stuck-at fault-sim coverage 64/64 with latency 1/6/2.1
 // (crates/rrtl-sim-ir/examples/fault_sim.rs; docs/rrtl-optimizations.md:1411-1416).
 #include <algorithm>
@@ -828,13 +827,14 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
     for (uint32_t q = 0; q < r->n_record; ++q) {
       const ValueLayout& L = P.signals[r->record[q]].layout;
       if (L.width == 1) {
+        // hash terms of 1-bit signals cover 32-lane packed words
         for (uint32_t w = 0; w < words; ++w) {
           uint32_t packed = 0;
           for (uint32_t b = 0; b < 32 && w * 32 + b < lanes; ++b) packed |= (s->values[s->vidx(L.offset, 0, w * 32 + b)] & 1u) << b;
-          if (r->record_mode & RRTL_REC_TRACE) r->out_trace[(c * r->n_record + q) * words + w] = packed;
           if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, w, packed);
         }
-      } else {
+      }
+      {
         for (uint32_t i = 0; i < L.limbs; ++i)
           for (uint32_t lane = 0; lane < lanes; ++lane) {
             uint32_t v = s->values[s->vidx(L.offset, i, lane)];
@@ -847,7 +847,7 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
               for (uint32_t q2 = 0; q2 < r->n_record; ++q2) total += (size_t)P.signals[r->record[q2]].layout.limbs;
               r->out_trace[(c * total + base + i) * lanes + lane] = v;
             }
-            if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, (uint64_t)lane * L.limbs + i, v);
+            if ((r->record_mode & RRTL_REC_HASH) && L.width != 1) h += o_hash_term(c, q, (uint64_t)lane * L.limbs + i, v);
           }
       }
     }

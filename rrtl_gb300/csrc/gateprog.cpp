@@ -384,7 +384,10 @@ GateProgram build_gate_program(const MachineProgram& mp) {
       free_general[res].pop_back();
       return s;
     }
-    while ((next_slot & 3) != res) free_general[next_slot & 3].push_back(next_slot++);
+    while ((next_slot & 3) != res) {
+      const uint32_t skipped = next_slot++;
+      free_general[skipped & 3].push_back(skipped);
+    }
     return next_slot++;
   };
 

@@ -43,8 +43,9 @@ RRTL_HD uint32_t stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, 
 }
 
 // One term of the per-cycle output hash. `idx` is the 32-lane word index for
-// 1-bit recorded signals and lane*limbs+limb for wider ones; the per-cycle
-// hash is the wrapping sum of all terms, so any evaluation order agrees.
+// 1-bit recorded signals (value = the packed word, lanes past the batch end
+// cleared) and lane*limbs+limb for wider ones; the per-cycle hash is the
+// wrapping sum of all terms, so any evaluation order and either engine agree.
 RRTL_HD uint64_t hash_term(uint64_t cycle, uint32_t rec, uint64_t idx, uint32_t value) {
   uint64_t salt = smix64((cycle << 20) ^ (uint64_t)rec ^ 0x5851F42D4C957F2Dull);
   return smix64((uint64_t)value ^ (idx << 32) ^ salt);

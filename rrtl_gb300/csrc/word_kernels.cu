@@ -172,9 +172,14 @@ __global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) 
           uint32_t v = R.values[(size_t)(rc.sig_off + l) * R.lanes_pad + lane];
           if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
           if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
+          if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
+            // 1-bit signals hash as 32-lane packed words, the gate engine's unit
+            const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
+            if ((threadIdx.x & 31u) == 0 && live) h += hash_term(ca, k, lane >> 5, packed);
+          }
           if (!live) continue;
           if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
-          if (R.mode & RRTL_REC_HASH) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
+          if ((R.mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
         }
       }
       if (R.mode & RRTL_REC_HASH) {
