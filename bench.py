@@ -131,7 +131,7 @@ def profiled_traffic(name):
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None, None
-    lanes = cycles = None
+    lanes = None
     traffic = None
     with open(p) as f:
         for line in f:
@@ -140,14 +140,12 @@ def profiled_traffic(name):
                 traffic = float(s.split(":", 1)[1])
             elif s.startswith("traffic_lanes:"):
                 lanes = int(s.split(":", 1)[1])
-            elif s.startswith("traffic_cycles:"):
-                cycles = int(s.split(":", 1)[1])
-    if traffic is None:
+    if traffic is None or not lanes:
         return None, None
-    return traffic, (lanes, cycles)
+    return traffic, lanes
 
 
-def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
+def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=15.0):
     """The reference's CPU engine restated (bit-parallel interpreter, 64 lanes
     per u64, lanes split over all host threads) on a bounded sample."""
     from oracle import binding as ob
@@ -160,7 +158,7 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
     t = time.perf_counter()
     ob.bp_run_parallel(od, lanes, run, threads)
     dt = max(time.perf_counter() - t, 1e-3)
-    cycles = max(1, min(1000, int(budget_s / dt)))
+    cycles = max(1, int(budget_s / dt))
     h = np.zeros(cycles, dtype=np.uint64)
     run = ob.make_run(cycles, SEED, stim_idx, rec_idx, 2, out_hash=h)
     t = time.perf_counter()
@@ -342,14 +340,19 @@ def main():
     bpl = net_stream_bytes_per_lane_cycle(gate_fanins(js), FFS, PIS, POS)
     algo_bytes = bpl * LANES * CYCLES
     achieved = algo_bytes / (ms_step / 1000.0) / 1e9
-    traffic, tshape = profiled_traffic("gate_fused_kernel_c2.md")
-    if traffic is not None and tshape[0]:
-        traffic = traffic * (LANES * CYCLES) / (tshape[0] * tshape[1])
+    # DRAM traffic of one launch grows with lanes (closing write-back of every
+    # net), not with cycles (per-cycle work stays in shared memory and L2)
+    traffic, tlanes = profiled_traffic("gate_fused_kernel_c2.md")
+    if traffic is not None:
+        traffic = traffic * LANES / tlanes
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                 else "fallback", "bytes_per_lane_cycle": bpl,
                 "model": "net-streaming bytes per lane-cycle (fanin reads + output write per gate, D read + Q write "
-                         "per flop, inputs and outputs), 4 bytes per 32 lanes"}
+                         "per flop, inputs and outputs), 4 bytes per 32 lanes",
+                "note": "nets stay in shared memory for all cycles of a tile, so measured DRAM traffic per launch "
+                        "(traffic) is far below the streamed bytes (achieved*time); the kernel is bound by SM issue "
+                        "and the shared-memory pipe, not HBM"}
     out = {
         "metric": METRIC, "value": value, "unit": "lane-cycles/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
