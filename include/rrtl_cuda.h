@@ -221,6 +221,33 @@ rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
  * context stream around the kernels of that call). */
 rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms);
 
+/* ---- allocation-free tick_many (word engine) -----------------------------
+ * No counterpart in the reference: it exists for callers that may not call
+ * cudaMalloc or cudaFree, such as a serving process that has divided device
+ * memory among tenants up front and forbids later allocations, or a
+ * latency-critical loop that cannot risk the implicit device synchronisation
+ * cudaFree (and at times cudaMalloc) performs.
+ *
+ * Runs tick_many(steps) of a word-engine design (settle, then per step
+ * capture, memory write, commit, settle) on lane state the caller owns:
+ *   values   device array [total_signal_words][lanes_pad] of u32
+ *   memories device array [total_memory_words_per_lane][lanes_pad] of u32
+ *            (may be NULL when the design has no memories)
+ * with lanes_pad = lanes rounded up to a multiple of 128; the word at
+ * [word][lane] is limb `word` of lane `lane` in the PackedSimulatorStorage
+ * order. The call allocates nothing: the register capture buffer it needs
+ * lives in a fixed device array of 2^20 u32 words that the library defines,
+ * so total capture words (one per register limb) x lanes_pad may not exceed
+ * 2^20; larger requests fail with RRTL_E_ARG (E_NOALLOC_SIZE). Every GPU that
+ * loads the library holds that array until the process exits. The first call
+ * on a device looks up the array's device address; make that first call
+ * before any stream capture begins. All calls share the array and it keeps
+ * the previous call's contents, which every call overwrites before reading;
+ * calls whose work overlaps on the GPU race on it. Runs on the design's
+ * context stream and returns after the work finishes. */
+rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* design, uint32_t* values, uint32_t* memories, uint32_t lanes,
+                                        uint64_t steps);
+
 #ifdef __cplusplus
 }
 #endif

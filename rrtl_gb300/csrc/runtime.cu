@@ -44,6 +44,11 @@ using namespace rrtl;
 
 static thread_local std::string g_last_error;
 
+namespace rrtl {
+// Error reporting for entry points defined outside this file.
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace rrtl
+
 template <class F>
 static rrtl_status guard(F&& f) {
   try {

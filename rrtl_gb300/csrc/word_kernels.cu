@@ -12,7 +12,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <string>
+
 #include "../../include/rrtl_cuda.h"
+#include "runtime.h"
 #include "stim.h"
 #include "word_dev.h"
 
@@ -217,4 +221,99 @@ cudaError_t word_prepare(size_t smem) {
   return cudaFuncSetAttribute(word_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free tick_many.
+//
+// Some callers cannot call cudaMalloc or cudaFree: a serving process that has
+// divided device memory among tenants up front and forbids any further
+// allocation, or a latency-critical loop that must not risk the implicit
+// device-wide synchronisation cudaFree (and at times cudaMalloc) performs.
+// rrtl_word_tick_many_noalloc serves them: the caller owns the lane state, and
+// the only scratch the kernel needs, the register capture buffer plus a status
+// word, lives in the fixed device array below.
+//
+// The array is file-scope device memory of fixed size, loaded with the
+// library and held by every GPU that loads it until the process exits. All
+// calls share it and it keeps the last call's contents; captures are written
+// before they are read every cycle and the status word is cleared at the
+// start of each call, so nothing else needs clearing. Two calls whose work
+// overlaps on the GPU (different streams, threads or contexts of the same
+// device) race on this array and corrupt each other's results.
+
+constexpr size_t kNoAllocScratchWords = (size_t)1 << 20;  // 4 MiB of capture words
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords + 64];
+
+void set_last_error(const std::string& msg);
+
+namespace {
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[64] = {};  // per-device address of g_noalloc_scratch
+
+// Host code cannot use the array's name as a device address; look the address
+// up once per device, with that device current.
+cudaError_t noalloc_scratch(int device, uint32_t** out) {
+  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[device] = static_cast<uint32_t*>(p);
+  }
+  *out = g_noalloc_ptr[device];
+  return cudaSuccess;
+}
+}  // namespace
+
 }  // namespace rrtl
+
+extern "C" rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* d, uint32_t* values, uint32_t* memories,
+                                                   uint32_t lanes, uint64_t steps) {
+  using namespace rrtl;
+  auto fail_with = [](rrtl_status st, const std::string& msg) {
+    set_last_error(msg);
+    return st;
+  };
+  if (!d || !values) return fail_with(RRTL_E_ARG, "E_ARG: null argument");
+  if (d->engine != RRTL_ENGINE_WORD) return fail_with(RRTL_E_UNSUPPORTED, "E_NOALLOC: the design runs on the gate engine");
+  if (lanes == 0) return fail_with(RRTL_E_LANES, "E_GPU_LANES: GPU simulator requires at least one lane");
+  if (steps >= (1ull << 32)) return fail_with(RRTL_E_ARG, "E_GPU_STEPS: tick_many step count exceeds 2^32");
+  if (d->mp.source.total_memory_words_per_lane > 0 && !memories) return fail_with(RRTL_E_ARG, "E_ARG: memories is null");
+  if ((size_t)d->wdev.n_vslots * 128u * 8u > 96u * 1024u)
+    return fail_with(RRTL_E_UNSUPPORTED, "E_WORD_SCOPE: design needs more live value slots than shared memory holds");
+  const uint32_t lanes_pad = (lanes + 127u) / 128u * 128u;
+  const size_t cap_words = (size_t)d->wp.total_capture_words * lanes_pad;
+  if (cap_words > kNoAllocScratchWords)
+    return fail_with(RRTL_E_ARG, "E_NOALLOC_SIZE: " + std::to_string(d->wp.total_capture_words) + " capture words x " +
+                                     std::to_string(lanes_pad) + " padded lanes exceed the fixed scratch of " +
+                                     std::to_string(kNoAllocScratchWords) + " words");
+  cudaError_t e = cudaSetDevice(d->ctx->device);
+  uint32_t* scratch = nullptr;
+  if (e == cudaSuccess) e = noalloc_scratch(d->ctx->device, &scratch);
+  if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: scratch lookup: ") + cudaGetErrorString(e));
+  uint32_t* status = scratch + kNoAllocScratchWords;
+  cudaStream_t st = d->ctx->stream;
+  e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: ") + cudaGetErrorString(e));
+  WordRunDev R{};
+  R.cycles = steps;
+  R.lanes = lanes;
+  R.lanes_pad = lanes_pad;
+  R.values = values;
+  R.mems = memories;
+  R.caps = scratch;
+  R.start_settle = 1;
+  R.final_settle = 1;
+  R.err = status;
+  if (steps > 0) {
+    e = launch_word(d->wdev, R, true, st);
+    if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: word_kernel: ") + cudaGetErrorString(e));
+  }
+  uint32_t err = 0;
+  e = cudaMemcpyAsync(&err, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: ") + cudaGetErrorString(e));
+  if (err) return fail_with((rrtl_status)err, "E_TIMEOUT: a bounded device wait gave up");
+  set_last_error("");
+  return RRTL_OK;
+}

@@ -122,6 +122,7 @@ EXPORTS = (
     "rrtl_batch_restore",
     "rrtl_batch_set_path",
     "rrtl_batch_last_kernel_ms",
+    "rrtl_word_tick_many_noalloc",
 )
 
 _lib = None
@@ -170,6 +171,7 @@ def lib():
         "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_path": [c_void_p, c_uint32],
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
+        "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
