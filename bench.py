@@ -248,6 +248,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--lanes", type=int, default=LANES, help="lanes per GPU (profiling cases)")
     ap.add_argument("--cycles", type=int, default=CYCLES, help="cycles per step (profiling cases)")
+    ap.add_argument("--tile-words", type=int, default=0, help="fused tile width in 32-lane words (0 = automatic)")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
     args.warmup = max(args.warmup, 3)
@@ -267,6 +268,7 @@ def main():
     cd = sim.CompiledDesign(js, meta.top, ctx)
     info = cd.info
     g = sim.GpuBatchSimulator(cd, lanes=LANES)
+    g.set_tile_words(args.tile_words)
     dev = torch.device("cuda", local)
     hash_dev = [torch.zeros(CYCLES, dtype=torch.int64, device=dev) for _ in range(args.steps + args.warmup)]
 
@@ -280,6 +282,7 @@ def main():
     for i in range(args.warmup):
         device_run(i)
     ctx.synchronize()
+    tile_words = g.tile_words
     if dist:
         dist.barrier()
     with ClockSampler(local) as clocks:
@@ -360,7 +363,8 @@ def main():
         "config": {"workload": f"gate netlist {GATES} gates / {FFS} FF / {PIS} PI / {POS} PO / depth {DEPTH} / "
                                f"window {WINDOW}", "lanes_per_gpu": LANES, "cycles_per_step": CYCLES,
                    "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective)",
-                   "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": "fused persistent kernel"},
+                   "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": "fused persistent kernel",
+                   "tile_words": tile_words},
         "gate_evals_per_s": value * info.n_gates,
         "design": {"gates": info.n_gates, "levels": info.n_levels, "nets": info.n_nets, "slots": info.n_slots,
                    "flops": info.n_regs},

@@ -217,6 +217,15 @@ rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv,
 enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1 };
 rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
 
+/* Gate engine, fused path: 32-lane words per tile (8, 4, 2 or 1; 0 = chosen
+ * per run from the design's level profile and the batch's size). A tile's
+ * nets occupy W words of shared memory each, so designs with many live nets
+ * run narrower tiles. No counterpart in the reference (an engine tuning knob).
+ * rrtl_batch_tile_words reports the width of the last fused run (0 after a
+ * run on the plain path). */
+rrtl_status rrtl_batch_set_tile_words(rrtl_batch* b, uint32_t words);
+rrtl_status rrtl_batch_tile_words(rrtl_batch* b, uint32_t* words);
+
 /* Device time of the last run/tick_many in milliseconds (CUDA events on the
  * context stream around the kernels of that call). */
 rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms);

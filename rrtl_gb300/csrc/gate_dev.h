@@ -23,7 +23,7 @@ struct GateRecDev {
 struct GateForceDev {
   uint32_t slot;
   uint32_t net;
-  uint32_t word;  // 0..7 inside the tile
+  uint32_t word;  // word inside the tile (fused tiles are W words, plain tiles 8)
   uint32_t mask;
   uint32_t val;
   uint32_t pad;
@@ -41,7 +41,7 @@ struct GatePieceDev {
 
 struct GateProgDev {
   // fused path (slots in shared memory)
-  const uint2* srecs;          // [groups*4] packed slot records (pack_smem_record)
+  const uint2* srecs;          // [groups*group] packed slot records (pack_smem_record)
   const GatePieceDev* pieces;
   const uint4* segs;           // {lut, begin, end, 0}: truth-table runs, group indices relative to the piece
   uint32_t n_pieces, n_slots, n_levels, piece_groups;
@@ -50,13 +50,14 @@ struct GateProgDev {
   const uint32_t* src_slot;
   uint32_t n_src;
   const GateRegDev* sregs;     // slot-based commit list
-  const uint32_t* wb_net;      // [groups*4] global net of each cell's signal output, or ~0
+  const uint32_t* wb_net;      // [groups*group] global net of each cell's signal output, or ~0
   // plain path (nets in HBM)
-  const uint4* grecs;          // [groups*4] {a, b, c, out | lut << 24}
+  const uint4* grecs;          // [groups*group] {a, b, c, out | lut << 24}
   const uint32_t* level_group_begin;  // [n_levels+1]
   const GateRegDev* gregs;     // net-based commit list
   uint32_t n_regs;
   uint32_t const0_slot, const1_slot;
+  uint32_t group;              // cells per group G = 32 / W, W = words per fused tile
 };
 
 struct GateRunDev {

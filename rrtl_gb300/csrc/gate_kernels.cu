@@ -4,17 +4,19 @@
 // cycle follows the run order documented in include/rrtl_cuda.h: stimulus,
 // settle (levels), record, register commit, register forces.
 //
-//  gate_fused_kernel  persistent: one CTA per SM walks 8-word tiles; a tile's
-//                     nets live in shared memory for all cycles, and the cell
-//                     records are streamed level piece by level piece from
-//                     HBM/L2 into a shared-memory ring by cp.async.bulk (TMA
-//                     bulk copy) with mbarrier completion.
-//  gate_plain_kernel  one launch per cycle; nets live in HBM, read and written
-//                     once per cell per cycle (the baseline path).
+//  gate_fused_kernel<W>  persistent: one CTA per SM walks tiles of W words; a
+//                        tile's nets live in shared memory for all cycles, and
+//                        the cell records are streamed level piece by level
+//                        piece from HBM/L2 into a shared-memory ring by
+//                        cp.async.bulk (TMA bulk copy) with mbarrier completion.
+//                        W = 8, 4, 2 or 1: a design with more live nets runs
+//                        narrower tiles so that its slots still fit on chip.
+//  gate_plain_kernel     one launch per cycle; nets live in HBM, read and
+//                        written once per cell per cycle (the baseline path).
 //
-// Warp layout: lane = 8*gsub + w; w is the word inside the tile and gsub picks
-// one of the four cells of a group. All cells of a group share one truth
-// table, so the table is warp-uniform and evaluates as one LOP3.
+// Fused warp layout: lane = W*gsub + w; w is the word inside the tile and gsub
+// picks one of the G = 32/W cells of a group. All cells of a group share one
+// truth table, so the table is warp-uniform and evaluates as one LOP3.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,15 +29,13 @@ namespace rrtl {
 constexpr int kFusedThreads = 1024;
 constexpr int kFusedWarps = kFusedThreads / 32;
 constexpr int kPlainThreads = 256;
-constexpr int kRing = 4;                 // record ring buffers
-constexpr uint32_t kSpinLimit = 1u << 22; // bounded mbarrier wait
+constexpr int kRing = 4;                  // record ring buffers
+constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier wait
 constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slot array
 #ifndef RRTL_FUSED_UNROLL
-#define RRTL_FUSED_UNROLL 2                // groups per unrolled step of a truth-table run
+#define RRTL_FUSED_UNROLL 2  // groups per unrolled step of a truth-table run
 #endif
-#ifndef RRTL_WARP_SPLIT
-#define RRTL_WARP_SPLIT 0                  // 0: contiguous group ranges per warp, 1: round robin
-#endif
+constexpr int kUnroll = RRTL_FUSED_UNROLL;
 static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -76,7 +76,7 @@ __device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
   return d;
 }
 
-// Runtime truth table (plain path): Shannon expansion on a, then b, then c.
+// Runtime truth table: Shannon expansion on a, then b, then c.
 __device__ __forceinline__ uint32_t lut_eval(uint32_t t, uint32_t a, uint32_t b, uint32_t c) {
   uint32_t m0 = 0u - (t & 1u), m1 = 0u - ((t >> 1) & 1u), m2 = 0u - ((t >> 2) & 1u), m3 = 0u - ((t >> 3) & 1u);
   uint32_t m4 = 0u - ((t >> 4) & 1u), m5 = 0u - ((t >> 5) & 1u), m6 = 0u - ((t >> 6) & 1u), m7 = 0u - ((t >> 7) & 1u);
@@ -105,47 +105,46 @@ __device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateR
   }
 }
 
+// Bytes of the fused kernel's slot array, rounded so the tables behind it
+// stay 16-byte aligned.
+__host__ __device__ __forceinline__ size_t fused_slot_bytes(uint32_t n_slots, uint32_t words) {
+  return ((size_t)n_slots * words * 4u + 15u) & ~(size_t)15u;
+}
+
 // ------------------------------------------------------------ fused path --
 
 // Evaluate groups [g, e) of one truth-table run. `rb` is this thread's record
 // in group 0 of the staged piece and `Sw` this thread's word column of the
 // slot array; both are shared memory, so every access below is an LDS/STS.
-constexpr int kStride = RRTL_WARP_SPLIT ? kFusedWarps : 1;
-constexpr int kUnroll = RRTL_FUSED_UNROLL;
-
-template <int L>
+template <int W, int L>
 __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw, int g, int e) {
+  constexpr int G = 32 / W;
   constexpr bool kUseA = (L & 0x0F) != ((L >> 4) & 0x0F);
   constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
   constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
 #pragma unroll kUnroll
-  for (; g < e; g += kStride) {
-    const uint2 r = rb[g * 4];
-    const uint32_t va = kUseA ? Sw[(r.x & 0xFFFFu) * 8u] : 0u;
-    const uint32_t vb = kUseB ? Sw[(r.x >> 16) * 8u] : 0u;
-    const uint32_t vc = kUseC ? Sw[(r.y & 0xFFFFu) * 8u] : 0u;
-    Sw[(r.y >> 16) * 8u] = lop3<L>(va, vb, vc);
+  for (; g < e; ++g) {
+    const uint2 r = rb[g * G];
+    const uint32_t va = kUseA ? Sw[(r.x & 0xFFFFu) * W] : 0u;
+    const uint32_t vb = kUseB ? Sw[(r.x >> 16) * W] : 0u;
+    const uint32_t vc = kUseC ? Sw[(r.y & 0xFFFFu) * W] : 0u;
+    Sw[(r.y >> 16) * W] = lop3<L>(va, vb, vc);
   }
 }
 
 #define RRTL_CASE(n) \
-  case n: run_seg<n>(rb, Sw, b, e); break;
+  case n: run_seg<W, n>(rb, Sw, b, e); break;
 #define RRTL_CASE4(n) RRTL_CASE(n) RRTL_CASE(n + 1) RRTL_CASE(n + 2) RRTL_CASE(n + 3)
 #define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
 #define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
 
 // This warp's share [g0, g1) of a piece, dispatched once per truth-table run.
+template <int W>
 __device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
                                            const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0, int g1) {
   for (uint32_t s = s0; s < s1; ++s) {
     const uint4 sg = segs[s];
-#if RRTL_WARP_SPLIT
-    // round robin: this warp takes groups g0, g0+32, ... (g1 = group count of the piece)
-    const int first = (int)sg.y + (((g0 - (int)sg.y) % kFusedWarps) + kFusedWarps) % kFusedWarps;
-    const int b = first, e = (int)sg.z;
-#else
     const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
-#endif
     if (b >= e) continue;
     switch (sg.x) {
       RRTL_CASE64(0)
@@ -159,57 +158,58 @@ __device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, uint32_
 
 // Final settle: same evaluation with a runtime truth table, plus a copy of
 // every signal net to the global state.
+template <int W>
 __device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
                                                      const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0,
                                                      int g1, const uint32_t* __restrict__ wb, uint32_t* nets,
                                                      size_t words_pad, uint32_t col) {
+  constexpr int G = 32 / W;
   for (uint32_t s = s0; s < s1; ++s) {
     const uint4 sg = segs[s];
-#if RRTL_WARP_SPLIT
-    const int b = (int)sg.y + (((g0 - (int)sg.y) % kFusedWarps) + kFusedWarps) % kFusedWarps, e = (int)sg.z;
-#else
     const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
-#endif
-    for (int g = b; g < e; g += kStride) {
-      const uint2 r = rb[g * 4];
-      const uint32_t v = lut_eval(sg.x, Sw[(r.x & 0xFFFFu) * 8u], Sw[(r.x >> 16) * 8u], Sw[(r.y & 0xFFFFu) * 8u]);
-      Sw[(r.y >> 16) * 8u] = v;
-      const uint32_t net = __ldg(wb + g * 4);
+    for (int g = b; g < e; ++g) {
+      const uint2 r = rb[g * G];
+      const uint32_t v = lut_eval(sg.x, Sw[(r.x & 0xFFFFu) * W], Sw[(r.x >> 16) * W], Sw[(r.y & 0xFFFFu) * W]);
+      Sw[(r.y >> 16) * W] = v;
+      const uint32_t net = __ldg(wb + g * G);
       if (net != 0xFFFFFFFFu) nets[(size_t)net * words_pad + col] = v;
     }
   }
 }
 
+template <int W>
 __device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, uint32_t tile, uint32_t stage,
                                              uint32_t stages) {
   const uint32_t* off = R.force_off + (size_t)tile * (stages + 1);
   uint32_t b = __ldg(off + stage), e = __ldg(off + stage + 1);
   for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
     GateForceDev f = R.forces[i];
-    uint32_t& v = S[f.slot * 8 + f.word];
+    uint32_t& v = S[f.slot * W + f.word];
     v = (v & ~f.mask) | (f.val & f.mask);
   }
 }
 
+template <int W>
 __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDev P, GateRunDev R) {
+  constexpr uint32_t G = 32 / W;
   extern __shared__ __align__(128) uint8_t smem[];
-  const uint32_t piece_bytes = P.piece_groups * 32u;
+  const size_t ring_stride = (size_t)P.piece_groups * G;  // uint2 records per ring buffer
   // layout: [record ring][128-byte header: 4 mbarriers, hash accumulator,
   // detect state][slots][piece table][segment table]; every region after the
   // ring starts on a 16-byte boundary (the segment table is read as uint4)
   uint2* ring = reinterpret_cast<uint2*>(smem);
-  uint8_t* hdr = smem + (size_t)kRing * piece_bytes;
+  uint8_t* hdr = smem + (size_t)kRing * ring_stride * 8u;
   uint64_t* bars = reinterpret_cast<uint64_t*>(hdr);
   unsigned long long* hacc = reinterpret_cast<unsigned long long*>(hdr + kRing * 8);
   uint32_t* dstate = reinterpret_cast<uint32_t*>(hdr + kRing * 8 + 8);  // diff[8], detected[8]
   uint32_t* S = reinterpret_cast<uint32_t*>(hdr + kFusedHeader);
   // piece and segment tables, staged once per launch
-  GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(S + (size_t)P.n_slots * 8);
+  GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(hdr + kFusedHeader + fused_slot_bytes(P.n_slots, W));
   uint4* segs = reinterpret_cast<uint4*>(pieces + P.n_pieces);
   __shared__ int s_abort;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t w = lane & 7u, gsub = lane >> 3;
+  const uint32_t w = lane % W, gsub = lane / W;
   const bool resident = P.n_pieces <= (uint32_t)kRing;
   const uint32_t stages = P.n_levels + 1;
 
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
     uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
     for (uint64_t q = 0; q < n0; ++q) {
       const GatePieceDev pc = P.pieces[q % P.n_pieces];
-      bulk_load(ring + (size_t)(q % kRing) * P.piece_groups * 4, P.srecs + (size_t)pc.group_begin * 4, pc.n_groups * 32u,
+      bulk_load(ring + (q % kRing) * ring_stride, P.srecs + (size_t)pc.group_begin * G, pc.n_groups * G * 8u,
                 &bars[q % kRing]);
     }
   }
@@ -243,8 +243,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   // publishes them to every thread. The wait for piece q+1 is folded into the
   // barrier that closes piece q, so each piece costs one barrier.
   auto wait_piece = [&](uint64_t qq) {
-    if (qq >= total_q && resident) return;
-    if (!resident && qq >= total_q) return;
+    if (qq >= total_q) return;
     if (resident && qq >= P.n_pieces) return;
     uint32_t buf = resident ? (uint32_t)qq : (uint32_t)(qq % kRing);
     uint32_t par = resident ? 0u : (uint32_t)((qq / kRing) & 1u);
@@ -257,18 +256,17 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   __syncthreads();
 
   for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !s_abort; tile += gridDim.x) {
-    const uint32_t col0 = tile * 8u;
+    const uint32_t col0 = tile * W;
     // constants, scratch, sources
-    for (uint32_t i = tid; i < 8u; i += blockDim.x) {
-      S[0 * 8 + i] = 0u;
-      S[P.const0_slot * 8 + i] = 0u;
-      S[P.const1_slot * 8 + i] = 0xFFFFFFFFu;
-      dstate[i] = 0u;
-      dstate[8 + i] = 0u;
+    for (uint32_t i = tid; i < W; i += blockDim.x) {
+      S[0 * W + i] = 0u;
+      S[P.const0_slot * W + i] = 0u;
+      S[P.const1_slot * W + i] = 0xFFFFFFFFu;
     }
-    for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
-      uint32_t k = i >> 3, ww = i & 7u;
-      S[__ldg(P.src_slot + k) * 8 + ww] = R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww];
+    if (tid < 16u) dstate[tid] = 0u;
+    for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
+      uint32_t k = i / W, ww = i % W;
+      S[__ldg(P.src_slot + k) * W + ww] = R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww];
     }
     __syncthreads();
 
@@ -278,16 +276,16 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       if (final_pass) {
         // register slots may host other nets during a settle: write the
         // sources back before the final settle recomputes every signal
-        for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
-          uint32_t k = i >> 3, ww = i & 7u;
-          R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * 8 + ww];
+        for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
+          uint32_t k = i / W, ww = i % W;
+          R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * W + ww];
         }
       } else {
-        for (uint32_t i = tid; i < R.n_stim * 8u; i += blockDim.x) {
-          const GateStimDev& s = R.stim[i >> 3];
+        for (uint32_t i = tid; i < R.n_stim * W; i += blockDim.x) {
+          const GateStimDev& s = R.stim[i / W];
           if (s.kind == RRTL_STIM_HOLD) continue;
-          uint32_t ww = i & 7u;
-          uint32_t& slot = S[s.slot * 8 + ww];
+          uint32_t ww = i % W;
+          uint32_t& slot = S[s.slot * W + ww];
           slot = stim_value(s, R, c, col0 + ww, slot);
         }
       }
@@ -295,20 +293,16 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
         const GatePieceDev pc = pieces[p];
         const uint32_t buf = resident ? p : (uint32_t)(q % kRing);
-        const uint2* rb = ring + (size_t)buf * P.piece_groups * 4 + gsub;
-#if RRTL_WARP_SPLIT
-        const int g0 = (int)warp, g1 = (int)pc.n_groups;
-#else
+        const uint2* rb = ring + buf * ring_stride + gsub;
         const int g0 = (int)((pc.n_groups * warp) / kFusedWarps), g1 = (int)((pc.n_groups * (warp + 1)) / kFusedWarps);
-#endif
         if (final_pass)
-          eval_piece_writeback(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1, P.wb_net + (size_t)pc.group_begin * 4 + gsub,
-                               R.nets, R.words_pad, col0 + w);
+          eval_piece_writeback<W>(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1,
+                                  P.wb_net + (size_t)pc.group_begin * G + gsub, R.nets, R.words_pad, col0 + w);
         else
-          eval_piece(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1);
+          eval_piece<W>(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1);
         if (pc.last_of_level && R.has_forces) {
           __syncthreads();
-          apply_forces(R, S, tile, pc.level + 1, stages);
+          apply_forces<W>(R, S, tile, pc.level + 1, stages);
         }
         if (tid == 0) wait_piece(q + 1);
         __syncthreads();
@@ -316,7 +310,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
         if (!resident && tid == 0 && q + kRing < total_q) {
           uint64_t nq = q + kRing;
           const GatePieceDev npc = pieces[nq % P.n_pieces];
-          bulk_load(ring + (size_t)buf * P.piece_groups * 4, P.srecs + (size_t)npc.group_begin * 4, npc.n_groups * 32u,
+          bulk_load(ring + buf * ring_stride, P.srecs + (size_t)npc.group_begin * G, npc.n_groups * G * 8u,
                     &bars[buf]);
         }
       }
@@ -325,9 +319,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       // record
       if (R.n_rec) {
         unsigned long long h = 0ull;
-        for (uint32_t i = tid; i < R.n_rec * 8u; i += blockDim.x) {
-          uint32_t k = i >> 3, ww = i & 7u, gw = col0 + ww;
-          uint32_t v = S[R.rec[k].slot * 8 + ww] & valid_mask(gw, R.lanes);
+        for (uint32_t i = tid; i < R.n_rec * W; i += blockDim.x) {
+          uint32_t k = i / W, ww = i % W, gw = col0 + ww;
+          uint32_t v = S[R.rec[k].slot * W + ww] & valid_mask(gw, R.lanes);
           if (gw < R.words) {
             if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
             if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
@@ -344,7 +338,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
           if (t) atomicAdd(R.out_hash + c, t);
           *hacc = 0ull;
         }
-        if ((R.mode & RRTL_REC_DETECT) && tid < 8u) {
+        if ((R.mode & RRTL_REC_DETECT) && tid < W) {
           uint32_t gw = col0 + tid;
           uint32_t nb = dstate[tid] & ~dstate[8 + tid] & valid_mask(gw, R.lanes);
           dstate[8 + tid] |= nb;
@@ -357,29 +351,29 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
         }
       }
       // commit (D and reset nets are never register nets, so one pass is safe)
-      for (uint32_t i = tid; i < P.n_regs * 8u; i += blockDim.x) {
-        GateRegDev r = P.sregs[i >> 3];
-        uint32_t ww = i & 7u;
-        uint32_t d = S[r.d * 8 + ww];
+      for (uint32_t i = tid; i < P.n_regs * W; i += blockDim.x) {
+        GateRegDev r = P.sregs[i / W];
+        uint32_t ww = i % W;
+        uint32_t d = S[r.d * W + ww];
         if (r.flags & 1u) {
-          uint32_t m = S[r.rst * 8 + ww];
+          uint32_t m = S[r.rst * W + ww];
           if (r.flags & 2u) m = ~m;
           uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
           d = (m & rv) | (~m & d);
         }
-        S[r.q * 8 + ww] = d;
+        S[r.q * W + ww] = d;
       }
       __syncthreads();
       if (R.has_forces) {
-        apply_forces(R, S, tile, 0, stages);
+        apply_forces<W>(R, S, tile, 0, stages);
         __syncthreads();
       }
     }
     if (s_abort) break;
     if (!R.final_settle) {
-      for (uint32_t i = tid; i < P.n_src * 8u; i += blockDim.x) {
-        uint32_t k = i >> 3, ww = i & 7u;
-        R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * 8 + ww];
+      for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
+        uint32_t k = i / W, ww = i % W;
+        R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * W + ww];
       }
     }
     __syncthreads();
@@ -395,7 +389,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
 
 // ------------------------------------------------------------ plain path --
 
-// One launch = one cycle (phase 0) or one settle with no stimulus/commit (phase 1).
+// One launch = one cycle (phase 0) or one settle with no stimulus/commit
+// (phase 1). Tiles are 8 words; a warp evaluates 4 consecutive cells x 8
+// words (a group of G >= 4 cells is G/4 such quads).
 __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P, GateRunDev R, uint64_t c,
                                                                     int phase) {
   __shared__ unsigned long long hacc;
@@ -406,6 +402,7 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
   uint32_t* G = R.nets;
   const size_t wp = R.words_pad;
   const uint32_t stages = P.n_levels + 1;
+  const uint32_t quads_per_group = P.group / 4u;
   if (tid == 0) hacc = 0ull;
   if (tid < 8) diff[tid] = 0u;
   if (phase == 0) {
@@ -419,9 +416,9 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
   }
   __syncthreads();
   for (uint32_t L = 0; L < P.n_levels; ++L) {
-    uint32_t g0 = P.level_group_begin[L], g1 = P.level_group_begin[L + 1];
-    for (uint32_t g = g0 + warp; g < g1; g += nwarps) {
-      uint4 r = P.grecs[(size_t)g * 4 + gsub];
+    uint32_t q0 = P.level_group_begin[L] * quads_per_group, q1 = P.level_group_begin[L + 1] * quads_per_group;
+    for (uint32_t qd = q0 + warp; qd < q1; qd += nwarps) {
+      uint4 r = P.grecs[(size_t)qd * 4 + gsub];
       uint32_t va = G[(size_t)r.x * wp + col], vb = G[(size_t)r.y * wp + col], vc = G[(size_t)r.z * wp + col];
       G[(size_t)(r.w & 0xFFFFFFu) * wp + col] = lut_eval(r.w >> 24, va, vb, vc);
     }
@@ -492,18 +489,36 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
 // ------------------------------------------------------------- launchers --
 
 size_t gate_fused_smem_bytes(const GateProgDev& P) {
-  return (size_t)kRing * P.piece_groups * 32u + kFusedHeader + (size_t)P.n_slots * 8u * 4u +
+  const uint32_t G = P.group, W = 32u / P.group;
+  return (size_t)kRing * P.piece_groups * G * 8u + kFusedHeader + fused_slot_bytes(P.n_slots, W) +
          (size_t)P.n_pieces * sizeof(GatePieceDev) + (size_t)P.n_segs * 16u;
 }
 static_assert(sizeof(GatePieceDev) == 32, "piece descriptor layout");
 
-cudaError_t gate_fused_prepare(size_t smem) {
-  return cudaFuncSetAttribute(gate_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+template <int W>
+static cudaError_t fused_prepare_w(size_t smem) {
+  return cudaFuncSetAttribute(gate_fused_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t gate_fused_prepare(const GateProgDev& P, size_t smem) {
+  switch (P.group) {
+    case 4: return fused_prepare_w<8>(smem);
+    case 8: return fused_prepare_w<4>(smem);
+    case 16: return fused_prepare_w<2>(smem);
+    case 32: return fused_prepare_w<1>(smem);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem,
                               cudaStream_t st) {
-  gate_fused_kernel<<<grid, kFusedThreads, smem, st>>>(P, R);
+  switch (P.group) {
+    case 4: gate_fused_kernel<8><<<grid, kFusedThreads, smem, st>>>(P, R); break;
+    case 8: gate_fused_kernel<4><<<grid, kFusedThreads, smem, st>>>(P, R); break;
+    case 16: gate_fused_kernel<2><<<grid, kFusedThreads, smem, st>>>(P, R); break;
+    case 32: gate_fused_kernel<1><<<grid, kFusedThreads, smem, st>>>(P, R); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

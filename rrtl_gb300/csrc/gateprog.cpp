@@ -210,9 +210,14 @@ struct Builder {
 
 }  // namespace
 
-GateProgram build_gate_program(const MachineProgram& mp) {
+GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   const PackedProgram& P = mp.source;
   GateProgram gp;
+  if (tile_words != 8 && tile_words != 4 && tile_words != 2 && tile_words != 1)
+    throw RrtlError("E_GATE_SCOPE", "tile width must be 1, 2, 4 or 8 words");
+  gp.tile_words = tile_words;
+  gp.group = 32 / tile_words;
+  const uint32_t G = gp.group;
   for (auto& s : P.signals)
     if (s.layout.width != 1) throw RrtlError("E_GATE_SCOPE", "signal `" + s.name + "` is wider than 1 bit");
   if (!P.memories.empty()) throw RrtlError("E_GATE_SCOPE", "memories are outside the gate engine");
@@ -337,10 +342,10 @@ GateProgram build_gate_program(const MachineProgram& mp) {
   auto end_live = [&](uint32_t n) { return std::max(last_use[n], gp.net_level[n]) >= kEnd; };
 
   // ---- on-chip slots
-  // Slot s occupies banks 8*(s%4)..8*(s%4)+7 of every 32-bank row pair (8
-  // words per slot), so the four cells of a group conflict only when two of
-  // their operand rows share s%4. Cells are grouped to spread operand rows
-  // over the four residues and each group's outputs get distinct residues.
+  // With W words per slot, slot s occupies banks W*(s%G) .. W*(s%G)+W-1 of the
+  // 32 banks (G = 32/W), so the G cells of a group conflict only when two of
+  // their operand rows share s%G. Cells are grouped to spread operand rows
+  // over the residues and each group's outputs get distinct residues.
   //
   // Registers are rewritten by every commit, so between a register's last
   // read in the settle and the commit its slot can host nets that die before
@@ -368,10 +373,10 @@ GateProgram build_gate_program(const MachineProgram& mp) {
     int32_t lu = std::max(last_use[n], gp.net_level[n]);
     if (lu < kEnd) dying[lu].push_back(n);
   }
-  std::vector<uint32_t> free_general[4], free_q[4];
+  std::vector<std::vector<uint32_t>> free_general(G), free_q(G);
   auto release = [&](uint32_t s) {
     bool q = s < slot_is_q.size() && slot_is_q[s];
-    (q ? free_q : free_general)[s & 3].push_back(s);
+    (q ? free_q : free_general)[s % G].push_back(s);
   };
   auto take = [&](bool live_to_end, uint32_t res) -> uint32_t {
     if (!live_to_end && !free_q[res].empty()) {
@@ -384,9 +389,9 @@ GateProgram build_gate_program(const MachineProgram& mp) {
       free_general[res].pop_back();
       return s;
     }
-    while ((next_slot & 3) != res) {
+    while (next_slot % G != res) {
       const uint32_t skipped = next_slot++;
-      free_general[skipped & 3].push_back(skipped);
+      free_general[skipped % G].push_back(skipped);
     }
     return next_slot++;
   };
@@ -396,11 +401,15 @@ GateProgram build_gate_program(const MachineProgram& mp) {
   std::vector<GateCell> grouped;
   gp.level_group_begin.assign(gp.n_levels + 1, 0);
   const int kLook = 48;
+  // per operand position: distinct rows per residue in the group being built
+  std::vector<uint32_t> cnt(3 * G);
+  std::vector<uint32_t> stamp(3 * (size_t)65536, 0);
+  uint32_t group_id = 0;
   for (uint32_t L = 0; L < gp.n_levels; ++L) {
     for (uint32_t s : q_free_after[L]) release(s);
     if (L > 0)
       for (uint32_t n : dying[L - 1]) release((uint32_t)gp.net_slot[n]);
-    gp.level_group_begin[L] = (uint32_t)(grouped.size() / kGroup);
+    gp.level_group_begin[L] = (uint32_t)(grouped.size() / G);
     std::vector<uint32_t>& cs = cells_at[L];
     std::stable_sort(cs.begin(), cs.end(), [&](uint32_t x, uint32_t y) { return gp.cells[x].lut < gp.cells[y].lut; });
     for (size_t i = 0; i < cs.size();) {
@@ -412,30 +421,39 @@ GateProgram build_gate_program(const MachineProgram& mp) {
       std::vector<uint32_t> rem(cs.begin() + i, cs.begin() + j);
       size_t head = 0;
       std::vector<uint8_t> taken(rem.size(), 0);
+      auto slot_in = [&](uint32_t cell, int p) { return (uint32_t)gp.net_slot[gp.cells[cell].in[p]]; };
       while (head < rem.size()) {
         while (head < rem.size() && taken[head]) ++head;
         if (head == rem.size()) break;
+        ++group_id;
+        std::fill(cnt.begin(), cnt.end(), 0u);
+        auto add = [&](uint32_t cell) {
+          for (int p = 0; p < 3; ++p) {
+            if (!use[p]) continue;
+            uint32_t sl = slot_in(cell, p);
+            uint32_t& st = stamp[(size_t)p * 65536 + (sl & 0xFFFF)];
+            if (st == group_id) continue;  // row already read by this group: broadcast
+            st = group_id;
+            cnt[p * G + sl % G]++;
+          }
+        };
         std::vector<uint32_t> grp{rem[head]};
         taken[head] = 1;
+        add(rem[head]);
         // greedy: add the candidate that adds the fewest operand-row conflicts
-        for (uint32_t pick = 1; pick < kGroup; ++pick) {
-          int best = -1, best_cost = 1 << 30;
+        for (uint32_t pick = 1; pick < G; ++pick) {
+          int best = -1;
+          uint32_t best_cost = ~0u;
           int seen = 0;
           for (size_t k = head + 1; k < rem.size() && seen < kLook; ++k) {
             if (taken[k]) continue;
             ++seen;
-            int cost = 0;
+            uint32_t cost = 0;
             for (int p = 0; p < 3; ++p) {
               if (!use[p]) continue;
-              uint32_t cand = (uint32_t)gp.net_slot[gp.cells[rem[k]].in[p]];
-              int same = 0;
-              bool dup = false;
-              for (uint32_t m : grp) {
-                uint32_t sl = (uint32_t)gp.net_slot[gp.cells[m].in[p]];
-                if (sl == cand) dup = true;
-                else if ((sl & 3) == (cand & 3)) ++same;
-              }
-              if (!dup) cost += same;
+              uint32_t sl = slot_in(rem[k], p);
+              if (stamp[(size_t)p * 65536 + (sl & 0xFFFF)] == group_id) continue;
+              cost += cnt[p * G + sl % G];
             }
             if (cost < best_cost) {
               best_cost = cost;
@@ -446,17 +464,18 @@ GateProgram build_gate_program(const MachineProgram& mp) {
           if (best < 0) break;
           grp.push_back(rem[best]);
           taken[best] = 1;
+          add(rem[best]);
         }
         // outputs: distinct residues; residue 0 last when padding (scratch slot 0) shares the group
-        const bool padded = grp.size() < kGroup;
-        const uint32_t order[4] = {padded ? 1u : 0u, padded ? 2u : 1u, padded ? 3u : 2u, padded ? 0u : 3u};
+        const bool padded = grp.size() < G;
         for (size_t k = 0; k < grp.size(); ++k) {
           GateCell c = gp.cells[grp[k]];
-          gp.net_slot[c.out] = (int32_t)take(end_live(c.out), order[k]);
+          const uint32_t res = (uint32_t)((k + (padded ? 1 : 0)) % G);
+          gp.net_slot[c.out] = (int32_t)take(end_live(c.out), res);
           if (slot_is_q.size() <= (size_t)gp.net_slot[c.out]) slot_is_q.resize(gp.net_slot[c.out] + 1, 0);
           grouped.push_back(c);
         }
-        while (grouped.size() % kGroup) {
+        while (grouped.size() % G) {
           GateCell pad;
           pad.lut = lut;
           pad.level = (int32_t)L;
@@ -468,7 +487,7 @@ GateProgram build_gate_program(const MachineProgram& mp) {
       i = j;
     }
   }
-  gp.level_group_begin[gp.n_levels] = (uint32_t)(grouped.size() / kGroup);
+  gp.level_group_begin[gp.n_levels] = (uint32_t)(grouped.size() / G);
   gp.cells = std::move(grouped);
   for (uint32_t n = 0; n < gp.n_nets; ++n) gp.net_end_live.push_back(end_live(n) ? 1 : 0);
   for (uint32_t n = 0; n < gp.n_nets; ++n)
@@ -496,8 +515,8 @@ void build_pieces(GateProgram& gp, uint32_t piece_groups) {
       pc.seg_begin = (uint32_t)gp.segments.size();
       for (uint32_t g = pc.group_begin; g < end;) {
         uint32_t h = g;
-        uint8_t lut = gp.cells[(size_t)g * kGroup].lut;
-        while (h < end && gp.cells[(size_t)h * kGroup].lut == lut) ++h;
+        uint8_t lut = gp.cells[(size_t)g * gp.group].lut;
+        while (h < end && gp.cells[(size_t)h * gp.group].lut == lut) ++h;
         gp.segments.push_back(GateSegment{lut, g - pc.group_begin, h - pc.group_begin});
         g = h;
       }

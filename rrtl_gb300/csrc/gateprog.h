@@ -15,10 +15,12 @@
 //  2. Register next-state expressions (tick_next) become cells too; their
 //     outputs are the D nets read by the commit.
 //  3. Cells are levelized (level = 1 + deepest input producer) and, within a
-//     level, sorted by truth table and padded to groups of kGroup cells that
-//     share one table, so a warp evaluates one table per group.
+//     level, sorted by truth table and padded to groups of G = 32/W cells that
+//     share one table, W being the words per tile (8, 4, 2 or 1): a warp
+//     evaluates one group, G cells x W words, with one truth table.
 //  4. Nets get on-chip slots by liveness over the level order; sources
-//     (inputs, registers, constants) keep permanent slots.
+//     (inputs, constants) keep permanent slots, registers keep theirs except
+//     between their last read and the commit.
 #pragma once
 
 #include <cstdint>
@@ -29,8 +31,7 @@
 
 namespace rrtl {
 
-constexpr uint32_t kGroup = 4;        // cells per warp group (32 lanes / 8 words)
-constexpr uint32_t kTileWords = 8;    // 32-lane words per CTA tile in the fused kernel
+constexpr uint32_t kPadWords = 8;     // net rows are padded to a multiple of 8 words (plain-kernel tile)
 constexpr uint32_t kNetConst0 = 0;    // all-zero net
 constexpr uint32_t kNetConst1 = 1;    // all-ones net
 constexpr uint32_t kMaxSlots = 65535; // 16-bit slot fields in packed records
@@ -67,6 +68,8 @@ struct GateSegment {
 };
 
 struct GateProgram {
+  uint32_t tile_words = 8;              // W: 32-lane words per tile in the fused kernel
+  uint32_t group = 4;                   // G = 32 / W cells per group
   uint32_t n_signals = 0;
   uint32_t n_nets = 0;                  // global net array rows
   std::vector<uint32_t> signal_net;     // packed signal -> net
@@ -90,7 +93,7 @@ struct GateProgram {
 };
 
 // Throws RrtlError("E_GATE_SCOPE", ...) when the program is outside the gate engine's scope.
-GateProgram build_gate_program(const MachineProgram& mp);
+GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words = 8);
 
 // Split every level into nearly equal pieces of at most `piece_groups` groups
 // and record the truth-table runs of each piece.

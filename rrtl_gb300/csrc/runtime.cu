@@ -4,6 +4,7 @@
 #include "runtime.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 
@@ -11,7 +12,7 @@ namespace rrtl {
 
 // kernels (gate_kernels.cu, word_kernels.cu)
 size_t gate_fused_smem_bytes(const GateProgDev& P);
-cudaError_t gate_fused_prepare(size_t smem);
+cudaError_t gate_fused_prepare(const GateProgDev& P, size_t smem);
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st);
 cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st);
@@ -89,9 +90,22 @@ const PackedSignal& signal_of(rrtl_design* d, uint32_t s) {
   return d->mp.source.signals[s];
 }
 
-void upload_gate_program(rrtl_design* d) {
-  const GateProgram& gp = d->gp;
-  uint32_t n_groups = (uint32_t)(gp.cells.size() / kGroup);
+constexpr uint32_t kRingBufs = 4;  // record ring buffers of the fused kernel
+
+uint32_t log2_words(uint32_t W) { return W == 8 ? 3u : W == 4 ? 2u : W == 2 ? 1u : 0u; }
+
+// Build and upload the gate program for fused tile width W. The fused path
+// needs the slots (W words each), a 4-deep record ring and the piece/segment
+// tables in one CTA's shared memory; pieces take what the slots leave (up to
+// 512 groups) and shrink until the tables fit too.
+GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
+  uint32_t li = log2_words(W);
+  if (d->gvar[li]) return d->gvar[li].get();
+  auto v = std::make_unique<GateVariant>();
+  v->W = W;
+  v->gp = build_gate_program(d->mp, W);
+  GateProgram& gp = v->gp;
+  const uint32_t G = gp.group;
   REQUIRE(gp.n_nets + 1 < (1u << 24), RRTL_E_UNSUPPORTED, "E_GATE_SCOPE: more than 16M nets");
   const uint32_t scratch_net = gp.n_nets;  // extra row for padding cells
   std::vector<uint4> grecs(gp.cells.size());
@@ -107,35 +121,33 @@ void upload_gate_program(rrtl_design* d) {
     uint32_t fl = (r.has_reset ? 1u : 0u) | (r.active_low ? 2u : 0u) | (r.reset_value ? 4u : 0u);
     gregs.push_back(GateRegDev{r.q_net, r.d_net, r.rst_net, fl});
   }
-  upload(d->d_grecs, grecs);
-  upload(d->d_wb, wb);
-  upload(d->d_lgb, gp.level_group_begin);
-  upload(d->d_gregs, gregs);
+  upload(v->d_grecs, grecs);
+  upload(v->d_wb, wb);
+  upload(v->d_lgb, gp.level_group_begin);
+  upload(v->d_gregs, gregs);
 
-  // fused program: slots and a 4-deep record ring must fit shared memory;
-  // pieces take whatever the slots leave (up to 1024 groups per piece)
-  // the piece/segment tables (staged in shared memory too) depend on the piece
-  // size, so shrink pieces until everything fits
-  size_t slot_bytes = (size_t)gp.n_slots * kTileWords * 4 + 256;
-  d->fused_ok = gp.n_slots <= kMaxSlots && slot_bytes + 4 * 32 * 32 <= d->ctx->max_smem;
-  uint32_t piece_groups = 32;
-  if (d->fused_ok) {
-    size_t per_buf = (d->ctx->max_smem - slot_bytes) / 4;
-    piece_groups = (uint32_t)std::min<size_t>(512, per_buf / 32) & ~7u;
+  const size_t max_smem = d->ctx->max_smem;
+  const size_t slot_bytes = (((size_t)gp.n_slots * W * 4 + 15) & ~(size_t)15) + 128;  // slots + header
+  const size_t group_bytes = (size_t)G * 8;                                           // records of one group
+  v->fused_ok = gp.n_slots <= kMaxSlots && slot_bytes + kRingBufs * 8 * group_bytes <= max_smem;
+  uint32_t piece_groups = 8;
+  if (v->fused_ok) {
+    size_t per_buf = (max_smem - slot_bytes) / kRingBufs;
+    piece_groups = (uint32_t)std::min<size_t>(512, per_buf / group_bytes) & ~7u;
     for (;;) {
-      build_pieces(d->gp, piece_groups);
+      build_pieces(gp, piece_groups);
       size_t tables = gp.pieces.size() * sizeof(GatePieceDev) + gp.segments.size() * 16;
-      if (slot_bytes + tables + (size_t)4 * piece_groups * 32 <= d->ctx->max_smem) break;
-      if (piece_groups <= 32) {
-        d->fused_ok = false;
+      if (slot_bytes + tables + (size_t)kRingBufs * piece_groups * group_bytes <= max_smem) break;
+      if (piece_groups <= 8) {
+        v->fused_ok = false;
         break;
       }
-      piece_groups -= 32;
+      piece_groups -= 8;
     }
   } else {
-    build_pieces(d->gp, 256);
+    build_pieces(gp, 256);
   }
-  if (d->fused_ok) {
+  if (v->fused_ok) {
     std::vector<uint2> srecs(gp.cells.size());
     int32_t c0 = gp.net_slot[kNetConst0];
     for (size_t i = 0; i < gp.cells.size(); ++i) {
@@ -157,45 +169,97 @@ void upload_gate_program(rrtl_design* d) {
       sregs.push_back(GateRegDev{(uint32_t)gp.net_slot[r.q_net], (uint32_t)gp.net_slot[r.d_net],
                                  (uint32_t)gp.net_slot[r.rst_net], fl});
     }
-    upload(d->d_srecs, srecs);
-    upload(d->d_pieces, pieces);
-    upload(d->d_segs, segs);
-    upload(d->d_src_net, gp.source_nets);
-    upload(d->d_src_slot, src_slot);
-    upload(d->d_sregs, sregs);
+    upload(v->d_srecs, srecs);
+    upload(v->d_pieces, pieces);
+    upload(v->d_segs, segs);
+    upload(v->d_src_net, gp.source_nets);
+    upload(v->d_src_slot, src_slot);
+    upload(v->d_sregs, sregs);
   }
-  GateProgDev& G = d->gdev;
-  G = GateProgDev{};
-  G.srecs = d->d_srecs.as<uint2>();
-  G.pieces = d->d_pieces.as<GatePieceDev>();
-  G.segs = d->d_segs.as<uint4>();
-  G.n_segs = (uint32_t)gp.segments.size();
-  G.n_pieces = (uint32_t)gp.pieces.size();
-  G.n_slots = gp.n_slots;
-  G.n_levels = gp.n_levels;
-  G.piece_groups = piece_groups;
-  G.src_net = d->d_src_net.as<uint32_t>();
-  G.src_slot = d->d_src_slot.as<uint32_t>();
-  G.n_src = (uint32_t)gp.source_nets.size();
-  G.sregs = d->d_sregs.as<GateRegDev>();
-  G.wb_net = d->d_wb.as<uint32_t>();
-  G.grecs = d->d_grecs.as<uint4>();
-  G.level_group_begin = d->d_lgb.as<uint32_t>();
-  G.gregs = d->d_gregs.as<GateRegDev>();
-  G.n_regs = (uint32_t)gp.regs.size();
-  G.const0_slot = d->fused_ok ? (uint32_t)gp.net_slot[kNetConst0] : 0;
-  G.const1_slot = d->fused_ok ? (uint32_t)gp.net_slot[kNetConst1] : 0;
-  (void)n_groups;
-  if (d->fused_ok) {
-    d->fused_smem = gate_fused_smem_bytes(G);
-    if (d->fused_smem > d->ctx->max_smem) {
-      d->fused_ok = false;
+  GateProgDev& P = v->gdev;
+  P = GateProgDev{};
+  P.srecs = v->d_srecs.as<uint2>();
+  P.pieces = v->d_pieces.as<GatePieceDev>();
+  P.segs = v->d_segs.as<uint4>();
+  P.n_segs = (uint32_t)gp.segments.size();
+  P.n_pieces = (uint32_t)gp.pieces.size();
+  P.n_slots = gp.n_slots;
+  P.n_levels = gp.n_levels;
+  P.piece_groups = piece_groups;
+  P.src_net = v->d_src_net.as<uint32_t>();
+  P.src_slot = v->d_src_slot.as<uint32_t>();
+  P.n_src = (uint32_t)gp.source_nets.size();
+  P.sregs = v->d_sregs.as<GateRegDev>();
+  P.wb_net = v->d_wb.as<uint32_t>();
+  P.grecs = v->d_grecs.as<uint4>();
+  P.level_group_begin = v->d_lgb.as<uint32_t>();
+  P.gregs = v->d_gregs.as<GateRegDev>();
+  P.n_regs = (uint32_t)gp.regs.size();
+  P.const0_slot = v->fused_ok ? (uint32_t)gp.net_slot[kNetConst0] : 0;
+  P.const1_slot = v->fused_ok ? (uint32_t)gp.net_slot[kNetConst1] : 0;
+  P.group = G;
+  if (v->fused_ok) {
+    v->fused_smem = gate_fused_smem_bytes(P);
+    if (v->fused_smem > max_smem) {
+      v->fused_ok = false;
     } else {
-      cuda_check(gate_fused_prepare(d->fused_smem), "gate_fused_prepare");
+      cuda_check(gate_fused_prepare(P, v->fused_smem), "gate_fused_prepare");
     }
   }
   // nets that hold their end-of-cycle value in a slot (recordable on the fused path)
-  d->end_live = gp.net_end_live;
+  v->end_live = gp.net_end_live;
+  d->gvar[li] = std::move(v);
+  return d->gvar[li].get();
+}
+
+// Load-time variant: the widest tile whose slots fit on chip. Slot counts
+// barely depend on W, so a miss at W = 8 predicts the width that fits.
+void build_gate_variants(rrtl_design* d) {
+  GateVariant* v8 = gate_variant(d, 8);
+  d->gate_base = 3;
+  d->gate_w_max = v8->fused_ok ? 8 : 0;
+  if (v8->fused_ok || v8->gp.n_slots > kMaxSlots) return;
+  for (uint32_t W = 4; W >= 1; W /= 2) {
+    size_t need = (size_t)v8->gp.n_slots * W * 4 + 128 + kRingBufs * 8 * (32 / W) * 8;
+    if (need > d->ctx->max_smem && W > 1) continue;
+    GateVariant* v = gate_variant(d, W);
+    if (v->fused_ok) {
+      d->gate_base = log2_words(W);
+      d->gate_w_max = W;
+      return;
+    }
+  }
+}
+
+// Fused tile width for a run over `words` 32-lane words. Cost model per SM:
+// every tile runs every level; a warp evaluates one group of G = 32/W cells
+// per step, 32 warps share a level, and each level piece ends in a CTA
+// barrier worth about kBarrierSteps group steps. A step costs more at small
+// W because G cells rarely find their inputs in G distinct shared-memory
+// banks (kStepCost, by log2 W). Tiles are spread over the SMs in whole rounds.
+uint32_t choose_tile_words(rrtl_design* d, uint32_t words) {
+  constexpr double kBarrierSteps = 4.0;
+  constexpr double kStepCost[4] = {1.45, 1.25, 1.1, 1.0};
+  const GateProgram& gp = d->gp();
+  const uint32_t sms = d->ctx->sm_count;
+  double best = INFINITY;
+  uint32_t best_w = d->gate_w_max;
+  for (uint32_t W = d->gate_w_max; W >= 1; W /= 2) {
+    const uint32_t G = 32 / W;
+    double per_tile = 0;
+    for (uint32_t L = 0; L < gp.n_levels; ++L) {
+      double cells = (double)(gp.level_group_begin[L + 1] - gp.level_group_begin[L]) * gp.group;
+      double groups = std::ceil(cells / G);
+      per_tile += std::ceil(groups / 32.0) * kStepCost[log2_words(W)] + kBarrierSteps * std::max(1.0, std::ceil(groups / 512.0));
+    }
+    uint32_t tiles = (words + W - 1) / W;
+    double t = std::ceil((double)tiles / sms) * per_tile;
+    if (t < best * 0.97) {  // a narrower tile must win clearly
+      best = t;
+      best_w = W;
+    }
+  }
+  return best_w;
 }
 
 void upload_word_program(rrtl_design* d) {
@@ -242,33 +306,35 @@ void check_err_word(rrtl_batch* b) {
   }
 }
 
-// Forces grouped per 8-word tile and per stage (stage 0 after commit, L+1 after level L).
-void build_forces(rrtl_batch* b) {
-  rrtl_design* d = b->d;
-  const GateProgram& gp = d->gp;
-  uint32_t stages = gp.n_levels + 1;
+// Forces grouped per tile of `tile_words` words and per stage (stage 0 after
+// commit, L+1 after level L). `v` gives the on-chip slots of the fused path
+// (null for the plain path, which addresses nets).
+void build_forces(rrtl_batch* b, ForceTable& ft, uint32_t tile_words, const GateVariant* v) {
+  const GateProgram& gp = b->d->gp();
+  const uint32_t stages = gp.n_levels + 1;
+  const uint32_t n_tiles = b->words_pad / tile_words;
   std::map<std::tuple<uint32_t, uint32_t, uint32_t, uint32_t>, std::pair<uint32_t, uint32_t>> merged;  // (tile, stage, net, word)
   for (auto& f : b->faults) {
     uint32_t net = gp.signal_net[f.signal];
     int32_t lv = gp.net_level[net];
     uint32_t stage = lv < 0 ? 0u : (uint32_t)lv + 1u;
     uint32_t gw = f.lane / 32, bit = f.lane % 32;
-    auto& mv = merged[std::make_tuple(gw / 8, stage, net, gw % 8)];
+    auto& mv = merged[std::make_tuple(gw / tile_words, stage, net, gw % tile_words)];
     mv.first |= 1u << bit;
     if (f.value) mv.second |= 1u << bit;
     else mv.second &= ~(1u << bit);
   }
   std::vector<GateForceDev> fs;
-  std::vector<uint32_t> off((size_t)b->n_tiles * (stages + 1), 0);
+  std::vector<uint32_t> off((size_t)n_tiles * (stages + 1), 0);
   size_t k = 0;
   auto it = merged.begin();
-  for (uint32_t t = 0; t < b->n_tiles; ++t)
+  for (uint32_t t = 0; t < n_tiles; ++t)
     for (uint32_t s = 0; s <= stages; ++s) {
       off[(size_t)t * (stages + 1) + s] = (uint32_t)k;
       if (s == stages) continue;
       while (it != merged.end() && std::get<0>(it->first) == t && std::get<1>(it->first) == s) {
         uint32_t net = std::get<2>(it->first);
-        int32_t slot = gp.net_slot.empty() ? 0 : gp.net_slot[net];
+        int32_t slot = v ? v->gp.net_slot[net] : 0;
         fs.push_back(GateForceDev{(uint32_t)std::max(slot, 0), net, std::get<3>(it->first), it->second.first,
                                   it->second.second, 0});
         ++k;
@@ -276,18 +342,27 @@ void build_forces(rrtl_batch* b) {
       }
     }
   // the per-tile table stores stages+1 boundaries; the last boundary of tile t is the first of tile t+1
-  for (uint32_t t = 0; t < b->n_tiles; ++t) off[(size_t)t * (stages + 1) + stages] = t + 1 < b->n_tiles ? off[(size_t)(t + 1) * (stages + 1)] : (uint32_t)k;
-  upload(b->d_forces, fs);
-  upload(b->d_force_off, off);
-  b->has_forces = !fs.empty();
+  for (uint32_t t = 0; t < n_tiles; ++t)
+    off[(size_t)t * (stages + 1) + stages] = t + 1 < n_tiles ? off[(size_t)(t + 1) * (stages + 1)] : (uint32_t)k;
+  upload(ft.d_forces, fs);
+  upload(ft.d_off, off);
+  ft.any = !fs.empty();
+  ft.valid = true;
+}
+
+void invalidate_forces(rrtl_batch* b) {
+  b->forces_plain.valid = false;
+  for (auto& f : b->forces_fused) f.valid = false;
 }
 
 // ---- gate engine run
 void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
   rrtl_design* d = b->d;
-  const GateProgram& gp = d->gp;
   cudaStream_t st = d->ctx->stream;
-  bool fused = b->path == RRTL_PATH_FUSED && d->fused_ok;
+  const uint32_t W = b->path == RRTL_PATH_FUSED ? (b->tile_words ? b->tile_words : choose_tile_words(d, b->words)) : 0;
+  GateVariant* v = W ? gate_variant(d, W) : d->gvar[d->gate_base].get();
+  const GateProgram& gp = v->gp;
+  bool fused = W && v->fused_ok;
   std::vector<GateStimDev> stim;
   for (uint32_t i = 0; i < run.n_stim; ++i) {
     const rrtl_stim& s = run.stim[i];
@@ -303,7 +378,7 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
   for (uint32_t i = 0; i < run.n_record; ++i) {
     signal_of(d, run.record[i]);
     uint32_t net = gp.signal_net[run.record[i]];
-    if (fused && !d->end_live[net]) fused = false;  // value not held to the end of the cycle: use the plain path
+    if (fused && !v->end_live[net]) fused = false;  // value not held to the end of the cycle: use the plain path
     rec.push_back(GateRecDev{0u, net});
   }
   if (fused)
@@ -328,10 +403,12 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
   R.lanes = b->lanes;
   R.words = b->words;
   R.words_pad = b->words_pad;
-  R.n_tiles = b->n_tiles;
-  R.force_off = b->d_force_off.as<uint32_t>();
-  R.forces = b->d_forces.as<GateForceDev>();
-  R.has_forces = b->has_forces ? 1u : 0u;
+  R.n_tiles = b->words_pad / (fused ? W : kPadWords);
+  ForceTable& ft = fused ? b->forces_fused[log2_words(W)] : b->forces_plain;
+  if (!ft.valid) build_forces(b, ft, fused ? W : kPadWords, fused ? v : nullptr);
+  R.force_off = ft.d_off.as<uint32_t>();
+  R.forces = ft.d_forces.as<GateForceDev>();
+  R.has_forces = ft.any ? 1u : 0u;
   R.final_settle = 1;
   R.nets = b->d_nets.as<uint32_t>();
   R.err = b->d_err.as<uint32_t>();
@@ -374,12 +451,13 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
 
   Timer tm(b);
   if (fused) {
-    uint32_t grid = std::min<uint32_t>(b->n_tiles, d->ctx->sm_count);
-    cuda_check(launch_gate_fused(d->gdev, R, grid, d->fused_smem, st), "gate_fused_kernel");
+    uint32_t grid = std::min<uint32_t>(R.n_tiles, d->ctx->sm_count);
+    cuda_check(launch_gate_fused(v->gdev, R, grid, v->fused_smem, st), "gate_fused_kernel");
   } else {
-    for (uint64_t c = 0; c < run.cycles; ++c) cuda_check(launch_gate_plain(d->gdev, R, c, 0, st), "gate_plain_kernel");
-    cuda_check(launch_gate_plain(d->gdev, R, 0, 1, st), "gate_plain_kernel");
+    for (uint64_t c = 0; c < run.cycles; ++c) cuda_check(launch_gate_plain(v->gdev, R, c, 0, st), "gate_plain_kernel");
+    cuda_check(launch_gate_plain(v->gdev, R, 0, 1, st), "gate_plain_kernel");
   }
+  b->last_tile_words = fused ? W : 0;
   tm.stop();
   if (!device_ptrs) {
     if (want_trace) cuda_check(cudaMemcpyAsync(run.out_trace, R.out_trace, trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
@@ -616,14 +694,13 @@ rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, c
     d->mp = lower_to_machine_program(pp);
     bool gate = true;
     try {
-      d->gp = build_gate_program(d->mp);
+      build_gate_variants(d.get());
     } catch (const RrtlError& e) {
       if (e.code != "E_GATE_SCOPE") throw;
       gate = false;
     }
     if (gate) {
       d->engine = RRTL_ENGINE_GATE;
-      upload_gate_program(d.get());
     } else {
       d->engine = RRTL_ENGINE_WORD;
       d->wp = build_word_program(d->mp);
@@ -652,12 +729,13 @@ rrtl_status rrtl_design_info_get(rrtl_design* d, rrtl_design_info* out) {
     i.total_memory_words_per_lane = P.total_memory_words_per_lane;
     i.engine = d->engine;
     if (d->engine == RRTL_ENGINE_GATE) {
-      i.n_gates = d->gp.n_real_cells;
-      i.n_levels = d->gp.n_levels;
-      i.n_nets = d->gp.n_nets;
-      i.n_slots = d->fused_ok ? d->gp.n_slots : 0;
-      i.n_regs = (uint32_t)d->gp.regs.size();
-      i.source_instrs = d->gp.source_instrs;
+      const GateProgram& gp = d->gp();
+      i.n_gates = gp.n_real_cells;
+      i.n_levels = gp.n_levels;
+      i.n_nets = gp.n_nets;
+      i.n_slots = d->gate_w_max ? gp.n_slots : 0;
+      i.n_regs = (uint32_t)gp.regs.size();
+      i.source_instrs = gp.source_instrs;
     } else {
       i.n_gates = (uint32_t)d->wp.code.size();
       i.n_levels = (uint32_t)d->mp.comb.packets.size();
@@ -716,15 +794,13 @@ rrtl_status rrtl_batch_create(rrtl_design* d, uint32_t lanes, rrtl_batch** out) 
     cuda_check(cudaMemset(b->d_err.p, 0, 16), "memset");
     if (d->engine == RRTL_ENGINE_GATE) {
       b->words = (lanes + 31) / 32;
-      b->words_pad = round_up(b->words, kTileWords);
-      b->n_tiles = b->words_pad / kTileWords;
-      b->rows = d->gp.n_nets + 1;
+      b->words_pad = round_up(b->words, kPadWords);
+      b->rows = d->gp().n_nets + 1;
       size_t bytes = (size_t)b->rows * b->words_pad * 4;
       b->d_nets.reserve(bytes);
       cuda_check(cudaMemset(b->d_nets.p, 0, bytes), "memset nets");
       cuda_check(cudaMemset(b->d_nets.as<uint8_t>() + (size_t)kNetConst1 * b->words_pad * 4, 0xFF, (size_t)b->words_pad * 4),
                  "memset const1");
-      build_forces(b.get());
     } else {
       b->lanes_pad = round_up(lanes, kWordThreads);
       const PackedProgram& P = d->mp.source;
@@ -764,7 +840,7 @@ rrtl_status rrtl_batch_lanes(rrtl_batch* b, uint32_t* out) {
 }
 
 static void gate_set_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words) {
-  uint32_t net = b->d->gp.signal_net[signal];
+  uint32_t net = b->d->gp().signal_net[signal];
   std::vector<uint32_t> row(b->words_pad, 0);
   for (uint32_t w = 0; w < b->words; ++w) {
     uint32_t valid = b->lanes - w * 32;
@@ -777,7 +853,7 @@ static void gate_set_bits(rrtl_batch* b, uint32_t signal, const uint32_t* words)
 }
 
 static void gate_get_bits(rrtl_batch* b, uint32_t signal, uint32_t* words) {
-  uint32_t net = b->d->gp.signal_net[signal];
+  uint32_t net = b->d->gp().signal_net[signal];
   cuda_check(cudaMemcpyAsync(words, b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad, (size_t)b->words * 4,
                              cudaMemcpyDeviceToHost, b->d->ctx->stream),
              "d2h signal");
@@ -894,9 +970,9 @@ rrtl_status rrtl_batch_get_signals_bits(rrtl_batch* b, const uint32_t* signals, 
       cudaStream_t st = b->d->ctx->stream;
       // one 2-D copy per run of consecutive net rows
       for (size_t i = 0; i < n;) {
-        uint32_t net = b->d->gp.signal_net[signals[i]];
+        uint32_t net = b->d->gp().signal_net[signals[i]];
         size_t j = i + 1;
-        while (j < n && b->d->gp.signal_net[signals[j]] == net + (j - i)) ++j;
+        while (j < n && b->d->gp().signal_net[signals[j]] == net + (j - i)) ++j;
         cuda_check(cudaMemcpy2DAsync(out + i * words, (size_t)words * 4, b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad,
                                      (size_t)b->words_pad * 4, (size_t)words * 4, j - i, cudaMemcpyDeviceToHost, st),
                    "d2h signals");
@@ -1028,7 +1104,7 @@ rrtl_status rrtl_batch_set_faults(rrtl_batch* b, const rrtl_fault* faults, size_
     REQUIRE(b && (faults || n == 0), RRTL_E_ARG, "E_ARG: null argument");
     set_device(b->d->ctx);
     REQUIRE(b->d->engine == RRTL_ENGINE_GATE, RRTL_E_UNSUPPORTED, "E_FAULT: fault injection needs the gate engine");
-    const GateProgram& gp = b->d->gp;
+    const GateProgram& gp = b->d->gp();
     for (size_t i = 0; i < n; ++i) {
       const rrtl_fault& f = faults[i];
       REQUIRE(f.lane < b->lanes, RRTL_E_ARG, "E_FAULT_LANE: lane out of range");
@@ -1040,7 +1116,7 @@ rrtl_status rrtl_batch_set_faults(rrtl_batch* b, const rrtl_fault* faults, size_
       REQUIRE(f.value <= 1, RRTL_E_ARG, "E_FAULT: stuck-at value must be 0 or 1");
     }
     b->faults.assign(faults, faults + n);
-    build_forces(b);
+    invalidate_forces(b);
   });
 }
 
@@ -1110,6 +1186,30 @@ rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path) {
     REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
     REQUIRE(path == RRTL_PATH_FUSED || path == RRTL_PATH_PLAIN, RRTL_E_ARG, "E_ARG: unknown path");
     b->path = path;
+  });
+}
+
+rrtl_status rrtl_batch_set_tile_words(rrtl_batch* b, uint32_t words) {
+  return guard([&] {
+    REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(words == 0 || words == 1 || words == 2 || words == 4 || words == 8, RRTL_E_ARG,
+            "E_ARG: tile width must be 0, 1, 2, 4 or 8 words");
+    REQUIRE(b->d->engine == RRTL_ENGINE_GATE || words == 0, RRTL_E_UNSUPPORTED, "E_ARG: tile width is a gate-engine setting");
+    set_device(b->d->ctx);
+    if (words) {
+      GateVariant* v = gate_variant(b->d, words);
+      REQUIRE(v->fused_ok, RRTL_E_UNSUPPORTED,
+              "E_GATE_SCOPE: " + std::to_string(v->gp.n_slots) + " net slots of " + std::to_string(words) +
+                  " words do not fit in shared memory");
+    }
+    b->tile_words = words;
+  });
+}
+
+rrtl_status rrtl_batch_tile_words(rrtl_batch* b, uint32_t* words) {
+  return guard([&] {
+    REQUIRE(b && words, RRTL_E_ARG, "E_ARG: null argument");
+    *words = b->last_tile_words;
   });
 }
 

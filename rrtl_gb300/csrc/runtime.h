@@ -45,6 +45,24 @@ void upload(DevBuf& b, const std::vector<T>& v) {
   if (!v.empty()) cuda_check(cudaMemcpy(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
 }
 
+// The gate program for one fused tile width W, with its device copy.
+struct GateVariant {
+  uint32_t W = 8;
+  GateProgram gp;
+  std::vector<uint8_t> end_live;  // net is resident at the end of a cycle (recordable on the fused path)
+  GateProgDev gdev{};
+  bool fused_ok = false;
+  size_t fused_smem = 0;
+  DevBuf d_srecs, d_pieces, d_segs, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
+};
+
+// Per-tile, per-stage force table of a batch for one tile width.
+struct ForceTable {
+  bool valid = false;
+  bool any = false;
+  DevBuf d_off, d_forces;
+};
+
 }  // namespace rrtl
 
 // Handles are reference counted: a design holds its context and a batch its
@@ -66,13 +84,12 @@ struct rrtl_design {
   std::string top;
   rrtl::MachineProgram mp;
   uint32_t engine = 0;
-  // gate engine
-  rrtl::GateProgram gp;
-  std::vector<uint8_t> end_live;  // net is resident at the end of a cycle (recordable on the fused path)
-  rrtl::GateProgDev gdev{};
-  bool fused_ok = false;
-  size_t fused_smem = 0;
-  rrtl::DevBuf d_srecs, d_pieces, d_segs, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
+  // gate engine: one program per fused tile width W (index log2 W), built on
+  // demand; nets, levels and registers are the same in every variant
+  std::unique_ptr<rrtl::GateVariant> gvar[4];
+  uint32_t gate_base = 3;   // log2 W of the variant built at load time
+  uint32_t gate_w_max = 0;  // widest W whose slots fit on chip, 0 if none
+  const rrtl::GateProgram& gp() const { return gvar[gate_base]->gp; }
   // word engine
   rrtl::WordProgram wp;
   rrtl::WordProgDev wdev{};
@@ -87,11 +104,12 @@ struct rrtl_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   rrtl::DevBuf d_err;
   // gate engine state
-  uint32_t words = 0, words_pad = 0, n_tiles = 0, rows = 0;
+  uint32_t words = 0, words_pad = 0, rows = 0;
+  uint32_t tile_words = 0;  // requested fused tile width, 0 = chosen per run
+  uint32_t last_tile_words = 0;  // tile width of the last fused run, 0 after a plain run
   rrtl::DevBuf d_nets;
   std::vector<rrtl_fault> faults;
-  rrtl::DevBuf d_force_off, d_forces;
-  bool has_forces = false;
+  rrtl::ForceTable forces_plain, forces_fused[4];  // plain: 8-word tiles; fused: per log2 W
   // word engine state
   uint32_t lanes_pad = 0;
   rrtl::DevBuf d_values, d_mem, d_caps;

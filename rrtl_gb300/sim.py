@@ -121,6 +121,8 @@ EXPORTS = (
     "rrtl_batch_snapshot",
     "rrtl_batch_restore",
     "rrtl_batch_set_path",
+    "rrtl_batch_set_tile_words",
+    "rrtl_batch_tile_words",
     "rrtl_batch_last_kernel_ms",
     "rrtl_word_tick_many_noalloc",
 )
@@ -170,6 +172,8 @@ def lib():
         "rrtl_batch_snapshot": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_path": [c_void_p, c_uint32],
+        "rrtl_batch_set_tile_words": [c_void_p, c_uint32],
+        "rrtl_batch_tile_words": [c_void_p, P(c_uint32)],
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
     }
@@ -400,6 +404,17 @@ class GpuBatchSimulator:
 
     def set_path(self, path: int):
         check(lib().rrtl_batch_set_path(self.h, path))
+
+    def set_tile_words(self, words: int):
+        """Gate engine, fused path: 32-lane words per tile (8, 4, 2, 1; 0 = automatic)."""
+        check(lib().rrtl_batch_set_tile_words(self.h, words))
+
+    @property
+    def tile_words(self) -> int:
+        """Tile width of the last fused run (0 after a plain-path run)."""
+        v = c_uint32()
+        check(lib().rrtl_batch_tile_words(self.h, byref(v)))
+        return v.value
 
     @property
     def last_kernel_ms(self) -> float:

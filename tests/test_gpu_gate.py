@@ -153,6 +153,83 @@ def test_netlist_trace_and_hash_match_oracle(small_netlist, path, lanes):
         assert np.array_equal(g.get_signal_bits(name), ref["sim"].get_bits(od.signal(name))), name
 
 
+@pytest.mark.parametrize("words", [8, 4, 2, 1])
+@pytest.mark.parametrize("lanes", [33, 300, 2048])
+def test_netlist_tile_widths_match_oracle(small_netlist, words, lanes):
+    """Every fused tile width gives the oracle's traces, hashes and final state."""
+    d, meta, cd, od = small_netlist
+    cycles = 21
+    stim, rec = netlist_run_spec(meta)
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g.set_tile_words(words)
+    res = g.run(cycles, seed=321, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
+    assert g.tile_words == words
+    ref = oracle_bp_run(od, lanes, cycles, 321, [(od.signal(n), k, p) for n, k, p in stim],
+                        [od.signal(r) for r in rec], 3)
+    assert np.array_equal(res["trace"], ref["trace"])
+    assert np.array_equal(res["hash"], ref["hash"])
+    ref["sim"].settle()
+    for name in meta.regs[::7] + meta.gate_names[::131] + meta.outputs:
+        assert np.array_equal(g.get_signal_bits(name), ref["sim"].get_bits(od.signal(name))), name
+
+
+@pytest.mark.parametrize("words", [4, 1])
+def test_netlist_faults_tile_widths_match_oracle(small_netlist, words):
+    d, meta, cd, od = small_netlist
+    lanes, cycles = 700, 24
+    rng = Rng(91 + words)
+    sites = meta.gate_names + meta.regs + meta.outputs
+    faults = [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]
+    stim, rec = netlist_run_spec(meta)
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g.set_tile_words(words)
+    g.set_faults(faults)
+    res = g.run(cycles, seed=17, stim=stim, record=rec, mode=sim.REC_HASH | sim.REC_DETECT)
+    ref = oracle_bp_run(od, lanes, cycles, 17, [(od.signal(n), k, p) for n, k, p in stim],
+                        [od.signal(r) for r in rec], 6, faults=[(l, od.signal(s), v) for l, s, v in faults])
+    assert np.array_equal(res["hash"], ref["hash"])
+    assert np.array_equal(res["detect"], ref["detect"])
+
+
+def test_auto_tile_width_is_a_valid_width(small_netlist):
+    d, meta, cd, od = small_netlist
+    stim, rec = netlist_run_spec(meta)
+    for lanes in (32, 4096, 65536):
+        g = sim.GpuBatchSimulator(cd, lanes=lanes)
+        g.run(2, seed=1, stim=stim, record=rec, mode=sim.REC_HASH)
+        assert g.tile_words in (1, 2, 4, 8)
+    g.set_path(sim.PATH_PLAIN)
+    g.run(1, seed=1, stim=stim, record=rec, mode=sim.REC_HASH)
+    assert g.tile_words == 0
+    with pytest.raises(sim.RrtlError):
+        g.set_tile_words(3)
+
+
+def test_large_netlist_runs_fused_at_narrow_tiles(engine):
+    """100k gates and 4,096 flops: the slots need more shared memory than one
+    CTA has at 8 words per tile, so the fused path runs narrower tiles; it
+    matches the oracle on a lane slice and the plain path on every hash."""
+    d, meta = gate_netlist(n_gates=100_000, n_ff=4096, depth=60, seed=3)
+    js = d.to_json()
+    cd = sim.CompiledDesign(js, meta.top)
+    stim, rec = netlist_run_spec(meta)
+    g = sim.GpuBatchSimulator(cd, lanes=4096)
+    with pytest.raises(sim.RrtlError):
+        g.set_tile_words(8)
+    res = g.run(12, seed=8, stim=stim, record=rec, mode=sim.REC_HASH)
+    assert g.tile_words in (1, 2, 4)
+    gp = sim.GpuBatchSimulator(cd, lanes=4096)
+    gp.set_path(sim.PATH_PLAIN)
+    resp = gp.run(12, seed=8, stim=stim, record=rec, mode=sim.REC_HASH)
+    assert np.array_equal(res["hash"], resp["hash"])
+    od = ob.OracleDesign(js, meta.top)
+    g = sim.GpuBatchSimulator(cd, lanes=96)
+    res = g.run(12, seed=8, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
+    ref = oracle_bp_run(od, 96, 12, 8, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec], 3)
+    assert np.array_equal(res["trace"], ref["trace"])
+    assert np.array_equal(res["hash"], ref["hash"])
+
+
 def test_netlist_faults_match_oracle(small_netlist):
     d, meta, cd, od = small_netlist
     lanes, cycles = 500, 30
@@ -219,14 +296,18 @@ def test_full_size_netlist_fused_equals_plain(engine):
     stim, rec = netlist_run_spec(meta)
     lanes, cycles = 8192, 20
     out = {}
-    for path in (sim.PATH_FUSED, sim.PATH_PLAIN):
+    for key in ("plain", 8, 2, 1):
         g = sim.GpuBatchSimulator(cd, lanes=lanes)
-        g.set_path(path)
+        if key == "plain":
+            g.set_path(sim.PATH_PLAIN)
+        else:
+            g.set_tile_words(key)
         res = g.run(cycles, seed=4, stim=stim, record=rec, mode=sim.REC_HASH)
-        out[path] = (res["hash"], [g.get_signal_bits(q) for q in meta.regs[::64]])
-    assert np.array_equal(out[0][0], out[1][0])
-    for a, b in zip(out[0][1], out[1][1]):
-        assert np.array_equal(a, b)
+        out[key] = (res["hash"], [g.get_signal_bits(q) for q in meta.regs[::64]])
+    for key in (8, 2, 1):
+        assert np.array_equal(out[key][0], out["plain"][0]), key
+        for a, b in zip(out[key][1], out["plain"][1]):
+            assert np.array_equal(a, b), key
     od = ob.OracleDesign(js, meta.top)
     g = sim.GpuBatchSimulator(cd, lanes=256)
     res = g.run(cycles, seed=4, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
