@@ -6,6 +6,10 @@
 
 namespace rrtl {
 
+// Warps of the fused gate kernel's CTA; a staged piece carries one run range
+// per warp.
+constexpr uint32_t kGateFusedWarps = 32;
+
 struct GateStimDev {
   uint32_t slot;  // on-chip slot (fused path)
   uint32_t net;   // global net row (plain path)
@@ -34,18 +38,19 @@ struct GateRegDev {
   uint32_t q, d, rst, flags;
 };
 
+// One staged piece (see PieceBlob): where it lies in the blob, its size and
+// the size of its run header.
 struct GatePieceDev {
   uint32_t group_begin, n_groups, level, last_of_level;
-  uint32_t seg_begin, seg_end, pad0, pad1;
+  uint32_t off_words, bytes, hdr_bytes, pad;
 };
 
 struct GateProgDev {
   // fused path (slots in shared memory)
-  const uint2* srecs;          // [groups*group] packed slot records (pack_smem_record)
+  const uint32_t* blob;        // staged pieces: run headers and packed slot records (PieceBlob)
   const GatePieceDev* pieces;
-  const uint4* segs;           // {lut, begin, end, 0}: truth-table runs, group indices relative to the piece
   uint32_t n_pieces, n_slots, n_levels, piece_groups;
-  uint32_t n_segs;
+  uint32_t ring_bytes;         // bytes of one ring buffer (largest piece)
   const uint32_t* src_net;     // sources loaded per tile and written back
   const uint32_t* src_slot;
   uint32_t n_src;

@@ -14,9 +14,9 @@
 //  gate_plain_kernel     one launch per cycle; nets live in HBM, read and
 //                        written once per cell per cycle (the baseline path).
 //
-// Fused warp layout: lane = W*gsub + w; w is the word inside the tile and gsub
-// picks one of the G = 32/W cells of a group. All cells of a group share one
-// truth table, so the table is warp-uniform and evaluates as one LOP3.
+// Fused warp layout: a group is G = 32/W cells that share one truth table, so
+// the table is warp-uniform and evaluates as one LOP3 with an immediate
+// table. A thread owns V words of one cell (see FusedShape).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -26,14 +26,17 @@
 
 namespace rrtl {
 
-constexpr int kFusedThreads = 1024;
-constexpr int kFusedWarps = kFusedThreads / 32;
+constexpr int kFusedWarps = (int)kGateFusedWarps;
+constexpr int kFusedThreads = kFusedWarps * 32;
 constexpr int kPlainThreads = 256;
 constexpr int kRing = 4;                  // record ring buffers
 constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier wait
 constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slot array
 #ifndef RRTL_FUSED_UNROLL
-#define RRTL_FUSED_UNROLL 2  // groups per unrolled step of a truth-table run
+#define RRTL_FUSED_UNROLL 1  // warp steps per unrolled iteration of a truth-table run
+#endif
+#ifndef RRTL_FUSED_V
+#define RRTL_FUSED_V 2  // words per thread in the fused kernel (tiles of 2+ words)
 #endif
 constexpr int kUnroll = RRTL_FUSED_UNROLL;
 static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
@@ -112,41 +115,78 @@ __host__ __device__ __forceinline__ size_t fused_slot_bytes(uint32_t n_slots, ui
 }
 
 // ------------------------------------------------------------ fused path --
+//
+// A thread owns V consecutive words (V = 2 for W >= 2: one 64-bit shared
+// access moves both). Lanes 16h..16h+15 form half-warp h; a half-warp covers
+// one group (G cells x W words), so a warp step evaluates groups g and g+1
+// of one truth-table run. Cells of a group sit in G distinct bank residues,
+// so each half-warp access is one shared-memory wavefront.
 
-// Evaluate groups [g, e) of one truth-table run. `rb` is this thread's record
-// in group 0 of the staged piece and `Sw` this thread's word column of the
-// slot array; both are shared memory, so every access below is an LDS/STS.
+template <int W>
+struct FusedShape {
+  static constexpr int V = W >= 2 ? RRTL_FUSED_V : 1;  // words per thread
+  static constexpr int G = 32 / W;                      // cells per group
+  static constexpr int kSteps = V;                      // groups per warp step
+};
+
+template <int V>
+struct WordVec;
+template <>
+struct WordVec<1> {
+  using T = uint32_t;
+};
+template <>
+struct WordVec<2> {
+  using T = uint2;
+};
+
+template <int L>
+__device__ __forceinline__ uint32_t lopv(uint32_t a, uint32_t b, uint32_t c) {
+  return lop3<L>(a, b, c);
+}
+template <int L>
+__device__ __forceinline__ uint2 lopv(uint2 a, uint2 b, uint2 c) {
+  return make_uint2(lop3<L>(a.x, b.x, c.x), lop3<L>(a.y, b.y, c.y));
+}
+
+// Evaluate this thread's cell in groups h+b, h+b+V, ... < e of one
+// truth-table run. `rb` is this thread's record in group 0 of the staged
+// piece and `Sv` its word column of the slot array (row stride W/V vectors);
+// both are shared memory, so every access below is an LDS/STS.
 template <int W, int L>
-__device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw, int g, int e) {
-  constexpr int G = 32 / W;
+__device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
+                                        int g, int e) {
+  using Sh = FusedShape<W>;
+  using T = typename WordVec<Sh::V>::T;
+  constexpr int R = W / Sh::V;
   constexpr bool kUseA = (L & 0x0F) != ((L >> 4) & 0x0F);
   constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
   constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
+  const T zero{};
 #pragma unroll kUnroll
-  for (; g < e; ++g) {
-    const uint2 r = rb[g * G];
-    const uint32_t va = kUseA ? Sw[(r.x & 0xFFFFu) * W] : 0u;
-    const uint32_t vb = kUseB ? Sw[(r.x >> 16) * W] : 0u;
-    const uint32_t vc = kUseC ? Sw[(r.y & 0xFFFFu) * W] : 0u;
-    Sw[(r.y >> 16) * W] = lop3<L>(va, vb, vc);
+  for (; g < e; g += Sh::kSteps) {
+    const uint2 r = rb[g * Sh::G];
+    const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
+    const T vb = kUseB ? Sv[(r.x >> 16) * R] : zero;
+    const T vc = kUseC ? Sv[(r.y & 0xFFFFu) * R] : zero;
+    Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
   }
 }
 
 #define RRTL_CASE(n) \
-  case n: run_seg<W, n>(rb, Sw, b, e); break;
+  case n: run_seg<W, n>(rb, Sv, b + h, e); break;
 #define RRTL_CASE4(n) RRTL_CASE(n) RRTL_CASE(n + 1) RRTL_CASE(n + 2) RRTL_CASE(n + 3)
 #define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
 #define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
 
-// This warp's share [g0, g1) of a piece, dispatched once per truth-table run.
+// This warp's runs [k0, k1) of a staged piece, dispatched once per run.
 template <int W>
-__device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
-                                           const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0, int g1) {
-  for (uint32_t s = s0; s < s1; ++s) {
-    const uint4 sg = segs[s];
-    const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
-    if (b >= e) continue;
-    switch (sg.x) {
+__device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
+                                           const uint32_t* __restrict__ runs, uint32_t k0, uint32_t k1, int h) {
+  for (uint32_t k = k0; k < k1; ++k) {
+    const uint32_t run = runs[k];
+    const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
+    switch (run & 0xFFu) {
       RRTL_CASE64(0)
       RRTL_CASE64(64)
       RRTL_CASE64(128)
@@ -156,23 +196,36 @@ __device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, uint32_
   }
 }
 
+__device__ __forceinline__ uint32_t lut_v(uint32_t t, uint32_t a, uint32_t b, uint32_t c) { return lut_eval(t, a, b, c); }
+__device__ __forceinline__ uint2 lut_v(uint32_t t, uint2 a, uint2 b, uint2 c) {
+  return make_uint2(lut_eval(t, a.x, b.x, c.x), lut_eval(t, a.y, b.y, c.y));
+}
+__device__ __forceinline__ void store_net(uint32_t* p, uint32_t v) { p[0] = v; }
+__device__ __forceinline__ void store_net(uint32_t* p, uint2 v) {
+  p[0] = v.x;
+  p[1] = v.y;
+}
+
 // Final settle: same evaluation with a runtime truth table, plus a copy of
-// every signal net to the global state.
+// every signal net to the global state (`col` = this thread's first word).
 template <int W>
-__device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb, uint32_t* __restrict__ Sw,
-                                                     const uint4* __restrict__ segs, uint32_t s0, uint32_t s1, int g0,
-                                                     int g1, const uint32_t* __restrict__ wb, uint32_t* nets,
-                                                     size_t words_pad, uint32_t col) {
-  constexpr int G = 32 / W;
-  for (uint32_t s = s0; s < s1; ++s) {
-    const uint4 sg = segs[s];
-    const int b = max(g0, (int)sg.y), e = min(g1, (int)sg.z);
-    for (int g = b; g < e; ++g) {
-      const uint2 r = rb[g * G];
-      const uint32_t v = lut_eval(sg.x, Sw[(r.x & 0xFFFFu) * W], Sw[(r.x >> 16) * W], Sw[(r.y & 0xFFFFu) * W]);
-      Sw[(r.y >> 16) * W] = v;
-      const uint32_t net = __ldg(wb + g * G);
-      if (net != 0xFFFFFFFFu) nets[(size_t)net * words_pad + col] = v;
+__device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb,
+                                                     typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
+                                                     const uint32_t* __restrict__ runs, uint32_t k0, uint32_t k1, int h,
+                                                     const uint32_t* __restrict__ wb, uint32_t* nets, size_t words_pad,
+                                                     uint32_t col) {
+  using Sh = FusedShape<W>;
+  constexpr int R = W / Sh::V;
+  for (uint32_t k = k0; k < k1; ++k) {
+    const uint32_t run = runs[k];
+    const uint32_t lut = run & 0xFFu;
+    const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
+    for (int g = b + h; g < e; g += Sh::kSteps) {
+      const uint2 r = rb[g * Sh::G];
+      const auto v = lut_v(lut, Sv[(r.x & 0xFFFFu) * R], Sv[(r.x >> 16) * R], Sv[(r.y & 0xFFFFu) * R]);
+      Sv[(r.y >> 16) * R] = v;
+      const uint32_t net = __ldg(wb + g * Sh::G);
+      if (net != 0xFFFFFFFFu) store_net(nets + (size_t)net * words_pad + col, v);
     }
   }
 }
@@ -193,23 +246,27 @@ template <int W>
 __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDev P, GateRunDev R) {
   constexpr uint32_t G = 32 / W;
   extern __shared__ __align__(128) uint8_t smem[];
-  const size_t ring_stride = (size_t)P.piece_groups * G;  // uint2 records per ring buffer
-  // layout: [record ring][128-byte header: 4 mbarriers, hash accumulator,
-  // detect state][slots][piece table][segment table]; every region after the
-  // ring starts on a 16-byte boundary (the segment table is read as uint4)
-  uint2* ring = reinterpret_cast<uint2*>(smem);
-  uint8_t* hdr = smem + (size_t)kRing * ring_stride * 8u;
+  const size_t ring_bytes = P.ring_bytes;  // one ring buffer: a staged piece
+  // layout: [piece ring][128-byte header: 4 mbarriers, hash accumulator,
+  // detect state][slots][piece table]; every region starts on a 16-byte
+  // boundary (ring buffers are bulk-copy destinations)
+  uint8_t* ring = smem;
+  uint8_t* hdr = smem + (size_t)kRing * ring_bytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(hdr);
   unsigned long long* hacc = reinterpret_cast<unsigned long long*>(hdr + kRing * 8);
   uint32_t* dstate = reinterpret_cast<uint32_t*>(hdr + kRing * 8 + 8);  // diff[8], detected[8]
   uint32_t* S = reinterpret_cast<uint32_t*>(hdr + kFusedHeader);
-  // piece and segment tables, staged once per launch
+  // piece table, staged once per launch
   GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(hdr + kFusedHeader + fused_slot_bytes(P.n_slots, W));
-  uint4* segs = reinterpret_cast<uint4*>(pieces + P.n_pieces);
   __shared__ int s_abort;
 
+  using Sh = FusedShape<W>;
+  using T = typename WordVec<Sh::V>::T;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const uint32_t w = lane % W, gsub = lane / W;
+  // lane -> (half h, cell c of the group, first word w of this thread)
+  const uint32_t h = Sh::V == 2 ? lane >> 4 : 0u;
+  const uint32_t hl = Sh::V == 2 ? lane & 15u : lane;
+  const uint32_t cidx = hl / (W / Sh::V), w = (hl % (W / Sh::V)) * Sh::V;
   const bool resident = P.n_pieces <= (uint32_t)kRing;
   const uint32_t stages = P.n_levels + 1;
 
@@ -219,7 +276,6 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   const uint64_t total_q = resident ? P.n_pieces : (uint64_t)my_tiles * passes * P.n_pieces;
 
   for (uint32_t i = tid; i < P.n_pieces; i += blockDim.x) pieces[i] = P.pieces[i];
-  for (uint32_t i = tid; i < P.n_segs; i += blockDim.x) segs[i] = P.segs[i];
   if (tid == 0) {
     s_abort = 0;
     *hacc = 0ull;
@@ -232,13 +288,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
     uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
     for (uint64_t q = 0; q < n0; ++q) {
       const GatePieceDev pc = P.pieces[q % P.n_pieces];
-      bulk_load(ring + (q % kRing) * ring_stride, P.srecs + (size_t)pc.group_begin * G, pc.n_groups * G * 8u,
-                &bars[q % kRing]);
+      bulk_load(ring + (q % kRing) * ring_bytes, P.blob + pc.off_words, pc.bytes, &bars[q % kRing]);
     }
   }
 
   uint64_t q = 0;
-  uint32_t* const Sw = S + w;
+  T* const Sv = reinterpret_cast<T*>(S + w);
   // Thread 0 waits for a piece's records; the CTA barrier that follows
   // publishes them to every thread. The wait for piece q+1 is folded into the
   // barrier that closes piece q, so each piece costs one barrier.
@@ -293,13 +348,17 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
         const GatePieceDev pc = pieces[p];
         const uint32_t buf = resident ? p : (uint32_t)(q % kRing);
-        const uint2* rb = ring + buf * ring_stride + gsub;
-        const int g0 = (int)((pc.n_groups * warp) / kFusedWarps), g1 = (int)((pc.n_groups * (warp + 1)) / kFusedWarps);
-        if (final_pass)
-          eval_piece_writeback<W>(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1,
-                                  P.wb_net + (size_t)pc.group_begin * G + gsub, R.nets, R.words_pad, col0 + w);
-        else
-          eval_piece<W>(rb, Sw, segs, pc.seg_begin, pc.seg_end, g0, g1);
+        {
+          // the staged piece: per-warp run ranges, the run list, then the records
+          const uint32_t* ph = reinterpret_cast<const uint32_t*>(ring + buf * ring_bytes);
+          const uint2* rb = reinterpret_cast<const uint2*>(ring + buf * ring_bytes + pc.hdr_bytes) + cidx;
+          const uint32_t kr = ph[warp], k0 = kr & 0xFFFFu, k1 = kr >> 16;
+          if (final_pass)
+            eval_piece_writeback<W>(rb, Sv, ph + kFusedWarps, k0, k1, (int)h,
+                                    P.wb_net + (size_t)pc.group_begin * G + cidx, R.nets, R.words_pad, col0 + w);
+          else
+            eval_piece<W>(rb, Sv, ph + kFusedWarps, k0, k1, (int)h);
+        }
         if (pc.last_of_level && R.has_forces) {
           __syncthreads();
           apply_forces<W>(R, S, tile, pc.level + 1, stages);
@@ -310,8 +369,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
         if (!resident && tid == 0 && q + kRing < total_q) {
           uint64_t nq = q + kRing;
           const GatePieceDev npc = pieces[nq % P.n_pieces];
-          bulk_load(ring + buf * ring_stride, P.srecs + (size_t)npc.group_begin * G, npc.n_groups * G * 8u,
-                    &bars[buf]);
+          bulk_load(ring + buf * ring_bytes, P.blob + npc.off_words, npc.bytes, &bars[buf]);
         }
       }
       if (s_abort) break;
@@ -351,8 +409,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
         }
       }
       // commit (D and reset nets are never register nets, so one pass is safe)
+#pragma unroll 4
       for (uint32_t i = tid; i < P.n_regs * W; i += blockDim.x) {
-        GateRegDev r = P.sregs[i / W];
+        const uint4 rr = __ldg(reinterpret_cast<const uint4*>(P.sregs) + i / W);
+        const GateRegDev r{rr.x, rr.y, rr.z, rr.w};
         uint32_t ww = i % W;
         uint32_t d = S[r.d * W + ww];
         if (r.flags & 1u) {
@@ -489,9 +549,9 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
 // ------------------------------------------------------------- launchers --
 
 size_t gate_fused_smem_bytes(const GateProgDev& P) {
-  const uint32_t G = P.group, W = 32u / P.group;
-  return (size_t)kRing * P.piece_groups * G * 8u + kFusedHeader + fused_slot_bytes(P.n_slots, W) +
-         (size_t)P.n_pieces * sizeof(GatePieceDev) + (size_t)P.n_segs * 16u;
+  const uint32_t W = 32u / P.group;
+  return (size_t)kRing * P.ring_bytes + kFusedHeader + fused_slot_bytes(P.n_slots, W) +
+         (size_t)P.n_pieces * sizeof(GatePieceDev);
 }
 static_assert(sizeof(GatePieceDev) == 32, "piece descriptor layout");
 

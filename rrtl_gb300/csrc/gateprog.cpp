@@ -526,4 +526,44 @@ void build_pieces(GateProgram& gp, uint32_t piece_groups) {
   }
 }
 
+PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps) {
+  PieceBlob pb;
+  const uint32_t G = gp.group;
+  const int32_t c0 = gp.net_slot[kNetConst0];
+  for (const GatePiece& pc : gp.pieces) {
+    std::vector<uint32_t> hdr(warps, 0), runs;
+    for (uint32_t k = 0; k < warps; ++k) {
+      const uint32_t g0 = (uint32_t)((uint64_t)pc.n_groups * k / warps), g1 = (uint32_t)((uint64_t)pc.n_groups * (k + 1) / warps);
+      const uint32_t first = (uint32_t)runs.size();
+      for (uint32_t s = pc.seg_begin; s < pc.seg_end; ++s) {
+        const GateSegment& sg = gp.segments[s];
+        const uint32_t b = std::max(g0, sg.begin), e = std::min(g1, sg.end);
+        if (b < e) runs.push_back(pack_run(sg.lut, b, e));
+      }
+      hdr[k] = first | ((uint32_t)runs.size() << 16);
+    }
+    if (pc.n_groups >= 4096 || runs.size() >= 65536) throw RrtlError("E_GATE_SCOPE", "piece too large for its header");
+    const uint32_t start = (uint32_t)pb.words.size();
+    pb.words.insert(pb.words.end(), hdr.begin(), hdr.end());
+    pb.words.insert(pb.words.end(), runs.begin(), runs.end());
+    while (pb.words.size() % 4) pb.words.push_back(0);
+    const uint32_t hdr_bytes = (uint32_t)(pb.words.size() - start) * 4;
+    for (uint32_t g = pc.group_begin; g < pc.group_begin + pc.n_groups; ++g)
+      for (uint32_t k = 0; k < G; ++k) {
+        const GateCell& c = gp.cells[(size_t)g * G + k];
+        const uint32_t a = c.pad ? c0 : gp.net_slot[c.in[0]], b = c.pad ? c0 : gp.net_slot[c.in[1]];
+        const uint32_t cc = c.pad ? c0 : gp.net_slot[c.in[2]], o = c.pad ? 0 : gp.net_slot[c.out];
+        const uint64_t x = pack_smem_record(a, b, cc, o);
+        pb.words.push_back((uint32_t)x);
+        pb.words.push_back((uint32_t)(x >> 32));
+      }
+    while (pb.words.size() % 4) pb.words.push_back(0);
+    pb.off_words.push_back(start);
+    pb.bytes.push_back((uint32_t)(pb.words.size() - start) * 4);
+    pb.hdr_bytes.push_back(hdr_bytes);
+    pb.max_bytes = std::max(pb.max_bytes, pb.bytes.back());
+  }
+  return pb;
+}
+
 }  // namespace rrtl

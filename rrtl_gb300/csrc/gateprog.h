@@ -100,9 +100,28 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words = 8
 void build_pieces(GateProgram& gp, uint32_t piece_groups);
 
 // Packed 8-byte record for one cell in shared memory: four 16-bit slot
-// fields a, b, c, out (the truth table comes from the piece's segments).
+// fields a, b, c, out (the truth table comes from the piece's runs).
 inline uint64_t pack_smem_record(uint32_t a, uint32_t b, uint32_t c, uint32_t out) {
   return (uint64_t)a | ((uint64_t)b << 16) | ((uint64_t)c << 32) | ((uint64_t)out << 48);
 }
+
+// One truth-table run of a warp's share of a piece: groups [b, e) relative to
+// the piece, all with table `lut` (b, e < 4096).
+inline uint32_t pack_run(uint32_t lut, uint32_t b, uint32_t e) { return lut | (b << 8) | (e << 20); }
+
+// The pieces as the fused kernel stages them: per piece a header, then the
+// packed records of its cells (group-major, G per group). The header starts
+// with one word per compute warp, `first | last << 16`, naming the warp's
+// runs [first, last) in the run list that follows it; warp k's share is the
+// groups [n*k/warps, n*(k+1)/warps) of the piece. Headers are padded to 16
+// bytes and every piece starts on a 16-byte boundary (bulk-copy rules).
+struct PieceBlob {
+  std::vector<uint32_t> words;
+  std::vector<uint32_t> off_words;  // per piece: first word
+  std::vector<uint32_t> bytes;      // per piece: header + records
+  std::vector<uint32_t> hdr_bytes;  // per piece: header
+  uint32_t max_bytes = 0;
+};
+PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps);
 
 }  // namespace rrtl

@@ -131,13 +131,15 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
   const size_t group_bytes = (size_t)G * 8;                                           // records of one group
   v->fused_ok = gp.n_slots <= kMaxSlots && slot_bytes + kRingBufs * 8 * group_bytes <= max_smem;
   uint32_t piece_groups = 8;
+  PieceBlob blob;
   if (v->fused_ok) {
     size_t per_buf = (max_smem - slot_bytes) / kRingBufs;
     piece_groups = (uint32_t)std::min<size_t>(512, per_buf / group_bytes) & ~7u;
     for (;;) {
       build_pieces(gp, piece_groups);
-      size_t tables = gp.pieces.size() * sizeof(GatePieceDev) + gp.segments.size() * 16;
-      if (slot_bytes + tables + (size_t)kRingBufs * piece_groups * group_bytes <= max_smem) break;
+      blob = build_piece_blob(gp, kGateFusedWarps);
+      size_t need = slot_bytes + gp.pieces.size() * sizeof(GatePieceDev) + (size_t)kRingBufs * blob.max_bytes;
+      if (need <= max_smem) break;
       if (piece_groups <= 8) {
         v->fused_ok = false;
         break;
@@ -148,20 +150,12 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     build_pieces(gp, 256);
   }
   if (v->fused_ok) {
-    std::vector<uint2> srecs(gp.cells.size());
-    int32_t c0 = gp.net_slot[kNetConst0];
-    for (size_t i = 0; i < gp.cells.size(); ++i) {
-      const GateCell& c = gp.cells[i];
-      uint32_t a = c.pad ? c0 : gp.net_slot[c.in[0]], b = c.pad ? c0 : gp.net_slot[c.in[1]];
-      uint32_t cc = c.pad ? c0 : gp.net_slot[c.in[2]], o = c.pad ? 0 : gp.net_slot[c.out];
-      uint64_t x = pack_smem_record(a, b, cc, o);
-      srecs[i] = make_uint2((uint32_t)x, (uint32_t)(x >> 32));
-    }
     std::vector<GatePieceDev> pieces;
-    for (auto& p : gp.pieces)
-      pieces.push_back(GatePieceDev{p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u, p.seg_begin, p.seg_end, 0, 0});
-    std::vector<uint4> segs;
-    for (auto& sg : gp.segments) segs.push_back(make_uint4(sg.lut, sg.begin, sg.end, 0));
+    for (size_t i = 0; i < gp.pieces.size(); ++i) {
+      const GatePiece& p = gp.pieces[i];
+      pieces.push_back(GatePieceDev{p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u, blob.off_words[i],
+                                    blob.bytes[i], blob.hdr_bytes[i], 0});
+    }
     std::vector<uint32_t> src_slot;
     for (uint32_t n : gp.source_nets) src_slot.push_back((uint32_t)gp.net_slot[n]);
     for (auto& r : gp.regs) {
@@ -169,19 +163,17 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
       sregs.push_back(GateRegDev{(uint32_t)gp.net_slot[r.q_net], (uint32_t)gp.net_slot[r.d_net],
                                  (uint32_t)gp.net_slot[r.rst_net], fl});
     }
-    upload(v->d_srecs, srecs);
+    upload(v->d_srecs, blob.words);
     upload(v->d_pieces, pieces);
-    upload(v->d_segs, segs);
     upload(v->d_src_net, gp.source_nets);
     upload(v->d_src_slot, src_slot);
     upload(v->d_sregs, sregs);
   }
   GateProgDev& P = v->gdev;
   P = GateProgDev{};
-  P.srecs = v->d_srecs.as<uint2>();
+  P.blob = v->d_srecs.as<uint32_t>();
   P.pieces = v->d_pieces.as<GatePieceDev>();
-  P.segs = v->d_segs.as<uint4>();
-  P.n_segs = (uint32_t)gp.segments.size();
+  P.ring_bytes = blob.max_bytes;
   P.n_pieces = (uint32_t)gp.pieces.size();
   P.n_slots = gp.n_slots;
   P.n_levels = gp.n_levels;

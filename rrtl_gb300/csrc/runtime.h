@@ -53,7 +53,7 @@ struct GateVariant {
   GateProgDev gdev{};
   bool fused_ok = false;
   size_t fused_smem = 0;
-  DevBuf d_srecs, d_pieces, d_segs, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
+  DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
 };
 
 // Per-tile, per-stage force table of a batch for one tile width.
