@@ -7,8 +7,12 @@
 namespace rrtl {
 
 // Warps of the fused gate kernel's CTA; a staged piece carries one run range
-// per warp.
-constexpr uint32_t kGateFusedWarps = 32;
+// per warp. CTAs of fewer warps run several per SM (1024 threads per SM).
+#ifndef RRTL_FUSED_WARPS
+#define RRTL_FUSED_WARPS 32
+#endif
+constexpr uint32_t kGateFusedWarps = RRTL_FUSED_WARPS;
+constexpr uint32_t kGateFusedCtasPerSm = 32 / kGateFusedWarps;
 
 struct GateStimDev {
   uint32_t slot;  // on-chip slot (fused path)
@@ -42,7 +46,7 @@ struct GateRegDev {
 // the size of its run header.
 struct GatePieceDev {
   uint32_t group_begin, n_groups, level, last_of_level;
-  uint32_t off_words, bytes, hdr_bytes, pad;
+  uint32_t off_words, bytes, pad0, pad1;
 };
 
 struct GateProgDev {
@@ -51,6 +55,7 @@ struct GateProgDev {
   const GatePieceDev* pieces;
   uint32_t n_pieces, n_slots, n_levels, piece_groups;
   uint32_t ring_bytes;         // bytes of one ring buffer (largest piece)
+  uint32_t hdr_bytes;          // run header of every staged piece
   const uint32_t* src_net;     // sources loaded per tile and written back
   const uint32_t* src_slot;
   uint32_t n_src;

@@ -35,11 +35,15 @@ constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slo
 #ifndef RRTL_FUSED_UNROLL
 #define RRTL_FUSED_UNROLL 1  // warp steps per unrolled iteration of a truth-table run
 #endif
+#ifndef RRTL_REC_PREFETCH
+#define RRTL_REC_PREFETCH 0  // 1: load the next step's record before this step's operands
+#endif
 #ifndef RRTL_FUSED_V
 #define RRTL_FUSED_V 2  // words per thread in the fused kernel (tiles of 2+ words)
 #endif
 constexpr int kUnroll = RRTL_FUSED_UNROLL;
 static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
+static_assert(kRing == 4, "ring parity arithmetic assumes four buffers");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -149,10 +153,12 @@ __device__ __forceinline__ uint2 lopv(uint2 a, uint2 b, uint2 c) {
   return make_uint2(lop3<L>(a.x, b.x, c.x), lop3<L>(a.y, b.y, c.y));
 }
 
-// Evaluate this thread's cell in groups h+b, h+b+V, ... < e of one
-// truth-table run. `rb` is this thread's record in group 0 of the staged
-// piece and `Sv` its word column of the slot array (row stride W/V vectors);
-// both are shared memory, so every access below is an LDS/STS.
+// Evaluate this thread's cell in groups g, g+V, ... < e of one truth-table
+// run (g already offset by the half-warp). `rb` is this thread's record in
+// group 0 of the staged piece and `Sv` its word column of the slot array (row
+// stride W/V vectors); both are shared memory, so every access below is an
+// LDS/STS. The next step's record load is issued before this step's operands
+// are read, so its latency overlaps the step.
 template <int W, int L>
 __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
                                         int g, int e) {
@@ -163,6 +169,22 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
   constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
   constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
   const T zero{};
+#if RRTL_REC_PREFETCH
+  if (g >= e) return;
+  uint2 r = rb[g * Sh::G];
+#pragma unroll kUnroll
+  for (;;) {
+    const int gn = g + Sh::kSteps;
+    const uint2 rn = gn < e ? rb[gn * Sh::G] : r;
+    const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
+    const T vb = kUseB ? Sv[(r.x >> 16) * R] : zero;
+    const T vc = kUseC ? Sv[(r.y & 0xFFFFu) * R] : zero;
+    Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
+    if (gn >= e) break;
+    g = gn;
+    r = rn;
+  }
+#else
 #pragma unroll kUnroll
   for (; g < e; g += Sh::kSteps) {
     const uint2 r = rb[g * Sh::G];
@@ -171,6 +193,7 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
     const T vc = kUseC ? Sv[(r.y & 0xFFFFu) * R] : zero;
     Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
   }
+#endif
 }
 
 #define RRTL_CASE(n) \
@@ -179,21 +202,28 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
 #define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
 #define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
 
-// This warp's runs [k0, k1) of a staged piece, dispatched once per run.
+// One truth-table run (pack_run) of this warp's share.
+template <int W>
+__device__ __forceinline__ void eval_run(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
+                                         uint32_t run, int h) {
+  const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
+  switch (run & 0xFFu) {
+    RRTL_CASE64(0)
+    RRTL_CASE64(64)
+    RRTL_CASE64(128)
+    RRTL_CASE64(192)
+    default: break;
+  }
+}
+
+// This warp's share of a staged piece: its first run (from its header word)
+// and its further runs extra[k0, k1).
 template <int W>
 __device__ __forceinline__ void eval_piece(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
-                                           const uint32_t* __restrict__ runs, uint32_t k0, uint32_t k1, int h) {
-  for (uint32_t k = k0; k < k1; ++k) {
-    const uint32_t run = runs[k];
-    const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
-    switch (run & 0xFFu) {
-      RRTL_CASE64(0)
-      RRTL_CASE64(64)
-      RRTL_CASE64(128)
-      RRTL_CASE64(192)
-      default: break;
-    }
-  }
+                                           uint32_t run0, const uint32_t* __restrict__ extra, uint32_t k0, uint32_t k1,
+                                           int h) {
+  eval_run<W>(rb, Sv, run0, h);
+  for (uint32_t k = k0; k < k1; ++k) eval_run<W>(rb, Sv, extra[k], h);
 }
 
 __device__ __forceinline__ uint32_t lut_v(uint32_t t, uint32_t a, uint32_t b, uint32_t c) { return lut_eval(t, a, b, c); }
@@ -209,25 +239,31 @@ __device__ __forceinline__ void store_net(uint32_t* p, uint2 v) {
 // Final settle: same evaluation with a runtime truth table, plus a copy of
 // every signal net to the global state (`col` = this thread's first word).
 template <int W>
-__device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb,
-                                                     typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
-                                                     const uint32_t* __restrict__ runs, uint32_t k0, uint32_t k1, int h,
-                                                     const uint32_t* __restrict__ wb, uint32_t* nets, size_t words_pad,
-                                                     uint32_t col) {
+__device__ __forceinline__ void writeback_run(const uint2* __restrict__ rb,
+                                              typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv, uint32_t run, int h,
+                                              const uint32_t* __restrict__ wb, uint32_t* nets, size_t words_pad,
+                                              uint32_t col) {
   using Sh = FusedShape<W>;
   constexpr int R = W / Sh::V;
-  for (uint32_t k = k0; k < k1; ++k) {
-    const uint32_t run = runs[k];
-    const uint32_t lut = run & 0xFFu;
-    const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
-    for (int g = b + h; g < e; g += Sh::kSteps) {
-      const uint2 r = rb[g * Sh::G];
-      const auto v = lut_v(lut, Sv[(r.x & 0xFFFFu) * R], Sv[(r.x >> 16) * R], Sv[(r.y & 0xFFFFu) * R]);
-      Sv[(r.y >> 16) * R] = v;
-      const uint32_t net = __ldg(wb + g * Sh::G);
-      if (net != 0xFFFFFFFFu) store_net(nets + (size_t)net * words_pad + col, v);
-    }
+  const uint32_t lut = run & 0xFFu;
+  const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
+  for (int g = b + h; g < e; g += Sh::kSteps) {
+    const uint2 r = rb[g * Sh::G];
+    const auto v = lut_v(lut, Sv[(r.x & 0xFFFFu) * R], Sv[(r.x >> 16) * R], Sv[(r.y & 0xFFFFu) * R]);
+    Sv[(r.y >> 16) * R] = v;
+    const uint32_t net = __ldg(wb + g * Sh::G);
+    if (net != 0xFFFFFFFFu) store_net(nets + (size_t)net * words_pad + col, v);
   }
+}
+
+template <int W>
+__device__ __forceinline__ void eval_piece_writeback(const uint2* __restrict__ rb,
+                                                     typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv, uint32_t run0,
+                                                     const uint32_t* __restrict__ extra, uint32_t k0, uint32_t k1, int h,
+                                                     const uint32_t* __restrict__ wb, uint32_t* nets, size_t words_pad,
+                                                     uint32_t col) {
+  writeback_run<W>(rb, Sv, run0, h, wb, nets, words_pad, col);
+  for (uint32_t k = k0; k < k1; ++k) writeback_run<W>(rb, Sv, extra[k], h, wb, nets, words_pad, col);
 }
 
 template <int W>
@@ -243,7 +279,7 @@ __device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, u
 }
 
 template <int W>
-__global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDev P, GateRunDev R) {
+__global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused_kernel(GateProgDev P, GateRunDev R) {
   constexpr uint32_t G = 32 / W;
   extern __shared__ __align__(128) uint8_t smem[];
   const size_t ring_bytes = P.ring_bytes;  // one ring buffer: a staged piece
@@ -258,7 +294,6 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
   uint32_t* S = reinterpret_cast<uint32_t*>(hdr + kFusedHeader);
   // piece table, staged once per launch
   GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(hdr + kFusedHeader + fused_slot_bytes(P.n_slots, W));
-  __shared__ int s_abort;
 
   using Sh = FusedShape<W>;
   using T = typename WordVec<Sh::V>::T;
@@ -277,40 +312,54 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
 
   for (uint32_t i = tid; i < P.n_pieces; i += blockDim.x) pieces[i] = P.pieces[i];
   if (tid == 0) {
-    s_abort = 0;
     *hacc = 0ull;
     for (int i = 0; i < kRing; ++i) mbar_init(&bars[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  if (tid == 0) {
-    uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
-    for (uint64_t q = 0; q < n0; ++q) {
-      const GatePieceDev pc = P.pieces[q % P.n_pieces];
-      bulk_load(ring + (q % kRing) * ring_bytes, P.blob + pc.off_words, pc.bytes, &bars[q % kRing]);
-    }
-  }
-
-  uint64_t q = 0;
-  T* const Sv = reinterpret_cast<T*>(S + w);
-  // Thread 0 waits for a piece's records; the CTA barrier that follows
-  // publishes them to every thread. The wait for piece q+1 is folded into the
-  // barrier that closes piece q, so each piece costs one barrier.
-  auto wait_piece = [&](uint64_t qq) {
-    if (qq >= total_q) return;
-    if (resident && qq >= P.n_pieces) return;
-    uint32_t buf = resident ? (uint32_t)qq : (uint32_t)(qq % kRing);
-    uint32_t par = resident ? 0u : (uint32_t)((qq / kRing) & 1u);
-    if (!mbar_wait(&bars[buf], par)) {
-      s_abort = 1;
-      atomicExch(R.err, (uint32_t)RRTL_E_TIMEOUT);
-    }
+  // Ring bookkeeping. Piece q of this CTA's stream lands in buffer q % kRing;
+  // its copy completes phase (q / kRing) & 1 of that buffer's mbarrier.
+  // Thread 0 keeps the ring full: at the start of piece q it refills the
+  // buffer that piece q-1 released (the CTA barrier ending q-1 guarantees
+  // no warp still reads it); after its share of piece q it waits for piece
+  // q+1 to land, and the barrier that ends piece q publishes that piece to
+  // every thread. With at most kRing
+  // pieces the buffers are filled once and stay resident. A wait that runs
+  // out sets the error word, and the barrier's OR ends the CTA's work.
+  uint64_t issued = 0;      // copies issued (thread 0)
+  uint32_t next_piece = 0;  // piece index of the next copy (thread 0)
+  uint32_t next_off = 0, next_bytes = 0;  // its blob offset and size, loaded one copy ahead
+  int abort_flag = 0;       // thread 0: a bounded wait ran out
+  auto load_next = [&]() {
+    next_off = pieces[next_piece].off_words;
+    next_bytes = pieces[next_piece].bytes;
   };
-  if (tid == 0) wait_piece(0);
-  __syncthreads();
+  auto issue_next = [&]() {
+    const uint32_t b = (uint32_t)issued & (kRing - 1u);
+    bulk_load(ring + b * ring_bytes, P.blob + next_off, next_bytes, &bars[b]);
+    ++issued;
+    if (++next_piece == P.n_pieces) next_piece = 0;
+    load_next();
+  };
+  auto timed_out = [&]() {
+    abort_flag = 1;
+    atomicExch(R.err, (uint32_t)RRTL_E_TIMEOUT);
+  };
+  if (tid == 0) {
+    const uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
+    load_next();
+    while (issued < n0) issue_next();
+    const uint32_t first = resident ? P.n_pieces : (total_q ? 1u : 0u);
+    for (uint32_t b = 0; b < first; ++b)
+      if (!mbar_wait(&bars[b], 0u)) timed_out();
+  }
+  uint64_t q = 0;  // pieces consumed
+  T* const Sv = reinterpret_cast<T*>(S + w);
+  const uint32_t hdr_bytes = P.hdr_bytes;
+  bool aborted = __syncthreads_or(abort_flag) != 0;
 
-  for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !s_abort; tile += gridDim.x) {
+  for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !aborted; tile += gridDim.x) {
     const uint32_t col0 = tile * W;
     // constants, scratch, sources
     for (uint32_t i = tid; i < W; i += blockDim.x) {
@@ -346,33 +395,35 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
       }
       __syncthreads();
       for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
-        const GatePieceDev pc = pieces[p];
-        const uint32_t buf = resident ? p : (uint32_t)(q % kRing);
+        const uint32_t buf = resident ? p : ((uint32_t)q & (kRing - 1u));
+        if (!resident && tid == 0 && q > 0 && issued < total_q) issue_next();
         {
-          // the staged piece: per-warp run ranges, the run list, then the records
-          const uint32_t* ph = reinterpret_cast<const uint32_t*>(ring + buf * ring_bytes);
-          const uint2* rb = reinterpret_cast<const uint2*>(ring + buf * ring_bytes + pc.hdr_bytes) + cidx;
-          const uint32_t kr = ph[warp], k0 = kr & 0xFFFFu, k1 = kr >> 16;
+          // the staged piece: two header words per warp, the further runs, then the records
+          const uint8_t* pb = ring + buf * ring_bytes;
+          const uint2 hw = reinterpret_cast<const uint2*>(pb)[warp];
+          const uint32_t* extra = reinterpret_cast<const uint32_t*>(pb) + 2 * kFusedWarps;
+          const uint2* rb = reinterpret_cast<const uint2*>(pb + hdr_bytes) + cidx;
           if (final_pass)
-            eval_piece_writeback<W>(rb, Sv, ph + kFusedWarps, k0, k1, (int)h,
-                                    P.wb_net + (size_t)pc.group_begin * G + cidx, R.nets, R.words_pad, col0 + w);
+            eval_piece_writeback<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h,
+                                    P.wb_net + (size_t)pieces[p].group_begin * G + cidx, R.nets, R.words_pad, col0 + w);
           else
-            eval_piece<W>(rb, Sv, ph + kFusedWarps, k0, k1, (int)h);
+            eval_piece<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h);
         }
-        if (pc.last_of_level && R.has_forces) {
+        if (!resident && tid == 0) {
+          // warp 0 has a lighter share: wait for the next piece while the others finish
+          const uint64_t qn = q + 1;
+          if (qn < total_q && !mbar_wait(&bars[(uint32_t)qn & (kRing - 1u)], ((uint32_t)qn >> 2) & 1u)) timed_out();
+        }
+        if (R.has_forces && pieces[p].last_of_level) {
           __syncthreads();
-          apply_forces<W>(R, S, tile, pc.level + 1, stages);
+          apply_forces<W>(R, S, tile, pieces[p].level + 1, stages);
         }
-        if (tid == 0) wait_piece(q + 1);
-        __syncthreads();
-        if (s_abort) break;
-        if (!resident && tid == 0 && q + kRing < total_q) {
-          uint64_t nq = q + kRing;
-          const GatePieceDev npc = pieces[nq % P.n_pieces];
-          bulk_load(ring + buf * ring_bytes, P.blob + npc.off_words, npc.bytes, &bars[buf]);
+        if (__syncthreads_or(abort_flag)) {
+          aborted = true;
+          break;
         }
       }
-      if (s_abort) break;
+      if (aborted) break;
       if (final_pass) break;
       // record
       if (R.n_rec) {
@@ -429,7 +480,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
         __syncthreads();
       }
     }
-    if (s_abort) break;
+    if (aborted) break;
     if (!R.final_settle) {
       for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
         uint32_t k = i / W, ww = i % W;
@@ -438,12 +489,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1) gate_fused_kernel(GateProgDe
     }
     __syncthreads();
   }
-  if (s_abort && tid == 0) {
-    // let any copy still in flight land before the CTA's shared memory is released
-    for (int i = 0; i < kRing; ++i) {
-      uint64_t last = q + i;
-      if (last < total_q) (void)mbar_wait(&bars[last % kRing], (uint32_t)((last / kRing) & 1u));
-    }
+  if (aborted && tid == 0 && !resident) {
+    // let every copy still in flight land before the CTA's shared memory is released
+    for (uint64_t k = q; k < issued; ++k) (void)mbar_wait(&bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u);
   }
 }
 
@@ -567,6 +615,23 @@ cudaError_t gate_fused_prepare(const GateProgDev& P, size_t smem) {
     case 16: return fused_prepare_w<2>(smem);
     case 32: return fused_prepare_w<1>(smem);
     default: return cudaErrorInvalidValue;
+  }
+}
+
+// Resident CTAs of the fused kernel per SM at `smem` bytes of shared memory.
+template <int W>
+static int fused_ctas_w(size_t smem) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, gate_fused_kernel<W>, kFusedThreads, smem) != cudaSuccess) n = 1;
+  return n > 0 ? n : 1;
+}
+
+int gate_fused_ctas_per_sm(const GateProgDev& P, size_t smem) {
+  switch (P.group) {
+    case 4: return fused_ctas_w<8>(smem);
+    case 8: return fused_ctas_w<4>(smem);
+    case 16: return fused_ctas_w<2>(smem);
+    default: return fused_ctas_w<1>(smem);
   }
 }
 

@@ -526,28 +526,88 @@ void build_pieces(GateProgram& gp, uint32_t piece_groups) {
   }
 }
 
-PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps) {
+// Split one piece's truth-table runs over `warps` warps. A warp step covers
+// `steps_per` groups of one run, and every run a warp takes costs about
+// `run_cost` steps of dispatch. The split fills warps in order, cutting runs
+// at multiples of `steps_per` groups, with the smallest per-warp cost cap
+// (found by bisection) that lets `warps` warps take every group; warp 0,
+// which also keeps the ring full, gets `lead_weight` of the cap.
+static std::vector<std::vector<uint32_t>> split_piece(const GateProgram& gp, const GatePiece& pc, uint32_t warps,
+                                                      double lead_weight, uint32_t steps_per, double run_cost) {
+  // greedy fill under cap `cap`; returns warps used (warps + 1 when it does not fit)
+  auto fill = [&](double cap, std::vector<std::vector<uint32_t>>* out) -> uint32_t {
+    uint32_t k = 0;
+    double used = 0;
+    for (uint32_t s = pc.seg_begin; s < pc.seg_end; ++s) {
+      const GateSegment& sg = gp.segments[s];
+      uint32_t b = sg.begin;
+      while (b < sg.end) {
+        if (k >= warps) return warps + 1;
+        const double c = (k == 0 ? lead_weight : 1.0) * cap;
+        const double room = c - used - run_cost;
+        const uint32_t left = sg.end - b;
+        uint32_t take = room >= 1.0 ? (uint32_t)room * steps_per : 0u;
+        if (take >= left) take = left;
+        if (take > 0) {
+          if (out) (*out)[k].push_back(pack_run(sg.lut, b, b + take));
+          used += run_cost + (double)((take + steps_per - 1) / steps_per);
+          b += take;
+        }
+        if (b < sg.end) {
+          ++k;
+          used = 0;
+        }
+      }
+    }
+    return k + 1;
+  };
+  double lo = 0, hi = run_cost;
+  for (uint32_t s = pc.seg_begin; s < pc.seg_end; ++s)
+    hi += (double)((gp.segments[s].end - gp.segments[s].begin + steps_per - 1) / steps_per) + run_cost;
+  hi = hi / std::min(lead_weight, 1.0) + 1.0;
+  for (int it = 0; it < 40 && hi - lo > 0.25; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (fill(mid, nullptr) <= warps) hi = mid;
+    else lo = mid;
+  }
+  std::vector<std::vector<uint32_t>> out(warps);
+  if (fill(hi, &out) > warps) throw RrtlError("E_INTERNAL", "piece split failed");
+  return out;
+}
+
+PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps, double lead_weight, uint32_t steps_per,
+                           double run_cost) {
   PieceBlob pb;
   const uint32_t G = gp.group;
   const int32_t c0 = gp.net_slot[kNetConst0];
+  // per piece: the header words (2 per warp + extra runs), built first to size the common header
+  std::vector<std::vector<uint32_t>> heads;
+  uint32_t max_extra = 0;
   for (const GatePiece& pc : gp.pieces) {
-    std::vector<uint32_t> hdr(warps, 0), runs;
+    if (pc.n_groups >= 4096) throw RrtlError("E_GATE_SCOPE", "piece too large for its header");
+    std::vector<std::vector<uint32_t>> split = split_piece(gp, pc, warps, lead_weight, steps_per, run_cost);
+    std::vector<uint32_t> head(2 * warps, 0), extra;
     for (uint32_t k = 0; k < warps; ++k) {
-      const uint32_t g0 = (uint32_t)((uint64_t)pc.n_groups * k / warps), g1 = (uint32_t)((uint64_t)pc.n_groups * (k + 1) / warps);
-      const uint32_t first = (uint32_t)runs.size();
-      for (uint32_t s = pc.seg_begin; s < pc.seg_end; ++s) {
-        const GateSegment& sg = gp.segments[s];
-        const uint32_t b = std::max(g0, sg.begin), e = std::min(g1, sg.end);
-        if (b < e) runs.push_back(pack_run(sg.lut, b, e));
-      }
-      hdr[k] = first | ((uint32_t)runs.size() << 16);
+      const std::vector<uint32_t>& mine = split[k];
+      head[2 * k] = mine.empty() ? 0u : mine[0];
+      const uint32_t first = (uint32_t)extra.size();
+      for (size_t i = 1; i < mine.size(); ++i) extra.push_back(mine[i]);
+      head[2 * k + 1] = first | ((uint32_t)extra.size() << 16);
     }
-    if (pc.n_groups >= 4096 || runs.size() >= 65536) throw RrtlError("E_GATE_SCOPE", "piece too large for its header");
+    if (extra.size() >= 65536) throw RrtlError("E_GATE_SCOPE", "piece too large for its header");
+    max_extra = std::max(max_extra, (uint32_t)extra.size());
+    head.insert(head.end(), extra.begin(), extra.end());
+    heads.push_back(std::move(head));
+  }
+  const uint32_t hdr_words = (2 * warps + max_extra + 3) & ~3u;
+  pb.hdr_bytes = hdr_words * 4;
+  for (size_t i = 0; i < gp.pieces.size(); ++i) {
+    const GatePiece& pc = gp.pieces[i];
     const uint32_t start = (uint32_t)pb.words.size();
-    pb.words.insert(pb.words.end(), hdr.begin(), hdr.end());
-    pb.words.insert(pb.words.end(), runs.begin(), runs.end());
-    while (pb.words.size() % 4) pb.words.push_back(0);
-    const uint32_t hdr_bytes = (uint32_t)(pb.words.size() - start) * 4;
+    std::vector<uint32_t>& head = heads[i];
+    // extra-run indices are relative to the extra list, which starts after the 2*warps words
+    pb.words.insert(pb.words.end(), head.begin(), head.end());
+    pb.words.resize(start + hdr_words, 0);
     for (uint32_t g = pc.group_begin; g < pc.group_begin + pc.n_groups; ++g)
       for (uint32_t k = 0; k < G; ++k) {
         const GateCell& c = gp.cells[(size_t)g * G + k];
@@ -560,7 +620,6 @@ PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps) {
     while (pb.words.size() % 4) pb.words.push_back(0);
     pb.off_words.push_back(start);
     pb.bytes.push_back((uint32_t)(pb.words.size() - start) * 4);
-    pb.hdr_bytes.push_back(hdr_bytes);
     pb.max_bytes = std::max(pb.max_bytes, pb.bytes.back());
   }
   return pb;

@@ -109,19 +109,23 @@ inline uint64_t pack_smem_record(uint32_t a, uint32_t b, uint32_t c, uint32_t ou
 // the piece, all with table `lut` (b, e < 4096).
 inline uint32_t pack_run(uint32_t lut, uint32_t b, uint32_t e) { return lut | (b << 8) | (e << 20); }
 
-// The pieces as the fused kernel stages them: per piece a header, then the
-// packed records of its cells (group-major, G per group). The header starts
-// with one word per compute warp, `first | last << 16`, naming the warp's
-// runs [first, last) in the run list that follows it; warp k's share is the
-// groups [n*k/warps, n*(k+1)/warps) of the piece. Headers are padded to 16
-// bytes and every piece starts on a 16-byte boundary (bulk-copy rules).
+// The pieces as the fused kernel stages them: per piece a header of
+// `hdr_bytes` (the same for every piece), then the packed records of its
+// cells (group-major, G per group). Header words 2k and 2k+1 belong to warp
+// k: its first truth-table run (pack_run; 0 if it has none) and, as
+// `first | last << 16`, the range of its further runs in the list that starts
+// at word 2*warps. Warp shares are contiguous, balanced by cost: a warp step
+// covers `steps_per` groups and each run costs `run_cost` steps more; warp 0,
+// which also keeps the ring full, gets `lead_weight` of a normal share.
+// Every piece starts on a 16-byte boundary (bulk-copy rules).
 struct PieceBlob {
   std::vector<uint32_t> words;
   std::vector<uint32_t> off_words;  // per piece: first word
   std::vector<uint32_t> bytes;      // per piece: header + records
-  std::vector<uint32_t> hdr_bytes;  // per piece: header
+  uint32_t hdr_bytes = 0;
   uint32_t max_bytes = 0;
 };
-PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps);
+PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps, double lead_weight, uint32_t steps_per,
+                           double run_cost);
 
 }  // namespace rrtl

@@ -13,6 +13,7 @@ namespace rrtl {
 // kernels (gate_kernels.cu, word_kernels.cu)
 size_t gate_fused_smem_bytes(const GateProgDev& P);
 cudaError_t gate_fused_prepare(const GateProgDev& P, size_t smem);
+int gate_fused_ctas_per_sm(const GateProgDev& P, size_t smem);
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st);
 cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st);
@@ -91,6 +92,16 @@ const PackedSignal& signal_of(rrtl_design* d, uint32_t s) {
 }
 
 constexpr uint32_t kRingBufs = 4;  // record ring buffers of the fused kernel
+// Share of a piece's groups given to warp 0, which also keeps the ring full.
+#ifndef RRTL_LEAD_WARP_WEIGHT
+#define RRTL_LEAD_WARP_WEIGHT 0.7
+#endif
+constexpr double kLeadWarpWeight = RRTL_LEAD_WARP_WEIGHT;
+// Dispatch cost of one truth-table run, in warp steps (work split of a piece).
+#ifndef RRTL_RUN_COST
+#define RRTL_RUN_COST 4.0
+#endif
+constexpr double kRunCost = RRTL_RUN_COST;
 
 uint32_t log2_words(uint32_t W) { return W == 8 ? 3u : W == 4 ? 2u : W == 2 ? 1u : 0u; }
 
@@ -126,7 +137,11 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
   upload(v->d_lgb, gp.level_group_begin);
   upload(v->d_gregs, gregs);
 
-  const size_t max_smem = d->ctx->max_smem;
+  // shared memory of one CTA: all of it, or an equal share when several
+  // CTAs of fewer warps are meant to share an SM (1 KB per CTA is reserved)
+  const size_t max_smem = kGateFusedCtasPerSm == 1
+                              ? d->ctx->max_smem
+                              : std::min(d->ctx->max_smem, d->ctx->max_smem_sm / kGateFusedCtasPerSm - 1024);
   const size_t slot_bytes = (((size_t)gp.n_slots * W * 4 + 15) & ~(size_t)15) + 128;  // slots + header
   const size_t group_bytes = (size_t)G * 8;                                           // records of one group
   v->fused_ok = gp.n_slots <= kMaxSlots && slot_bytes + kRingBufs * 8 * group_bytes <= max_smem;
@@ -137,7 +152,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     piece_groups = (uint32_t)std::min<size_t>(512, per_buf / group_bytes) & ~7u;
     for (;;) {
       build_pieces(gp, piece_groups);
-      blob = build_piece_blob(gp, kGateFusedWarps);
+      blob = build_piece_blob(gp, kGateFusedWarps, kLeadWarpWeight, W >= 2 ? 2u : 1u, kRunCost);
       size_t need = slot_bytes + gp.pieces.size() * sizeof(GatePieceDev) + (size_t)kRingBufs * blob.max_bytes;
       if (need <= max_smem) break;
       if (piece_groups <= 8) {
@@ -154,7 +169,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     for (size_t i = 0; i < gp.pieces.size(); ++i) {
       const GatePiece& p = gp.pieces[i];
       pieces.push_back(GatePieceDev{p.group_begin, p.n_groups, p.level, p.last_of_level ? 1u : 0u, blob.off_words[i],
-                                    blob.bytes[i], blob.hdr_bytes[i], 0});
+                                    blob.bytes[i], 0, 0});
     }
     std::vector<uint32_t> src_slot;
     for (uint32_t n : gp.source_nets) src_slot.push_back((uint32_t)gp.net_slot[n]);
@@ -174,6 +189,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
   P.blob = v->d_srecs.as<uint32_t>();
   P.pieces = v->d_pieces.as<GatePieceDev>();
   P.ring_bytes = blob.max_bytes;
+  P.hdr_bytes = blob.hdr_bytes;
   P.n_pieces = (uint32_t)gp.pieces.size();
   P.n_slots = gp.n_slots;
   P.n_levels = gp.n_levels;
@@ -196,6 +212,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
       v->fused_ok = false;
     } else {
       cuda_check(gate_fused_prepare(P, v->fused_smem), "gate_fused_prepare");
+      v->fused_ctas = (uint32_t)gate_fused_ctas_per_sm(P, v->fused_smem);
     }
   }
   // nets that hold their end-of-cycle value in a slot (recordable on the fused path)
@@ -233,7 +250,7 @@ uint32_t choose_tile_words(rrtl_design* d, uint32_t words) {
   constexpr double kBarrierSteps = 4.0;
   constexpr double kStepCost[4] = {1.45, 1.25, 1.1, 1.0};
   const GateProgram& gp = d->gp();
-  const uint32_t sms = d->ctx->sm_count;
+  const uint32_t sms = d->ctx->sm_count * kGateFusedCtasPerSm;
   double best = INFINITY;
   uint32_t best_w = d->gate_w_max;
   for (uint32_t W = d->gate_w_max; W >= 1; W /= 2) {
@@ -242,7 +259,8 @@ uint32_t choose_tile_words(rrtl_design* d, uint32_t words) {
     for (uint32_t L = 0; L < gp.n_levels; ++L) {
       double cells = (double)(gp.level_group_begin[L + 1] - gp.level_group_begin[L]) * gp.group;
       double groups = std::ceil(cells / G);
-      per_tile += std::ceil(groups / 32.0) * kStepCost[log2_words(W)] + kBarrierSteps * std::max(1.0, std::ceil(groups / 512.0));
+      per_tile += std::ceil(groups / (double)kGateFusedWarps) * kStepCost[log2_words(W)] +
+                  kBarrierSteps * std::max(1.0, std::ceil(groups / 512.0));
     }
     uint32_t tiles = (words + W - 1) / W;
     double t = std::ceil((double)tiles / sms) * per_tile;
@@ -443,7 +461,7 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
 
   Timer tm(b);
   if (fused) {
-    uint32_t grid = std::min<uint32_t>(R.n_tiles, d->ctx->sm_count);
+    uint32_t grid = std::min<uint32_t>(R.n_tiles, d->ctx->sm_count * v->fused_ctas);
     cuda_check(launch_gate_fused(v->gdev, R, grid, v->fused_smem, st), "gate_fused_kernel");
   } else {
     for (uint64_t c = 0; c < run.cycles; ++c) cuda_check(launch_gate_plain(v->gdev, R, c, 0, st), "gate_plain_kernel");
@@ -602,11 +620,13 @@ rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out) {
     try {
       set_device(c);
       cuda_check(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "stream");
-      int sms = 0, smem = 0;
+      int sms = 0, smem = 0, smem_sm = 0;
       cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "attr");
       cuda_check(cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device), "attr");
+      cuda_check(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device), "attr");
       c->sm_count = (uint32_t)sms;
       c->max_smem = (size_t)smem;
+      c->max_smem_sm = (size_t)smem_sm;
       for (auto& e : c->events) cuda_check(cudaEventCreate(&e), "event");
     } catch (...) {
       delete c;

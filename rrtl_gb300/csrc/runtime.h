@@ -53,6 +53,7 @@ struct GateVariant {
   GateProgDev gdev{};
   bool fused_ok = false;
   size_t fused_smem = 0;
+  uint32_t fused_ctas = 1;  // resident fused CTAs per SM
   DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
 };
 
@@ -73,7 +74,8 @@ struct rrtl_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   uint32_t sm_count = 0;
-  size_t max_smem = 0;
+  size_t max_smem = 0;      // opt-in shared memory per block
+  size_t max_smem_sm = 0;   // shared memory per SM
   cudaEvent_t events[8] = {};
 };
 
