@@ -200,6 +200,81 @@ def gate_fanins(js):
     return out
 
 
+def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
+    """Uneven job stream (the C4 shape, scaled): jobs on netlists of 5k-200k
+    gates, lanes log-uniform 32-65,536, cycles log-uniform 10-5,000 (the C4
+    range 100-50,000 divided by 10 so the plain paths finish in the run), 30%
+    fault jobs. Persistent job queue vs the plain one-launch-per-cycle path
+    on the whole stream, and the plain path with each run's launches captured
+    as a CUDA graph on the first `graph_jobs` jobs; every job's hash and
+    detection vector must agree across the paths."""
+    from rrtl_gb300.workloads import job_faults, job_stream, job_stream_designs, netlist_run_spec
+
+    t0 = time.perf_counter()
+    designs = job_stream_designs(n_designs)
+    cds = []
+    for d, meta in designs:
+        stim, rec = netlist_run_spec(meta)
+        cds.append((meta, sim.CompiledDesign(d.to_json(), meta.top, ctx), stim, rec))
+    jobs = job_stream(n_jobs, len(cds), cycles_lo=10, cycles_hi=5000)
+    setup_s = time.perf_counter() - t0
+
+    def make(j, path):
+        meta, cd, _, _ = cds[j.design]
+        g = sim.GpuBatchSimulator(cd, lanes=j.lanes)
+        g.set_path(path)
+        if j.fault:
+            g.set_faults(job_faults(meta, j.lanes, j.seed))
+        return g
+
+    def mode(j):
+        return sim.REC_HASH | (sim.REC_DETECT if j.fault else 0)
+
+    lane_cycles = sum(j.lanes * j.cycles for j in jobs)
+    gate_evals = sum(j.lanes * j.cycles * cds[j.design][1].info.n_gates for j in jobs)
+    # persistent queue: one launch drains every job
+    batches = [make(j, sim.PATH_FUSED) for j in jobs]
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    q = [ctx.submit(g, j.cycles, seed=j.seed, stim=cds[j.design][2], record=cds[j.design][3], mode=mode(j))
+         for g, j in zip(batches, jobs)]
+    ctx.launch()
+    ctx.wait()
+    persist_s = time.perf_counter() - t0
+    persist_dev_ms = ctx.queue_ms
+    results = [jq.outputs for jq in q]
+    widths = sorted({g.tile_words for g in batches})
+    del batches, q
+    out = {"jobs": n_jobs, "designs_gates": [m.n_gates for m, _, _, _ in cds],
+           "fault_jobs": sum(j.fault for j in jobs), "lane_cycles": lane_cycles, "gate_evals": gate_evals,
+           "lanes": "log-uniform 32-65536", "cycles": "log-uniform 10-5000 (C4 range / 10)",
+           "persistent": {"value": lane_cycles / persist_s, "unit": "lane-cycles/s", "wall_s": persist_s,
+                          "device_ms": persist_dev_ms, "gate_evals_per_s": gate_evals / persist_s,
+                          "tile_words": widths, "launches": 1},
+           "setup_s": setup_s}
+    if plain:
+        same = True
+        for name, path, n in (("plain", sim.PATH_PLAIN, len(jobs)), ("plain_graph", sim.PATH_PLAIN_GRAPH, graph_jobs)):
+            tot = 0.0
+            sub = jobs[:n]
+            for j, ref in zip(sub, results):
+                g = make(j, path)
+                ctx.synchronize()
+                t0 = time.perf_counter()
+                r = g.run(j.cycles, seed=j.seed, stim=cds[j.design][2], record=cds[j.design][3], mode=mode(j))
+                tot += time.perf_counter() - t0
+                same = same and np.array_equal(r["hash"], ref["hash"]) and (
+                    r["detect"] is None or np.array_equal(r["detect"], ref["detect"]))
+                del g
+            sub_lc = sum(j.lanes * j.cycles for j in sub)
+            out[name] = {"value": sub_lc / tot, "unit": "lane-cycles/s", "wall_s": tot, "jobs": len(sub),
+                         "launches": sum(j.cycles + 1 for j in sub) if path == sim.PATH_PLAIN else len(sub)}
+        out["speedup_vs_plain"] = out["persistent"]["value"] / out["plain"]["value"]
+        out["speedup_vs_plain_graph"] = out["persistent"]["value"] / out["plain_graph"]["value"]
+        out["bitexact_across_paths"] = bool(same)
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -249,6 +324,9 @@ def main():
     ap.add_argument("--lanes", type=int, default=LANES, help="lanes per GPU (profiling cases)")
     ap.add_argument("--cycles", type=int, default=CYCLES, help="cycles per step (profiling cases)")
     ap.add_argument("--tile-words", type=int, default=0, help="fused tile width in 32-lane words (0 = automatic)")
+    ap.add_argument("--jobs", type=int, default=96, help="jobs in the uneven job-stream leg (0 = skip it)")
+    ap.add_argument("--job-designs", type=int, default=8, help="distinct netlists in the job stream")
+    ap.add_argument("--no-plain-jobs", action="store_true", help="job stream: skip the plain-path comparison")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
     args.warmup = max(args.warmup, 3)
@@ -374,6 +452,8 @@ def main():
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
     }
+    if args.jobs > 0:
+        out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import binding as ob
 

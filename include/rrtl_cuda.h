@@ -213,8 +213,10 @@ rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv,
 
 /* ---- execution path selection -------------------------------------------
  * RRTL_PATH_FUSED: persistent multi-cycle kernel with on-chip net slots (default).
- * RRTL_PATH_PLAIN: one kernel launch per cycle, nets in HBM (the baseline). */
-enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1 };
+ * RRTL_PATH_PLAIN: one kernel launch per cycle, nets in HBM (the baseline).
+ * RRTL_PATH_PLAIN_GRAPH: the plain path's per-cycle launches of one run
+ *   captured into a CUDA graph and submitted as one graph launch. */
+enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1, RRTL_PATH_PLAIN_GRAPH = 2 };
 rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
 
 /* Gate engine, fused path: 32-lane words per tile (8, 4, 2 or 1; 0 = chosen
@@ -229,6 +231,34 @@ rrtl_status rrtl_batch_tile_words(rrtl_batch* b, uint32_t* words);
 /* Device time of the last run/tick_many in milliseconds (CUDA events on the
  * context stream around the kernels of that call). */
 rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms);
+
+/* ---- device job queue ------------------------------------------------------
+ * The single-GPU form of the reference's lane-shard scheduler
+ * (DistributedRuntime, crates/rrtl-runtime/src/lib.rs:6785-7760): jobs are
+ * runs on gate-engine batches of any design, lane count, cycle count and
+ * fault list. rrtl_queue_launch packs every queued job into one persistent
+ * kernel that drains a device-side list of (job, tile) items, longest first,
+ * so uneven jobs share the GPU. A job's results are exactly those of
+ * rrtl_batch_run on the same batch. The run's arrays are copied at submit;
+ * its output buffers must stay valid until the job is finished. A batch
+ * holds at most one unfinished job. No counterpart in the reference's API
+ * (its scheduler is a Rust type, not a C ABI). */
+typedef struct {
+  rrtl_batch* batch;
+  rrtl_run run;
+} rrtl_job;
+
+enum { RRTL_JOB_QUEUED = 0, RRTL_JOB_RUNNING = 1, RRTL_JOB_DONE = 2, RRTL_JOB_FAILED = 3 };
+
+rrtl_status rrtl_queue_submit(rrtl_ctx* ctx, const rrtl_job* job, uint64_t* id);
+/* Launch every queued job (asynchronous). */
+rrtl_status rrtl_queue_launch(rrtl_ctx* ctx);
+/* Wait for every launched job and copy its outputs to the caller's buffers. */
+rrtl_status rrtl_queue_wait(rrtl_ctx* ctx);
+/* RRTL_JOB_*; a finished launch is completed (outputs copied) by the poll. */
+rrtl_status rrtl_queue_poll(rrtl_ctx* ctx, uint64_t id, uint32_t* status);
+/* Device time of the last launch (ms), valid after rrtl_queue_wait. */
+rrtl_status rrtl_queue_last_ms(rrtl_ctx* ctx, float* ms);
 
 /* ---- allocation-free tick_many (word engine) -----------------------------
  * No counterpart in the reference: it exists for callers that may not call

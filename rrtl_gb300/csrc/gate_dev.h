@@ -89,6 +89,28 @@ struct GateRunDev {
   uint32_t final_settle;
   uint32_t* nets;             // [rows][words_pad]
   uint32_t* err;              // device status word
+  unsigned long long cycle_base;  // absolute cycle of the launch's first cycle (stimulus, records)
+};
+
+// One job of the device-side queue: a run over one batch with its program.
+struct GateJobDev {
+  GateProgDev P;
+  GateRunDev R;
+};
+
+// One queue item: cycles [c0, c0 + ncyc) of one tile of one job; flags bit 0:
+// the job's closing settle follows.
+struct GateItemDev {
+  uint32_t job, tile;
+  unsigned long long c0;
+  uint32_t ncyc, flags;
+};
+
+struct GateQueueDev {
+  const GateJobDev* jobs;
+  const GateItemDev* items;
+  uint32_t n_items;
+  uint32_t* next;  // atomic item counter (zeroed before the launch)
 };
 
 }  // namespace rrtl

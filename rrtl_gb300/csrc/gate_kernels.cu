@@ -278,25 +278,63 @@ __device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, u
   }
 }
 
-template <int W>
-__global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused_kernel(GateProgDev P, GateRunDev R) {
-  constexpr uint32_t G = 32 / W;
-  extern __shared__ __align__(128) uint8_t smem[];
-  const size_t ring_bytes = P.ring_bytes;  // one ring buffer: a staged piece
-  // layout: [piece ring][128-byte header: 4 mbarriers, hash accumulator,
-  // detect state][slots][piece table]; every region starts on a 16-byte
-  // boundary (ring buffers are bulk-copy destinations)
-  uint8_t* ring = smem;
-  uint8_t* hdr = smem + (size_t)kRing * ring_bytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(hdr);
-  unsigned long long* hacc = reinterpret_cast<unsigned long long*>(hdr + kRing * 8);
-  uint32_t* dstate = reinterpret_cast<uint32_t*>(hdr + kRing * 8 + 8);  // diff[8], detected[8]
-  uint32_t* S = reinterpret_cast<uint32_t*>(hdr + kFusedHeader);
-  // piece table, staged once per launch
-  GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(hdr + kFusedHeader + fused_slot_bytes(P.n_slots, W));
+// Per-CTA state of the fused kernels that outlives one tile. The 128-byte
+// header at the start of shared memory holds the ring's mbarriers, the hash
+// accumulator and the detect state; everything after it is laid out per tile
+// from the tile's program: [piece ring][slots][piece table], each region on
+// a 16-byte boundary (ring buffers are bulk-copy destinations).
+struct FusedCta {
+  uint64_t* bars;
+  unsigned long long* hacc;
+  uint32_t* dstate;  // diff[8], detected[8]
+  uint8_t* dyn;
+  uint64_t q;       // pieces consumed (every thread)
+  uint64_t issued;  // copies issued (thread 0)
+  bool aborted;
+};
 
+__device__ __forceinline__ void fused_cta_init(FusedCta& cta, uint8_t* smem) {
+  cta.bars = reinterpret_cast<uint64_t*>(smem);
+  cta.hacc = reinterpret_cast<unsigned long long*>(smem + kRing * 8);
+  cta.dstate = reinterpret_cast<uint32_t*>(smem + kRing * 8 + 8);
+  cta.dyn = smem + kFusedHeader;
+  cta.q = 0;
+  cta.issued = 0;
+  cta.aborted = false;
+  if (threadIdx.x == 0) {
+    *cta.hacc = 0ull;
+    for (int i = 0; i < kRing; ++i) mbar_init(&cta.bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// After an abort, let every copy still in flight land before the CTA's shared
+// memory is released.
+__device__ __forceinline__ void fused_cta_drain(const FusedCta& cta) {
+  if (cta.aborted && threadIdx.x == 0)
+    for (uint64_t k = cta.q; k < cta.issued; ++k)
+      (void)mbar_wait(&cta.bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u);
+}
+
+// Cycles [c0, c0 + ncyc) of one tile (W words) of a run, then the closing
+// settle if `final_settle`. Net state is read from and written back to the
+// run's global net rows, so a run may be split into consecutive calls.
+template <int W>
+__device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDev& R, uint32_t tile, uint64_t c0,
+                                           uint64_t ncyc, bool final_settle, FusedCta& cta) {
+  constexpr uint32_t G = 32 / W;
   using Sh = FusedShape<W>;
   using T = typename WordVec<Sh::V>::T;
+  const size_t ring_bytes = P.ring_bytes;  // one ring buffer: a staged piece
+  uint8_t* ring = cta.dyn;
+  uint32_t* S = reinterpret_cast<uint32_t*>(cta.dyn + (size_t)kRing * ring_bytes);
+  GatePieceDev* pieces = reinterpret_cast<GatePieceDev*>(cta.dyn + (size_t)kRing * ring_bytes + fused_slot_bytes(P.n_slots, W));
+  uint64_t* bars = cta.bars;
+  uint32_t* dstate = cta.dstate;
+  unsigned long long* hacc = cta.hacc;
+
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   // lane -> (half h, cell c of the group, first word w of this thread)
   const uint32_t h = Sh::V == 2 ? lane >> 4 : 0u;
@@ -304,41 +342,55 @@ __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused
   const uint32_t cidx = hl / (W / Sh::V), w = (hl % (W / Sh::V)) * Sh::V;
   const bool resident = P.n_pieces <= (uint32_t)kRing;
   const uint32_t stages = P.n_levels + 1;
+  const uint64_t passes = ncyc + (final_settle ? 1u : 0u);
+  const uint64_t q0 = cta.q;
+  const uint64_t q_end = q0 + (resident ? (uint64_t)P.n_pieces : passes * P.n_pieces);
+  const uint32_t col0 = tile * W;
+  T* const Sv = reinterpret_cast<T*>(S + w);
+  const uint32_t hdr_bytes = P.hdr_bytes;
 
-  uint32_t my_tiles = 0;
-  for (uint32_t t = blockIdx.x; t < R.n_tiles; t += gridDim.x) ++my_tiles;
-  const uint64_t passes = R.cycles + (R.final_settle ? 1u : 0u);
-  const uint64_t total_q = resident ? P.n_pieces : (uint64_t)my_tiles * passes * P.n_pieces;
-
+  // piece table, constants, scratch, sources, detect state
   for (uint32_t i = tid; i < P.n_pieces; i += blockDim.x) pieces[i] = P.pieces[i];
-  if (tid == 0) {
-    *hacc = 0ull;
-    for (int i = 0; i < kRing; ++i) mbar_init(&bars[i], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  for (uint32_t i = tid; i < W; i += blockDim.x) {
+    S[0 * W + i] = 0u;
+    S[P.const0_slot * W + i] = 0u;
+    S[P.const1_slot * W + i] = 0xFFFFFFFFu;
+  }
+  if (tid < 8u) {
+    // lanes already detected by an earlier part of this run stay detected
+    uint32_t det = 0u;
+    if ((R.mode & RRTL_REC_DETECT) && tid < W && col0 + tid < R.words)
+      for (uint32_t b = 0; b < 32u; ++b)
+        if (R.detect[(col0 + tid) * 32u + b] != 0xFFFFFFFFu) det |= 1u << b;
+    dstate[tid] = 0u;
+    dstate[8 + tid] = det;
+  }
+  for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
+    uint32_t k = i / W, ww = i % W;
+    S[__ldg(P.src_slot + k) * W + ww] = R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww];
   }
   __syncthreads();
+
   // Ring bookkeeping. Piece q of this CTA's stream lands in buffer q % kRing;
   // its copy completes phase (q / kRing) & 1 of that buffer's mbarrier.
   // Thread 0 keeps the ring full: at the start of piece q it refills the
-  // buffer that piece q-1 released (the CTA barrier ending q-1 guarantees
-  // no warp still reads it); after its share of piece q it waits for piece
-  // q+1 to land, and the barrier that ends piece q publishes that piece to
-  // every thread. With at most kRing
-  // pieces the buffers are filled once and stay resident. A wait that runs
-  // out sets the error word, and the barrier's OR ends the CTA's work.
-  uint64_t issued = 0;      // copies issued (thread 0)
-  uint32_t next_piece = 0;  // piece index of the next copy (thread 0)
+  // buffer that piece q-1 released (the CTA barrier ending q-1 guarantees no
+  // warp still reads it); after its share of piece q it waits for piece q+1
+  // to land, and the barrier that ends piece q publishes that piece to every
+  // thread. A program of at most kRing pieces is loaded once per tile and
+  // stays resident. A wait that runs out sets the error word, and the
+  // barrier's OR ends the CTA's work.
+  uint32_t next_piece = 0;                // piece index of the next copy (thread 0)
   uint32_t next_off = 0, next_bytes = 0;  // its blob offset and size, loaded one copy ahead
-  int abort_flag = 0;       // thread 0: a bounded wait ran out
+  int abort_flag = 0;                     // thread 0: a bounded wait ran out
   auto load_next = [&]() {
     next_off = pieces[next_piece].off_words;
     next_bytes = pieces[next_piece].bytes;
   };
   auto issue_next = [&]() {
-    const uint32_t b = (uint32_t)issued & (kRing - 1u);
+    const uint32_t b = (uint32_t)cta.issued & (kRing - 1u);
     bulk_load(ring + b * ring_bytes, P.blob + next_off, next_bytes, &bars[b]);
-    ++issued;
+    ++cta.issued;
     if (++next_piece == P.n_pieces) next_piece = 0;
     load_next();
   };
@@ -346,153 +398,178 @@ __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused
     abort_flag = 1;
     atomicExch(R.err, (uint32_t)RRTL_E_TIMEOUT);
   };
-  if (tid == 0) {
-    const uint64_t n0 = total_q < (uint64_t)kRing ? total_q : (uint64_t)kRing;
+  if (tid == 0 && q_end > q0) {
     load_next();
-    while (issued < n0) issue_next();
-    const uint32_t first = resident ? P.n_pieces : (total_q ? 1u : 0u);
-    for (uint32_t b = 0; b < first; ++b)
-      if (!mbar_wait(&bars[b], 0u)) timed_out();
+    const uint64_t n0 = q_end - q0 < (uint64_t)kRing ? q_end : q0 + kRing;
+    while (cta.issued < n0) issue_next();
+    const uint64_t first = resident ? q_end : q0 + 1;
+    for (uint64_t k = q0; k < first; ++k)
+      if (!mbar_wait(&bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u)) timed_out();
   }
-  uint64_t q = 0;  // pieces consumed
-  T* const Sv = reinterpret_cast<T*>(S + w);
-  const uint32_t hdr_bytes = P.hdr_bytes;
-  bool aborted = __syncthreads_or(abort_flag) != 0;
+  if (__syncthreads_or(abort_flag)) {
+    cta.aborted = true;
+    return;
+  }
+  uint64_t q = q0;
 
-  for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !aborted; tile += gridDim.x) {
-    const uint32_t col0 = tile * W;
-    // constants, scratch, sources
-    for (uint32_t i = tid; i < W; i += blockDim.x) {
-      S[0 * W + i] = 0u;
-      S[P.const0_slot * W + i] = 0u;
-      S[P.const1_slot * W + i] = 0xFFFFFFFFu;
-    }
-    if (tid < 16u) dstate[tid] = 0u;
-    for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
-      uint32_t k = i / W, ww = i % W;
-      S[__ldg(P.src_slot + k) * W + ww] = R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww];
-    }
-    __syncthreads();
-
-    for (uint64_t pass = 0; pass < passes; ++pass) {
-      const bool final_pass = pass == R.cycles;
-      const uint64_t c = pass;
-      if (final_pass) {
-        // register slots may host other nets during a settle: write the
-        // sources back before the final settle recomputes every signal
-        for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
-          uint32_t k = i / W, ww = i % W;
-          R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * W + ww];
-        }
-      } else {
-        for (uint32_t i = tid; i < R.n_stim * W; i += blockDim.x) {
-          const GateStimDev& s = R.stim[i / W];
-          if (s.kind == RRTL_STIM_HOLD) continue;
-          uint32_t ww = i % W;
-          uint32_t& slot = S[s.slot * W + ww];
-          slot = stim_value(s, R, c, col0 + ww, slot);
-        }
-      }
-      __syncthreads();
-      for (uint32_t p = 0; p < P.n_pieces; ++p, ++q) {
-        const uint32_t buf = resident ? p : ((uint32_t)q & (kRing - 1u));
-        if (!resident && tid == 0 && q > 0 && issued < total_q) issue_next();
-        {
-          // the staged piece: two header words per warp, the further runs, then the records
-          const uint8_t* pb = ring + buf * ring_bytes;
-          const uint2 hw = reinterpret_cast<const uint2*>(pb)[warp];
-          const uint32_t* extra = reinterpret_cast<const uint32_t*>(pb) + 2 * kFusedWarps;
-          const uint2* rb = reinterpret_cast<const uint2*>(pb + hdr_bytes) + cidx;
-          if (final_pass)
-            eval_piece_writeback<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h,
-                                    P.wb_net + (size_t)pieces[p].group_begin * G + cidx, R.nets, R.words_pad, col0 + w);
-          else
-            eval_piece<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h);
-        }
-        if (!resident && tid == 0) {
-          // warp 0 has a lighter share: wait for the next piece while the others finish
-          const uint64_t qn = q + 1;
-          if (qn < total_q && !mbar_wait(&bars[(uint32_t)qn & (kRing - 1u)], ((uint32_t)qn >> 2) & 1u)) timed_out();
-        }
-        if (R.has_forces && pieces[p].last_of_level) {
-          __syncthreads();
-          apply_forces<W>(R, S, tile, pieces[p].level + 1, stages);
-        }
-        if (__syncthreads_or(abort_flag)) {
-          aborted = true;
-          break;
-        }
-      }
-      if (aborted) break;
-      if (final_pass) break;
-      // record
-      if (R.n_rec) {
-        unsigned long long h = 0ull;
-        for (uint32_t i = tid; i < R.n_rec * W; i += blockDim.x) {
-          uint32_t k = i / W, ww = i % W, gw = col0 + ww;
-          uint32_t v = S[R.rec[k].slot * W + ww] & valid_mask(gw, R.lanes);
-          if (gw < R.words) {
-            if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
-            if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
-            if (R.mode & RRTL_REC_DETECT) atomicOr(&dstate[ww], v ^ (0u - (v & 1u)));
-          }
-        }
-        if (R.mode & RRTL_REC_HASH) {
-          for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
-          if (lane == 0 && h) atomicAdd(hacc, h);
-        }
-        __syncthreads();
-        if (tid == 0 && (R.mode & RRTL_REC_HASH)) {
-          unsigned long long t = *hacc;
-          if (t) atomicAdd(R.out_hash + c, t);
-          *hacc = 0ull;
-        }
-        if ((R.mode & RRTL_REC_DETECT) && tid < W) {
-          uint32_t gw = col0 + tid;
-          uint32_t nb = dstate[tid] & ~dstate[8 + tid] & valid_mask(gw, R.lanes);
-          dstate[8 + tid] |= nb;
-          dstate[tid] = 0u;
-          while (nb) {
-            uint32_t b = __ffs(nb) - 1u;
-            R.detect[gw * 32u + b] = (uint32_t)c;
-            nb &= nb - 1u;
-          }
-        }
-      }
-      // commit (D and reset nets are never register nets, so one pass is safe)
-#pragma unroll 4
-      for (uint32_t i = tid; i < P.n_regs * W; i += blockDim.x) {
-        const uint4 rr = __ldg(reinterpret_cast<const uint4*>(P.sregs) + i / W);
-        const GateRegDev r{rr.x, rr.y, rr.z, rr.w};
-        uint32_t ww = i % W;
-        uint32_t d = S[r.d * W + ww];
-        if (r.flags & 1u) {
-          uint32_t m = S[r.rst * W + ww];
-          if (r.flags & 2u) m = ~m;
-          uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
-          d = (m & rv) | (~m & d);
-        }
-        S[r.q * W + ww] = d;
-      }
-      __syncthreads();
-      if (R.has_forces) {
-        apply_forces<W>(R, S, tile, 0, stages);
-        __syncthreads();
-      }
-    }
-    if (aborted) break;
-    if (!R.final_settle) {
+  for (uint64_t pass = 0; pass < passes; ++pass) {
+    const bool final_pass = pass == ncyc;
+    const uint64_t c = c0 + pass;
+    if (final_pass) {
+      // register slots may host other nets during a settle: write the
+      // sources back before the final settle recomputes every signal
       for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
         uint32_t k = i / W, ww = i % W;
         R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * W + ww];
       }
+    } else {
+      for (uint32_t i = tid; i < R.n_stim * W; i += blockDim.x) {
+        const GateStimDev& st = R.stim[i / W];
+        if (st.kind == RRTL_STIM_HOLD) continue;
+        uint32_t ww = i % W;
+        uint32_t& slot = S[st.slot * W + ww];
+        slot = stim_value(st, R, c, col0 + ww, slot);
+      }
     }
     __syncthreads();
+    for (uint32_t p = 0; p < P.n_pieces; ++p) {
+      const uint32_t buf = (uint32_t)(resident ? q0 + p : q) & (kRing - 1u);
+      if (!resident && tid == 0 && q > q0 && cta.issued < q_end) issue_next();
+      {
+        // the staged piece: two header words per warp, the further runs, then the records
+        const uint8_t* pb = ring + buf * ring_bytes;
+        const uint2 hw = reinterpret_cast<const uint2*>(pb)[warp];
+        const uint32_t* extra = reinterpret_cast<const uint32_t*>(pb) + 2 * kFusedWarps;
+        const uint2* rb = reinterpret_cast<const uint2*>(pb + hdr_bytes) + cidx;
+        if (final_pass)
+          eval_piece_writeback<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h,
+                                  P.wb_net + (size_t)pieces[p].group_begin * G + cidx, R.nets, R.words_pad, col0 + w);
+        else
+          eval_piece<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h);
+      }
+      if (!resident && tid == 0) {
+        // warp 0 has a lighter share: wait for the next piece while the others finish
+        const uint64_t qn = q + 1;
+        if (qn < q_end && !mbar_wait(&bars[(uint32_t)qn & (kRing - 1u)], ((uint32_t)qn >> 2) & 1u)) timed_out();
+      }
+      if (R.has_forces && pieces[p].last_of_level) {
+        __syncthreads();
+        apply_forces<W>(R, S, tile, pieces[p].level + 1, stages);
+      }
+      if (!resident) ++q;
+      if (__syncthreads_or(abort_flag)) {
+        cta.q = q;
+        cta.aborted = true;
+        return;
+      }
+    }
+    if (final_pass) break;
+    // record
+    if (R.n_rec) {
+      unsigned long long hs = 0ull;
+      for (uint32_t i = tid; i < R.n_rec * W; i += blockDim.x) {
+        uint32_t k = i / W, ww = i % W, gw = col0 + ww;
+        uint32_t v = S[R.rec[k].slot * W + ww] & valid_mask(gw, R.lanes);
+        if (gw < R.words) {
+          if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
+          if (R.mode & RRTL_REC_HASH) hs += hash_term(c, k, gw, v);
+          if (R.mode & RRTL_REC_DETECT) atomicOr(&dstate[ww], v ^ (0u - (v & 1u)));
+        }
+      }
+      if (R.mode & RRTL_REC_HASH) {
+        for (int o = 16; o > 0; o >>= 1) hs += __shfl_xor_sync(0xFFFFFFFFu, hs, o);
+        if (lane == 0 && hs) atomicAdd(hacc, hs);
+      }
+      __syncthreads();
+      if (tid == 0 && (R.mode & RRTL_REC_HASH)) {
+        unsigned long long t = *hacc;
+        if (t) atomicAdd(R.out_hash + c, t);
+        *hacc = 0ull;
+      }
+      if ((R.mode & RRTL_REC_DETECT) && tid < W) {
+        uint32_t gw = col0 + tid;
+        uint32_t nb = dstate[tid] & ~dstate[8 + tid] & valid_mask(gw, R.lanes);
+        dstate[8 + tid] |= nb;
+        dstate[tid] = 0u;
+        while (nb) {
+          uint32_t b = __ffs(nb) - 1u;
+          R.detect[gw * 32u + b] = (uint32_t)c;
+          nb &= nb - 1u;
+        }
+      }
+    }
+    // commit (D and reset nets are never register nets, so one pass is safe)
+#pragma unroll 4
+    for (uint32_t i = tid; i < P.n_regs * W; i += blockDim.x) {
+      const uint4 rr = __ldg(reinterpret_cast<const uint4*>(P.sregs) + i / W);
+      const GateRegDev r{rr.x, rr.y, rr.z, rr.w};
+      uint32_t ww = i % W;
+      uint32_t d = S[r.d * W + ww];
+      if (r.flags & 1u) {
+        uint32_t m = S[r.rst * W + ww];
+        if (r.flags & 2u) m = ~m;
+        uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
+        d = (m & rv) | (~m & d);
+      }
+      S[r.q * W + ww] = d;
+    }
+    __syncthreads();
+    if (R.has_forces) {
+      apply_forces<W>(R, S, tile, 0, stages);
+      __syncthreads();
+    }
   }
-  if (aborted && tid == 0 && !resident) {
-    // let every copy still in flight land before the CTA's shared memory is released
-    for (uint64_t k = q; k < issued; ++k) (void)mbar_wait(&bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u);
+  cta.q = q_end;
+  if (!final_settle) {
+    for (uint32_t i = tid; i < P.n_src * W; i += blockDim.x) {
+      uint32_t k = i / W, ww = i % W;
+      R.nets[(size_t)__ldg(P.src_net + k) * R.words_pad + col0 + ww] = S[__ldg(P.src_slot + k) * W + ww];
+    }
   }
+  __syncthreads();
+}
+
+template <int W>
+__global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused_kernel(GateProgDev P, GateRunDev R) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  FusedCta cta;
+  fused_cta_init(cta, smem);
+  for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !cta.aborted; tile += gridDim.x)
+    fused_tile<W>(P, R, tile, R.cycle_base, R.cycles, R.final_settle != 0, cta);
+  fused_cta_drain(cta);
+}
+
+// Persistent job-queue kernel: CTAs take (job, tile, cycle range) items from
+// a device-side list with an atomic counter until the list is empty. Every
+// job carries its own program (any tile width), run descriptor and state, so
+// uneven jobs share one launch; items are listed longest first.
+__global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_queue_kernel(GateQueueDev Q) {
+  extern __shared__ __align__(128) uint8_t smem[];
+  __shared__ uint32_t s_item;
+  __shared__ GateJobDev s_job;
+  FusedCta cta;
+  fused_cta_init(cta, smem);
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(Q.next, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= Q.n_items) break;
+    const GateItemDev item = Q.items[it];
+    // stage the job descriptor; the barrier also orders the s_item read before its next write
+    for (uint32_t i = threadIdx.x; i < sizeof(GateJobDev) / 4; i += blockDim.x)
+      reinterpret_cast<uint32_t*>(&s_job)[i] = reinterpret_cast<const uint32_t*>(Q.jobs + item.job)[i];
+    __syncthreads();
+    const uint64_t c0 = item.c0;
+    const bool fin = (item.flags & 1u) != 0;
+    switch (s_job.P.group) {
+      case 4: fused_tile<8>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      case 8: fused_tile<4>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      case 16: fused_tile<2>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      default: fused_tile<1>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+    }
+    if (cta.aborted) break;
+  }
+  fused_cta_drain(cta);
 }
 
 // ------------------------------------------------------------ plain path --
@@ -598,7 +675,7 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
 
 size_t gate_fused_smem_bytes(const GateProgDev& P) {
   const uint32_t W = 32u / P.group;
-  return (size_t)kRing * P.ring_bytes + kFusedHeader + fused_slot_bytes(P.n_slots, W) +
+  return kFusedHeader + (size_t)kRing * P.ring_bytes + fused_slot_bytes(P.n_slots, W) +
          (size_t)P.n_pieces * sizeof(GatePieceDev);
 }
 static_assert(sizeof(GatePieceDev) == 32, "piece descriptor layout");
@@ -644,6 +721,21 @@ cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_
     case 32: gate_fused_kernel<1><<<grid, kFusedThreads, smem, st>>>(P, R); break;
     default: return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+size_t gate_queue_static_smem() {
+  cudaFuncAttributes a{};
+  if (cudaFuncGetAttributes(&a, gate_queue_kernel) != cudaSuccess) return 1024;
+  return a.sharedSizeBytes;
+}
+
+cudaError_t gate_queue_prepare(size_t smem) {
+  return cudaFuncSetAttribute(gate_queue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem, cudaStream_t st) {
+  gate_queue_kernel<<<grid, kFusedThreads, smem, st>>>(Q);
   return cudaGetLastError();
 }
 

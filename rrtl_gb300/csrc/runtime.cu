@@ -13,6 +13,9 @@ namespace rrtl {
 // kernels (gate_kernels.cu, word_kernels.cu)
 size_t gate_fused_smem_bytes(const GateProgDev& P);
 cudaError_t gate_fused_prepare(const GateProgDev& P, size_t smem);
+cudaError_t gate_queue_prepare(size_t smem);
+size_t gate_queue_static_smem();
+cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem, cudaStream_t st);
 int gate_fused_ctas_per_sm(const GateProgDev& P, size_t smem);
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st);
@@ -25,6 +28,11 @@ constexpr size_t kWordSmemBudget = 96 * 1024;
 void cuda_check(cudaError_t e, const char* what) {
   if (e == cudaErrorMemoryAllocation) fail(RRTL_E_OOM, std::string("E_OOM: ") + what + ": " + cudaGetErrorString(e));
   if (e != cudaSuccess) fail(RRTL_E_DEVICE, std::string("E_DEVICE: ") + what + ": " + cudaGetErrorString(e));
+}
+
+JobQueue::~JobQueue() {
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
 }
 
 DevBuf::~DevBuf() {
@@ -164,6 +172,8 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
   } else {
     build_pieces(gp, 256);
   }
+  for (const GatePiece& pc : gp.pieces)
+    v->tile_cycle_cost += std::ceil((double)pc.n_groups / (kGateFusedWarps * (W >= 2 ? 2.0 : 1.0))) + 4.0;
   if (v->fused_ok) {
     std::vector<GatePieceDev> pieces;
     for (size_t i = 0; i < gp.pieces.size(); ++i) {
@@ -211,7 +221,9 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     if (v->fused_smem > max_smem) {
       v->fused_ok = false;
     } else {
-      cuda_check(gate_fused_prepare(P, v->fused_smem), "gate_fused_prepare");
+      // the limit is per kernel, not per design: allow the device maximum so
+      // every design's variant of this width can launch
+      cuda_check(gate_fused_prepare(P, d->ctx->max_smem), "gate_fused_prepare");
       v->fused_ctas = (uint32_t)gate_fused_ctas_per_sm(P, v->fused_smem);
     }
   }
@@ -366,10 +378,15 @@ void invalidate_forces(rrtl_batch* b) {
 }
 
 // ---- gate engine run
-void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
+// Validate a run, pick the program variant and upload its stimulus and record
+// tables; stages host input traces and zeroes hash/detect outputs on the
+// context stream. `want_fused` asks for the fused path (it falls back to the
+// plain path when a recorded net does not stay on chip to the end of a cycle).
+GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
-  const uint32_t W = b->path == RRTL_PATH_FUSED ? (b->tile_words ? b->tile_words : choose_tile_words(d, b->words)) : 0;
+  GatePrepared g;
+  const uint32_t W = want_fused ? (b->tile_words ? b->tile_words : choose_tile_words(d, b->words)) : 0;
   GateVariant* v = W ? gate_variant(d, W) : d->gvar[d->gate_base].get();
   const GateProgram& gp = v->gp;
   bool fused = W && v->fused_ok;
@@ -382,7 +399,7 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
     REQUIRE(s.kind <= RRTL_STIM_TRACE, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
     if (s.kind == RRTL_STIM_TRACE)
       REQUIRE(s.param < run.n_trace_cols && run.input_trace, RRTL_E_ARG, "E_GPU_STIM: trace column out of range");
-    stim.push_back(GateStimDev{fused ? (uint32_t)gp.net_slot[net] : 0u, net, s.kind, 0, s.param});
+    stim.push_back(GateStimDev{0u, net, s.kind, 0, s.param});
   }
   std::vector<GateRecDev> rec;
   for (uint32_t i = 0; i < run.n_record; ++i) {
@@ -391,17 +408,17 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
     if (fused && !v->end_live[net]) fused = false;  // value not held to the end of the cycle: use the plain path
     rec.push_back(GateRecDev{0u, net});
   }
-  if (fused)
+  if (fused) {
     for (auto& r : rec) r.slot = (uint32_t)gp.net_slot[r.net];
-  if (fused)
     for (auto& s : stim) s.slot = (uint32_t)gp.net_slot[s.net];
+  }
   REQUIRE(!(run.record_mode & (RRTL_REC_TRACE | RRTL_REC_HASH | RRTL_REC_DETECT)) || run.n_record > 0, RRTL_E_ARG,
           "E_GPU_RECORD: recording needs at least one signal");
   REQUIRE(run.cycles < (1ull << 32), RRTL_E_ARG, "E_GPU_STEPS: cycle count exceeds 2^32");
   upload(b->d_stim, stim);
   upload(b->d_rec, rec);
 
-  GateRunDev R{};
+  GateRunDev& R = g.R;
   R.cycles = run.cycles;
   R.seed = run.seed;
   R.n_stim = (uint32_t)stim.size();
@@ -422,16 +439,18 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
   R.final_settle = 1;
   R.nets = b->d_nets.as<uint32_t>();
   R.err = b->d_err.as<uint32_t>();
+  R.cycle_base = 0;
 
   size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->words * 4;
-  size_t trace_out_bytes = (size_t)run.cycles * run.n_record * b->words * 4;
-  size_t hash_bytes = (size_t)run.cycles * 8;
-  size_t det_bytes = (size_t)b->lanes * 4;
-  bool want_trace = run.record_mode & RRTL_REC_TRACE, want_hash = run.record_mode & RRTL_REC_HASH,
-       want_det = run.record_mode & RRTL_REC_DETECT;
-  REQUIRE(!want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
-  REQUIRE(!want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
-  REQUIRE(!want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
+  g.trace_out_bytes = (size_t)run.cycles * run.n_record * b->words * 4;
+  g.hash_bytes = (size_t)run.cycles * 8;
+  g.det_bytes = (size_t)b->lanes * 4;
+  g.want_trace = run.record_mode & RRTL_REC_TRACE;
+  g.want_hash = run.record_mode & RRTL_REC_HASH;
+  g.want_det = run.record_mode & RRTL_REC_DETECT;
+  REQUIRE(!g.want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
+  REQUIRE(!g.want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
+  REQUIRE(!g.want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
   if (device_ptrs) {
     R.in_trace = run.input_trace;
     R.out_trace = run.out_trace;
@@ -443,36 +462,77 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
       cuda_check(cudaMemcpyAsync(b->d_in_trace.p, run.input_trace, trace_in_bytes, cudaMemcpyHostToDevice, st), "h2d trace");
       R.in_trace = b->d_in_trace.as<uint32_t>();
     }
-    if (want_trace) {
-      b->d_out_trace.reserve(std::max<size_t>(trace_out_bytes, 16));
+    if (g.want_trace) {
+      b->d_out_trace.reserve(std::max<size_t>(g.trace_out_bytes, 16));
       R.out_trace = b->d_out_trace.as<uint32_t>();
     }
-    if (want_hash) {
-      b->d_hash.reserve(std::max<size_t>(hash_bytes, 16));
+    if (g.want_hash) {
+      b->d_hash.reserve(std::max<size_t>(g.hash_bytes, 16));
       R.out_hash = b->d_hash.as<unsigned long long>();
     }
-    if (want_det) {
-      b->d_detect.reserve(std::max<size_t>(det_bytes, 16));
+    if (g.want_det) {
+      b->d_detect.reserve(std::max<size_t>(g.det_bytes, 16));
       R.detect = b->d_detect.as<uint32_t>();
     }
   }
-  if (want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, hash_bytes, st), "memset hash");
-  if (want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, det_bytes, st), "memset detect");
+  if (g.want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, g.hash_bytes, st), "memset hash");
+  if (g.want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, g.det_bytes, st), "memset detect");
+  g.v = v;
+  g.fused = fused;
+  g.W = fused ? W : 0;
+  return g;
+}
 
-  Timer tm(b);
-  if (fused) {
-    uint32_t grid = std::min<uint32_t>(R.n_tiles, d->ctx->sm_count * v->fused_ctas);
-    cuda_check(launch_gate_fused(v->gdev, R, grid, v->fused_smem, st), "gate_fused_kernel");
-  } else {
-    for (uint64_t c = 0; c < run.cycles; ++c) cuda_check(launch_gate_plain(v->gdev, R, c, 0, st), "gate_plain_kernel");
-    cuda_check(launch_gate_plain(v->gdev, R, 0, 1, st), "gate_plain_kernel");
+// Copy a prepared run's recorded outputs to the caller's host buffers.
+void gate_copy_out(rrtl_batch* b, const GatePrepared& g, const rrtl_run& run) {
+  cudaStream_t st = b->d->ctx->stream;
+  if (g.want_trace)
+    cuda_check(cudaMemcpyAsync(run.out_trace, g.R.out_trace, g.trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
+  if (g.want_hash)
+    cuda_check(cudaMemcpyAsync(run.out_hash, g.R.out_hash, g.hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
+  if (g.want_det) cuda_check(cudaMemcpyAsync(run.detect, g.R.detect, g.det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+}
+
+// The plain path: one launch per cycle plus the closing settle. With `graph`
+// the launches are captured into a CUDA graph and replayed as one submission.
+void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st, bool graph) {
+  if (!graph) {
+    for (uint64_t c = 0; c < cycles; ++c) cuda_check(launch_gate_plain(g.v->gdev, g.R, c, 0, st), "gate_plain_kernel");
+    cuda_check(launch_gate_plain(g.v->gdev, g.R, 0, 1, st), "gate_plain_kernel");
+    return;
   }
-  b->last_tile_words = fused ? W : 0;
+  cudaGraph_t graph_h = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  cudaError_t e = cudaSuccess;
+  for (uint64_t c = 0; c < cycles && e == cudaSuccess; ++c) e = launch_gate_plain(g.v->gdev, g.R, c, 0, st);
+  if (e == cudaSuccess) e = launch_gate_plain(g.v->gdev, g.R, 0, 1, st);
+  cudaError_t e2 = cudaStreamEndCapture(st, &graph_h);
+  cuda_check(e, "gate_plain_kernel (capture)");
+  cuda_check(e2, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(&exec, graph_h, 0);
+  cudaGraphDestroy(graph_h);
+  cuda_check(e, "cudaGraphInstantiate");
+  e = cudaGraphLaunch(exec, st);
+  cudaGraphExecDestroy(exec);
+  cuda_check(e, "cudaGraphLaunch");
+}
+
+void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
+  rrtl_design* d = b->d;
+  cudaStream_t st = d->ctx->stream;
+  GatePrepared g = gate_prepare(b, run, device_ptrs, b->path == RRTL_PATH_FUSED);
+  Timer tm(b);
+  if (g.fused) {
+    uint32_t grid = std::min<uint32_t>(g.R.n_tiles, d->ctx->sm_count * g.v->fused_ctas);
+    cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
+  } else {
+    gate_plain_launches(g, run.cycles, st, b->path == RRTL_PATH_PLAIN_GRAPH && run.cycles > 0);
+  }
+  b->last_tile_words = g.W;
   tm.stop();
   if (!device_ptrs) {
-    if (want_trace) cuda_check(cudaMemcpyAsync(run.out_trace, R.out_trace, trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
-    if (want_hash) cuda_check(cudaMemcpyAsync(run.out_hash, R.out_hash, hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
-    if (want_det) cuda_check(cudaMemcpyAsync(run.detect, R.detect, det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+    gate_copy_out(b, g, run);
     check_err_word(b);
     cuda_check(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "elapsed");
   }
@@ -560,10 +620,13 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   if (want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, det_bytes, st), "memset detect");
   R.vspill = nullptr;
   Timer tm(b);
-  if (b->path == RRTL_PATH_PLAIN && run.cycles > 1) {
-    // one launch per cycle: the baseline path
+  if (b->path != RRTL_PATH_FUSED && run.cycles > 1) {
+    // one launch per cycle: the baseline path (captured into a CUDA graph on RRTL_PATH_PLAIN_GRAPH)
+    const bool graph = b->path == RRTL_PATH_PLAIN_GRAPH;
+    if (graph) cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaError_t ce = cudaSuccess;
     WordRunDev R1 = R;
-    for (uint64_t c = 0; c < run.cycles; ++c) {
+    for (uint64_t c = 0; c < run.cycles && ce == cudaSuccess; ++c) {
       R1.cycles = 1;
       R1.start_settle = (c == 0) ? R.start_settle : 0;
       R1.final_settle = (c + 1 == run.cycles) ? R.final_settle : 0;
@@ -572,7 +635,22 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
       R1.out_trace = R.out_trace ? R.out_trace + (size_t)c * rec_limbs * b->lanes : nullptr;
       R1.out_hash = R.out_hash ? R.out_hash + c : nullptr;
       R1.cycle_base = c;
-      cuda_check(launch_word(d->wdev, R1, smem_slots, st), "word_kernel");
+      ce = launch_word(d->wdev, R1, smem_slots, st);
+    }
+    if (graph) {
+      cudaGraph_t gh = nullptr;
+      cudaError_t e2 = cudaStreamEndCapture(st, &gh);
+      cuda_check(ce, "word_kernel (capture)");
+      cuda_check(e2, "cudaStreamEndCapture");
+      cudaGraphExec_t exec = nullptr;
+      cudaError_t e3 = cudaGraphInstantiate(&exec, gh, 0);
+      cudaGraphDestroy(gh);
+      cuda_check(e3, "cudaGraphInstantiate");
+      e3 = cudaGraphLaunch(exec, st);
+      cudaGraphExecDestroy(exec);
+      cuda_check(e3, "cudaGraphLaunch");
+    } else {
+      cuda_check(ce, "word_kernel");
     }
   } else {
     cuda_check(launch_word(d->wdev, R, smem_slots, st), "word_kernel");
@@ -585,6 +663,136 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
     check_err_word(b);
     cuda_check(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "elapsed");
   }
+}
+
+// ---- device job queue
+
+JobQueue& queue_of(rrtl_ctx* c) {
+  if (!c->queue) {
+    c->queue = std::make_unique<JobQueue>();
+    cuda_check(cudaEventCreate(&c->queue->ev0), "event");
+    cuda_check(cudaEventCreate(&c->queue->ev1), "event");
+  }
+  return *c->queue;
+}
+
+// Copy results of every job of the finished launches out and record their
+// status. Called once the stream has passed the launches' end.
+void queue_finish(rrtl_ctx* c) {
+  JobQueue& Q = queue_of(c);
+  std::vector<QueueJob> keep;
+  for (QueueJob& j : Q.jobs) {
+    if (j.status != RRTL_JOB_RUNNING) {
+      keep.push_back(std::move(j));
+      continue;
+    }
+    rrtl_batch* b = j.batch;
+    uint32_t e = 0;
+    cudaError_t ce = cudaMemcpy(&e, b->d_err.p, 4, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess && e == 0) {
+      try {
+        gate_copy_out(b, j.prep, j.run);
+        cuda_check(cudaStreamSynchronize(c->stream), "sync");
+        j.status = RRTL_JOB_DONE;
+      } catch (const ApiError&) {
+        j.status = RRTL_JOB_FAILED;
+      }
+    } else {
+      if (e) cudaMemset(b->d_err.p, 0, 4);
+      j.status = RRTL_JOB_FAILED;
+    }
+    b->queued = false;
+    Q.finished[j.id] = j.status;
+  }
+  Q.jobs.swap(keep);
+}
+
+uint64_t queue_submit(rrtl_ctx* c, const rrtl_job& job) {
+  rrtl_batch* b = job.batch;
+  REQUIRE(b, RRTL_E_ARG, "E_ARG: job has no batch");
+  REQUIRE(b->d->ctx == c, RRTL_E_ARG, "E_QUEUE: the job's batch belongs to another context");
+  REQUIRE(b->d->engine == RRTL_ENGINE_GATE, RRTL_E_UNSUPPORTED, "E_QUEUE: the job queue runs gate-engine batches");
+  REQUIRE(!b->queued, RRTL_E_ARG, "E_QUEUE: the batch already has a job in the queue");
+  REQUIRE(job.run.n_stim == 0 || job.run.stim, RRTL_E_ARG, "E_ARG: stim is null");
+  REQUIRE(job.run.n_record == 0 || job.run.record, RRTL_E_ARG, "E_ARG: record is null");
+  JobQueue& Q = queue_of(c);
+  QueueJob j;
+  j.id = Q.next_id++;
+  j.batch = b;
+  j.run = job.run;
+  j.stim.assign(job.run.stim, job.run.stim + job.run.n_stim);
+  j.record.assign(job.run.record, job.run.record + job.run.n_record);
+  j.run.stim = j.stim.data();
+  j.run.record = j.record.data();
+  j.status = RRTL_JOB_QUEUED;
+  b->queued = true;
+  Q.jobs.push_back(std::move(j));
+  Q.jobs.back().run.stim = Q.jobs.back().stim.data();
+  Q.jobs.back().run.record = Q.jobs.back().record.data();
+  return Q.jobs.back().id;
+}
+
+// One persistent launch over every queued job: each job's tiles become items
+// (all cycles of one tile), listed longest first; jobs whose recorded nets
+// leave the chip, or whose shared memory exceeds what the queue kernel can
+// take, run on their own kernels first on the same stream.
+void queue_launch(rrtl_ctx* c) {
+  JobQueue& Q = queue_of(c);
+  cudaStream_t st = c->stream;
+  const size_t qmax = c->max_smem - gate_queue_static_smem();
+  std::vector<GateJobDev> jobs;
+  std::vector<std::pair<double, GateItemDev>> items;
+  size_t smem = 0;
+  const uint32_t launch = ++Q.launches;
+  cuda_check(cudaEventRecord(Q.ev0, st), "event");
+  for (QueueJob& j : Q.jobs) {
+    if (j.status != RRTL_JOB_QUEUED) continue;
+    rrtl_batch* b = j.batch;
+    b->path = RRTL_PATH_FUSED;
+    j.prep = gate_prepare(b, j.run, false, true);
+    j.status = RRTL_JOB_RUNNING;
+    j.launch = launch;
+    const GatePrepared& g = j.prep;
+    if (!g.fused || g.v->fused_smem > qmax) {
+      if (g.fused) {
+        uint32_t grid = std::min<uint32_t>(g.R.n_tiles, c->sm_count * g.v->fused_ctas);
+        cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
+      } else {
+        gate_plain_launches(g, j.run.cycles, st, false);
+      }
+      b->last_tile_words = g.W;
+      continue;
+    }
+    const uint32_t ji = (uint32_t)jobs.size();
+    jobs.push_back(GateJobDev{g.v->gdev, g.R});
+    smem = std::max(smem, g.v->fused_smem);
+    const double cost = (double)(j.run.cycles + 1) * g.v->tile_cycle_cost;
+    for (uint32_t t = 0; t < g.R.n_tiles; ++t)
+      items.push_back({cost, GateItemDev{ji, t, 0ull, (uint32_t)j.run.cycles, 1u}});
+    b->last_tile_words = g.W;
+  }
+  std::stable_sort(items.begin(), items.end(),
+                   [](const std::pair<double, GateItemDev>& x, const std::pair<double, GateItemDev>& y) {
+                     return x.first > y.first;
+                   });
+  Q.last_items = (uint32_t)items.size();
+  if (!items.empty()) {
+    std::vector<GateItemDev> flat;
+    flat.reserve(items.size());
+    for (auto& it : items) flat.push_back(it.second);
+    upload(Q.d_jobs, jobs);
+    upload(Q.d_items, flat);
+    Q.d_next.reserve(16);
+    cuda_check(cudaMemsetAsync(Q.d_next.p, 0, 4, st), "memset queue");
+    if (smem > Q.smem_set) {
+      cuda_check(gate_queue_prepare(smem), "gate_queue_prepare");
+      Q.smem_set = smem;
+    }
+    GateQueueDev QD{Q.d_jobs.as<GateJobDev>(), Q.d_items.as<GateItemDev>(), (uint32_t)flat.size(), Q.d_next.as<uint32_t>()};
+    const uint32_t grid = std::min<uint32_t>((uint32_t)flat.size(), c->sm_count);
+    cuda_check(launch_gate_queue(QD, grid, smem, st), "gate_queue_kernel");
+  }
+  cuda_check(cudaEventRecord(Q.ev1, st), "event");
 }
 
 void batch_eval(rrtl_batch* b) {
@@ -642,6 +850,7 @@ static void ctx_release(rrtl_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto& e : ctx->events)
     if (e) cudaEventDestroy(e);
+  ctx->queue.reset();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -1196,8 +1405,69 @@ rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv,
 rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path) {
   return guard([&] {
     REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
-    REQUIRE(path == RRTL_PATH_FUSED || path == RRTL_PATH_PLAIN, RRTL_E_ARG, "E_ARG: unknown path");
+    REQUIRE(path == RRTL_PATH_FUSED || path == RRTL_PATH_PLAIN || path == RRTL_PATH_PLAIN_GRAPH, RRTL_E_ARG,
+            "E_ARG: unknown path");
     b->path = path;
+  });
+}
+
+rrtl_status rrtl_queue_submit(rrtl_ctx* ctx, const rrtl_job* job, uint64_t* id) {
+  return guard([&] {
+    REQUIRE(ctx && job && id, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    *id = queue_submit(ctx, *job);
+  });
+}
+
+rrtl_status rrtl_queue_launch(rrtl_ctx* ctx) {
+  return guard([&] {
+    REQUIRE(ctx, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    queue_launch(ctx);
+  });
+}
+
+rrtl_status rrtl_queue_wait(rrtl_ctx* ctx) {
+  return guard([&] {
+    REQUIRE(ctx, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    JobQueue& Q = queue_of(ctx);
+    cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
+    cuda_check(cudaEventElapsedTime(&Q.last_ms, Q.ev0, Q.ev1), "elapsed");
+    queue_finish(ctx);
+  });
+}
+
+rrtl_status rrtl_queue_poll(rrtl_ctx* ctx, uint64_t id, uint32_t* status) {
+  return guard([&] {
+    REQUIRE(ctx && status, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    JobQueue& Q = queue_of(ctx);
+    auto it = Q.finished.find(id);
+    if (it != Q.finished.end()) {
+      *status = it->second;
+      return;
+    }
+    for (QueueJob& j : Q.jobs)
+      if (j.id == id) {
+        if (j.status == RRTL_JOB_RUNNING && cudaEventQuery(Q.ev1) == cudaSuccess) {
+          cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
+          cudaEventElapsedTime(&Q.last_ms, Q.ev0, Q.ev1);
+          queue_finish(ctx);
+          *status = Q.finished.at(id);
+        } else {
+          *status = j.status;
+        }
+        return;
+      }
+    fail(RRTL_E_ARG, "E_QUEUE: unknown job id");
+  });
+}
+
+rrtl_status rrtl_queue_last_ms(rrtl_ctx* ctx, float* ms) {
+  return guard([&] {
+    REQUIRE(ctx && ms, RRTL_E_ARG, "E_ARG: null argument");
+    *ms = queue_of(ctx).last_ms;
   });
 }
 

@@ -54,6 +54,7 @@ struct GateVariant {
   bool fused_ok = false;
   size_t fused_smem = 0;
   uint32_t fused_ctas = 1;  // resident fused CTAs per SM
+  double tile_cycle_cost = 0;  // estimated warp steps of one tile-cycle (job ordering)
   DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
 };
 
@@ -62,6 +63,43 @@ struct ForceTable {
   bool valid = false;
   bool any = false;
   DevBuf d_off, d_forces;
+};
+
+// A gate-engine run made ready for a launch: program variant, device run
+// descriptor and the sizes of its outputs.
+struct GatePrepared {
+  GateVariant* v = nullptr;
+  GateRunDev R{};
+  bool fused = false;
+  uint32_t W = 0;
+  size_t trace_out_bytes = 0, hash_bytes = 0, det_bytes = 0;
+  bool want_trace = false, want_hash = false, want_det = false;
+};
+
+// One submitted job of the device job queue.
+struct QueueJob {
+  uint64_t id = 0;
+  rrtl_batch* batch = nullptr;
+  rrtl_run run{};
+  std::vector<rrtl_stim> stim;    // owned copies of the run's arrays
+  std::vector<uint32_t> record;
+  uint32_t status = 0;            // RRTL_JOB_*
+  uint32_t launch = 0;            // launch that carries it
+  GatePrepared prep;
+};
+
+// Jobs submitted to a context and the device buffers of its queue launches.
+struct JobQueue {
+  uint64_t next_id = 1;
+  uint32_t launches = 0;
+  std::vector<QueueJob> jobs;                 // queued or running
+  std::unordered_map<uint64_t, uint32_t> finished;  // id -> RRTL_JOB_DONE / RRTL_JOB_FAILED
+  DevBuf d_jobs, d_items, d_next;
+  size_t smem_set = 0;                        // dynamic shared memory the queue kernel is prepared for
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;   // around the last launch
+  float last_ms = 0.f;
+  uint32_t last_items = 0;
+  ~JobQueue();
 };
 
 }  // namespace rrtl
@@ -77,6 +115,7 @@ struct rrtl_ctx {
   size_t max_smem = 0;      // opt-in shared memory per block
   size_t max_smem_sm = 0;   // shared memory per SM
   cudaEvent_t events[8] = {};
+  std::unique_ptr<rrtl::JobQueue> queue;
 };
 
 struct rrtl_design {
@@ -108,6 +147,7 @@ struct rrtl_batch {
   // gate engine state
   uint32_t words = 0, words_pad = 0, rows = 0;
   uint32_t tile_words = 0;  // requested fused tile width, 0 = chosen per run
+  bool queued = false;      // a job of this batch is in the context's job queue
   uint32_t last_tile_words = 0;  // tile width of the last fused run, 0 after a plain run
   rrtl::DevBuf d_nets;
   std::vector<rrtl_fault> faults;

@@ -22,7 +22,8 @@ LIB_PATH = os.path.join(_HERE, "_lib", "librrtl_gb300.so")
 
 STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE = 0, 1, 2, 3, 4
 REC_TRACE, REC_HASH, REC_DETECT = 1, 2, 4
-PATH_FUSED, PATH_PLAIN = 0, 1
+PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH = 0, 1, 2
+JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 ENGINE_GATE, ENGINE_WORD = 1, 2
 
 _STATUS = {
@@ -65,6 +66,10 @@ class Run(ctypes.Structure):
         ("out_hash", POINTER(c_uint64)),
         ("detect", POINTER(c_uint32)),
     ]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("batch", c_void_p), ("run", Run)]
 
 
 class Fault(ctypes.Structure):
@@ -122,6 +127,11 @@ EXPORTS = (
     "rrtl_batch_restore",
     "rrtl_batch_set_path",
     "rrtl_batch_set_tile_words",
+    "rrtl_queue_submit",
+    "rrtl_queue_launch",
+    "rrtl_queue_wait",
+    "rrtl_queue_poll",
+    "rrtl_queue_last_ms",
     "rrtl_batch_tile_words",
     "rrtl_batch_last_kernel_ms",
     "rrtl_word_tick_many_noalloc",
@@ -173,6 +183,11 @@ def lib():
         "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_path": [c_void_p, c_uint32],
         "rrtl_batch_set_tile_words": [c_void_p, c_uint32],
+        "rrtl_queue_submit": [c_void_p, P(Job), P(c_uint64)],
+        "rrtl_queue_launch": [c_void_p],
+        "rrtl_queue_wait": [c_void_p],
+        "rrtl_queue_poll": [c_void_p, c_uint64, P(c_uint32)],
+        "rrtl_queue_last_ms": [c_void_p, P(c_float)],
         "rrtl_batch_tile_words": [c_void_p, P(c_uint32)],
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
@@ -218,6 +233,37 @@ class Context:
     def synchronize(self):
         check(lib().rrtl_ctx_synchronize(self.h))
 
+    # -- device job queue (rrtl_queue_*)
+    def submit(self, batch: "GpuBatchSimulator", cycles: int, seed: int = 0, stim: Iterable = (),
+               record: Iterable = (), mode: int = 0, input_trace: Optional[np.ndarray] = None) -> "QueuedJob":
+        """Queue a run on `batch`; its outputs fill the returned job's arrays once it finishes."""
+        out = batch.alloc_outputs(cycles, list(record), mode)
+        r = batch.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
+        j = Job()
+        j.batch = batch.h
+        j.run = r
+        jid = c_uint64()
+        check(lib().rrtl_queue_submit(self.h, byref(j), byref(jid)))
+        job = QueuedJob(self, jid.value, out, (r, batch))
+        return job
+
+    def launch(self):
+        check(lib().rrtl_queue_launch(self.h))
+
+    def wait(self):
+        check(lib().rrtl_queue_wait(self.h))
+
+    def poll(self, job_id: int) -> int:
+        v = c_uint32()
+        check(lib().rrtl_queue_poll(self.h, job_id, byref(v)))
+        return v.value
+
+    @property
+    def queue_ms(self) -> float:
+        f = c_float()
+        check(lib().rrtl_queue_last_ms(self.h, byref(f)))
+        return f.value
+
     def close(self):
         if self.h:
             lib().rrtl_ctx_destroy(self.h)
@@ -228,6 +274,17 @@ class Context:
             self.close()
         except Exception:
             pass
+
+
+class QueuedJob:
+    """A job in a context's device queue; `outputs` holds trace/hash/detect arrays."""
+
+    def __init__(self, ctx: Context, job_id: int, outputs: dict, keep):
+        self.ctx, self.id, self.outputs, self._keep = ctx, job_id, outputs, keep
+
+    @property
+    def status(self) -> int:
+        return self.ctx.poll(self.id)
 
 
 _default_ctx: Optional[Context] = None
@@ -446,10 +503,8 @@ class GpuBatchSimulator:
         r._keep = (arr, rec, input_trace, out_trace, out_hash, detect)
         return r
 
-    def run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
-            input_trace: Optional[np.ndarray] = None):
-        """Run `cycles` cycles; returns dict(trace=..., hash=..., detect=...) for the requested records."""
-        record = list(record)
+    def alloc_outputs(self, cycles: int, record: list, mode: int) -> dict:
+        """Host arrays for a run's recorded outputs (None where not requested)."""
         engine = self.design.info.engine
         words = (self.lanes + 31) // 32
         out_trace = out_hash = detect = None
@@ -463,9 +518,16 @@ class GpuBatchSimulator:
             out_hash = np.zeros(cycles, dtype=np.uint64)
         if mode & REC_DETECT:
             detect = np.zeros(self.lanes, dtype=np.uint32)
-        r = self.make_run(cycles, seed, stim, record, mode, input_trace, out_trace, out_hash, detect)
-        check(lib().rrtl_batch_run(self.h, byref(r)))
         return {"trace": out_trace, "hash": out_hash, "detect": detect}
+
+    def run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
+            input_trace: Optional[np.ndarray] = None):
+        """Run `cycles` cycles; returns dict(trace=..., hash=..., detect=...) for the requested records."""
+        record = list(record)
+        out = self.alloc_outputs(cycles, record, mode)
+        r = self.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
+        check(lib().rrtl_batch_run(self.h, byref(r)))
+        return out
 
     def set_faults(self, faults: Sequence[tuple]):
         """faults: (lane, signal, value) triples; signal by name or index."""

@@ -14,6 +14,7 @@ Workloads:
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 from typing import Dict, List
 
@@ -343,3 +344,50 @@ def cpu_rom(lanes: int, seed: int = 3):
             imm = rng.below(256) if op in (13, 14, 15) else rng.below(1 << 16)
             rom[a, 0, lane] = op | (rd << 4) | (rs1 << 8) | (rs2 << 12) | (imm << 16)
     return rom
+
+
+# --------------------------------------------------------------- job stream --
+@dataclass
+class JobSpec:
+    """One job of the uneven job stream: a run on a fresh batch of a design."""
+    design: int        # index into the stream's design list
+    lanes: int
+    cycles: int
+    seed: int          # stimulus seed
+    fault: bool        # one stuck-at fault per lane (lanes 32k are the fault-free references)
+
+
+def log_uniform_int(rng: Rng, lo: int, hi: int) -> int:
+    return int(round(math.exp(math.log(lo) + rng.uniform() * (math.log(hi) - math.log(lo)))))
+
+
+def job_stream_designs(n_designs: int = 8, gates_lo: int = 5_000, gates_hi: int = 200_000, seed: int = 40):
+    """Netlists of the 50k-gate family with gate counts log-uniform in [lo, hi]:
+    flip-flops scale with gates (2,048 per 50k), 64 PIs, 64 POs, depth 40."""
+    rng = Rng(seed)
+    out = []
+    for i in range(n_designs):
+        g = log_uniform_int(rng, gates_lo, gates_hi)
+        out.append(gate_netlist(n_gates=g, n_ff=max(64, g * 2048 // 50_000), depth=40, seed=seed * 1000 + i))
+    return out
+
+
+def job_stream(n_jobs: int, n_designs: int, lanes_lo: int = 32, lanes_hi: int = 65_536, cycles_lo: int = 100,
+               cycles_hi: int = 50_000, fault_frac: float = 0.3, seed: int = 41) -> List[JobSpec]:
+    """Jobs with log-uniform lanes and cycles over `n_designs` designs; a
+    `fault_frac` share are fault-simulation jobs."""
+    rng = Rng(seed)
+    jobs = []
+    for i in range(n_jobs):
+        jobs.append(JobSpec(design=rng.below(n_designs), lanes=log_uniform_int(rng, lanes_lo, lanes_hi),
+                            cycles=log_uniform_int(rng, cycles_lo, cycles_hi), seed=seed * 100_000 + i,
+                            fault=rng.uniform() < fault_frac))
+    return jobs
+
+
+def job_faults(meta: NetlistMeta, lanes: int, seed: int):
+    """One stuck-at fault per lane at a seeded random net (wires, flops,
+    outputs); lane 0 of every 32-lane word stays fault-free as the reference."""
+    rng = Rng(seed ^ 0xFA17)
+    sites = meta.gate_names + meta.regs + meta.outputs
+    return [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]
