@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -275,6 +276,93 @@ def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
     return out
 
 
+def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000)):
+    """Serving loop (the C5 shape): Poisson arrivals over three resident
+    designs (the 50k-gate netlist, the 8-stage CPU, a 500k-gate / 20k-FF
+    netlist of the same family); lanes log-uniform 64-16,384, cycles
+    log-uniform 1,000-50,000 divided by `cycle_div`, stimulus from a
+    per-request seed (CPU requests: a per-request window of a hashed ROM).
+    Reports throughput and p50/p99 latency per arrival rate; a sample of
+    requests is re-run alone and must match bit for bit."""
+    from rrtl_gb300.workloads import (Rng, cpu_rom_hashed, gate_netlist, log_uniform_int, netlist_run_spec,
+                                      pipelined_cpu)
+
+    t0 = time.perf_counter()
+    d_big, m_big = gate_netlist(n_gates=big[0], n_ff=big[1], depth=40, seed=5)
+    s_big, r_big = netlist_run_spec(m_big)
+    cd_big = sim.CompiledDesign(d_big.to_json(), m_big.top, ctx)
+    del d_big
+    cd_cpu = sim.CompiledDesign(pipelined_cpu(), "Cpu8", ctx)
+    rom_pool = cpu_rom_hashed(32768, seed=9)
+    cd_c2, s_c2, r_c2 = c2
+    designs = [("c2", cd_c2, s_c2, r_c2), ("cpu", cd_cpu, [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)],
+                                          ["out_pc", "out_acc"]), ("big", cd_big, s_big, r_big)]
+    setup_s = time.perf_counter() - t0
+    out = {"designs": {"c2": cd_c2.info.n_gates, "cpu": "8-stage CPU (word engine)", "big": cd_big.info.n_gates},
+           "lanes": "log-uniform 64-16384", "cycles": f"log-uniform 1000-50000 / {cycle_div}",
+           "chunk_cycles": chunk, "duration_s": duration_s, "setup_s": setup_s, "rates": []}
+
+    def spec(rng, i):
+        k = rng.below(3)
+        lanes = log_uniform_int(rng, 64, 16384)
+        cycles = max(1, log_uniform_int(rng, 1000, 50000) // cycle_div)
+        return k, lanes, cycles, 7000 + i
+
+    def submit(server, k, lanes, cycles, seed):
+        name, cd, stim, rec = designs[k]
+        mems = None
+        if name == "cpu":
+            off = seed % (rom_pool.shape[2] - lanes + 1)
+            mems = {"rom": rom_pool[:, :, off:off + lanes]}
+        return server.submit(cd, lanes, cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH, memories=mems)
+
+    for rate in rates:
+        server = sim.Server(ctx, chunk_cycles=chunk)
+        rng = Rng(int(rate * 1000) + 1)
+        handles = []
+        t_start = time.perf_counter()
+        t_next = t_start
+        i = 0
+        while True:
+            t_next += -math.log(1.0 - rng.uniform()) / rate
+            if t_next - t_start > duration_s:
+                break
+            k, lanes, cycles, seed = spec(rng, i)
+            i += 1
+            wait = t_next - time.perf_counter()
+            if wait > 0:
+                time.sleep(wait)
+            handles.append(((k, lanes, cycles, seed), submit(server, k, lanes, cycles, seed)))
+        server.drain()
+        t_end = time.perf_counter()
+        infos = [h.info() for _, h in handles]
+        lat = np.array([(x["done_ns"] - x["submit_ns"]) / 1e6 for x in infos])
+        queue = np.array([(x["admit_ns"] - x["submit_ns"]) / 1e6 for x in infos])
+        lc = sum(sp[1] * sp[2] for sp, _ in handles)
+        st = server.stats
+        # bit-exact: a sample of requests re-run alone on fresh batches
+        same = True
+        for sp, h in handles[:: max(1, len(handles) // 4)][:4]:
+            k, lanes, cycles, seed = sp
+            name, cd, stim, rec = designs[k]
+            g = sim.GpuBatchSimulator(cd, lanes=lanes)
+            if name == "cpu":
+                off = seed % (rom_pool.shape[2] - lanes + 1)
+                g.set_memory_limbs("rom", rom_pool[:, :, off:off + lanes])
+            ref = g.run(cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH)
+            same = same and np.array_equal(ref["hash"], h.outputs["hash"])
+            del g
+        server.close()
+        out["rates"].append({"rate_per_s": rate, "requests": len(handles), "failed": st["failed"],
+                             "throughput": lc / (t_end - t_start), "unit": "lane-cycles/s",
+                             "wall_s": t_end - t_start, "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                             "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                             "p50_queue_ms": float(np.percentile(queue, 50)) if len(queue) else None,
+                             "rounds": st["rounds"], "gpu_busy_frac": st["busy_ns"] / 1e9 / (t_end - t_start),
+                             "bitexact_sample": bool(same)})
+    return out
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -327,6 +415,8 @@ def main():
     ap.add_argument("--jobs", type=int, default=96, help="jobs in the uneven job-stream leg (0 = skip it)")
     ap.add_argument("--job-designs", type=int, default=8, help="distinct netlists in the job stream")
     ap.add_argument("--no-plain-jobs", action="store_true", help="job stream: skip the plain-path comparison")
+    ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
     args.warmup = max(args.warmup, 3)
@@ -454,6 +544,9 @@ def main():
     }
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
+    if args.serve_rates:
+        rates = [float(x) for x in args.serve_rates.split(",") if x]
+        out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), rates, args.serve_seconds)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import binding as ob
 

@@ -260,6 +260,64 @@ rrtl_status rrtl_queue_poll(rrtl_ctx* ctx, uint64_t id, uint32_t* status);
 /* Device time of the last launch (ms), valid after rrtl_queue_wait. */
 rrtl_status rrtl_queue_last_ms(rrtl_ctx* ctx, float* ms);
 
+/* ---- serving loop ----------------------------------------------------------
+ * Continuous batching of simulation requests on one GPU. Producer threads
+ * submit requests (a design, a lane count, a run and optional faults); a
+ * device-owner thread admits them first come first served while their device
+ * state fits the memory budget, keeps each request's lane state on the device
+ * until it finishes, and drives rounds in which every active request advances
+ * by up to `chunk_cycles` cycles (gate-engine requests share one launch of
+ * the persistent job-queue kernel). Requests arriving during a round join at
+ * the next one. Each result equals the same run alone on a fresh batch. While
+ * a server runs, its context must not be used from other threads except
+ * through rrtl_server_* calls. No counterpart in the reference's API. */
+typedef struct rrtl_server rrtl_server;
+
+typedef struct {
+  uint64_t hbm_budget;    /* bytes of device memory for request state; 0 = 90% of free memory */
+  uint32_t chunk_cycles;  /* cycles each active request advances per round; 0 = 256 */
+  uint32_t max_active;    /* requests on the device at once; 0 = no limit */
+} rrtl_server_opts;
+
+typedef struct {
+  uint32_t memory;        /* memory index (rrtl_design_memory) */
+  const uint32_t* data;   /* [addr][limb][lane], as rrtl_batch_set_memory_limbs */
+  size_t n;
+} rrtl_mem_init;
+
+typedef struct {
+  rrtl_design* design;
+  uint32_t lanes;
+  uint32_t n_faults;
+  const rrtl_fault* faults;      /* gate engine: stuck-at faults of the request's lanes */
+  uint32_t n_mem_init;
+  const rrtl_mem_init* mem_init; /* word engine: memory contents loaded before the run */
+  rrtl_run run;                  /* host output buffers, filled when the request finishes */
+} rrtl_request;
+
+typedef struct {
+  uint32_t status;   /* RRTL_JOB_* */
+  uint64_t submit_ns, admit_ns, done_ns;  /* steady-clock times (0 = not yet) */
+} rrtl_request_info;
+
+typedef struct {
+  uint64_t rounds, completed, failed, lane_cycles, busy_ns, pending;
+} rrtl_server_stats;
+
+rrtl_status rrtl_server_create(rrtl_ctx* ctx, const rrtl_server_opts* opts, rrtl_server** out);
+/* Thread-safe. The request's arrays are copied; its output buffers must stay
+ * valid until it finishes. */
+rrtl_status rrtl_server_submit(rrtl_server* s, const rrtl_request* req, uint64_t* id);
+rrtl_status rrtl_server_info(rrtl_server* s, uint64_t id, rrtl_request_info* info);
+/* Block until the request finishes (timeout_ms 0 = no limit); returns its error if it failed. */
+rrtl_status rrtl_server_wait(rrtl_server* s, uint64_t id, uint32_t timeout_ms);
+rrtl_status rrtl_server_drain(rrtl_server* s);
+rrtl_status rrtl_server_stats_get(rrtl_server* s, rrtl_server_stats* out);
+/* Forget a finished request (its id becomes unknown). */
+rrtl_status rrtl_server_release(rrtl_server* s, uint64_t id);
+/* Finish every submitted request, stop the owner thread, free the server. */
+rrtl_status rrtl_server_destroy(rrtl_server* s);
+
 /* ---- allocation-free tick_many (word engine) -----------------------------
  * No counterpart in the reference: it exists for callers that may not call
  * cudaMalloc or cudaFree, such as a serving process that has divided device

@@ -88,7 +88,7 @@ static rrtl_status guard(F&& f) {
 
 // ------------------------------------------------------------------ helpers --
 
-namespace {
+namespace rrtl {
 
 uint32_t round_up(uint32_t x, uint32_t m) { return (x + m - 1) / m * m; }
 
@@ -539,9 +539,13 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
 }
 
 // ---- word engine run
-void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle) {
+// Validate a word-engine run and upload its stimulus and record tables;
+// stages host input traces and zeroes hash/detect outputs on the context
+// stream. `start_settle`: settle before the first cycle.
+WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
+  WordPrepared g;
   std::vector<WordStimDev> stim;
   for (uint32_t i = 0; i < run.n_stim; ++i) {
     const rrtl_stim& s = run.stim[i];
@@ -562,7 +566,7 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
           "E_GPU_RECORD: recording needs at least one signal");
   upload(b->d_stim, stim);
   upload(b->d_rec, rec);
-  WordRunDev R{};
+  WordRunDev& R = g.R;
   R.cycles = run.cycles;
   R.seed = run.seed;
   R.n_stim = (uint32_t)stim.size();
@@ -577,21 +581,24 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   R.values = b->d_values.as<uint32_t>();
   R.mems = b->d_mem.as<uint32_t>();
   R.caps = b->d_caps.as<uint32_t>();
-  R.final_settle = final_settle;
+  R.final_settle = 1;
   R.start_settle = start_settle;
   R.err = b->d_err.as<uint32_t>();
-  bool smem_slots = word_smem_slots(d);
-  REQUIRE(smem_slots, RRTL_E_UNSUPPORTED,
+  R.vspill = nullptr;
+  g.smem_slots = word_smem_slots(d);
+  REQUIRE(g.smem_slots, RRTL_E_UNSUPPORTED,
           "E_WORD_SCOPE: design needs " + std::to_string(d->wdev.n_vslots) + " live value slots, more than shared memory holds");
+  g.rec_limbs = rec_limbs;
   size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->lanes * 4;
-  size_t trace_out_bytes = (size_t)run.cycles * rec_limbs * b->lanes * 4;
-  size_t hash_bytes = (size_t)run.cycles * 8;
-  size_t det_bytes = (size_t)b->lanes * 4;
-  bool want_trace = run.record_mode & RRTL_REC_TRACE, want_hash = run.record_mode & RRTL_REC_HASH,
-       want_det = run.record_mode & RRTL_REC_DETECT;
-  REQUIRE(!want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
-  REQUIRE(!want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
-  REQUIRE(!want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
+  g.trace_out_bytes = (size_t)run.cycles * rec_limbs * b->lanes * 4;
+  g.hash_bytes = (size_t)run.cycles * 8;
+  g.det_bytes = (size_t)b->lanes * 4;
+  g.want_trace = run.record_mode & RRTL_REC_TRACE;
+  g.want_hash = run.record_mode & RRTL_REC_HASH;
+  g.want_det = run.record_mode & RRTL_REC_DETECT;
+  REQUIRE(!g.want_trace || run.out_trace, RRTL_E_ARG, "E_GPU_RECORD: out_trace is null");
+  REQUIRE(!g.want_hash || run.out_hash, RRTL_E_ARG, "E_GPU_RECORD: out_hash is null");
+  REQUIRE(!g.want_det || run.detect, RRTL_E_ARG, "E_GPU_RECORD: detect is null");
   if (device_ptrs) {
     R.in_trace = run.input_trace;
     R.out_trace = run.out_trace;
@@ -603,40 +610,61 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
       cuda_check(cudaMemcpyAsync(b->d_in_trace.p, run.input_trace, trace_in_bytes, cudaMemcpyHostToDevice, st), "h2d trace");
       R.in_trace = b->d_in_trace.as<uint32_t>();
     }
-    if (want_trace) {
-      b->d_out_trace.reserve(std::max<size_t>(trace_out_bytes, 16));
+    if (g.want_trace) {
+      b->d_out_trace.reserve(std::max<size_t>(g.trace_out_bytes, 16));
       R.out_trace = b->d_out_trace.as<uint32_t>();
     }
-    if (want_hash) {
-      b->d_hash.reserve(std::max<size_t>(hash_bytes, 16));
+    if (g.want_hash) {
+      b->d_hash.reserve(std::max<size_t>(g.hash_bytes, 16));
       R.out_hash = b->d_hash.as<unsigned long long>();
     }
-    if (want_det) {
-      b->d_detect.reserve(std::max<size_t>(det_bytes, 16));
+    if (g.want_det) {
+      b->d_detect.reserve(std::max<size_t>(g.det_bytes, 16));
       R.detect = b->d_detect.as<uint32_t>();
     }
   }
-  if (want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, hash_bytes, st), "memset hash");
-  if (want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, det_bytes, st), "memset detect");
-  R.vspill = nullptr;
+  if (g.want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, g.hash_bytes, st), "memset hash");
+  if (g.want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, g.det_bytes, st), "memset detect");
+  return g;
+}
+
+// Launch cycles [c0, c0 + n) of a prepared word run (one kernel; the settle
+// before the first cycle only when c0 == 0, the closing one if `last`).
+cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0, uint64_t n, bool last, cudaStream_t st) {
+  WordRunDev R1 = g.R;
+  R1.cycles = n;
+  R1.start_settle = c0 == 0 ? g.R.start_settle : 0;
+  R1.final_settle = last ? 1u : 0u;
+  // per-cycle pointers shift so cycle c0 of the run is cycle 0 of the launch's buffers
+  R1.in_trace = g.R.in_trace ? g.R.in_trace + (size_t)c0 * g.R.n_trace_cols * g.R.lanes : nullptr;
+  R1.out_trace = g.R.out_trace ? g.R.out_trace + (size_t)c0 * g.rec_limbs * g.R.lanes : nullptr;
+  R1.out_hash = g.R.out_hash ? g.R.out_hash + c0 : nullptr;
+  R1.cycle_base = c0;
+  return launch_word(d->wdev, R1, g.smem_slots, st);
+}
+
+void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {
+  cudaStream_t st = b->d->ctx->stream;
+  if (g.want_trace)
+    cuda_check(cudaMemcpyAsync(run.out_trace, g.R.out_trace, g.trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
+  if (g.want_hash)
+    cuda_check(cudaMemcpyAsync(run.out_hash, g.R.out_hash, g.hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
+  if (g.want_det) cuda_check(cudaMemcpyAsync(run.detect, g.R.detect, g.det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+}
+
+void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle) {
+  rrtl_design* d = b->d;
+  cudaStream_t st = d->ctx->stream;
+  WordPrepared g = word_prepare(b, run, device_ptrs, start_settle);
+  g.R.final_settle = final_settle;
   Timer tm(b);
   if (b->path != RRTL_PATH_FUSED && run.cycles > 1) {
     // one launch per cycle: the baseline path (captured into a CUDA graph on RRTL_PATH_PLAIN_GRAPH)
     const bool graph = b->path == RRTL_PATH_PLAIN_GRAPH;
     if (graph) cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     cudaError_t ce = cudaSuccess;
-    WordRunDev R1 = R;
-    for (uint64_t c = 0; c < run.cycles && ce == cudaSuccess; ++c) {
-      R1.cycles = 1;
-      R1.start_settle = (c == 0) ? R.start_settle : 0;
-      R1.final_settle = (c + 1 == run.cycles) ? R.final_settle : 0;
-      // per-cycle pointers shift so cycle c of this launch is cycle 0 of its buffers
-      R1.in_trace = R.in_trace ? R.in_trace + (size_t)c * run.n_trace_cols * b->lanes : nullptr;
-      R1.out_trace = R.out_trace ? R.out_trace + (size_t)c * rec_limbs * b->lanes : nullptr;
-      R1.out_hash = R.out_hash ? R.out_hash + c : nullptr;
-      R1.cycle_base = c;
-      ce = launch_word(d->wdev, R1, smem_slots, st);
-    }
+    for (uint64_t c = 0; c < run.cycles && ce == cudaSuccess; ++c)
+      ce = word_chunk(d, g, c, 1, c + 1 == run.cycles && final_settle, st);
     if (graph) {
       cudaGraph_t gh = nullptr;
       cudaError_t e2 = cudaStreamEndCapture(st, &gh);
@@ -653,13 +681,11 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
       cuda_check(ce, "word_kernel");
     }
   } else {
-    cuda_check(launch_word(d->wdev, R, smem_slots, st), "word_kernel");
+    cuda_check(launch_word(d->wdev, g.R, g.smem_slots, st), "word_kernel");
   }
   tm.stop();
   if (!device_ptrs) {
-    if (want_trace) cuda_check(cudaMemcpyAsync(run.out_trace, R.out_trace, trace_out_bytes, cudaMemcpyDeviceToHost, st), "d2h trace");
-    if (want_hash) cuda_check(cudaMemcpyAsync(run.out_hash, R.out_hash, hash_bytes, cudaMemcpyDeviceToHost, st), "d2h hash");
-    if (want_det) cuda_check(cudaMemcpyAsync(run.detect, R.detect, det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
+    word_copy_out(b, g, run);
     check_err_word(b);
     cuda_check(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1), "elapsed");
   }
@@ -784,9 +810,10 @@ void queue_launch(rrtl_ctx* c) {
     upload(Q.d_items, flat);
     Q.d_next.reserve(16);
     cuda_check(cudaMemsetAsync(Q.d_next.p, 0, 4, st), "memset queue");
-    if (smem > Q.smem_set) {
-      cuda_check(gate_queue_prepare(smem), "gate_queue_prepare");
-      Q.smem_set = smem;
+    if (!Q.smem_set) {
+      // the limit is per kernel: allow every job this queue can take
+      cuda_check(gate_queue_prepare(qmax), "gate_queue_prepare");
+      Q.smem_set = qmax;
     }
     GateQueueDev QD{Q.d_jobs.as<GateJobDev>(), Q.d_items.as<GateItemDev>(), (uint32_t)flat.size(), Q.d_next.as<uint32_t>()};
     const uint32_t grid = std::min<uint32_t>((uint32_t)flat.size(), c->sm_count);
@@ -809,7 +836,7 @@ void batch_tick_many(rrtl_batch* b, uint64_t steps, bool sync) {
   if (sync) check_err_word(b);
 }
 
-}  // namespace
+}  // namespace rrtl
 
 // -------------------------------------------------------------------- C ABI --
 

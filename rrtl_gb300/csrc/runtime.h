@@ -76,6 +76,15 @@ struct GatePrepared {
   bool want_trace = false, want_hash = false, want_det = false;
 };
 
+// A word-engine run made ready for chunked launches.
+struct WordPrepared {
+  WordRunDev R{};
+  bool smem_slots = false;
+  uint32_t rec_limbs = 0;
+  size_t trace_out_bytes = 0, hash_bytes = 0, det_bytes = 0;
+  bool want_trace = false, want_hash = false, want_det = false;
+};
+
 // One submitted job of the device job queue.
 struct QueueJob {
   uint64_t id = 0;
@@ -101,6 +110,19 @@ struct JobQueue {
   uint32_t last_items = 0;
   ~JobQueue();
 };
+
+// Runtime internals shared by the C ABI and the serving loop.
+GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused);
+void gate_copy_out(rrtl_batch* b, const GatePrepared& g, const rrtl_run& run);
+void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st, bool graph);
+WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle);
+cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0, uint64_t n, bool last, cudaStream_t st);
+void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run);
+size_t gate_queue_static_smem();
+cudaError_t gate_queue_prepare(size_t smem);
+cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem, cudaStream_t st);
+cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
+void set_last_error(const std::string& msg);
 
 }  // namespace rrtl
 

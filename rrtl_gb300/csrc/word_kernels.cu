@@ -144,7 +144,8 @@ __global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) 
   const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
   WordLane W{P, R, kSmem ? vsm + threadIdx.x : R.vspill + lane, kSmem ? blockDim.x : R.lanes_pad, lane, R.lanes_pad};
   const bool live = lane < R.lanes;
-  bool detected = false;
+  // a lane detected by an earlier launch of the same run stays detected
+  bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
   if (R.start_settle) {
     W.run(P.comb_b, P.comb_e);
     W.run(P.async_b, P.async_e);

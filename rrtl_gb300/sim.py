@@ -132,6 +132,14 @@ EXPORTS = (
     "rrtl_queue_wait",
     "rrtl_queue_poll",
     "rrtl_queue_last_ms",
+    "rrtl_server_create",
+    "rrtl_server_submit",
+    "rrtl_server_info",
+    "rrtl_server_wait",
+    "rrtl_server_drain",
+    "rrtl_server_stats_get",
+    "rrtl_server_release",
+    "rrtl_server_destroy",
     "rrtl_batch_tile_words",
     "rrtl_batch_last_kernel_ms",
     "rrtl_word_tick_many_noalloc",
@@ -188,6 +196,14 @@ def lib():
         "rrtl_queue_wait": [c_void_p],
         "rrtl_queue_poll": [c_void_p, c_uint64, P(c_uint32)],
         "rrtl_queue_last_ms": [c_void_p, P(c_float)],
+        "rrtl_server_create": [c_void_p, P(ServerOpts), P(c_void_p)],
+        "rrtl_server_submit": [c_void_p, P(Request), P(c_uint64)],
+        "rrtl_server_info": [c_void_p, c_uint64, P(RequestInfo)],
+        "rrtl_server_wait": [c_void_p, c_uint64, c_uint32],
+        "rrtl_server_drain": [c_void_p],
+        "rrtl_server_stats_get": [c_void_p, P(ServerStats)],
+        "rrtl_server_release": [c_void_p, c_uint64],
+        "rrtl_server_destroy": [c_void_p],
         "rrtl_batch_tile_words": [c_void_p, P(c_uint32)],
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
@@ -555,6 +571,118 @@ class GpuBatchSimulator:
     def close(self):
         if self.h:
             lib().rrtl_batch_destroy(self.h)
+            self.h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- serving --
+class MemInit(ctypes.Structure):
+    _fields_ = [("memory", c_uint32), ("data", POINTER(c_uint32)), ("n", c_size_t)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("design", c_void_p), ("lanes", c_uint32), ("n_faults", c_uint32), ("faults", POINTER(Fault)),
+                ("n_mem_init", c_uint32), ("mem_init", POINTER(MemInit)), ("run", Run)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("status", c_uint32), ("submit_ns", c_uint64), ("admit_ns", c_uint64), ("done_ns", c_uint64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("rounds", c_uint64), ("completed", c_uint64), ("failed", c_uint64), ("lane_cycles", c_uint64),
+                ("busy_ns", c_uint64), ("pending", c_uint64)]
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget", c_uint64), ("chunk_cycles", c_uint32), ("max_active", c_uint32)]
+
+
+class _RunShape:
+    """A design and a lane count: enough to build a run without a batch."""
+
+    def __init__(self, design: CompiledDesign, lanes: int):
+        self.design, self.lanes = design, lanes
+
+    _sig = GpuBatchSimulator._sig
+    make_run = GpuBatchSimulator.make_run
+    alloc_outputs = GpuBatchSimulator.alloc_outputs
+
+
+class ServedRequest:
+    """A request submitted to a Server; `outputs` fills in when it finishes."""
+
+    def __init__(self, server: "Server", rid: int, outputs: dict, keep):
+        self.server, self.id, self.outputs, self._keep = server, rid, outputs, keep
+
+    def info(self) -> dict:
+        return self.server.info(self.id)
+
+    def wait(self, timeout_ms: int = 0):
+        self.server.wait(self.id, timeout_ms)
+        return self.outputs
+
+
+class Server:
+    """The serving loop (rrtl_server_*): continuous batching of requests on one GPU."""
+
+    def __init__(self, ctx: Optional[Context] = None, hbm_budget: int = 0, chunk_cycles: int = 0, max_active: int = 0):
+        self.ctx = ctx or default_context()
+        o = ServerOpts(hbm_budget, chunk_cycles, max_active)
+        self.h = c_void_p()
+        check(lib().rrtl_server_create(self.ctx.h, byref(o), byref(self.h)))
+
+    def submit(self, design: CompiledDesign, lanes: int, cycles: int, seed: int = 0, stim: Iterable = (),
+               record: Iterable = (), mode: int = 0, faults: Sequence[tuple] = (),
+               input_trace: Optional[np.ndarray] = None, memories: Optional[dict] = None) -> ServedRequest:
+        """memories: {name: [addr][limb][lane] array} loaded before the run (word engine)."""
+        shape = _RunShape(design, lanes)
+        record = list(record)
+        out = shape.alloc_outputs(cycles, record, mode)
+        r = shape.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
+        fa = (Fault * max(1, len(faults)))(*[Fault(l, shape._sig(s), v) for l, s, v in faults])
+        q = Request()
+        q.design = design.h
+        q.lanes = lanes
+        q.n_faults = len(faults)
+        q.faults = ctypes.cast(fa, POINTER(Fault))
+        mems = [(design.memory(n)[0], np.ascontiguousarray(a, dtype=np.uint32).ravel()) for n, a in (memories or {}).items()]
+        mi = (MemInit * max(1, len(mems)))(*[MemInit(i, _u32p(a), a.size) for i, a in mems])
+        q.n_mem_init = len(mems)
+        q.mem_init = ctypes.cast(mi, POINTER(MemInit))
+        q.run = r
+        rid = c_uint64()
+        check(lib().rrtl_server_submit(self.h, byref(q), byref(rid)))
+        return ServedRequest(self, rid.value, out, (r, fa, mi, mems, design))
+
+    def info(self, rid: int) -> dict:
+        i = RequestInfo()
+        check(lib().rrtl_server_info(self.h, rid, byref(i)))
+        return {"status": i.status, "submit_ns": i.submit_ns, "admit_ns": i.admit_ns, "done_ns": i.done_ns}
+
+    def wait(self, rid: int, timeout_ms: int = 0):
+        check(lib().rrtl_server_wait(self.h, rid, timeout_ms))
+
+    def drain(self):
+        check(lib().rrtl_server_drain(self.h))
+
+    def release(self, rid: int):
+        check(lib().rrtl_server_release(self.h, rid))
+
+    @property
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(lib().rrtl_server_stats_get(self.h, byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self):
+        if self.h:
+            check(lib().rrtl_server_destroy(self.h))
             self.h = c_void_p()
 
     def __del__(self):

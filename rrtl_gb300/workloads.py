@@ -346,6 +346,33 @@ def cpu_rom(lanes: int, seed: int = 3):
     return rom
 
 
+def _smix64_np(z):
+    import numpy as np
+
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def cpu_rom_hashed(lanes: int, seed: int = 3):
+    """Same instruction format and distribution as cpu_rom, drawn from a
+    counter hash of (seed, lane, address) so large batches build fast."""
+    import numpy as np
+
+    with np.errstate(over="ignore"):
+        idx = np.arange(256 * lanes, dtype=np.uint64).reshape(256, lanes)
+        base = _smix64_np(idx ^ np.uint64((seed * 0xD1B54A32D192ED03) & MASK64))
+        f = [_smix64_np(base + np.uint64(k)) for k in range(5)]
+    op = (f[0] % np.uint64(16)).astype(np.uint32)
+    rd, rs1, rs2 = [(x % np.uint64(16)).astype(np.uint32) for x in f[1:4]]
+    imm_small = (f[4] % np.uint64(256)).astype(np.uint32)
+    imm_big = (f[4] % np.uint64(1 << 16)).astype(np.uint32)
+    imm = np.where(op >= 13, imm_small, imm_big)
+    rom = op | (rd << 4) | (rs1 << 8) | (rs2 << 12) | (imm << 16)
+    return rom.reshape(256, 1, lanes).astype(np.uint32)
+
+
 # --------------------------------------------------------------- job stream --
 @dataclass
 class JobSpec:
