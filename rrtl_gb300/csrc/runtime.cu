@@ -22,8 +22,8 @@ cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_
 cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st);
 cudaError_t word_prepare(size_t smem);
 
-constexpr uint32_t kWordThreads = 128;
-constexpr size_t kWordSmemBudget = 96 * 1024;
+constexpr uint32_t kWordThreads = kWordBlockLanes;
+constexpr size_t kWordSmemBudget = kWordSmemLimit;
 
 void cuda_check(cudaError_t e, const char* what) {
   if (e == cudaErrorMemoryAllocation) fail(RRTL_E_OOM, std::string("E_OOM: ") + what + ": " + cudaGetErrorString(e));
@@ -630,7 +630,7 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
 
 // Launch cycles [c0, c0 + n) of a prepared word run (one kernel; the settle
 // before the first cycle only when c0 == 0, the closing one if `last`).
-cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0, uint64_t n, bool last, cudaStream_t st) {
+WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last) {
   WordRunDev R1 = g.R;
   R1.cycles = n;
   R1.start_settle = c0 == 0 ? g.R.start_settle : 0;
@@ -640,7 +640,11 @@ cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0,
   R1.out_trace = g.R.out_trace ? g.R.out_trace + (size_t)c0 * g.rec_limbs * g.R.lanes : nullptr;
   R1.out_hash = g.R.out_hash ? g.R.out_hash + c0 : nullptr;
   R1.cycle_base = c0;
-  return launch_word(d->wdev, R1, g.smem_slots, st);
+  return R1;
+}
+
+cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0, uint64_t n, bool last, cudaStream_t st) {
+  return launch_word(d->wdev, word_chunk_desc(g, c0, n, last), g.smem_slots, st);
 }
 
 void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {

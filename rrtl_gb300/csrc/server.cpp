@@ -94,8 +94,11 @@ struct rrtl_server {
   // device-owner thread state
   std::vector<std::shared_ptr<Request>> active;
   size_t used = 0;
-  DevBuf d_jobs, d_items, d_next;
+  DevBuf d_jobs, d_items, d_next, d_wjobs;
   bool queue_ready = false;
+  size_t word_smem_set = 0;
+  cudaStream_t word_stream = nullptr;  // word-engine launches overlap the gate queue kernel
+  cudaEvent_t staged = nullptr;        // this round's uploads and memsets are done on the context stream
   // statistics (under mu)
   uint64_t rounds = 0, completed = 0, failed = 0, lane_cycles = 0, busy_ns = 0;
 
@@ -163,7 +166,9 @@ void rrtl_server::round() {
   const uint64_t t0 = now_ns();
   std::vector<GateJobDev> jobs;
   std::vector<GateItemDev> items;
-  size_t smem = 0;
+  std::vector<WordJobDev> wjobs;
+  uint32_t wblocks = 0;
+  size_t smem = 0, wsmem = 0;
   std::vector<std::pair<double, uint32_t>> order;
   for (auto& rp : active) {
     Request& r = *rp;
@@ -186,8 +191,26 @@ void rrtl_server::round() {
         items.push_back(GateItemDev{ji, t, (unsigned long long)r.done_cycles, (uint32_t)r.chunk, last ? 1u : 0u});
       }
     } else {
-      cuda_check(word_chunk(r.design, r.wp, r.done_cycles, r.chunk, last, st), "word_kernel");
+      WordJobDev wj{};
+      wj.P = r.design->wdev;
+      wj.R = word_chunk_desc(r.wp, r.done_cycles, r.chunk, last);
+      wj.block_begin = wblocks;
+      wblocks += r.wp.R.lanes_pad / kWordBlockLanes;
+      wsmem = std::max(wsmem, (size_t)r.design->wdev.n_vslots * kWordBlockLanes * 8);
+      wjobs.push_back(wj);
     }
+  }
+  if (!wjobs.empty()) {
+    // one launch for every word-engine request, on the second stream, after this round's staging
+    if (wsmem > word_smem_set) {
+      cuda_check(word_multi_prepare(kWordSmemLimit), "word_multi_prepare");
+      word_smem_set = kWordSmemLimit;
+    }
+    upload(d_wjobs, wjobs);
+    cuda_check(cudaEventRecord(staged, st), "event");
+    cuda_check(cudaStreamWaitEvent(word_stream, staged, 0), "wait event");
+    cuda_check(launch_word_multi(d_wjobs.as<WordJobDev>(), (uint32_t)wjobs.size(), wblocks, wsmem, word_stream),
+               "word_multi_kernel");
   }
   if (!items.empty()) {
     std::stable_sort(order.begin(), order.end(),
@@ -209,6 +232,7 @@ void rrtl_server::round() {
                "gate_queue_kernel");
   }
   cuda_check(cudaStreamSynchronize(st), "sync");
+  cuda_check(cudaStreamSynchronize(word_stream), "sync");
   {
     std::lock_guard<std::mutex> lk(mu);
     ++rounds;
@@ -242,12 +266,35 @@ void rrtl_server::round() {
 
 void rrtl_server::loop() {
   cudaSetDevice(ctx->device);
+  if (cudaStreamCreateWithFlags(&word_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&staged, cudaEventDisableTiming) != cudaSuccess) {
+    // without its streams the loop cannot run: fail every request as it arrives
+    for (;;) {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] { return stop || !pending.empty(); });
+      while (!pending.empty()) {
+        Request& r = *pending.front();
+        r.status = RRTL_JOB_FAILED;
+        r.error = "E_DEVICE: serving loop could not create its stream";
+        r.t_done = now_ns();
+        ++failed;
+        pending.pop_front();
+      }
+      cv_done.notify_all();
+      if (stop) return;
+    }
+  }
   for (;;) {
     std::vector<std::shared_ptr<Request>> fresh;
     {
       std::unique_lock<std::mutex> lk(mu);
       if (active.empty()) cv_work.wait(lk, [&] { return stop || !pending.empty(); });
-      if (stop && pending.empty() && active.empty()) return;
+      if (stop && pending.empty() && active.empty()) {
+      lk.unlock();
+      cudaEventDestroy(staged);
+      cudaStreamDestroy(word_stream);
+      return;
+    }
       // admission: first come first served while the device memory budget and the slot count allow
       while (!pending.empty()) {
         Request& r = *pending.front();

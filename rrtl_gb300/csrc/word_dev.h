@@ -88,4 +88,12 @@ struct WordRunDev {
   uint32_t* err;
 };
 
+// One run of the multi-job word kernel: blocks [block_begin, next job's
+// block_begin) simulate its lanes, 128 per block.
+struct WordJobDev {
+  WordProgDev P;
+  WordRunDev R;
+  uint32_t block_begin, pad;
+};
+
 }  // namespace rrtl

@@ -138,10 +138,11 @@ struct WordLane {
   }
 };
 
+// One lane through one launch's cycles (the body shared by the single-run
+// and the multi-job kernels).
 template <bool kSmem>
-__global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) {
-  extern __shared__ unsigned long long vsm[];
-  const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRunDev& R, uint32_t lane,
+                                              unsigned long long* vsm) {
   WordLane W{P, R, kSmem ? vsm + threadIdx.x : R.vspill + lane, kSmem ? blockDim.x : R.lanes_pad, lane, R.lanes_pad};
   const bool live = lane < R.lanes;
   // a lane detected by an earlier launch of the same run stays detected
@@ -204,6 +205,44 @@ __global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) 
     W.run(P.comb_b, P.comb_e);
     W.run(P.async_b, P.async_e);
   }
+}
+
+template <bool kSmem>
+__global__ void __launch_bounds__(128) word_kernel(WordProgDev P, WordRunDev R) {
+  extern __shared__ unsigned long long vsm[];
+  word_lane_run<kSmem>(P, R, blockIdx.x * blockDim.x + threadIdx.x, vsm);
+}
+
+// Many word-engine runs in one launch: block b belongs to the job whose block
+// range holds it (jobs sorted by block_begin). Used by the serving loop so the
+// word-engine requests of a round run side by side.
+__global__ void __launch_bounds__(128) word_multi_kernel(const WordJobDev* __restrict__ jobs, uint32_t n_jobs) {
+  extern __shared__ unsigned long long vsm[];
+  __shared__ WordJobDev s_job;
+  __shared__ uint32_t s_j;
+  if (threadIdx.x == 0) {
+    uint32_t lo = 0, hi = n_jobs;  // last job with block_begin <= blockIdx.x
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (jobs[mid].block_begin <= blockIdx.x) lo = mid;
+      else hi = mid;
+    }
+    s_j = lo;
+  }
+  __syncthreads();
+  for (uint32_t i = threadIdx.x; i < sizeof(WordJobDev) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&s_job)[i] = reinterpret_cast<const uint32_t*>(jobs + s_j)[i];
+  __syncthreads();
+  word_lane_run<true>(s_job.P, s_job.R, (blockIdx.x - s_job.block_begin) * blockDim.x + threadIdx.x, vsm);
+}
+
+cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st) {
+  word_multi_kernel<<<blocks, 128, smem, st>>>(jobs, n_jobs);
+  return cudaGetLastError();
+}
+
+cudaError_t word_multi_prepare(size_t smem) {
+  return cudaFuncSetAttribute(word_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
 cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slots, cudaStream_t st) {
