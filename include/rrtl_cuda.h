@@ -165,7 +165,7 @@ typedef struct {
   uint64_t param;
 } rrtl_stim;
 
-enum { RRTL_REC_TRACE = 1, RRTL_REC_HASH = 2, RRTL_REC_DETECT = 4 };
+enum { RRTL_REC_TRACE = 1, RRTL_REC_HASH = 2, RRTL_REC_DETECT = 4, RRTL_REC_CHECK = 8 /* trace replay only */ };
 
 typedef struct {
   uint64_t cycles;
@@ -176,7 +176,8 @@ typedef struct {
   const uint32_t* record;      /* recorded signals (1-bit for the gate engine) */
   uint32_t record_mode;        /* RRTL_REC_* bitmask */
   uint32_t n_trace_cols;       /* columns of input_trace */
-  const uint32_t* input_trace; /* gate engine: [cycle][col][word]; word engine: [cycle][col][lane] (one limb) */
+  const uint32_t* input_trace; /* gate engine: [cycle][col][word]; word engine: [cycle][col][lane], limb l of a
+                                  RRTL_STIM_TRACE signal read from column param + l */
   uint32_t* out_trace;         /* gate engine: [cycle][rec][word]; word engine: [cycle][rec][limb][lane] */
   uint64_t* out_hash;          /* [cycle] per-cycle output hash */
   uint32_t* detect;            /* [lanes] first cycle a lane's recorded signals differ from lane 0 of its
@@ -190,6 +191,42 @@ rrtl_status rrtl_batch_run(rrtl_batch* b, const rrtl_run* run);
 /* Same, with every buffer pointer in `run` a device pointer of the batch's
  * device; returns without synchronising. */
 rrtl_status rrtl_batch_run_device(rrtl_batch* b, const rrtl_run* run);
+
+/* ---- trace replay (GpuBatchSimulator::replay_lane_trace, crates/rrtl-gpu-sim/src/lib.rs:989-1357;
+ * plan types GpuTraceReplayPlan / GpuTraceInputOp / GpuTraceCheckOp, :276-300) ----------------------
+ * Per step: the step's input ops store their lane values, the design settles,
+ * the step's checks compare one limb of a signal per lane with the expected
+ * values, and the clock ticks; after the last step the design settles. A
+ * signal keeps its value between input ops (starting from the batch state).
+ * Mismatches go to `log` = [count, then (step, check_index, lane, limb,
+ * expected, actual) for up to max_mismatches of them, in no fixed order];
+ * *n_mismatches is the full count. Gate engine: 1-bit signals, limb 0. */
+typedef struct {
+  uint64_t step;
+  uint32_t signal;
+  uint32_t limb;
+  const uint32_t* values;    /* [lanes] */
+} rrtl_trace_input;
+
+typedef struct {
+  uint64_t step;
+  uint32_t check_index;
+  uint32_t signal;
+  uint32_t limb;
+  uint32_t pad;
+  const uint32_t* expected;  /* [lanes] */
+} rrtl_trace_check;
+
+typedef struct {
+  uint64_t steps;
+  uint32_t n_inputs;
+  const rrtl_trace_input* inputs;
+  uint32_t n_checks;
+  const rrtl_trace_check* checks;
+} rrtl_trace;
+
+rrtl_status rrtl_batch_replay_trace(rrtl_batch* b, const rrtl_trace* trace, uint32_t max_mismatches, uint32_t* log,
+                                    uint64_t* n_mismatches);
 
 /* ---- fault injection (BitParallelSimulator::set_force, crates/rrtl-sim-ir/src/bitparallel.rs:96-126) */
 typedef struct {

@@ -817,7 +817,7 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
           if (st.kind == RRTL_STIM_RANDOM) v[i] = o_stim_lane_limb(r->seed, st.param, c, lane, L.width, i);
           else if (st.kind == RRTL_STIM_PULSE) v[i] = (i == 0 && c < st.param) ? 1u : 0u;
           else if (st.kind == RRTL_STIM_CONST) v[i] = i < 2 ? (uint32_t)(st.param >> (32 * i)) : 0u;
-          else if (st.kind == RRTL_STIM_TRACE) v[i] = i == 0 ? r->input_trace[(c * r->n_trace_cols + st.param) * lanes + lane] : 0u;
+          else if (st.kind == RRTL_STIM_TRACE) v[i] = r->input_trace[(c * r->n_trace_cols + st.param + i) * lanes + lane];
         }
         s->store_layout(L, lane, v);
       }

@@ -90,6 +90,12 @@ struct GateRunDev {
   uint32_t* nets;             // [rows][words_pad]
   uint32_t* err;              // device status word
   unsigned long long cycle_base;  // absolute cycle of the launch's first cycle (stimulus, records)
+  // trace checks (RRTL_REC_CHECK): per cycle and recorded net, the check index
+  // (~0: none) and the expected words; mismatches go to an atomic log
+  const uint32_t* chk_idx;    // [cycle][rec]
+  const uint32_t* chk_exp;    // [cycle][rec][words]
+  uint32_t* chk_log;          // [1 + 6*cap]: count, then (step, check, lane, limb, expected, actual)
+  uint32_t chk_cap;
 };
 
 // One job of the device-side queue: a run over one batch with its program.

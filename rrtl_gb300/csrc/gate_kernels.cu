@@ -21,6 +21,7 @@
 #include <stdint.h>
 
 #include "../../include/rrtl_cuda.h"
+#include "check_log.h"
 #include "gate_dev.h"
 #include "stim.h"
 
@@ -109,6 +110,20 @@ __device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateR
     case RRTL_STIM_TRACE:
       return gw < R.words ? R.in_trace[((size_t)c * R.n_trace_cols + s.param) * R.words + gw] : 0u;
     default: return cur;
+  }
+}
+
+// Trace check of recorded net k on 32-lane word gw at cycle c: every lane
+// whose bit differs from the expected word is logged (limb 0).
+__device__ __forceinline__ void check_word(const GateRunDev& R, uint64_t c, uint32_t k, uint32_t gw, uint32_t v) {
+  const uint32_t idx = R.chk_idx[(size_t)c * R.n_rec + k];
+  if (idx == 0xFFFFFFFFu) return;
+  const uint32_t exp = R.chk_exp[((size_t)c * R.n_rec + k) * R.words + gw];
+  uint32_t mm = (v ^ exp) & valid_mask(gw, R.lanes);
+  while (mm) {
+    const uint32_t b = __ffs(mm) - 1u;
+    log_mismatch(R.chk_log, R.chk_cap, c, idx, gw * 32u + b, 0u, (exp >> b) & 1u, (v >> b) & 1u);
+    mm &= mm - 1u;
   }
 }
 
@@ -474,6 +489,7 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
           if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
           if (R.mode & RRTL_REC_HASH) hs += hash_term(c, k, gw, v);
           if (R.mode & RRTL_REC_DETECT) atomicOr(&dstate[ww], v ^ (0u - (v & 1u)));
+          if (R.mode & RRTL_REC_CHECK) check_word(R, c, k, gw, v);
         }
       }
       if (R.mode & RRTL_REC_HASH) {
@@ -628,6 +644,7 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
         if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
         if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
         if (R.mode & RRTL_REC_DETECT) atomicOr(&diff[ww], v ^ (0u - (v & 1u)));
+        if (R.mode & RRTL_REC_CHECK) check_word(R, c, k, gw, v);
       }
     }
     if (R.mode & RRTL_REC_HASH) {

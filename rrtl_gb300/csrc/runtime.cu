@@ -382,7 +382,8 @@ void invalidate_forces(rrtl_batch* b) {
 // tables; stages host input traces and zeroes hash/detect outputs on the
 // context stream. `want_fused` asks for the fused path (it falls back to the
 // plain path when a recorded net does not stay on chip to the end of a cycle).
-GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused) {
+GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused,
+                          const CheckTables* chk) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
   GatePrepared g;
@@ -440,6 +441,13 @@ GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   R.nets = b->d_nets.as<uint32_t>();
   R.err = b->d_err.as<uint32_t>();
   R.cycle_base = 0;
+  REQUIRE(!(run.record_mode & RRTL_REC_CHECK) || chk, RRTL_E_ARG, "E_GPU_RECORD: checks are for trace replay");
+  if (chk) {
+    R.chk_idx = chk->idx;
+    R.chk_exp = chk->exp;
+    R.chk_log = chk->log;
+    R.chk_cap = chk->cap;
+  }
 
   size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->words * 4;
   g.trace_out_bytes = (size_t)run.cycles * run.n_record * b->words * 4;
@@ -518,10 +526,10 @@ void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st
   cuda_check(e, "cudaGraphLaunch");
 }
 
-void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
+void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckTables* chk = nullptr) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
-  GatePrepared g = gate_prepare(b, run, device_ptrs, b->path == RRTL_PATH_FUSED);
+  GatePrepared g = gate_prepare(b, run, device_ptrs, b->path == RRTL_PATH_FUSED, chk);
   Timer tm(b);
   if (g.fused) {
     uint32_t grid = std::min<uint32_t>(g.R.n_tiles, d->ctx->sm_count * g.v->fused_ctas);
@@ -542,7 +550,8 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs) {
 // Validate a word-engine run and upload its stimulus and record tables;
 // stages host input traces and zeroes hash/detect outputs on the context
 // stream. `start_settle`: settle before the first cycle.
-WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle) {
+WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle,
+                          const CheckTables* chk) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
   WordPrepared g;
@@ -585,6 +594,13 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   R.start_settle = start_settle;
   R.err = b->d_err.as<uint32_t>();
   R.vspill = nullptr;
+  REQUIRE(!(run.record_mode & RRTL_REC_CHECK) || chk, RRTL_E_ARG, "E_GPU_RECORD: checks are for trace replay");
+  if (chk) {
+    R.chk_idx = chk->idx;
+    R.chk_exp = chk->exp;
+    R.chk_log = chk->log;
+    R.chk_cap = chk->cap;
+  }
   g.smem_slots = word_smem_slots(d);
   REQUIRE(g.smem_slots, RRTL_E_UNSUPPORTED,
           "E_WORD_SCOPE: design needs " + std::to_string(d->wdev.n_vslots) + " live value slots, more than shared memory holds");
@@ -639,6 +655,8 @@ WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool 
   R1.in_trace = g.R.in_trace ? g.R.in_trace + (size_t)c0 * g.R.n_trace_cols * g.R.lanes : nullptr;
   R1.out_trace = g.R.out_trace ? g.R.out_trace + (size_t)c0 * g.rec_limbs * g.R.lanes : nullptr;
   R1.out_hash = g.R.out_hash ? g.R.out_hash + c0 : nullptr;
+  R1.chk_idx = g.R.chk_idx ? g.R.chk_idx + (size_t)c0 * g.rec_limbs : nullptr;
+  R1.chk_exp = g.R.chk_exp ? g.R.chk_exp + (size_t)c0 * g.rec_limbs * g.R.lanes : nullptr;
   R1.cycle_base = c0;
   return R1;
 }
@@ -656,10 +674,11 @@ void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {
   if (g.want_det) cuda_check(cudaMemcpyAsync(run.detect, g.R.detect, g.det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
 }
 
-void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle) {
+void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle,
+              const CheckTables* chk = nullptr) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
-  WordPrepared g = word_prepare(b, run, device_ptrs, start_settle);
+  WordPrepared g = word_prepare(b, run, device_ptrs, start_settle, chk);
   g.R.final_settle = final_settle;
   Timer tm(b);
   if (b->path != RRTL_PATH_FUSED && run.cycles > 1) {
@@ -824,6 +843,136 @@ void queue_launch(rrtl_ctx* c) {
     cuda_check(launch_gate_queue(QD, grid, smem, st), "gate_queue_kernel");
   }
   cuda_check(cudaEventRecord(Q.ev1, st), "event");
+}
+
+// Trace replay (GpuBatchSimulator::replay_lane_trace, crates/rrtl-gpu-sim/src/lib.rs:989-1357):
+// per step the step's input ops are stored, the design settles, the step's
+// checks compare signal limbs per lane with expected values and log
+// mismatches, and the clock ticks. Sparse input ops become dense trace
+// columns (a signal keeps its last value between ops, starting from the
+// batch's current state); checks ride on the record stage.
+uint64_t batch_replay(rrtl_batch* b, const rrtl_trace& t, uint32_t cap, uint32_t* log) {
+  rrtl_design* d = b->d;
+  const bool gate = d->engine == RRTL_ENGINE_GATE;
+  const uint32_t unit = gate ? b->words : b->lanes;  // 32-bit values per column per step
+  REQUIRE(t.steps < (1ull << 32), RRTL_E_ARG, "E_GPU_TRACE_STEPS: trace replay step count exceeds 2^32");
+  REQUIRE(t.n_inputs == 0 || t.inputs, RRTL_E_ARG, "E_ARG: inputs is null");
+  REQUIRE(t.n_checks == 0 || t.checks, RRTL_E_ARG, "E_ARG: checks is null");
+  const uint64_t steps = t.steps;
+  auto limbs_of = [&](uint32_t sig) { return signal_of(d, sig).layout.limbs; };
+  // input columns: every limb of every driven signal
+  std::map<uint32_t, uint32_t> in_col;
+  uint32_t ncols = 0;
+  for (uint32_t i = 0; i < t.n_inputs; ++i) {
+    const rrtl_trace_input& op = t.inputs[i];
+    const PackedSignal& ps = signal_of(d, op.signal);
+    REQUIRE(op.limb < ps.layout.limbs, RRTL_E_ARG, "E_GPU_TRACE_INPUTS: limb out of range");
+    REQUIRE(op.step < steps, RRTL_E_ARG, "E_GPU_TRACE_INPUTS: step out of range");
+    REQUIRE(op.values, RRTL_E_ARG, "E_ARG: input values are null");
+    REQUIRE(!gate || ps.layout.width == 1, RRTL_E_ARG, "E_GPU_WIDE_SIGNAL: the gate engine replays 1-bit signals");
+    if (!in_col.count(op.signal)) {
+      in_col[op.signal] = ncols;
+      ncols += ps.layout.limbs;
+    }
+  }
+  std::vector<uint32_t> cur((size_t)ncols * unit, 0), trace((size_t)steps * ncols * unit, 0);
+  for (auto& kv : in_col) {
+    uint32_t* dst = cur.data() + (size_t)kv.second * unit;
+    if (gate) {
+      const uint32_t net = d->gp().signal_net[kv.first];
+      cuda_check(cudaStreamSynchronize(d->ctx->stream), "sync");
+      cuda_check(cudaMemcpy(dst, b->d_nets.as<uint32_t>() + (size_t)net * b->words_pad, (size_t)b->words * 4,
+                            cudaMemcpyDeviceToHost),
+                 "d2h signal");
+    } else {
+      std::vector<uint32_t> v((size_t)limbs_of(kv.first) * b->lanes);
+      rrtl_status st = rrtl_batch_get_signal_limbs(b, kv.first, v.data(), v.size());
+      if (st) fail(st, g_last_error);
+      std::copy(v.begin(), v.end(), dst);
+    }
+  }
+  std::vector<uint32_t> order(t.n_inputs);
+  for (uint32_t i = 0; i < t.n_inputs; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return t.inputs[x].step < t.inputs[y].step; });
+  size_t k = 0;
+  for (uint64_t s = 0; s < steps; ++s) {
+    for (; k < order.size() && t.inputs[order[k]].step == s; ++k) {
+      const rrtl_trace_input& op = t.inputs[order[k]];
+      uint32_t* dst = cur.data() + (size_t)(in_col[op.signal] + op.limb) * unit;
+      if (gate) {
+        std::fill(dst, dst + unit, 0u);
+        for (uint32_t l = 0; l < b->lanes; ++l)
+          if (op.values[l] & 1u) dst[l / 32] |= 1u << (l % 32);
+      } else {
+        std::copy(op.values, op.values + b->lanes, dst);
+      }
+    }
+    std::copy(cur.begin(), cur.end(), trace.begin() + (size_t)s * ncols * unit);
+  }
+  std::vector<rrtl_stim> stim;
+  for (auto& kv : in_col) stim.push_back(rrtl_stim{kv.first, RRTL_STIM_TRACE, kv.second});
+  // checks: recorded signals, one row per limb
+  std::map<uint32_t, uint32_t> rec_row;
+  std::vector<uint32_t> rec;
+  uint32_t rows = 0;
+  for (uint32_t i = 0; i < t.n_checks; ++i) {
+    const rrtl_trace_check& op = t.checks[i];
+    const PackedSignal& ps = signal_of(d, op.signal);
+    REQUIRE(op.limb < ps.layout.limbs, RRTL_E_ARG, "E_GPU_TRACE_CHECKS: limb out of range");
+    REQUIRE(op.step < steps, RRTL_E_ARG, "E_GPU_TRACE_CHECKS: step out of range");
+    REQUIRE(op.expected, RRTL_E_ARG, "E_ARG: expected values are null");
+    REQUIRE(!gate || ps.layout.width == 1, RRTL_E_ARG, "E_GPU_WIDE_SIGNAL: the gate engine replays 1-bit signals");
+    if (!rec_row.count(op.signal)) {
+      rec_row[op.signal] = rows;
+      rec.push_back(op.signal);
+      rows += gate ? 1 : ps.layout.limbs;
+    }
+  }
+  std::vector<uint32_t> idx((size_t)steps * rows, 0xFFFFFFFFu), exp((size_t)steps * rows * unit, 0);
+  for (uint32_t i = 0; i < t.n_checks; ++i) {
+    const rrtl_trace_check& op = t.checks[i];
+    const size_t row = (size_t)op.step * rows + rec_row[op.signal] + op.limb;
+    idx[row] = op.check_index;
+    uint32_t* dst = exp.data() + row * unit;
+    if (gate) {
+      std::fill(dst, dst + unit, 0u);
+      for (uint32_t l = 0; l < b->lanes; ++l)
+        if (op.expected[l] & 1u) dst[l / 32] |= 1u << (l % 32);
+    } else {
+      const uint32_t width = signal_of(d, op.signal).layout.width;
+      const bool last = op.limb + 1 == limbs_of(op.signal);
+      for (uint32_t l = 0; l < b->lanes; ++l) dst[l] = last ? op.expected[l] & final_limb_mask(width) : op.expected[l];
+    }
+  }
+  upload(b->d_chk_idx, idx);
+  upload(b->d_chk_exp, exp);
+  b->d_chk_log.reserve(std::max<size_t>((1 + (size_t)cap * 6) * 4, 16));
+  cudaStream_t st = d->ctx->stream;
+  cuda_check(cudaMemsetAsync(b->d_chk_log.p, 0, 4, st), "memset log");
+  CheckTables ct;
+  ct.idx = b->d_chk_idx.as<uint32_t>();
+  ct.exp = b->d_chk_exp.as<uint32_t>();
+  ct.log = b->d_chk_log.as<uint32_t>();
+  ct.cap = cap;
+  rrtl_run r{};
+  r.cycles = steps;
+  r.n_stim = (uint32_t)stim.size();
+  r.stim = stim.data();
+  r.n_record = (uint32_t)rec.size();
+  r.record = rec.data();
+  r.record_mode = rec.empty() ? 0u : (uint32_t)RRTL_REC_CHECK;
+  r.n_trace_cols = ncols;
+  r.input_trace = ncols ? trace.data() : nullptr;
+  if (gate) gate_run(b, r, false, &ct);
+  else word_run(b, r, false, false, true, &ct);
+  uint32_t count = 0;
+  cuda_check(cudaMemcpy(&count, b->d_chk_log.p, 4, cudaMemcpyDeviceToHost), "d2h log");
+  const uint32_t kept = std::min(count, cap);
+  if (log) {
+    log[0] = count;
+    if (kept) cuda_check(cudaMemcpy(log + 1, b->d_chk_log.as<uint32_t>() + 1, (size_t)kept * 6 * 4, cudaMemcpyDeviceToHost), "d2h log");
+  }
+  return count;
 }
 
 void batch_eval(rrtl_batch* b) {
@@ -1348,6 +1497,16 @@ rrtl_status rrtl_batch_run_device(rrtl_batch* b, const rrtl_run* run) {
     REQUIRE(run->n_record == 0 || run->record, RRTL_E_ARG, "E_ARG: record is null");
     if (b->d->engine == RRTL_ENGINE_GATE) gate_run(b, *run, true);
     else word_run(b, *run, true, false, true);
+  });
+}
+
+rrtl_status rrtl_batch_replay_trace(rrtl_batch* b, const rrtl_trace* trace, uint32_t max_mismatches, uint32_t* log,
+                                    uint64_t* n_mismatches) {
+  return guard([&] {
+    REQUIRE(b && trace, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(b->d->ctx);
+    const uint64_t n = batch_replay(b, *trace, std::max<uint32_t>(max_mismatches, 1), log);
+    if (n_mismatches) *n_mismatches = n;
   });
 }
 

@@ -111,11 +111,21 @@ struct JobQueue {
   ~JobQueue();
 };
 
+// Device tables of a trace replay's checks (RRTL_REC_CHECK).
+struct CheckTables {
+  const uint32_t* idx = nullptr;
+  const uint32_t* exp = nullptr;
+  uint32_t* log = nullptr;
+  uint32_t cap = 0;
+};
+
 // Runtime internals shared by the C ABI and the serving loop.
-GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused);
+GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool want_fused,
+                          const CheckTables* chk = nullptr);
 void gate_copy_out(rrtl_batch* b, const GatePrepared& g, const rrtl_run& run);
 void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st, bool graph);
-WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle);
+WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle,
+                          const CheckTables* chk = nullptr);
 cudaError_t word_chunk(const rrtl_design* d, const WordPrepared& g, uint64_t c0, uint64_t n, bool last, cudaStream_t st);
 void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run);
 size_t gate_queue_static_smem();
@@ -184,4 +194,5 @@ struct rrtl_batch {
   rrtl::DevBuf d_values, d_mem, d_caps;
   // per-run scratch
   rrtl::DevBuf d_stim, d_rec, d_in_trace, d_out_trace, d_hash, d_detect;
+  rrtl::DevBuf d_chk_idx, d_chk_exp, d_chk_log;  // trace replay
 };

@@ -86,6 +86,11 @@ struct WordRunDev {
   unsigned long long cycle_base;  // absolute index of this launch's first cycle (stimulus, hash, detect);
                                   // buffers are indexed from the launch's first cycle
   uint32_t* err;
+  // trace checks (RRTL_REC_CHECK), per cycle and recorded limb row
+  const uint32_t* chk_idx;    // [cycle][rec limb rows], ~0 = no check
+  const uint32_t* chk_exp;    // [cycle][rec limb rows][lanes]
+  uint32_t* chk_log;          // [1 + 6*cap]
+  uint32_t chk_cap;
 };
 
 // One run of the multi-job word kernel: blocks [block_begin, next job's

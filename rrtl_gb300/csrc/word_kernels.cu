@@ -17,6 +17,7 @@
 
 #include "../../include/rrtl_cuda.h"
 #include "runtime.h"
+#include "check_log.h"
 #include "stim.h"
 #include "word_dev.h"
 
@@ -162,7 +163,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
         else if (s.kind == RRTL_STIM_PULSE) v = (l == 0 && ca < s.param) ? 1u : 0u;
         else if (s.kind == RRTL_STIM_CONST) v = l < 2 ? (uint32_t)(s.param >> (32 * l)) : 0u;
         else if (s.kind == RRTL_STIM_TRACE)
-          v = (l == 0 && live) ? R.in_trace[((size_t)c * R.n_trace_cols + s.param) * R.lanes + lane] : 0u;
+          v = live ? R.in_trace[((size_t)c * R.n_trace_cols + s.param + l) * R.lanes + lane] : 0u;
         if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
         R.values[(size_t)(s.sig_off + l) * R.lanes_pad + lane] = v;
       }
@@ -185,6 +186,14 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
           }
           if (!live) continue;
           if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
+          if (R.mode & RRTL_REC_CHECK) {
+            const size_t row = (size_t)c * R.rec_limbs + rc.base + l;
+            const uint32_t idx = R.chk_idx[row];
+            if (idx != 0xFFFFFFFFu) {
+              const uint32_t exp = R.chk_exp[row * R.lanes + lane];
+              if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
+            }
+          }
           if ((R.mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
         }
       }

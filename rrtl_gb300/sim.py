@@ -21,7 +21,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "librrtl_gb300.so")
 
 STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE = 0, 1, 2, 3, 4
-REC_TRACE, REC_HASH, REC_DETECT = 1, 2, 4
+REC_TRACE, REC_HASH, REC_DETECT, REC_CHECK = 1, 2, 4, 8
 PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH = 0, 1, 2
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 ENGINE_GATE, ENGINE_WORD = 1, 2
@@ -66,6 +66,20 @@ class Run(ctypes.Structure):
         ("out_hash", POINTER(c_uint64)),
         ("detect", POINTER(c_uint32)),
     ]
+
+
+class TraceInput(ctypes.Structure):
+    _fields_ = [("step", c_uint64), ("signal", c_uint32), ("limb", c_uint32), ("values", POINTER(c_uint32))]
+
+
+class TraceCheck(ctypes.Structure):
+    _fields_ = [("step", c_uint64), ("check_index", c_uint32), ("signal", c_uint32), ("limb", c_uint32),
+                ("pad", c_uint32), ("expected", POINTER(c_uint32))]
+
+
+class Trace(ctypes.Structure):
+    _fields_ = [("steps", c_uint64), ("n_inputs", c_uint32), ("inputs", POINTER(TraceInput)),
+                ("n_checks", c_uint32), ("checks", POINTER(TraceCheck))]
 
 
 class Job(ctypes.Structure):
@@ -123,6 +137,7 @@ EXPORTS = (
     "rrtl_batch_run",
     "rrtl_batch_run_device",
     "rrtl_batch_set_faults",
+    "rrtl_batch_replay_trace",
     "rrtl_batch_snapshot",
     "rrtl_batch_restore",
     "rrtl_batch_set_path",
@@ -187,6 +202,7 @@ def lib():
         "rrtl_batch_run": [c_void_p, P(Run)],
         "rrtl_batch_run_device": [c_void_p, P(Run)],
         "rrtl_batch_set_faults": [c_void_p, P(Fault), c_size_t],
+        "rrtl_batch_replay_trace": [c_void_p, P(Trace), c_uint32, P(c_uint32), P(c_uint64)],
         "rrtl_batch_snapshot": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_path": [c_void_p, c_uint32],
@@ -544,6 +560,32 @@ class GpuBatchSimulator:
         r = self.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
         check(lib().rrtl_batch_run(self.h, byref(r)))
         return out
+
+    def replay_trace(self, steps: int, inputs: Sequence[tuple] = (), checks: Sequence[tuple] = (),
+                     max_mismatches: int = 1024):
+        """Trace replay (GpuBatchSimulator::replay_lane_trace). inputs: (step, signal, limb, values[lanes]);
+        checks: (step, check_index, signal, limb, expected[lanes]). Returns (count, mismatches) with
+        mismatches as (step, check_index, lane, limb, expected, actual) tuples (at most max_mismatches)."""
+        keep = []
+        ins = (TraceInput * max(1, len(inputs)))()
+        for i, (st, sig, limb, vals) in enumerate(inputs):
+            a = np.ascontiguousarray(vals, dtype=np.uint32)
+            keep.append(a)
+            ins[i] = TraceInput(st, self._sig(sig), limb, _u32p(a))
+        chs = (TraceCheck * max(1, len(checks)))()
+        for i, (st, ci, sig, limb, exp) in enumerate(checks):
+            a = np.ascontiguousarray(exp, dtype=np.uint32)
+            keep.append(a)
+            chs[i] = TraceCheck(st, ci, self._sig(sig), limb, 0, _u32p(a))
+        t = Trace(steps, len(inputs), ctypes.cast(ins, POINTER(TraceInput)), len(checks),
+                  ctypes.cast(chs, POINTER(TraceCheck)))
+        cap = max(1, max_mismatches)
+        log = np.zeros(1 + 6 * cap, dtype=np.uint32)
+        n = c_uint64()
+        check(lib().rrtl_batch_replay_trace(self.h, byref(t), cap, _u32p(log), byref(n)))
+        kept = min(n.value, cap)
+        rows = log[1:1 + 6 * kept].reshape(kept, 6)
+        return n.value, [tuple(int(x) for x in r) for r in rows]
 
     def set_faults(self, faults: Sequence[tuple]):
         """faults: (lane, signal, value) triples; signal by name or index."""
