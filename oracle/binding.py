@@ -100,6 +100,9 @@ def lib():
         L.orc_bp_run.restype = c_int
         L.orc_bp_run_parallel.argtypes = [c_void_p, c_uint32, POINTER(Run), c_uint32]
         L.orc_bp_run_parallel.restype = c_int
+        L.orc_bp_emit_c.argtypes = [c_void_p, POINTER(Stim), c_uint32, POINTER(c_uint32), c_uint32, ctypes.c_char_p,
+                                    ctypes.c_size_t, POINTER(ctypes.c_size_t)]
+        L.orc_bp_emit_c.restype = c_int
         L.orc_scalar_new.argtypes = [c_void_p]
         L.orc_scalar_new.restype = c_void_p
         L.orc_scalar_free.argtypes = [c_void_p]
@@ -369,3 +372,86 @@ def crc_step(c: int, din: int) -> int:
         bit = ((c >> 31) & 1) ^ ((din >> i) & 1)
         c = ((c << 1) & 0xFFFFFFFF) ^ (0x04C11DB7 if bit else 0)
     return c
+
+
+class BitParallelAot:
+    """The reference's AOT bit-parallel engine restated (BitParallelAot,
+    crates/rrtl-sim-ir/src/bitparallel.rs:348-528): the design emitted as
+    straight-line u64 C (orc_bp_emit_c), compiled with the host C compiler at
+    -O3 and run over disjoint 64-lane group ranges on all host threads
+    (tick_many_parallel, :513-523). Stimulus and output hash follow this
+    library's run protocol, so its per-cycle hash equals the GPU engines'."""
+
+    def __init__(self, design: "OracleDesign", stim, record, cc: str = "gcc", opt: str = "-O3"):
+        import hashlib
+        import subprocess
+
+        st = (Stim * max(1, len(stim)))(*[Stim(a, b, c) for a, b, c in stim])
+        rec = np.asarray(record, dtype=np.uint32)
+        need = ctypes.c_size_t()
+        rp = rec.ctypes.data_as(POINTER(c_uint32))
+        if lib().orc_bp_emit_c(design.h, st, len(stim), rp, len(rec), None, 0, ctypes.byref(need)):
+            raise OracleError(lib().orc_last_error().decode())
+        buf = ctypes.create_string_buffer(need.value)
+        if lib().orc_bp_emit_c(design.h, st, len(stim), rp, len(rec), buf, need.value, ctypes.byref(need)):
+            raise OracleError(lib().orc_last_error().decode())
+        src = buf.value
+        tag = hashlib.sha1(src + opt.encode()).hexdigest()[:16]
+        d = os.path.join(_HERE, "_build", "aot")
+        os.makedirs(d, exist_ok=True)
+        so = os.path.join(d, f"bp_{tag}.so")
+        if not os.path.exists(so):
+            # the source comes as translation units; compile them in parallel, then link
+            parts = src.split(b"\n//@@PART@@\n")
+            objs, procs = [], []
+            for i, part in enumerate(parts):
+                cpath = os.path.join(d, f"bp_{tag}_{i}.c")
+                with open(cpath, "wb") as f:
+                    f.write(part)
+                obj = cpath[:-2] + f".{os.getpid()}.o"
+                objs.append(obj)
+                procs.append(subprocess.Popen([cc, opt, "-fPIC", "-c", "-o", obj, cpath], stdout=subprocess.PIPE,
+                                              stderr=subprocess.PIPE))
+            for p in procs:
+                _, err = p.communicate()
+                if p.returncode:
+                    raise RuntimeError(f"{cc} failed: {err.decode()[-2000:]}")
+            tmp = so + f".{os.getpid()}.tmp"
+            r = subprocess.run([cc, "-shared", "-o", tmp] + objs, capture_output=True, text=True)
+            if r.returncode:
+                raise RuntimeError(f"{cc} link failed: {r.stderr[-2000:]}")
+            os.replace(tmp, so)
+            for o in objs:
+                os.remove(o)
+        self.lib = ctypes.CDLL(so)
+        self.lib.run_bp.argtypes = [POINTER(ctypes.c_uint64), ctypes.c_long, ctypes.c_long, ctypes.c_long,
+                                    ctypes.c_long, ctypes.c_uint64, POINTER(ctypes.c_uint64)]
+        self.lib.run_bp.restype = None
+        self.ns = design.num_signals
+
+    def run(self, lanes: int, cycles: int, seed: int, threads: int = 0):
+        """`cycles` cycles of `lanes` lanes (a multiple of 64) from the zero
+        state; returns the per-cycle hash summed over all lanes."""
+        from concurrent.futures import ThreadPoolExecutor
+
+        assert lanes % 64 == 0
+        groups = lanes // 64
+        threads = threads or (os.cpu_count() or 1)
+        chunks = max(1, min(groups, threads * 4))
+        bounds = [groups * i // chunks for i in range(chunks + 1)]
+        hashes = [np.zeros(cycles, dtype=np.uint64) for _ in range(chunks)]
+
+        def work(i):
+            g0, g1 = bounds[i], bounds[i + 1]
+            if g1 == g0:
+                return
+            st = np.zeros((g1 - g0) * self.ns, dtype=np.uint64)
+            self.lib.run_bp(st.ctypes.data_as(POINTER(ctypes.c_uint64)), g1 - g0, g0, 0, cycles, seed,
+                            hashes[i].ctypes.data_as(POINTER(ctypes.c_uint64)))
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(work, range(chunks)))
+        total = np.zeros(cycles, dtype=np.uint64)
+        for h in hashes:
+            total += h
+        return total

@@ -1002,6 +1002,148 @@ int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t th
 }
 
 // ---- ScalarSim (top-module signal ids, values as two u64 halves)
+// Bit-parallel AOT source (BitParallelAot, crates/rrtl-sim-ir/src/bitparallel.rs:348-528:
+// `aot::emit_block_c` / `generate_c`): the design's comb and tick_next blocks
+// as straight-line u64 C over one 64-lane group, inside a group loop and a
+// cycle loop. Unlike the reference's single function, the straight-line code
+// is cut at level boundaries into functions of about kAotChunk instructions
+// (values never cross levels), which keeps the C compiler's time linear in
+// the design size. To be comparable with the other engines it also runs this
+// library's run protocol per cycle: stimulus from the counter hash
+// (RANDOM / PULSE / CONST), settle, per-cycle output hash, capture/commit.
+// Entry: run_bp(st, groups, g_base, c0, cycles, seed, hash) with st the
+// [group][signal] state of `groups` groups starting at global group g_base.
+// The source comes as translation units separated by "//@@PART@@" lines.
+static const size_t kAotChunk = 1500;
+
+struct AotEmitter {
+  std::vector<std::string> fns;    // level functions
+  std::vector<std::string> calls;  // call statements, in order
+  std::vector<uint32_t> caps;      // tick_next capture destinations (index = nx slot)
+  int nfn = 0;
+
+  void block(const Block& b, const char* p, bool capture) {
+    std::string body;
+    size_t n = 0;
+    auto flush = [&]() {
+      if (body.empty()) return;
+      const std::string name = std::string("blk_") + p + std::to_string(nfn++);
+      fns.push_back("void " + name + "(u64* restrict s, u64* restrict nx) {\n" + body + "  (void)nx;\n}\n");
+      calls.push_back(name + "(s, nx);");
+      body.clear();
+      n = 0;
+    };
+    auto op = [&](uint32_t v) { return std::string(p) + std::to_string(v); };
+    for (auto& pk : b.packets) {
+      for (auto& in : pk.instrs) {
+        std::string rhs;
+        switch (in.kind) {
+          case IK::Signal: rhs = "s[" + std::to_string(in.index) + "]"; break;
+          case IK::Lit: rhs = (!in.lit.empty() && (in.lit[0] & 1)) ? "~0ull" : "0ull"; break;
+          case IK::Not: rhs = "~" + op(in.ops[0]); break;
+          case IK::And: rhs = "(" + op(in.ops[0]) + " & " + op(in.ops[1]) + ")"; break;
+          case IK::Or: rhs = "(" + op(in.ops[0]) + " | " + op(in.ops[1]) + ")"; break;
+          case IK::Xor: rhs = "(" + op(in.ops[0]) + " ^ " + op(in.ops[1]) + ")"; break;
+          case IK::Mux:
+            rhs = "((" + op(in.ops[0]) + " & " + op(in.ops[1]) + ") | (~" + op(in.ops[0]) + " & " + op(in.ops[2]) + "))";
+            break;
+          default: rhs = "0ull"; break;
+        }
+        body += "  u64 " + op(in.dst) + " = " + rhs + ";\n";
+        ++n;
+      }
+      for (auto& e : pk.effects) {
+        if (e.kind == EffK::StoreSignal && !capture) {
+          body += "  s[" + std::to_string(e.dst) + "] = " + op(e.value) + ";\n";
+        } else if (e.kind == EffK::CaptureReg) {
+          std::string v = op(e.value), nv = v;
+          if (e.has_reset) {
+            std::string a = "s[" + std::to_string(e.reset.signal) + "]";
+            if (e.reset.active_low) a = "(~" + a + ")";
+            const char* rv = (!e.reset.value.empty() && (e.reset.value[0] & 1)) ? "~0ull" : "0ull";
+            nv = "((" + a + " & " + rv + ") | (~" + a + " & " + v + "))";
+          }
+          if (capture) {
+            body += "  nx[" + std::to_string(caps.size()) + "] = " + nv + ";\n";
+            caps.push_back(e.dst);
+          } else if (e.has_reset) {
+            body += "  s[" + std::to_string(e.dst) + "] = " + nv + ";\n";  // asynchronous reset in a settle
+          }
+        }
+      }
+      // values are shared by the sub-packets of one level; the level's last
+      // sub-packet carries its effects, so cut only after a packet with effects
+      if (n >= kAotChunk && !pk.effects.empty()) flush();
+    }
+    flush();
+  }
+};
+
+int orc_bp_emit_c(void* dp, const rrtl_stim* stim, uint32_t n_stim, const uint32_t* rec, uint32_t n_rec, char* out,
+                  size_t cap, size_t* need) {
+  auto* d = (OracleDesign*)dp;
+  try {
+    BitParallel probe(d, 64);  // scope check (1-bit gate-level, no memories)
+    const MachineProgram& M = d->machine;
+    const size_t ns = M.source.signals.size();
+    AotEmitter em;
+    em.block(M.async_reset_comb, "a", false);
+    em.block(M.comb, "c", false);
+    const size_t n_settle = em.calls.size();
+    em.block(M.tick_next, "n", true);
+    // several translation units (separated by a marker line) so the level
+    // functions compile in parallel: the first holds run_bp, the others the
+    // level functions
+    const std::string head = "typedef unsigned long long u64;\ntypedef unsigned int u32;\n";
+    std::string c = head;
+    c += "static inline u64 sm(u64 z) { z += 0x9E3779B97F4A7C15ull; z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;\n"
+         "  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull; return z ^ (z >> 31); }\n";
+    c += "static inline u32 sw(u64 seed, u64 stream, u64 cycle, u64 idx) {\n"
+         "  u64 k = sm(seed ^ (stream * 0xD6E8FEB86659FD93ull));\n"
+         "  return (u32)sm(k ^ (cycle * 0xA0761D6478BD642Full) ^ (idx * 0xE7037ED1A0B428DBull)); }\n";
+    c += "static inline u64 ht(u64 cycle, u32 rec, u64 idx, u32 v) {\n"
+         "  u64 salt = sm((cycle << 20) ^ (u64)rec ^ 0x5851F42D4C957F2Dull); return sm((u64)v ^ (idx << 32) ^ salt); }\n";
+    for (const std::string& call : em.calls)
+      c += "void " + call.substr(0, call.find('(')) + "(u64* restrict s, u64* restrict nx);\n";
+    c += "void run_bp(u64* restrict st, long groups, long g_base, long c0, long nc, u64 seed, u64* restrict hash) {\n";
+    c += " u64 nx[" + std::to_string(std::max<size_t>(1, em.caps.size())) + "];\n";
+    c += " for (long c = c0; c < c0 + nc; ++c) {\n  u64 h = 0;\n  for (long gi = 0; gi < groups; ++gi) {\n";
+    c += "   u64* restrict s = st + gi * " + std::to_string(ns) + "L;\n   const u64 w0 = 2 * (u64)(g_base + gi);\n";
+    for (uint32_t k = 0; k < n_stim; ++k) {
+      const rrtl_stim& t = stim[k];
+      std::string v;
+      if (t.kind == RRTL_STIM_RANDOM)
+        v = "((u64)sw(seed, " + std::to_string(t.param) + "ull, c, w0) | ((u64)sw(seed, " + std::to_string(t.param) +
+            "ull, c, w0 + 1) << 32))";
+      else if (t.kind == RRTL_STIM_PULSE) v = "((u64)c < " + std::to_string(t.param) + "ull ? ~0ull : 0ull)";
+      else if (t.kind == RRTL_STIM_CONST) v = (t.param & 1) ? "~0ull" : "0ull";
+      else continue;
+      c += "   s[" + std::to_string(t.signal) + "] = " + v + ";\n";
+    }
+    for (size_t i = 0; i < n_settle; ++i) c += "   " + em.calls[i] + "\n";
+    for (uint32_t q = 0; q < n_rec; ++q) {
+      const std::string sv = "s[" + std::to_string(rec[q]) + "]";
+      c += "   h += ht(c, " + std::to_string(q) + "u, w0, (u32)" + sv + ") + ht(c, " + std::to_string(q) + "u, w0 + 1, (u32)(" +
+           sv + " >> 32));\n";
+    }
+    for (size_t i = n_settle; i < em.calls.size(); ++i) c += "   " + em.calls[i] + "\n";
+    for (size_t i = 0; i < em.caps.size(); ++i)
+      c += "   s[" + std::to_string(em.caps[i]) + "] = nx[" + std::to_string(i) + "];\n";
+    c += "  }\n  hash[c - c0] += h;\n }\n}\n";
+    const size_t parts = std::min<size_t>(em.fns.size(), 32);
+    for (size_t k = 0; k < parts; ++k) {
+      c += "\n//@@PART@@\n" + head;
+      for (size_t i = em.fns.size() * k / parts; i < em.fns.size() * (k + 1) / parts; ++i) c += em.fns[i];
+    }
+    if (need) *need = c.size() + 1;
+    if (out && cap > c.size()) memcpy(out, c.c_str(), c.size() + 1);
+    return 0;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return RRTL_E_DESIGN;
+  }
+}
+
 void* orc_scalar_new(void* dp) {
   auto* d = (OracleDesign*)dp;
   try { return ScalarSim::create(&d->design, d->top); } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
