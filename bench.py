@@ -54,6 +54,28 @@ def dist_setup():
     return 1, 0, 0, None
 
 
+def reduce_max(dist, value: float) -> float:
+    """Max of a host-side timing over all ranks (gloo); identity when single-process."""
+    if not dist:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def throughput(ws: int, lanes_per_rank: int, cycles: int, steps: int, ms: float) -> float:
+    """Whole-job lane-cycles/s: every rank's lanes over the slowest rank's time."""
+    return ws * lanes_per_rank * cycles * steps / (ms / 1000.0)
+
+
+def lane_shard(total_lanes: int, rank: int, ws: int):
+    """Global lane range [first, last) of a rank: contiguous, disjoint shards
+    (the reference's shard plan, crates/rrtl-runtime/src/lib.rs:168-175)."""
+    return total_lanes * rank // ws, total_lanes * (rank + 1) // ws
+
+
 def net_stream_bytes_per_lane_cycle(meta_fanins, n_ff, n_pi, n_po):
     """Net-streaming model: every gate reads its fanins and writes its output,
     each flop's D is read and Q written, inputs written and outputs read, one
@@ -379,6 +401,46 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
     return out
 
 
+def word_configs_leg(ctx, sim):
+    """The word-engine configs: the README Counter (1,024 lanes x 10,000
+    cycles, full output trace recorded) and the 8-stage pipelined CPU
+    (16,384 lanes x 20,000 cycles, per-lane hashed ROMs); each against the
+    plain one-launch-per-cycle path on 200 cycles of the same batch shape,
+    and the CPU's final state compared between the two paths."""
+    from rrtl_gb300.workloads import counter, cpu_rom_hashed, pipelined_cpu
+
+    out = {}
+    cd = sim.CompiledDesign(counter(), "Counter", ctx)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 1)]
+    for path, cyc, key in ((sim.PATH_FUSED, 10_000, "counter"), (sim.PATH_PLAIN, 200, None)):
+        g = sim.GpuBatchSimulator(cd, lanes=1024)
+        g.set_path(path)
+        g.run(cyc, seed=1, stim=stim, record=["out"], mode=sim.REC_TRACE)
+        v = 1024 * cyc / (g.last_kernel_ms / 1e3)
+        if key:
+            out[key] = {"lanes": 1024, "cycles": cyc, "value": v, "unit": "lane-cycles/s", "kernel_ms": g.last_kernel_ms,
+                        "trace_bytes": 1024 * cyc * 4}
+        else:
+            out["counter"]["plain"] = v
+    cd = sim.CompiledDesign(pipelined_cpu(), "Cpu8", ctx)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
+    rom = cpu_rom_hashed(16384, seed=3)
+    res = {}
+    for path, cyc in ((sim.PATH_FUSED, 20_000), (sim.PATH_PLAIN, 200)):
+        g = sim.GpuBatchSimulator(cd, lanes=16384)
+        g.set_path(path)
+        g.set_memory_limbs("rom", rom)
+        r = g.run(cyc, stim=stim, record=["out_pc", "out_acc"], mode=sim.REC_HASH)
+        res[path] = (1.0e3 * 16384 * cyc / g.last_kernel_ms, r["hash"], g)
+    # same first 200 cycles on both paths
+    same = bool(np.array_equal(res[sim.PATH_FUSED][1][:200], res[sim.PATH_PLAIN][1]))
+    out["cpu8"] = {"lanes": 16384, "cycles": 20_000, "value": res[sim.PATH_FUSED][0], "unit": "lane-cycles/s",
+                   "plain": res[sim.PATH_PLAIN][0], "hash_prefix_equal_plain": same,
+                   "note": "one thread per lane: 16,384 threads fill under a tenth of the GPU's thread slots, so "
+                           "the run is latency-bound"}
+    return out
+
+
 def run_reference(args, ws, rank):
     """The reference's CPU implementation of the path on the host cores: the
     AOT bit-parallel engine restated (see cpu_baseline), each step a bounded
@@ -434,6 +496,7 @@ def main():
     ap.add_argument("--job-designs", type=int, default=8, help="distinct netlists in the job stream")
     ap.add_argument("--no-plain-jobs", action="store_true", help="job stream: skip the plain-path comparison")
     ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
+    ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
@@ -460,7 +523,7 @@ def main():
 
     def device_run(i, path=sim.PATH_FUSED, cycles=CYCLES):
         g.set_path(path)
-        r = g.make_run(cycles, seed=SEED + i, stim=stim, record=rec, mode=sim.REC_HASH)
+        r = g.make_run(cycles, seed=SEED + i + 1000 * rank, stim=stim, record=rec, mode=sim.REC_HASH)
         r.out_hash = ctypes_u64(hash_dev[i].data_ptr())
         sim.check(sim.lib().rrtl_batch_run_device(g.h, sim.byref(r)))
 
@@ -477,12 +540,9 @@ def main():
             device_run(args.warmup + i)
         ctx.record(1)
         ms = ctx.elapsed_ms(0, 1)
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(dist, ms)
     lane_cycles = ws * LANES * CYCLES * args.steps
-    value = lane_cycles / (ms / 1000.0)
+    value = throughput(ws, LANES, CYCLES, args.steps, ms)
     ms_step = ms / args.steps
 
     # e2e: same steps through the C ABI with pinned host buffers
@@ -499,18 +559,15 @@ def main():
     ctx.record(2)
     for i in range(args.steps):
         g.set_path(sim.PATH_FUSED)
-        r = g.make_run(CYCLES, seed=SEED + i, stim=stim, record=rec, mode=sim.REC_HASH)
+        r = g.make_run(CYCLES, seed=SEED + i + 1000 * rank, stim=stim, record=rec, mode=sim.REC_HASH)
         r.out_hash = ctypes_u64(hash_host.data_ptr())
         sim.check(sim.lib().rrtl_batch_run(g.h, sim.byref(r)))
         sim.check(sim.lib().rrtl_batch_get_signals_bits(g.h, reg_idx.ctypes.data_as(sim.POINTER(sim.c_uint32)),
                                                         len(reg_idx), ctypes_u32(regs_host.data_ptr()), FFS * words))
     ctx.record(3)
     e2e_ms = ctx.elapsed_ms(2, 3)
-    if dist:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = lane_cycles / (e2e_ms / 1000.0)
+    e2e_ms = reduce_max(dist, e2e_ms)
+    e2e_value = throughput(ws, LANES, CYCLES, args.steps, e2e_ms)
 
     # plain one-launch-per-cycle path on the same workload (fewer cycles; same per-cycle work)
     plain = None
@@ -548,7 +605,8 @@ def main():
         "vs_baseline": None, "dtype": "u32 bit-sliced (32 lanes per word)", "data": "synthetic (seeded netlist and stimulus)",
         "config": {"workload": f"gate netlist {GATES} gates / {FFS} FF / {PIS} PI / {POS} PO / depth {DEPTH} / "
                                f"window {WINDOW}", "lanes_per_gpu": LANES, "cycles_per_step": CYCLES,
-                   "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective)",
+                   "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective; rank r simulates lanes "
+                                                     f"{lane_shard(LANES * ws, rank, ws)} of the job, seed offset by r)",
                    "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": "fused persistent kernel",
                    "tile_words": tile_words},
         "gate_evals_per_s": value * info.n_gates,
@@ -560,6 +618,8 @@ def main():
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
     }
+    if not args.no_word_configs:
+        out["word_configs"] = word_configs_leg(ctx, sim)
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:

@@ -263,6 +263,14 @@ rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
  * rrtl_batch_tile_words reports the width of the last fused run (0 after a
  * run on the plain path). */
 rrtl_status rrtl_batch_set_tile_words(rrtl_batch* b, uint32_t words);
+
+/* Autotuner (the reference's GPU autotune, crates/rrtl-gpu-sim/src/lib.rs:103-172,
+ * 2712-2721, re-aimed at this engine's knob): times `cycles` cycles of a
+ * scratch batch of `lanes` lanes at every tile width that fits and makes the
+ * fastest the choice for batches of that size (same power-of-two bucket of
+ * 32-lane words). Gate engine; the word engine has no width and reports 0. */
+rrtl_status rrtl_design_autotune(rrtl_design* design, uint32_t lanes, uint32_t cycles, uint32_t* best_words,
+                                 float* best_ms);
 rrtl_status rrtl_batch_tile_words(rrtl_batch* b, uint32_t* words);
 
 /* Device time of the last run/tick_many in milliseconds (CUDA events on the

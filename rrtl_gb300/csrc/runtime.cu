@@ -258,7 +258,15 @@ void build_gate_variants(rrtl_design* d) {
 // barrier worth about kBarrierSteps group steps. A step costs more at small
 // W because G cells rarely find their inputs in G distinct shared-memory
 // banks (kStepCost, by log2 W). Tiles are spread over the SMs in whole rounds.
+uint32_t lane_bucket(uint32_t words) {
+  uint32_t b = 0;
+  while ((1u << b) < words) ++b;
+  return b;
+}
+
 uint32_t choose_tile_words(rrtl_design* d, uint32_t words) {
+  auto tuned = d->tuned_w.find(lane_bucket(words));
+  if (tuned != d->tuned_w.end()) return tuned->second;
   constexpr double kBarrierSteps = 4.0;
   constexpr double kStepCost[4] = {1.45, 1.25, 1.1, 1.0};
   const GateProgram& gp = d->gp();
@@ -1658,6 +1666,61 @@ rrtl_status rrtl_queue_last_ms(rrtl_ctx* ctx, float* ms) {
   return guard([&] {
     REQUIRE(ctx && ms, RRTL_E_ARG, "E_ARG: null argument");
     *ms = queue_of(ctx).last_ms;
+  });
+}
+
+// Measured tile-width choice: time `cycles` cycles of a scratch batch of
+// `lanes` lanes (every input random) at each width whose slots fit on chip,
+// keep the fastest for batches of this size (lane bucket = ceil(log2 words)).
+rrtl_status rrtl_design_autotune(rrtl_design* d, uint32_t lanes, uint32_t cycles, uint32_t* best_words, float* best_ms) {
+  return guard([&] {
+    REQUIRE(d, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(lanes > 0, RRTL_E_LANES, "E_GPU_AUTOTUNE_LANES: autotuning needs at least one lane");
+    REQUIRE(cycles > 0, RRTL_E_ARG, "E_GPU_AUTOTUNE_STEPS: autotuning needs at least one cycle");
+    set_device(d->ctx);
+    if (d->engine != RRTL_ENGINE_GATE || !d->gate_w_max) {
+      if (best_words) *best_words = 0;
+      if (best_ms) *best_ms = 0.f;
+      return;
+    }
+    const GateProgram& gp = d->gp();
+    std::vector<rrtl_stim> stim;
+    for (uint32_t sig = 0; sig < gp.n_signals; ++sig)
+      if (d->mp.source.signals[sig].kind == PSK::Input) stim.push_back(rrtl_stim{sig, RRTL_STIM_RANDOM, sig});
+    rrtl_run run{};
+    run.cycles = cycles;
+    run.seed = 1;
+    run.n_stim = (uint32_t)stim.size();
+    run.stim = stim.data();
+    const uint32_t words = (lanes + 31) / 32;
+    uint32_t best = d->gate_w_max;
+    float best_t = INFINITY;
+    d->tuned_w.erase(lane_bucket(words));
+    for (uint32_t W = d->gate_w_max; W >= 1; W /= 2) {
+      if (!gate_variant(d, W)->fused_ok) continue;
+      rrtl_batch* b = nullptr;
+      rrtl_status st = rrtl_batch_create(d, lanes, &b);
+      if (st) fail(st, g_last_error);
+      b->tile_words = W;
+      float t = INFINITY;
+      try {
+        for (int rep = 0; rep < 3; ++rep) {
+          gate_run(b, run, false);
+          if (rep) t = std::min(t, b->last_ms);
+        }
+      } catch (...) {
+        rrtl_batch_destroy(b);
+        throw;
+      }
+      rrtl_batch_destroy(b);
+      if (t < best_t) {
+        best_t = t;
+        best = W;
+      }
+    }
+    d->tuned_w[lane_bucket(words)] = best;
+    if (best_words) *best_words = best;
+    if (best_ms) *best_ms = best_t;
   });
 }
 

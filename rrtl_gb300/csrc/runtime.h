@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <memory>
 #include <string>
 #include <unordered_map>
@@ -167,6 +168,7 @@ struct rrtl_design {
   std::unique_ptr<rrtl::GateVariant> gvar[4];
   uint32_t gate_base = 3;   // log2 W of the variant built at load time
   uint32_t gate_w_max = 0;  // widest W whose slots fit on chip, 0 if none
+  std::map<uint32_t, uint32_t> tuned_w;  // measured best W by lane bucket (ceil log2 of 32-lane words)
   const rrtl::GateProgram& gp() const { return gvar[gate_base]->gp; }
   // word engine
   rrtl::WordProgram wp;

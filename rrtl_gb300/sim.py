@@ -142,6 +142,7 @@ EXPORTS = (
     "rrtl_batch_restore",
     "rrtl_batch_set_path",
     "rrtl_batch_set_tile_words",
+    "rrtl_design_autotune",
     "rrtl_queue_submit",
     "rrtl_queue_launch",
     "rrtl_queue_wait",
@@ -207,6 +208,7 @@ def lib():
         "rrtl_batch_restore": [c_void_p, P(c_uint32), c_size_t, P(c_uint32), c_size_t],
         "rrtl_batch_set_path": [c_void_p, c_uint32],
         "rrtl_batch_set_tile_words": [c_void_p, c_uint32],
+        "rrtl_design_autotune": [c_void_p, c_uint32, c_uint32, P(c_uint32), P(c_float)],
         "rrtl_queue_submit": [c_void_p, P(Job), P(c_uint64)],
         "rrtl_queue_launch": [c_void_p],
         "rrtl_queue_wait": [c_void_p],
@@ -355,6 +357,12 @@ class CompiledDesign:
         check(lib().rrtl_design_signal(self.h, name.encode(), byref(idx), byref(w), byref(k)))
         self._cache[name] = (idx.value, w.value, k.value)
         return self._cache[name]
+
+    def autotune(self, lanes: int, cycles: int = 32):
+        """Time every fitting tile width on `lanes` lanes; returns (best words, ms of `cycles` cycles)."""
+        w, ms = c_uint32(), c_float()
+        check(lib().rrtl_design_autotune(self.h, lanes, cycles, byref(w), byref(ms)))
+        return w.value, ms.value
 
     def memory(self, name: str):
         idx, depth, w = c_uint32(), c_uint64(), c_uint32()

@@ -1,0 +1,45 @@
+"""Multi-GPU path of the benchmark on CPU: world_size-2 gloo ranks each own a
+lane shard (no data-path collective); the step time is the max over ranks and
+the throughput counts every rank's lanes (bench.py --gpus N semantics)."""
+import os
+
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+import bench
+
+
+def _rank(rank, ws, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        lanes_per_rank, cycles, steps = 4096, 100, 5
+        my_ms = 10.0 + 5.0 * rank  # rank 1 is the slow one
+        ms = bench.reduce_max(dist, my_ms)
+        value = bench.throughput(ws, lanes_per_rank, cycles, steps, ms)
+        first, last = bench.lane_shard(ws * lanes_per_rank, rank, ws)
+        gathered = [None] * ws
+        dist.all_gather_object(gathered, (first, last, ms, value))
+        if rank == 0:
+            out.put(gathered)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_lane_shards_and_max_time():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + os.getpid() % 2000
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (f0, l0, ms0, v0), (f1, l1, ms1, v1) = got
+    assert (f0, l0, f1, l1) == (0, 4096, 4096, 8192)  # disjoint, covering, contiguous
+    assert ms0 == ms1 == 15.0  # max over ranks
+    assert v0 == v1 == pytest.approx(2 * 4096 * 100 * 5 / 0.015)

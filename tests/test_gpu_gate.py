@@ -205,6 +205,18 @@ def test_auto_tile_width_is_a_valid_width(small_netlist):
         g.set_tile_words(3)
 
 
+def test_autotune_picks_a_measured_width(small_netlist):
+    d, meta, cd, od = small_netlist
+    stim, rec = netlist_run_spec(meta)
+    best, ms = cd.autotune(4096, cycles=8)
+    assert best in (1, 2, 4, 8) and ms > 0
+    g = sim.GpuBatchSimulator(cd, lanes=4000)  # same lane bucket
+    res = g.run(9, seed=3, stim=stim, record=rec, mode=sim.REC_HASH)
+    assert g.tile_words == best
+    ref = oracle_bp_run(od, 4000, 9, 3, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec], 2)
+    assert np.array_equal(res["hash"], ref["hash"])
+
+
 def test_large_netlist_runs_fused_at_narrow_tiles(engine):
     """100k gates and 4,096 flops: the slots need more shared memory than one
     CTA has at 8 words per tile, so the fused path runs narrower tiles; it
