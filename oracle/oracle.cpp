@@ -17,6 +17,7 @@
 // and the stuck-at fault-sim coverage 64/64 with latency 1/6/2.1
 // (crates/rrtl-sim-ir/examples/fault_sim.rs; docs/rrtl-optimizations.md:1411-1416).
 #include <algorithm>
+#include <functional>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1006,56 +1007,75 @@ int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t th
 // `aot::emit_block_c` / `generate_c`): the design's comb and tick_next blocks
 // as straight-line u64 C over one 64-lane group, inside a group loop and a
 // cycle loop. Unlike the reference's single function, the straight-line code
-// is cut at level boundaries into functions of about kAotChunk instructions
-// (values never cross levels), which keeps the C compiler's time linear in
-// the design size. To be comparable with the other engines it also runs this
+// is cut into functions of about kAotChunk instructions (see AotEmitter),
+// which keeps the C compiler's time linear in the design size. To be comparable with the other engines it also runs this
 // library's run protocol per cycle: stimulus from the counter hash
 // (RANDOM / PULSE / CONST), settle, per-cycle output hash, capture/commit.
 // Entry: run_bp(st, groups, g_base, c0, cycles, seed, hash) with st the
 // [group][signal] state of `groups` groups starting at global group g_base.
 // The source comes as translation units separated by "//@@PART@@" lines.
-static const size_t kAotChunk = 1500;
+static const size_t kAotChunk = 400;
 
 struct AotEmitter {
-  std::vector<std::string> fns;    // level functions
+  std::vector<std::string> fns;    // emitted functions
   std::vector<std::string> calls;  // call statements, in order
   std::vector<uint32_t> caps;      // tick_next capture destinations (index = nx slot)
   int nfn = 0;
 
+  // Emit a block level by level (a level = sub-packets up to the one that
+  // carries the effects; values never cross levels). Inside a level every
+  // effect's expression tree is emitted depth first right before the effect,
+  // sharing the values already emitted in the current function; functions
+  // are cut at effect boundaries after about kAotChunk instructions, and a
+  // value from an earlier function of the level is recomputed (a signal
+  // reloaded) rather than passed on. The C compiler's time stays linear in
+  // the design size.
   void block(const Block& b, const char* p, bool capture) {
     std::string body;
     size_t n = 0;
+    std::unordered_map<uint32_t, const Instr*> def;  // value id -> instruction (current level)
+    std::unordered_map<uint32_t, int> emitted;       // value id -> function index it was emitted in
     auto flush = [&]() {
       if (body.empty()) return;
-      const std::string name = std::string("blk_") + p + std::to_string(nfn++);
+      const std::string name = std::string("blk_") + p + std::to_string(nfn);
       fns.push_back("void " + name + "(u64* restrict s, u64* restrict nx) {\n" + body + "  (void)nx;\n}\n");
       calls.push_back(name + "(s, nx);");
       body.clear();
       n = 0;
+      ++nfn;
     };
     auto op = [&](uint32_t v) { return std::string(p) + std::to_string(v); };
-    for (auto& pk : b.packets) {
-      for (auto& in : pk.instrs) {
-        std::string rhs;
-        switch (in.kind) {
-          case IK::Signal: rhs = "s[" + std::to_string(in.index) + "]"; break;
-          case IK::Lit: rhs = (!in.lit.empty() && (in.lit[0] & 1)) ? "~0ull" : "0ull"; break;
-          case IK::Not: rhs = "~" + op(in.ops[0]); break;
-          case IK::And: rhs = "(" + op(in.ops[0]) + " & " + op(in.ops[1]) + ")"; break;
-          case IK::Or: rhs = "(" + op(in.ops[0]) + " | " + op(in.ops[1]) + ")"; break;
-          case IK::Xor: rhs = "(" + op(in.ops[0]) + " ^ " + op(in.ops[1]) + ")"; break;
-          case IK::Mux:
-            rhs = "((" + op(in.ops[0]) + " & " + op(in.ops[1]) + ") | (~" + op(in.ops[0]) + " & " + op(in.ops[2]) + "))";
-            break;
-          default: rhs = "0ull"; break;
-        }
-        body += "  u64 " + op(in.dst) + " = " + rhs + ";\n";
-        ++n;
+    std::function<void(uint32_t)> emit = [&](uint32_t v) {
+      auto e = emitted.find(v);
+      if (e != emitted.end() && e->second == nfn) return;
+      const Instr& in = *def.at(v);
+      for (uint32_t o : in.ops) emit(o);
+      std::string rhs;
+      switch (in.kind) {
+        case IK::Signal: rhs = "s[" + std::to_string(in.index) + "]"; break;
+        case IK::Lit: rhs = (!in.lit.empty() && (in.lit[0] & 1)) ? "~0ull" : "0ull"; break;
+        case IK::Not: rhs = "~" + op(in.ops[0]); break;
+        case IK::And: rhs = "(" + op(in.ops[0]) + " & " + op(in.ops[1]) + ")"; break;
+        case IK::Or: rhs = "(" + op(in.ops[0]) + " | " + op(in.ops[1]) + ")"; break;
+        case IK::Xor: rhs = "(" + op(in.ops[0]) + " ^ " + op(in.ops[1]) + ")"; break;
+        case IK::Mux:
+          rhs = "((" + op(in.ops[0]) + " & " + op(in.ops[1]) + ") | (~" + op(in.ops[0]) + " & " + op(in.ops[2]) + "))";
+          break;
+        default: rhs = "0ull"; break;
       }
+      body += "  u64 " + op(v) + " = " + rhs + ";\n";
+      emitted[v] = nfn;
+      ++n;
+    };
+    for (auto& pk : b.packets) {
+      for (auto& in : pk.instrs) def[in.dst] = &in;
+      if (pk.effects.empty()) continue;
       for (auto& e : pk.effects) {
         if (e.kind == EffK::StoreSignal && !capture) {
+          emit(e.value);
           body += "  s[" + std::to_string(e.dst) + "] = " + op(e.value) + ";\n";
-        } else if (e.kind == EffK::CaptureReg) {
+        } else if (e.kind == EffK::CaptureReg && (capture || e.has_reset)) {
+          emit(e.value);
           std::string v = op(e.value), nv = v;
           if (e.has_reset) {
             std::string a = "s[" + std::to_string(e.reset.signal) + "]";
@@ -1066,14 +1086,17 @@ struct AotEmitter {
           if (capture) {
             body += "  nx[" + std::to_string(caps.size()) + "] = " + nv + ";\n";
             caps.push_back(e.dst);
-          } else if (e.has_reset) {
+          } else {
             body += "  s[" + std::to_string(e.dst) + "] = " + nv + ";\n";  // asynchronous reset in a settle
           }
+        } else {
+          continue;
         }
+        if (n >= kAotChunk) flush();
       }
-      // values are shared by the sub-packets of one level; the level's last
-      // sub-packet carries its effects, so cut only after a packet with effects
-      if (n >= kAotChunk && !pk.effects.empty()) flush();
+      // next level: its values are new
+      def.clear();
+      emitted.clear();
     }
     flush();
   }
