@@ -12,6 +12,17 @@ namespace rrtl {
 #define RRTL_FUSED_WARPS 32
 #endif
 constexpr uint32_t kGateFusedWarps = RRTL_FUSED_WARPS;
+// 32-lane words one thread of the fused kernel owns for a tile of W words
+// (one 32/64/128-bit shared access moves them); a warp step covers V groups.
+#ifndef RRTL_FUSED_V
+#define RRTL_FUSED_V 4
+#endif
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+constexpr uint32_t gate_fused_vec(uint32_t W) {
+  return (uint32_t)RRTL_FUSED_V <= W ? (uint32_t)RRTL_FUSED_V : (W >= 2 ? 2u : 1u);
+}
 constexpr uint32_t kGateFusedCtasPerSm = 32 / kGateFusedWarps;
 
 struct GateStimDev {

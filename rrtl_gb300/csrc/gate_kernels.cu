@@ -34,15 +34,11 @@ constexpr int kRing = 4;                  // record ring buffers
 constexpr uint32_t kSpinLimit = 1u << 22;  // bounded mbarrier wait
 constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slot array
 #ifndef RRTL_FUSED_UNROLL
-#define RRTL_FUSED_UNROLL 1  // warp steps per unrolled iteration of a truth-table run
+#define RRTL_FUSED_UNROLL 1  // warp steps per unrolled iteration (unpaired loop)
 #endif
-#ifndef RRTL_REC_PREFETCH
-#define RRTL_REC_PREFETCH 0  // 1: load the next step's record before this step's operands
+#ifndef RRTL_PAIR_STEPS
+#define RRTL_PAIR_STEPS 1  // two warp steps per loop iteration, loads ahead of stores
 #endif
-#ifndef RRTL_FUSED_V
-#define RRTL_FUSED_V 2  // words per thread in the fused kernel (tiles of 2+ words)
-#endif
-constexpr int kUnroll = RRTL_FUSED_UNROLL;
 static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
 static_assert(kRing == 4, "ring parity arithmetic assumes four buffers");
 
@@ -135,17 +131,19 @@ __host__ __device__ __forceinline__ size_t fused_slot_bytes(uint32_t n_slots, ui
 
 // ------------------------------------------------------------ fused path --
 //
-// A thread owns V consecutive words (V = 2 for W >= 2: one 64-bit shared
-// access moves both). Lanes 16h..16h+15 form half-warp h; a half-warp covers
-// one group (G cells x W words), so a warp step evaluates groups g and g+1
-// of one truth-table run. Cells of a group sit in G distinct bank residues,
-// so each half-warp access is one shared-memory wavefront.
+// A thread owns V consecutive words (gate_fused_vec: one 64- or 128-bit
+// shared access moves them). The warp splits into V sub-warps of 32/V lanes;
+// sub-warp h covers one group (G cells x W words), so a warp step evaluates
+// groups g .. g+V-1 of one truth-table run. Cells of a group sit in G
+// distinct bank residues, so each sub-warp access is one shared-memory
+// wavefront.
 
 template <int W>
 struct FusedShape {
-  static constexpr int V = W >= 2 ? RRTL_FUSED_V : 1;  // words per thread
-  static constexpr int G = 32 / W;                      // cells per group
-  static constexpr int kSteps = V;                      // groups per warp step
+  static constexpr int V = (int)gate_fused_vec(W);  // words per thread
+  static constexpr int G = 32 / W;                  // cells per group
+  static constexpr int kSteps = V;                  // groups per warp step
+  static constexpr int kSub = 32 / V;               // lanes per sub-warp (one group)
 };
 
 template <int V>
@@ -158,6 +156,10 @@ template <>
 struct WordVec<2> {
   using T = uint2;
 };
+template <>
+struct WordVec<4> {
+  using T = uint4;
+};
 
 template <int L>
 __device__ __forceinline__ uint32_t lopv(uint32_t a, uint32_t b, uint32_t c) {
@@ -167,13 +169,16 @@ template <int L>
 __device__ __forceinline__ uint2 lopv(uint2 a, uint2 b, uint2 c) {
   return make_uint2(lop3<L>(a.x, b.x, c.x), lop3<L>(a.y, b.y, c.y));
 }
+template <int L>
+__device__ __forceinline__ uint4 lopv(uint4 a, uint4 b, uint4 c) {
+  return make_uint4(lop3<L>(a.x, b.x, c.x), lop3<L>(a.y, b.y, c.y), lop3<L>(a.z, b.z, c.z), lop3<L>(a.w, b.w, c.w));
+}
 
 // Evaluate this thread's cell in groups g, g+V, ... < e of one truth-table
-// run (g already offset by the half-warp). `rb` is this thread's record in
+// run (g already offset by the sub-warp). `rb` is this thread's record in
 // group 0 of the staged piece and `Sv` its word column of the slot array (row
 // stride W/V vectors); both are shared memory, so every access below is an
-// LDS/STS. The next step's record load is issued before this step's operands
-// are read, so its latency overlaps the step.
+// LDS/STS.
 template <int W, int L>
 __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv,
                                         int g, int e) {
@@ -184,23 +189,31 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
   constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
   constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
   const T zero{};
-#if RRTL_REC_PREFETCH
-  if (g >= e) return;
-  uint2 r = rb[g * Sh::G];
-#pragma unroll kUnroll
-  for (;;) {
-    const int gn = g + Sh::kSteps;
-    const uint2 rn = gn < e ? rb[gn * Sh::G] : r;
+#if RRTL_PAIR_STEPS
+  // two steps per iteration with every load before either store: cells of one
+  // piece never read each other's outputs, so the second step's loads may
+  // overtake the first step's store (the compiler cannot know that)
+  for (; g + Sh::kSteps < e; g += 2 * Sh::kSteps) {
+    const uint2 r0 = rb[g * Sh::G];
+    const uint2 r1 = rb[(g + Sh::kSteps) * Sh::G];
+    const T a0 = kUseA ? Sv[(r0.x & 0xFFFFu) * R] : zero;
+    const T a1 = kUseA ? Sv[(r1.x & 0xFFFFu) * R] : zero;
+    const T b0 = kUseB ? Sv[(r0.x >> 16) * R] : zero;
+    const T b1 = kUseB ? Sv[(r1.x >> 16) * R] : zero;
+    const T c0 = kUseC ? Sv[(r0.y & 0xFFFFu) * R] : zero;
+    const T c1 = kUseC ? Sv[(r1.y & 0xFFFFu) * R] : zero;
+    Sv[(r0.y >> 16) * R] = lopv<L>(a0, b0, c0);
+    Sv[(r1.y >> 16) * R] = lopv<L>(a1, b1, c1);
+  }
+  if (g < e) {
+    const uint2 r = rb[g * Sh::G];
     const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
     const T vb = kUseB ? Sv[(r.x >> 16) * R] : zero;
     const T vc = kUseC ? Sv[(r.y & 0xFFFFu) * R] : zero;
     Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
-    if (gn >= e) break;
-    g = gn;
-    r = rn;
   }
 #else
-#pragma unroll kUnroll
+#pragma unroll RRTL_FUSED_UNROLL
   for (; g < e; g += Sh::kSteps) {
     const uint2 r = rb[g * Sh::G];
     const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
@@ -245,10 +258,20 @@ __device__ __forceinline__ uint32_t lut_v(uint32_t t, uint32_t a, uint32_t b, ui
 __device__ __forceinline__ uint2 lut_v(uint32_t t, uint2 a, uint2 b, uint2 c) {
   return make_uint2(lut_eval(t, a.x, b.x, c.x), lut_eval(t, a.y, b.y, c.y));
 }
+__device__ __forceinline__ uint4 lut_v(uint32_t t, uint4 a, uint4 b, uint4 c) {
+  return make_uint4(lut_eval(t, a.x, b.x, c.x), lut_eval(t, a.y, b.y, c.y), lut_eval(t, a.z, b.z, c.z),
+                    lut_eval(t, a.w, b.w, c.w));
+}
 __device__ __forceinline__ void store_net(uint32_t* p, uint32_t v) { p[0] = v; }
 __device__ __forceinline__ void store_net(uint32_t* p, uint2 v) {
   p[0] = v.x;
   p[1] = v.y;
+}
+__device__ __forceinline__ void store_net(uint32_t* p, uint4 v) {
+  p[0] = v.x;
+  p[1] = v.y;
+  p[2] = v.z;
+  p[3] = v.w;
 }
 
 // Final settle: same evaluation with a runtime truth table, plus a copy of
@@ -351,9 +374,9 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
   unsigned long long* hacc = cta.hacc;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  // lane -> (half h, cell c of the group, first word w of this thread)
-  const uint32_t h = Sh::V == 2 ? lane >> 4 : 0u;
-  const uint32_t hl = Sh::V == 2 ? lane & 15u : lane;
+  // lane -> (sub-warp h, cell c of the group, first word w of this thread)
+  const uint32_t h = lane / Sh::kSub;
+  const uint32_t hl = lane % Sh::kSub;
   const uint32_t cidx = hl / (W / Sh::V), w = (hl % (W / Sh::V)) * Sh::V;
   const bool resident = P.n_pieces <= (uint32_t)kRing;
   const uint32_t stages = P.n_levels + 1;

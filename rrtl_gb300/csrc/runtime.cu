@@ -160,7 +160,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     piece_groups = (uint32_t)std::min<size_t>(512, per_buf / group_bytes) & ~7u;
     for (;;) {
       build_pieces(gp, piece_groups);
-      blob = build_piece_blob(gp, kGateFusedWarps, kLeadWarpWeight, W >= 2 ? 2u : 1u, kRunCost);
+      blob = build_piece_blob(gp, kGateFusedWarps, kLeadWarpWeight, gate_fused_vec(W), kRunCost);
       size_t need = slot_bytes + gp.pieces.size() * sizeof(GatePieceDev) + (size_t)kRingBufs * blob.max_bytes;
       if (need <= max_smem) break;
       if (piece_groups <= 8) {
@@ -173,7 +173,7 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     build_pieces(gp, 256);
   }
   for (const GatePiece& pc : gp.pieces)
-    v->tile_cycle_cost += std::ceil((double)pc.n_groups / (kGateFusedWarps * (W >= 2 ? 2.0 : 1.0))) + 4.0;
+    v->tile_cycle_cost += std::ceil((double)pc.n_groups / (kGateFusedWarps * (double)gate_fused_vec(W))) + 4.0;
   if (v->fused_ok) {
     std::vector<GatePieceDev> pieces;
     for (size_t i = 0; i < gp.pieces.size(); ++i) {
