@@ -23,6 +23,7 @@
 #include "../../include/rrtl_cuda.h"
 #include "check_log.h"
 #include "gate_dev.h"
+#include "lut_classes.h"
 #include "stim.h"
 
 namespace rrtl {
@@ -37,7 +38,10 @@ constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slo
 #define RRTL_FUSED_UNROLL 1  // warp steps per unrolled iteration (unpaired loop)
 #endif
 #ifndef RRTL_PAIR_STEPS
-#define RRTL_PAIR_STEPS 1  // two warp steps per loop iteration, loads ahead of stores
+#define RRTL_PAIR_STEPS 0  // 1: two warp steps per loop iteration, loads ahead of stores
+#endif
+#if !RRTL_PAIR_STEPS
+constexpr int kUnroll = RRTL_FUSED_UNROLL;
 #endif
 static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
 static_assert(kRing == 4, "ring parity arithmetic assumes four buffers");
@@ -213,7 +217,7 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
     Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
   }
 #else
-#pragma unroll RRTL_FUSED_UNROLL
+#pragma unroll kUnroll
   for (; g < e; g += Sh::kSteps) {
     const uint2 r = rb[g * Sh::G];
     const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
@@ -226,9 +230,6 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
 
 #define RRTL_CASE(n) \
   case n: run_seg<W, n>(rb, Sv, b + h, e); break;
-#define RRTL_CASE4(n) RRTL_CASE(n) RRTL_CASE(n + 1) RRTL_CASE(n + 2) RRTL_CASE(n + 3)
-#define RRTL_CASE16(n) RRTL_CASE4(n) RRTL_CASE4(n + 4) RRTL_CASE4(n + 8) RRTL_CASE4(n + 12)
-#define RRTL_CASE64(n) RRTL_CASE16(n) RRTL_CASE16(n + 16) RRTL_CASE16(n + 32) RRTL_CASE16(n + 48)
 
 // One truth-table run (pack_run) of this warp's share.
 template <int W>
@@ -236,11 +237,8 @@ __device__ __forceinline__ void eval_run(const uint2* __restrict__ rb, typename 
                                          uint32_t run, int h) {
   const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
   switch (run & 0xFFu) {
-    RRTL_CASE64(0)
-    RRTL_CASE64(64)
-    RRTL_CASE64(128)
-    RRTL_CASE64(192)
-    default: break;
+    RRTL_LUT_CLASSES(RRTL_CASE)
+    default: break;  // not a class representative: the lowering never emits it
   }
 }
 

@@ -8,6 +8,47 @@
 
 namespace rrtl {
 
+// Truth table of a LUT3 with its inputs permuted: input k of the new cell is
+// input p[k] of the old one (table bit index = a<<2 | b<<1 | c).
+static uint8_t permute_lut(uint8_t lut, const int p[3]) {
+  uint8_t out = 0;
+  for (int idx = 0; idx < 8; ++idx) {
+    const int nv[3] = {(idx >> 2) & 1, (idx >> 1) & 1, idx & 1};  // values of the new inputs a, b, c
+    int ov[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k) ov[p[k]] = nv[k];
+    const int oidx = (ov[0] << 2) | (ov[1] << 1) | ov[2];
+    if ((lut >> oidx) & 1) out |= (uint8_t)(1u << idx);
+  }
+  return out;
+}
+
+// Reorder a cell's inputs so its truth table is the smallest over the six
+// input orders: every table maps to one of 80 permutation classes, so the
+// fused kernel needs one specialised loop per class instead of per table.
+void canonicalize_inputs(GateCell& c) {
+  static const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  uint8_t best = c.lut;
+  int bi = 0;
+  for (int k = 1; k < 6; ++k) {
+    const uint8_t t = permute_lut(c.lut, perms[k]);
+    if (t < best) {
+      best = t;
+      bi = k;
+    }
+  }
+  const uint32_t in[3] = {c.in[0], c.in[1], c.in[2]};
+  for (int k = 0; k < 3; ++k) c.in[k] = in[perms[bi][k]];
+  c.lut = best;
+}
+
+bool lut_is_canonical(uint8_t lut) {
+  GateCell c;
+  c.lut = lut;
+  canonicalize_inputs(c);
+  return c.lut == lut;
+}
+
+
 namespace {
 
 const uint8_t kVarMask[3] = {0xF0, 0xCC, 0xAA};
@@ -123,6 +164,7 @@ struct Builder {
     GateCell c;
     c.lut = f.tt;
     for (int i = 0; i < 3; ++i) c.in[i] = i < f.n ? f.leaf[i] : kNetConst0;
+    canonicalize_inputs(c);
     c.out = out;
     gp.cells.push_back(c);
   }

@@ -92,6 +92,11 @@ struct GateProgram {
   uint64_t source_instrs = 0;
 };
 
+// Reorder a cell's inputs so its truth table is its permutation class's
+// smallest; lut_is_canonical says whether a table is such a representative.
+void canonicalize_inputs(GateCell& c);
+bool lut_is_canonical(uint8_t lut);
+
 // Throws RrtlError("E_GATE_SCOPE", ...) when the program is outside the gate engine's scope.
 GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words = 8);
 

@@ -132,3 +132,27 @@ def test_gate_netlist_shape(oracle_lib):
     # 20 gate levels plus the output buffers
     assert od.num_levels == 21
     assert sum(1 for i in range(od.num_signals) if od.kind(i) == 3) == 128
+
+
+def test_lut_class_list_is_the_permutation_representatives():
+    """rrtl_gb300/csrc/lut_classes.h lists exactly the truth tables that are
+    the smallest of their six input orders (the kernel's specialised loops)."""
+    import os
+    import re
+
+    def perm_lut(l, p):
+        out = 0
+        for idx in range(8):
+            nv = [(idx >> 2) & 1, (idx >> 1) & 1, idx & 1]
+            ov = [0, 0, 0]
+            for k in range(3):
+                ov[p[k]] = nv[k]
+            if (l >> ((ov[0] << 2) | (ov[1] << 1) | ov[2])) & 1:
+                out |= 1 << idx
+        return out
+
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    canon = sorted(l for l in range(256) if min(perm_lut(l, p) for p in perms) == l)
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "rrtl_gb300", "csrc", "lut_classes.h")).read()
+    listed = sorted(int(x) for x in re.findall(r"X\((\d+)\)", hdr.split("#define RRTL_LUT_CLASSES(X)")[1]))
+    assert listed == canon and len(canon) == 80
