@@ -314,7 +314,7 @@ def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
     return out
 
 
-def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000)):
+def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000), round_us=10_000):
     """Serving loop (the C5 shape): Poisson arrivals over three resident
     designs (the 50k-gate netlist, the 8-stage CPU, a 500k-gate / 20k-FF
     netlist of the same family); lanes log-uniform 64-16,384, cycles
@@ -338,7 +338,7 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
     setup_s = time.perf_counter() - t0
     out = {"designs": {"c2": cd_c2.info.n_gates, "cpu": "8-stage CPU (word engine)", "big": cd_big.info.n_gates},
            "lanes": "log-uniform 64-16384", "cycles": f"log-uniform 1000-50000 / {cycle_div}",
-           "chunk_cycles": chunk, "duration_s": duration_s, "setup_s": setup_s, "rates": []}
+           "chunk_cycles": chunk, "round_us": round_us, "duration_s": duration_s, "setup_s": setup_s, "rates": []}
 
     def spec(rng, i):
         k = rng.below(3)
@@ -355,7 +355,7 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
         return server.submit(cd, lanes, cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH, memories=mems)
 
     for rate in rates:
-        server = sim.Server(ctx, chunk_cycles=chunk)
+        server = sim.Server(ctx, chunk_cycles=chunk, round_us=round_us)
         rng = Rng(int(rate * 1000) + 1)
         handles = []
         t_start = time.perf_counter()

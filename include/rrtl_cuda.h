@@ -322,6 +322,9 @@ typedef struct {
   uint64_t hbm_budget;    /* bytes of device memory for request state; 0 = 90% of free memory */
   uint32_t chunk_cycles;  /* cycles each active request advances per round; 0 = 256 */
   uint32_t max_active;    /* requests on the device at once; 0 = no limit */
+  uint32_t round_us;      /* target round time: gate-engine chunks are sized per request from its
+                             program's cost so a round lasts about this long; 0 = fixed chunks */
+  uint32_t pad;
 } rrtl_server_opts;
 
 typedef struct {

@@ -31,6 +31,8 @@ using namespace rrtl;
 
 namespace {
 
+constexpr uint64_t kMinChunk = 8;  // adaptive chunks never fall below this many cycles
+
 uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
              std::chrono::steady_clock::now().time_since_epoch())
@@ -84,6 +86,8 @@ struct rrtl_server {
   size_t budget = 0;
   uint32_t chunk = 256;
   uint32_t max_active = 0;
+  double round_ms = 0;      // target round time (0: fixed chunks)
+  double ms_per_cost = 0;   // calibrated device time of one unit of tile-cycle cost
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Request>> pending;
@@ -170,6 +174,16 @@ void rrtl_server::round() {
   uint32_t wblocks = 0;
   size_t smem = 0, wsmem = 0;
   std::vector<std::pair<double, uint32_t>> order;
+  // adaptive chunks: every gate request's tiles get about the same cost c per
+  // round, with c chosen so the round (its longest tile, or all tiles spread
+  // over the SMs) lasts about round_ms
+  double cost_per_tile_round = 0;
+  if (round_ms > 0 && ms_per_cost > 0) {
+    double tiles = 0;
+    for (auto& rp : active)
+      if (rp->gate && rp->fused) tiles += rp->gp.R.n_tiles;
+    cost_per_tile_round = round_ms / ms_per_cost / std::max(1.0, tiles / std::max<uint32_t>(1, ctx->sm_count));
+  }
   for (auto& rp : active) {
     Request& r = *rp;
     const uint64_t left = r.run.cycles - r.done_cycles;
@@ -180,6 +194,10 @@ void rrtl_server::round() {
       continue;
     }
     r.chunk = std::min<uint64_t>(left, chunk);
+    if (r.gate && cost_per_tile_round > 0) {
+      const uint64_t want = (uint64_t)std::max((double)kMinChunk, cost_per_tile_round / std::max(r.gp.v->tile_cycle_cost, 1e-9));
+      r.chunk = std::min<uint64_t>(left, want);
+    }
     const bool last = r.done_cycles + r.chunk == r.run.cycles;
     if (r.gate) {
       const uint32_t ji = (uint32_t)jobs.size();
@@ -212,6 +230,12 @@ void rrtl_server::round() {
     cuda_check(launch_word_multi(d_wjobs.as<WordJobDev>(), (uint32_t)wjobs.size(), wblocks, wsmem, word_stream),
                "word_multi_kernel");
   }
+  double max_cost = 0, sum_cost = 0;
+  for (auto& o : order) {
+    max_cost = std::max(max_cost, o.first);
+    sum_cost += o.first;
+  }
+  const double crit = std::max(max_cost, sum_cost / std::max<uint32_t>(1, ctx->sm_count));
   if (!items.empty()) {
     std::stable_sort(order.begin(), order.end(),
                      [](const std::pair<double, uint32_t>& a, const std::pair<double, uint32_t>& b) { return a.first > b.first; });
@@ -232,7 +256,13 @@ void rrtl_server::round() {
                "gate_queue_kernel");
   }
   cuda_check(cudaStreamSynchronize(st), "sync");
+  const uint64_t t_gate = now_ns();
   cuda_check(cudaStreamSynchronize(word_stream), "sync");
+  if (crit > 0 && !items.empty()) {
+    // calibrate: the round's gate part took about its critical cost
+    const double m = (double)(t_gate - t0) / 1e6 / crit;
+    ms_per_cost = ms_per_cost > 0 ? 0.7 * ms_per_cost + 0.3 * m : m;
+  }
   {
     std::lock_guard<std::mutex> lk(mu);
     ++rounds;
@@ -346,6 +376,7 @@ rrtl_status rrtl_server_create(rrtl_ctx* ctx, const rrtl_server_opts* opts, rrtl
     s->budget = opts && opts->hbm_budget ? (size_t)opts->hbm_budget : free_b / 10 * 9;
     s->chunk = opts && opts->chunk_cycles ? opts->chunk_cycles : 256;
     s->max_active = opts ? opts->max_active : 0;
+    s->round_ms = opts ? opts->round_us / 1000.0 : 0.0;
     ctx->refs++;
     rrtl_server* raw = s.release();
     raw->owner = std::thread([raw] { raw->loop(); });

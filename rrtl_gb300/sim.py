@@ -650,7 +650,8 @@ class ServerStats(ctypes.Structure):
 
 
 class ServerOpts(ctypes.Structure):
-    _fields_ = [("hbm_budget", c_uint64), ("chunk_cycles", c_uint32), ("max_active", c_uint32)]
+    _fields_ = [("hbm_budget", c_uint64), ("chunk_cycles", c_uint32), ("max_active", c_uint32),
+                ("round_us", c_uint32), ("pad", c_uint32)]
 
 
 class _RunShape:
@@ -681,9 +682,10 @@ class ServedRequest:
 class Server:
     """The serving loop (rrtl_server_*): continuous batching of requests on one GPU."""
 
-    def __init__(self, ctx: Optional[Context] = None, hbm_budget: int = 0, chunk_cycles: int = 0, max_active: int = 0):
+    def __init__(self, ctx: Optional[Context] = None, hbm_budget: int = 0, chunk_cycles: int = 0, max_active: int = 0,
+                 round_us: int = 0):
         self.ctx = ctx or default_context()
-        o = ServerOpts(hbm_budget, chunk_cycles, max_active)
+        o = ServerOpts(hbm_budget, chunk_cycles, max_active, round_us, 0)
         self.h = c_void_p()
         check(lib().rrtl_server_create(self.ctx.h, byref(o), byref(self.h)))
 
