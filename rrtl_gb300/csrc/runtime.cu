@@ -314,8 +314,12 @@ void upload_word_program(rrtl_design* d) {
   W.commits = reinterpret_cast<const WCommitDev*>(d->d_wcap.as<uint8_t>() + wp.mems.size() * sizeof(WMemDev));
   W.n_commits = (uint32_t)wp.commits.size();
   W.n_vslots = std::max<uint32_t>(wp.n_vslots, 1);
+  W.n_sig_words = (uint32_t)d->mp.source.total_signal_words;
   size_t smem = (size_t)W.n_vslots * kWordThreads * 8u;
-  if (smem <= kWordSmemBudget) cuda_check(word_prepare(smem), "word_prepare");
+  // signal values stay in shared memory for a launch when they fit beside the slots
+  const size_t sig = (size_t)W.n_sig_words * kWordThreads * 4u;
+  W.sig_smem = smem + sig <= kWordSmemBudget ? 1u : 0u;
+  if (smem <= kWordSmemBudget) cuda_check(word_prepare(kWordSmemBudget), "word_prepare");
 }
 
 bool word_smem_slots(rrtl_design* d) { return (size_t)d->wdev.n_vslots * kWordThreads * 8u <= kWordSmemBudget; }

@@ -214,7 +214,8 @@ void rrtl_server::round() {
       wj.R = word_chunk_desc(r.wp, r.done_cycles, r.chunk, last);
       wj.block_begin = wblocks;
       wblocks += r.wp.R.lanes_pad / kWordBlockLanes;
-      wsmem = std::max(wsmem, (size_t)r.design->wdev.n_vslots * kWordBlockLanes * 8);
+      wsmem = std::max(wsmem, (size_t)r.design->wdev.n_vslots * kWordBlockLanes * 8 +
+                                  (r.design->wdev.sig_smem ? (size_t)r.design->wdev.n_sig_words * kWordBlockLanes * 4 : 0));
       wjobs.push_back(wj);
     }
   }

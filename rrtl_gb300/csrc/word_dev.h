@@ -52,6 +52,8 @@ struct WordProgDev {
   const WCommitDev* commits;
   uint32_t n_commits;
   uint32_t n_vslots;
+  uint32_t n_sig_words;  // signal value words per lane
+  uint32_t sig_smem;     // 1: a block keeps its lanes' signal values in shared memory for the launch
 };
 
 struct WordStimDev {

@@ -32,20 +32,23 @@ struct WordLane {
   uint32_t vstride;
   uint32_t lane;
   size_t LP;
+  uint32_t* sv;   // this lane's signal values: shared memory [word][block] or HBM [word][lanes_pad]
+  size_t svs;     // their word stride
 
   __device__ unsigned long long& V(uint32_t s) const { return vbase[(size_t)s * vstride]; }
+  __device__ uint32_t& SV(uint32_t off) const { return sv[(size_t)off * svs]; }
 
   __device__ unsigned long long load_sig(uint32_t off, bool two) const {
-    unsigned long long v = R.values[(size_t)off * LP + lane];
-    if (two) v |= (unsigned long long)R.values[(size_t)(off + 1) * LP + lane] << 32;
+    unsigned long long v = SV(off);
+    if (two) v |= (unsigned long long)SV(off + 1) << 32;
     return v;
   }
   __device__ void store_sig(uint32_t off, bool two, unsigned long long v) const {
-    R.values[(size_t)off * LP + lane] = (uint32_t)v;
-    if (two) R.values[(size_t)(off + 1) * LP + lane] = (uint32_t)(v >> 32);
+    SV(off) = (uint32_t)v;
+    if (two) SV(off + 1) = (uint32_t)(v >> 32);
   }
   __device__ bool reset_asserted(uint32_t off, bool active_low) const {
-    bool b = R.values[(size_t)off * LP + lane] & 1u;
+    bool b = SV(off) & 1u;
     return active_low ? !b : b;
   }
 
@@ -134,17 +137,24 @@ struct WordLane {
     for (uint32_t k = 0; k < P.n_commits; ++k) {
       const WCommitDev cm = P.commits[k];
       for (uint32_t l = 0; l < cm.limbs; ++l)
-        R.values[(size_t)(cm.sig_off + l) * LP + lane] = R.caps[(size_t)(cm.cap_off + l) * LP + lane];
+        SV(cm.sig_off + l) = R.caps[(size_t)(cm.cap_off + l) * LP + lane];
     }
   }
 };
 
 // One lane through one launch's cycles (the body shared by the single-run
 // and the multi-job kernels).
+// Shared memory of a word block: [value slots: n_vslots][block] (u64) then,
+// with sig_smem, [signal words: n_sig_words][block] (u32).
 template <bool kSmem>
 __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRunDev& R, uint32_t lane,
                                               unsigned long long* vsm) {
-  WordLane W{P, R, kSmem ? vsm + threadIdx.x : R.vspill + lane, kSmem ? blockDim.x : R.lanes_pad, lane, R.lanes_pad};
+  uint32_t* ssm = reinterpret_cast<uint32_t*>(vsm + (size_t)P.n_vslots * blockDim.x) + threadIdx.x;
+  const bool sig_smem = kSmem && P.sig_smem;
+  WordLane W{P, R, kSmem ? vsm + threadIdx.x : R.vspill + lane, kSmem ? blockDim.x : R.lanes_pad, lane, R.lanes_pad,
+             sig_smem ? ssm : R.values + lane, sig_smem ? (size_t)blockDim.x : (size_t)R.lanes_pad};
+  if (sig_smem)
+    for (uint32_t w = 0; w < P.n_sig_words; ++w) ssm[(size_t)w * blockDim.x] = R.values[(size_t)w * R.lanes_pad + lane];
   const bool live = lane < R.lanes;
   // a lane detected by an earlier launch of the same run stays detected
   bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
@@ -165,7 +175,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
         else if (s.kind == RRTL_STIM_TRACE)
           v = live ? R.in_trace[((size_t)c * R.n_trace_cols + s.param + l) * R.lanes + lane] : 0u;
         if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
-        R.values[(size_t)(s.sig_off + l) * R.lanes_pad + lane] = v;
+        W.SV(s.sig_off + l) = v;
       }
     }
     W.run(P.comb_b, P.comb_e);
@@ -176,7 +186,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
       for (uint32_t k = 0; k < R.n_rec; ++k) {
         const WordRecDev rc = R.rec[k];
         for (uint32_t l = 0; l < rc.limbs; ++l) {
-          uint32_t v = R.values[(size_t)(rc.sig_off + l) * R.lanes_pad + lane];
+          uint32_t v = W.SV(rc.sig_off + l);
           if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
           if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
           if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
@@ -214,6 +224,13 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
     W.run(P.comb_b, P.comb_e);
     W.run(P.async_b, P.async_e);
   }
+  if (sig_smem)
+    for (uint32_t w = 0; w < P.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = ssm[(size_t)w * blockDim.x];
+}
+
+// Dynamic shared memory a word block needs (value slots, staged signals).
+__host__ __device__ inline size_t word_block_smem(const WordProgDev& P, uint32_t threads) {
+  return (size_t)P.n_vslots * threads * 8u + (P.sig_smem ? (size_t)P.n_sig_words * threads * 4u : 0u);
 }
 
 template <bool kSmem>
@@ -258,8 +275,7 @@ cudaError_t launch_word(const WordProgDev& P, const WordRunDev& R, bool smem_slo
   const uint32_t threads = 128;
   uint32_t grid = R.lanes_pad / threads;
   if (smem_slots) {
-    size_t smem = (size_t)P.n_vslots * threads * 8u;
-    word_kernel<true><<<grid, threads, smem, st>>>(P, R);
+    word_kernel<true><<<grid, threads, word_block_smem(P, threads), st>>>(P, R);
   } else {
     word_kernel<false><<<grid, threads, 0, st>>>(P, R);
   }
