@@ -252,8 +252,11 @@ rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv,
  * RRTL_PATH_FUSED: persistent multi-cycle kernel with on-chip net slots (default).
  * RRTL_PATH_PLAIN: one kernel launch per cycle, nets in HBM (the baseline).
  * RRTL_PATH_PLAIN_GRAPH: the plain path's per-cycle launches of one run
- *   captured into a CUDA graph and submitted as one graph launch. */
-enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1, RRTL_PATH_PLAIN_GRAPH = 2 };
+ *   captured into a CUDA graph and submitted as one graph launch.
+ * RRTL_PATH_WORD_INTERP: word engine, one launch of the interpreted kernel
+ *   for the whole run even when the design has a compiled kernel (the fused
+ *   path runs the compiled one); gate-engine batches treat it as FUSED. */
+enum { RRTL_PATH_FUSED = 0, RRTL_PATH_PLAIN = 1, RRTL_PATH_PLAIN_GRAPH = 2, RRTL_PATH_WORD_INTERP = 3 };
 rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path);
 
 /* Gate engine, fused path: 32-lane words per tile (8, 4, 2 or 1; 0 = chosen
@@ -392,6 +395,32 @@ rrtl_status rrtl_server_destroy(rrtl_server* s);
  * context stream and returns after the work finishes. */
 rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* design, uint32_t* values, uint32_t* memories, uint32_t lanes,
                                         uint64_t steps);
+
+/* ---- per-design compiled word kernels ------------------------------------
+ * A word-engine design is also emitted as straight-line CUDA C++ (one
+ * statement per word instruction, value slots in registers) and compiled by
+ * NVRTC for the device on its first fused run; the fused path then runs the
+ * compiled kernel and RRTL_PATH_WORD_INTERP the interpreted one. This
+ * replaces the reference's generated per-design kernels (WGSL tick_many,
+ * crates/rrtl-gpu-sim/src/lib.rs:2857-2890, and gpu_codegen::emit_kernel,
+ * crates/rrtl-sim-ir/src/gpu_codegen.rs:503-557). Designs over 20,000 word
+ * instructions, or hosts without NVRTC, run interpreted.
+ *
+ * rrtl_design_word_jit: compiles the design's kernel if that has not been
+ * tried yet; *active = 1 when the compiled kernel is in use, *compile_ms the
+ * time emit + compile + load took. For a gate-engine design *active = 0.
+ * rrtl_last_error() holds the reason when *active = 0. */
+rrtl_status rrtl_design_word_jit(rrtl_design* design, uint32_t* active, float* compile_ms);
+
+/* Emit (and, when arch is not NULL, e.g. "sm_103a", compile) the compiled
+ * word kernel of a design without a device: for tests and inspection.
+ * source: buffer of source_cap bytes for the NUL-terminated CUDA source (may
+ * be NULL); *source_len its length. *cubin_bytes the compiled image's size
+ * (0 when not compiled); log (may be NULL) the compiler's messages.
+ * RRTL_E_UNSUPPORTED when the design is outside the word engine's scope
+ * (values over 64 bits) or the compiler fails. */
+rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const char* arch, char* source,
+                               size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log, size_t log_cap);
 
 #ifdef __cplusplus
 }

@@ -686,14 +686,31 @@ void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {
   if (g.want_det) cuda_check(cudaMemcpyAsync(run.detect, g.R.detect, g.det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
 }
 
+// The design's compiled word kernel, built on first use (nullptr when the
+// design runs interpreted; the reason stays in d->wjit->error).
+const WordJit* word_jit_get(rrtl_design* d) {
+  std::lock_guard<std::mutex> lk(d->wjit_mu);
+  if (!d->wjit) {
+    d->wjit = std::make_unique<WordJit>();
+    const char* env = getenv("RRTL_WORD_JIT");
+    if (env && env[0] == '0') d->wjit->error = "compiled word kernels are off (RRTL_WORD_JIT=0)";
+    else word_jit_build(d->wp, d->ctx->device, d->wjit.get());
+  }
+  return d->wjit->ok ? d->wjit.get() : nullptr;
+}
+
 void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle,
               const CheckTables* chk = nullptr) {
   rrtl_design* d = b->d;
-  cudaStream_t st = d->ctx->stream;
+  rrtl_ctx* ctx = d->ctx;
+  cudaStream_t st = ctx->stream;
   WordPrepared g = word_prepare(b, run, device_ptrs, start_settle, chk);
   g.R.final_settle = final_settle;
+  const bool per_cycle = (b->path == RRTL_PATH_PLAIN || b->path == RRTL_PATH_PLAIN_GRAPH) && run.cycles > 1;
+  // compile before the timed region opens
+  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_get(d) : nullptr;
   Timer tm(b);
-  if (b->path != RRTL_PATH_FUSED && run.cycles > 1) {
+  if (per_cycle) {
     // one launch per cycle: the baseline path (captured into a CUDA graph on RRTL_PATH_PLAIN_GRAPH)
     const bool graph = b->path == RRTL_PATH_PLAIN_GRAPH;
     if (graph) cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -715,6 +732,11 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
     } else {
       cuda_check(ce, "word_kernel");
     }
+  } else if (J) {
+    WordJitPlace pl;
+    const size_t smem = word_jit_place(d->wp, *J, d->wdev.n_sig_words, b->lanes_pad, run.cycles, ctx->sm_count,
+                                       ctx->max_smem, ctx->max_smem_sm, &pl);
+    cuda_check(launch_word_jit(*J, g.R, pl, smem, st), "rrtl_word_jit");
   } else {
     cuda_check(launch_word(d->wdev, g.R, g.smem_slots, st), "word_kernel");
   }
@@ -1128,6 +1150,60 @@ rrtl_status rrtl_design_destroy(rrtl_design* d) {
   return guard([&] {
     if (!d) return;
     design_release(d);
+  });
+}
+
+rrtl_status rrtl_design_word_jit(rrtl_design* d, uint32_t* active, float* compile_ms) {
+  std::string why;
+  const rrtl_status st = guard([&] {
+    REQUIRE(d && active, RRTL_E_ARG, "E_ARG: null argument");
+    *active = 0;
+    if (compile_ms) *compile_ms = 0.f;
+    if (d->engine != RRTL_ENGINE_WORD) {
+      why = "the design runs on the gate engine";
+      return;
+    }
+    set_device(d->ctx);
+    const WordJit* J = word_jit_get(d);
+    if (compile_ms) *compile_ms = (float)d->wjit->compile_ms;
+    *active = J ? 1u : 0u;
+    if (!J) why = d->wjit->error;
+  });
+  if (st == RRTL_OK && !why.empty()) g_last_error = why;
+  return st;
+}
+
+rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const char* arch, char* source,
+                               size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log, size_t log_cap) {
+  return guard([&] {
+    REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
+    if (cubin_bytes) *cubin_bytes = 0;
+    if (log && log_cap) log[0] = 0;
+    Design dz = design_from_json(json, len);
+    MachineProgram mp = lower_to_machine_program(lower_to_packed_program(dz, top));
+    WordProgram wp;
+    try {
+      wp = build_word_program(mp);
+    } catch (const RrtlError& e) {
+      fail(RRTL_E_UNSUPPORTED, e.what());
+    }
+    const std::string src = word_jit_source(wp);
+    if (source_len) *source_len = src.size();
+    if (source && source_cap) {
+      const size_t n = std::min(source_cap - 1, src.size());
+      memcpy(source, src.data(), n);
+      source[n] = 0;
+    }
+    if (!arch) return;
+    std::string lg;
+    std::vector<char> cubin = word_jit_compile(src, arch, &lg);
+    if (log && log_cap) {
+      const size_t n = std::min(log_cap - 1, lg.size());
+      memcpy(log, lg.data(), n);
+      log[n] = 0;
+    }
+    REQUIRE(!cubin.empty(), RRTL_E_UNSUPPORTED, "E_WORD_JIT: " + lg.substr(0, 400));
+    if (cubin_bytes) *cubin_bytes = (uint32_t)cubin.size();
   });
 }
 
@@ -1607,9 +1683,8 @@ rrtl_status rrtl_batch_restore(rrtl_batch* b, const uint32_t* values, size_t nv,
 rrtl_status rrtl_batch_set_path(rrtl_batch* b, uint32_t path) {
   return guard([&] {
     REQUIRE(b, RRTL_E_ARG, "E_ARG: null argument");
-    REQUIRE(path == RRTL_PATH_FUSED || path == RRTL_PATH_PLAIN || path == RRTL_PATH_PLAIN_GRAPH, RRTL_E_ARG,
-            "E_ARG: unknown path");
-    b->path = path;
+    REQUIRE(path <= RRTL_PATH_WORD_INTERP, RRTL_E_ARG, "E_ARG: unknown path");
+    b->path = path == RRTL_PATH_WORD_INTERP && b->d->engine == RRTL_ENGINE_GATE ? (uint32_t)RRTL_PATH_FUSED : path;
   });
 }
 

@@ -5,6 +5,7 @@
 
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -14,6 +15,7 @@
 #include "gateprog.h"
 #include "lower.h"
 #include "word_dev.h"
+#include "word_jit.h"
 #include "wordprog.h"
 
 namespace rrtl {
@@ -174,6 +176,8 @@ struct rrtl_design {
   rrtl::WordProgram wp;
   rrtl::WordProgDev wdev{};
   rrtl::DevBuf d_wcode, d_wcap, d_wlit;
+  std::mutex wjit_mu;
+  std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel, built on the first fused run
 };
 
 struct rrtl_batch {

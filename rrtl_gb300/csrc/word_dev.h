@@ -95,6 +95,21 @@ struct WordRunDev {
   uint32_t chk_cap;
 };
 
+// Shared-memory placement of one launch of a compiled word kernel. Rows are
+// [row][thread] u32 words: the signal words first (when staged), then each
+// staged memory. Memories past kJitPlacedMems always stay in HBM.
+constexpr uint32_t kJitPlacedMems = 8;
+struct WordJitPlace {
+  uint32_t sig_smem;      // 1: signal words staged from row 0
+  uint32_t n_sig_words;
+  uint32_t n_mems;        // memories with an entry below (min(memories, kJitPlacedMems))
+  uint32_t pad;
+  uint32_t mem_off[kJitPlacedMems];    // first word of memory k in a lane's memory block
+  uint32_t mem_words[kJitPlacedMems];  // depth x limbs
+  uint32_t smem_row[kJitPlacedMems];   // first shared-memory row, ~0 = stays in HBM
+  uint32_t written[kJitPlacedMems];    // 1: the design writes memory k (copied back after the launch)
+};
+
 // One run of the multi-job word kernel: blocks [block_begin, next job's
 // block_begin) simulate its lanes, 128 per block.
 struct WordJobDev {

@@ -1,0 +1,402 @@
+// Per-design compiled word kernels: emitter, NVRTC compile, load and launch.
+//
+// Each word instruction becomes one C++ statement on 64-bit locals (the value
+// slots), in program order, with the interpreter's semantics
+// (word_kernels.cu WordLane::run, which follows eval_machine_instr_lane,
+// crates/rrtl-sim-ir/src/lib.rs:9796-9907): every result masked to its
+// width, shifts of 64 or more giving 0, out-of-range memory reads giving 0
+// and out-of-range writes dropped (:12989-13008, 9759-9775). Widths, shift
+// amounts, literals and memory geometry are folded into the source as
+// constants. Streams keep their own locals (the word lowering allocates
+// slots per stream); register captures go to locals c<k> that the clock edge
+// commits after the memory writes, as the interpreter's capture buffer does.
+#include "word_jit.h"
+
+#include <dlfcn.h>
+#include <nvrtc.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <mutex>
+#include <set>
+
+// kJitHeaderCount, kJitHeaderNames, kJitHeaderTexts: the headers the
+// generated source includes, embedded at build time.
+#include "word_jit_headers.inc"
+
+#ifndef RRTL_CUDA_LIB_DIR
+#define RRTL_CUDA_LIB_DIR "/usr/local/cuda/lib64"
+#endif
+
+namespace rrtl {
+
+namespace {
+
+std::string hex(unsigned long long v) {
+  char b[32];
+  snprintf(b, sizeof b, "0x%llxull", v);
+  return b;
+}
+
+unsigned long long wmask(uint32_t w) { return w >= 64u ? ~0ull : ((1ull << w) - 1ull); }
+
+std::string u(uint64_t v) { return std::to_string(v) + "u"; }
+
+struct Emitter {
+  const WordProgram& wp;
+  std::string o;
+
+  explicit Emitter(const WordProgram& w) : wp(w) {}
+
+  static std::string V(uint32_t s) { return "v" + std::to_string(s); }
+
+  std::string mem(uint32_t k, const std::string& w) const {
+    if (k < kJitPlacedMems) return "MK(" + u(k) + ", " + w + ")";
+    return "MG((size_t)" + u(wp.mems[k].offset) + " + " + w + ")";
+  }
+  static std::string reset(uint32_t off, bool low) {
+    return std::string("(((SV(") + u(off) + ") & 1u) != 0u) != " + (low ? "true" : "false") + ")";
+  }
+  static std::string store(uint32_t off, bool two, const std::string& t) {
+    std::string s = "SV(" + u(off) + ") = (uint32_t)" + t + ";";
+    if (two) s += " SV(" + u(off + 1) + ") = (uint32_t)(" + t + " >> 32);";
+    return s;
+  }
+
+  void line(const std::string& s) {
+    o += "    ";
+    o += s;
+    o += '\n';
+  }
+
+  // Statement for one instruction (empty for opcodes the interpreter skips).
+  std::string stmt(const WInstr& I) const {
+    const unsigned long long m = wmask(I.width);
+    const std::string M = hex(m);
+    const std::string d = V(I.dst), a = V(I.a), b = V(I.b), c = V(I.c);
+    const bool two = I.flags & 1;
+    switch (I.op) {
+      case W_LIT: return d + " = " + hex(wp.lits[I.aux] & m) + ";";
+      case W_SIG: {
+        std::string s = "(u64)SV(" + u(I.aux) + ")";
+        if (two) s = "(" + s + " | ((u64)SV(" + u(I.aux + 1) + ") << 32))";
+        return d + " = " + s + " & " + M + ";";
+      }
+      case W_NOT: return d + " = ~" + a + " & " + M + ";";
+      case W_AND: return d + " = (" + a + " & " + b + ") & " + M + ";";
+      case W_OR: return d + " = (" + a + " | " + b + ") & " + M + ";";
+      case W_XOR: return d + " = (" + a + " ^ " + b + ") & " + M + ";";
+      case W_ADD: return d + " = (" + a + " + " + b + ") & " + M + ";";
+      case W_SUB: return d + " = (" + a + " - " + b + ") & " + M + ";";
+      case W_MUL: return d + " = (" + a + " * " + b + ") & " + M + ";";
+      case W_EQ: return d + " = (u64)(" + a + " == " + b + ");";
+      case W_NE: return d + " = (u64)(" + a + " != " + b + ");";
+      case W_LT: {
+        const std::string om = hex(wmask(I.aux));
+        return d + " = (u64)((" + a + " & " + om + ") < (" + b + " & " + om + "));";
+      }
+      case W_LTS: {
+        // operand width 0 compares zeros; past 64 bits there is no sign bit
+        if (I.aux == 0) return d + " = 0ull;";
+        const std::string om = hex(wmask(I.aux));
+        if (I.aux > 64) return d + " = (u64)((" + a + " & " + om + ") < (" + b + " & " + om + "));";
+        const std::string sb = hex(1ull << (I.aux - 1u));
+        return "{ const u64 x = " + a + " & " + om + ", y = " + b + " & " + om + "; const bool xs = (x & " + sb +
+               ") != 0ull, ys = (y & " + sb + ") != 0ull; " + d + " = (xs != ys) ? (u64)xs : (u64)(x < y); }";
+      }
+      case W_MUX: return d + " = ((" + a + " & 1ull) ? " + b + " : " + c + ") & " + M + ";";
+      case W_SLICE:
+        if (I.aux >= 64u) return d + " = 0ull;";
+        return d + " = (" + a + " >> " + u(I.aux) + ") & " + M + ";";
+      case W_MASK: return d + " = " + a + " & " + M + ";";
+      case W_SEXT: {
+        if (I.aux == 0) return d + " = 0ull;";
+        if (I.aux >= 64) return d + " = " + a + " & " + M + ";";
+        const std::string wm = hex(wmask(I.aux)), nwm = hex(~wmask(I.aux));
+        return "{ const u64 x = " + a + " & " + wm + "; " + d + " = (((x >> " + u(I.aux - 1u) + ") & 1ull) ? (x | " + nwm +
+               ") : x) & " + M + "; }";
+      }
+      case W_CAT:
+        if (I.aux >= 64u) return d + " = " + b + " & " + M + ";";
+        return d + " = ((" + a + " << " + u(I.aux) + ") | " + b + ") & " + M + ";";
+      case W_MEMRD: {
+        const WMemDev& Md = wp.mems[I.aux];
+        std::string s = "{ const u64 ad = " + a + "; u64 r = 0ull; if (ad < " + hex(Md.depth) +
+                        ") { const size_t w0 = (size_t)ad * " + u(Md.limbs) + "; r = (u64)" + mem(I.aux, "w0") + ";";
+        if (Md.limbs == 2) s += " r |= (u64)" + mem(I.aux, "w0 + 1u") + " << 32;";
+        s += " r &= " + hex(wmask(Md.width) & m) + "; } " + d + " = r; }";
+        return s;
+      }
+      case W_STORE: return "{ const u64 t = " + a + " & " + M + "; " + store(I.aux, two, "t") + " }";
+      case W_ASTORE:
+        return "if (" + reset(I.aux2, I.flags & 4) + ") { const u64 t = " + a + " & " + M + "; " + store(I.aux, two, "t") +
+               " }";
+      case W_CAPTURE: {
+        std::string t = a;
+        if (I.flags & 2) t = "(" + reset(I.aux2, I.flags & 4) + " ? " + hex(wp.lits[I.aux3]) + " : " + a + ")";
+        std::string s = "{ const u64 t = " + t + " & " + M + "; c" + std::to_string(I.aux) + " = (uint32_t)t;";
+        if (two) s += " c" + std::to_string(I.aux + 1) + " = (uint32_t)(t >> 32);";
+        return s + " }";
+      }
+      case W_MEMWR: {
+        const WMemDev& Md = wp.mems[I.aux];
+        std::string s = "if (" + a + " & 1ull) { const u64 ad = " + b + "; if (ad < " + hex(Md.depth) + ") { const u64 t = " +
+                        c + " & " + hex(wmask(Md.width)) + "; const size_t w0 = (size_t)ad * " + u(Md.limbs) + "; " +
+                        mem(I.aux, "w0") + " = (uint32_t)t;";
+        if (Md.limbs == 2) s += " " + mem(I.aux, "w0 + 1u") + " = (uint32_t)(t >> 32);";
+        return s + " } }";
+      }
+      default: return "";
+    }
+  }
+
+  static void uses(const WInstr& I, std::set<uint32_t>& s) {
+    switch (I.op) {
+      case W_LIT:
+      case W_SIG: s.insert(I.dst); break;
+      case W_NOT:
+      case W_SLICE:
+      case W_MASK:
+      case W_SEXT:
+      case W_MEMRD: s.insert(I.dst); s.insert(I.a); break;
+      case W_MUX: s.insert(I.dst); s.insert(I.a); s.insert(I.b); s.insert(I.c); break;
+      case W_STORE:
+      case W_ASTORE:
+      case W_CAPTURE: s.insert(I.a); break;
+      case W_MEMWR: s.insert(I.a); s.insert(I.b); s.insert(I.c); break;
+      default: s.insert(I.dst); s.insert(I.a); s.insert(I.b); break;
+    }
+  }
+
+  // One stream in its own scope with its own slot locals.
+  void block(uint32_t b, uint32_t e, const char* what) {
+    if (b == e) return;
+    std::set<uint32_t> slots;
+    for (uint32_t pc = b; pc < e; ++pc) uses(wp.code[pc], slots);
+    o += "  {  // ";
+    o += what;
+    o += '\n';
+    if (!slots.empty()) {
+      std::string decl = "u64";
+      bool first = true;
+      for (uint32_t s : slots) {
+        decl += (first ? " " : ", ") + V(s) + " = 0ull";
+        first = false;
+      }
+      line(decl + ";");
+    }
+    for (uint32_t pc = b; pc < e; ++pc) {
+      std::string s = stmt(wp.code[pc]);
+      if (!s.empty()) line(s);
+    }
+    o += "  }\n";
+  }
+
+  std::string source() {
+    const bool big = wp.code.size() > 4000;  // keep one copy of large settle bodies
+    o += "// Compiled word kernel (generated from the design's word program).\n";
+    o += "#include \"word_lane.h\"\n";
+    o += "namespace rrtl {\n";
+    o += "typedef unsigned long long u64;\n";
+    o += "struct JitLane : JitLaneBase {\n";
+    o += "  __device__ void settle();\n";
+    o += "  __device__ void edge();\n";
+    o += "};\n";
+    o += std::string(big ? "__device__ __noinline__" : "__device__ __forceinline__") + " void JitLane::settle() {\n";
+    block(wp.comb_b, wp.comb_e, "comb");
+    block(wp.async_b, wp.async_e, "async reset");
+    o += "}\n";
+    o += "__device__ __forceinline__ void JitLane::edge() {\n";
+    if (wp.total_capture_words) {
+      std::string decl = "  uint32_t";
+      for (uint32_t k = 0; k < wp.total_capture_words; ++k) decl += (k ? ", c" : " c") + std::to_string(k) + " = 0u";
+      o += decl + ";\n";
+    }
+    block(wp.next_b, wp.next_e, "tick_next: register captures");
+    block(wp.commit_b, wp.commit_e, "tick_commit: memory writes");
+    for (const WCommitDev& cm : wp.commits)
+      for (uint32_t l = 0; l < cm.limbs; ++l)
+        o += "  SV(" + u(cm.sig_off + l) + ") = c" + std::to_string(cm.cap_off + l) + ";\n";
+    o += "}\n";
+    o += "}  // namespace rrtl\n";
+    o += "extern \"C\" __global__ void __launch_bounds__(128) rrtl_word_jit(const rrtl::WordRunDev R, "
+         "const rrtl::WordJitPlace Pl) {\n";
+    o += "  extern __shared__ uint32_t rrtl_jsm[];\n";
+    o += "  rrtl::word_jit_run<rrtl::JitLane>(R, Pl, rrtl_jsm);\n";
+    o += "}\n";
+    return o;
+  }
+};
+
+// ---- NVRTC, opened at run time so the library loads without it
+struct Nvrtc {
+  bool ok = false;
+  std::string error;
+  decltype(&nvrtcCreateProgram) create = nullptr;
+  decltype(&nvrtcCompileProgram) compile = nullptr;
+  decltype(&nvrtcGetProgramLogSize) log_size = nullptr;
+  decltype(&nvrtcGetProgramLog) get_log = nullptr;
+  decltype(&nvrtcGetCUBINSize) cubin_size = nullptr;
+  decltype(&nvrtcGetCUBIN) get_cubin = nullptr;
+  decltype(&nvrtcDestroyProgram) destroy = nullptr;
+  decltype(&nvrtcGetErrorString) err_str = nullptr;
+
+  Nvrtc() {
+    void* h = nullptr;
+    for (const char* name : {"libnvrtc.so.13", "libnvrtc.so", RRTL_CUDA_LIB_DIR "/libnvrtc.so.13",
+                             RRTL_CUDA_LIB_DIR "/libnvrtc.so"}) {
+      h = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+      if (h) break;
+    }
+    if (!h) {
+      const char* e = dlerror();
+      error = std::string("NVRTC not found: ") + (e ? e : "dlopen failed");
+      return;
+    }
+    create = reinterpret_cast<decltype(create)>(dlsym(h, "nvrtcCreateProgram"));
+    compile = reinterpret_cast<decltype(compile)>(dlsym(h, "nvrtcCompileProgram"));
+    log_size = reinterpret_cast<decltype(log_size)>(dlsym(h, "nvrtcGetProgramLogSize"));
+    get_log = reinterpret_cast<decltype(get_log)>(dlsym(h, "nvrtcGetProgramLog"));
+    cubin_size = reinterpret_cast<decltype(cubin_size)>(dlsym(h, "nvrtcGetCUBINSize"));
+    get_cubin = reinterpret_cast<decltype(get_cubin)>(dlsym(h, "nvrtcGetCUBIN"));
+    destroy = reinterpret_cast<decltype(destroy)>(dlsym(h, "nvrtcDestroyProgram"));
+    err_str = reinterpret_cast<decltype(err_str)>(dlsym(h, "nvrtcGetErrorString"));
+    ok = create && compile && log_size && get_log && cubin_size && get_cubin && destroy && err_str;
+    if (!ok) error = "NVRTC library lacks an entry point";
+  }
+};
+
+Nvrtc& nvrtc() {
+  static Nvrtc n;
+  return n;
+}
+
+}  // namespace
+
+WordJit::~WordJit() {
+  if (lib) cudaLibraryUnload(lib);
+}
+
+std::string word_jit_source(const WordProgram& wp) { return Emitter(wp).source(); }
+
+std::vector<char> word_jit_compile(const std::string& src, const std::string& arch, std::string* log) {
+  Nvrtc& N = nvrtc();
+  if (!N.ok) {
+    *log = N.error;
+    return {};
+  }
+  nvrtcProgram prog = nullptr;
+  nvrtcResult r = N.create(&prog, src.c_str(), "rrtl_word_jit.cu", kJitHeaderCount, kJitHeaderTexts, kJitHeaderNames);
+  if (r != NVRTC_SUCCESS) {
+    *log = std::string("nvrtcCreateProgram: ") + N.err_str(r);
+    return {};
+  }
+  const std::string arch_opt = "--gpu-architecture=" + arch;
+  // -default-device: the C ABI header's host prototypes become inert device declarations
+  const char* opts[] = {arch_opt.c_str(), "-std=c++17", "-default-device"};
+  r = N.compile(prog, 3, opts);
+  size_t ls = 0;
+  N.log_size(prog, &ls);
+  std::string lg(ls, '\0');
+  if (ls) N.get_log(prog, &lg[0]);
+  *log = lg;
+  std::vector<char> cubin;
+  if (r == NVRTC_SUCCESS) {
+    size_t n = 0;
+    if (N.cubin_size(prog, &n) == NVRTC_SUCCESS && n) {
+      cubin.resize(n);
+      if (N.get_cubin(prog, cubin.data()) != NVRTC_SUCCESS) cubin.clear();
+    }
+  } else {
+    *log = std::string("nvrtcCompileProgram: ") + N.err_str(r) + "\n" + lg;
+  }
+  N.destroy(&prog);
+  return cubin;
+}
+
+void word_jit_build(const WordProgram& wp, int device, WordJit* J) {
+  const auto t0 = std::chrono::steady_clock::now();
+  J->written.assign(wp.mems.size(), 0);
+  for (const WInstr& I : wp.code)
+    if (I.op == W_MEMWR && I.aux < J->written.size()) J->written[I.aux] = 1;
+  if (wp.code.size() > kJitMaxInstrs) {
+    J->error = "word program of " + std::to_string(wp.code.size()) + " instructions runs interpreted";
+    return;
+  }
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+    J->error = "cudaGetDeviceProperties failed";
+    return;
+  }
+  const std::string arch = "sm_" + std::to_string(prop.major) + std::to_string(prop.minor) + "a";
+  const std::string src = word_jit_source(wp);
+  J->source_bytes = src.size();
+  std::string log;
+  std::vector<char> cubin = word_jit_compile(src, arch, &log);
+  if (cubin.empty()) {
+    J->error = log.size() > 2000 ? log.substr(0, 2000) : log;
+    return;
+  }
+  cudaError_t e = cudaLibraryLoadData(&J->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&J->fn, J->lib, "rrtl_word_jit");
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(reinterpret_cast<const void*>(J->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)prop.sharedMemPerBlockOptin);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    J->error = std::string("loading the compiled kernel: ") + cudaGetErrorString(e);
+    return;
+  }
+  J->ok = true;
+  J->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad, uint64_t cycles,
+                      uint32_t sm_count, size_t max_smem_block, size_t max_smem_sm, WordJitPlace* out) {
+  constexpr uint32_t kThreads = 128;
+  constexpr size_t kRowBytes = (size_t)kThreads * 4u;
+  WordJitPlace P{};
+  P.n_sig_words = n_sig_words;
+  P.n_mems = (uint32_t)std::min<size_t>(wp.mems.size(), kJitPlacedMems);
+  // several blocks per SM when there are lanes for them: split the SM's
+  // shared memory between them (one block's rows sit idle otherwise)
+  const uint32_t blocks = lanes_pad / kThreads;
+  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(4, (blocks + sm_count - 1) / std::max<uint32_t>(sm_count, 1)));
+  const size_t budget = std::min(max_smem_block, max_smem_sm / per_sm - 1024);
+  // staging costs one pass over the rows at each end of the launch: worth it
+  // when the launch runs a few cycles per staged row
+  auto worth = [&](uint64_t rows) { return rows <= 64 || rows <= 4 * cycles; };
+  size_t used = 0;
+  if (n_sig_words && (size_t)n_sig_words * kRowBytes <= budget && worth(n_sig_words)) {
+    P.sig_smem = 1;
+    used = (size_t)n_sig_words * kRowBytes;
+  }
+  std::vector<uint32_t> order;
+  for (uint32_t k = 0; k < P.n_mems; ++k) {
+    P.mem_off[k] = wp.mems[k].offset;
+    P.mem_words[k] = wp.mems[k].depth * wp.mems[k].limbs;
+    P.smem_row[k] = 0xFFFFFFFFu;
+    P.written[k] = k < J.written.size() ? J.written[k] : 1;
+    order.push_back(k);
+  }
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return P.mem_words[a] < P.mem_words[b]; });
+  for (uint32_t k : order) {
+    const size_t bytes = (size_t)P.mem_words[k] * kRowBytes;
+    if (used + bytes <= budget && worth(P.mem_words[k])) {
+      P.smem_row[k] = (uint32_t)(used / kRowBytes);
+      used += bytes;
+    }
+  }
+  *out = P;
+  return used;
+}
+
+cudaError_t launch_word_jit(const WordJit& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem, cudaStream_t st) {
+  WordRunDev r = R;
+  WordJitPlace p = Pl;
+  void* args[] = {&r, &p};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(J.fn), dim3(R.lanes_pad / 128u), dim3(128), args, smem, st);
+}
+
+}  // namespace rrtl

@@ -1,0 +1,57 @@
+// Per-design compiled word kernels.
+//
+// The reference emits a design as straight-line per-lane GPU code (WGSL
+// tick_many, crates/rrtl-gpu-sim/src/lib.rs:2857-2890, 3082-4126; the CUDA
+// emitter gpu_codegen::emit_kernel, crates/rrtl-sim-ir/src/gpu_codegen.rs:503-557).
+// Here the word program (wordprog.h) is emitted as CUDA C++, one statement per
+// word instruction in program order, compiled at design load by NVRTC for the
+// device's architecture and launched through the runtime's library API. The
+// run protocol around it (stimulus, record, commit order) is the same header
+// the interpreted kernel uses (word_lane.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "word_dev.h"
+#include "wordprog.h"
+
+namespace rrtl {
+
+struct WordJit {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t fn = nullptr;
+  bool ok = false;
+  std::string error;     // why there is no compiled kernel (empty when ok)
+  double compile_ms = 0; // emit + NVRTC + load
+  size_t source_bytes = 0;
+  std::vector<uint8_t> written;  // per memory: the design writes it
+  ~WordJit();
+};
+
+// Largest word program that is compiled (bigger ones run interpreted).
+constexpr size_t kJitMaxInstrs = 20000;
+
+// CUDA C++ source of a word program's compiled kernel `rrtl_word_jit`.
+std::string word_jit_source(const WordProgram& wp);
+
+// Compile `src` for `arch` (e.g. "sm_103a") with NVRTC; returns the cubin,
+// or an empty vector with `log` holding the compiler's messages.
+std::vector<char> word_jit_compile(const std::string& src, const std::string& arch, std::string* log);
+
+// Emit, compile and load the kernel of `wp` on the current device. Never
+// throws: failures leave ok = false and the reason in error.
+void word_jit_build(const WordProgram& wp, int device, WordJit* out);
+
+// Shared-memory placement for one launch over `lanes_pad` lanes and `cycles`
+// cycles; returns the dynamic shared memory bytes per 128-lane block.
+size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad,
+                      uint64_t cycles, uint32_t sm_count, size_t max_smem_block, size_t max_smem_sm,
+                      WordJitPlace* out);
+
+cudaError_t launch_word_jit(const WordJit& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem,
+                            cudaStream_t st);
+
+}  // namespace rrtl

@@ -17,9 +17,8 @@
 
 #include "../../include/rrtl_cuda.h"
 #include "runtime.h"
-#include "check_log.h"
-#include "stim.h"
 #include "word_dev.h"
+#include "word_lane.h"
 
 namespace rrtl {
 
@@ -140,6 +139,16 @@ struct WordLane {
         SV(cm.sig_off + l) = R.caps[(size_t)(cm.cap_off + l) * LP + lane];
     }
   }
+
+  __device__ void settle() const {
+    run(P.comb_b, P.comb_e);
+    run(P.async_b, P.async_e);
+  }
+  __device__ void edge() const {
+    run(P.next_b, P.next_e);
+    run(P.commit_b, P.commit_e);
+    commit();
+  }
 };
 
 // One lane through one launch's cycles (the body shared by the single-run
@@ -155,75 +164,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
              sig_smem ? ssm : R.values + lane, sig_smem ? (size_t)blockDim.x : (size_t)R.lanes_pad};
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) ssm[(size_t)w * blockDim.x] = R.values[(size_t)w * R.lanes_pad + lane];
-  const bool live = lane < R.lanes;
-  // a lane detected by an earlier launch of the same run stays detected
-  bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
-  if (R.start_settle) {
-    W.run(P.comb_b, P.comb_e);
-    W.run(P.async_b, P.async_e);
-  }
-  for (unsigned long long c = 0; c < R.cycles; ++c) {
-    const unsigned long long ca = R.cycle_base + c;
-    for (uint32_t k = 0; k < R.n_stim; ++k) {
-      const WordStimDev s = R.stim[k];
-      if (s.kind == RRTL_STIM_HOLD) continue;
-      for (uint32_t l = 0; l < s.limbs; ++l) {
-        uint32_t v = 0;
-        if (s.kind == RRTL_STIM_RANDOM) v = stim_lane_limb(R.seed, s.param, ca, lane, s.width, l);
-        else if (s.kind == RRTL_STIM_PULSE) v = (l == 0 && ca < s.param) ? 1u : 0u;
-        else if (s.kind == RRTL_STIM_CONST) v = l < 2 ? (uint32_t)(s.param >> (32 * l)) : 0u;
-        else if (s.kind == RRTL_STIM_TRACE)
-          v = live ? R.in_trace[((size_t)c * R.n_trace_cols + s.param + l) * R.lanes + lane] : 0u;
-        if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
-        W.SV(s.sig_off + l) = v;
-      }
-    }
-    W.run(P.comb_b, P.comb_e);
-    W.run(P.async_b, P.async_e);
-    if (R.n_rec) {
-      unsigned long long h = 0ull;
-      bool diff = false;
-      for (uint32_t k = 0; k < R.n_rec; ++k) {
-        const WordRecDev rc = R.rec[k];
-        for (uint32_t l = 0; l < rc.limbs; ++l) {
-          uint32_t v = W.SV(rc.sig_off + l);
-          if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
-          if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
-          if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
-            // 1-bit signals hash as 32-lane packed words, the gate engine's unit
-            const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
-            if ((threadIdx.x & 31u) == 0 && live) h += hash_term(ca, k, lane >> 5, packed);
-          }
-          if (!live) continue;
-          if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
-          if (R.mode & RRTL_REC_CHECK) {
-            const size_t row = (size_t)c * R.rec_limbs + rc.base + l;
-            const uint32_t idx = R.chk_idx[row];
-            if (idx != 0xFFFFFFFFu) {
-              const uint32_t exp = R.chk_exp[row * R.lanes + lane];
-              if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
-            }
-          }
-          if ((R.mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
-        }
-      }
-      if (R.mode & RRTL_REC_HASH) {
-        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
-        if ((threadIdx.x & 31u) == 0 && h) atomicAdd(R.out_hash + c, h);
-      }
-      if ((R.mode & RRTL_REC_DETECT) && live && diff && !detected) {
-        detected = true;
-        R.detect[lane] = (uint32_t)ca;
-      }
-    }
-    W.run(P.next_b, P.next_e);
-    W.run(P.commit_b, P.commit_e);
-    W.commit();
-  }
-  if (R.final_settle) {
-    W.run(P.comb_b, P.comb_e);
-    W.run(P.async_b, P.async_e);
-  }
+  word_lane_cycles(R, lane, W);
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = ssm[(size_t)w * blockDim.x];
 }

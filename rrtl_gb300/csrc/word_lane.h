@@ -1,0 +1,156 @@
+// Run protocol of one word-engine lane, shared by the interpreted word kernel
+// (word_kernels.cu) and the per-design compiled kernels (word_jit.cpp), so
+// both engines step a lane through exactly the same sequence:
+//
+//   per cycle: stimulus -> settle -> record (trace, hash, detect, checks)
+//              -> clock edge (register capture, memory writes, commit)
+//
+// with a settle before the first cycle when the run asks for one and a
+// closing settle after the last. This is the reference's replay order
+// (inputs, settle, check, tick: crates/rrtl-sim-ir/src/lib.rs:9540-9568).
+//
+// An engine type L provides
+//   uint32_t& SV(uint32_t word)  one signal word of the lane
+//   void settle()                comb stream, then the async-reset stream
+//   void edge()                  tick_next, tick_commit, register commit
+//
+// The header is also compiled at run time by NVRTC, so it includes only
+// headers that are handed to NVRTC with it.
+#pragma once
+
+#include <stdint.h>
+
+#include "../../include/rrtl_cuda.h"
+#include "check_log.h"
+#include "stim.h"
+#include "word_dev.h"
+
+namespace rrtl {
+
+template <class L>
+__device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t lane, L& W) {
+  const bool live = lane < R.lanes;
+  // a lane detected by an earlier launch of the same run stays detected
+  bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
+  if (R.start_settle) W.settle();
+  for (unsigned long long c = 0; c < R.cycles; ++c) {
+    const unsigned long long ca = R.cycle_base + c;
+    for (uint32_t k = 0; k < R.n_stim; ++k) {
+      const WordStimDev s = R.stim[k];
+      if (s.kind == RRTL_STIM_HOLD) continue;
+      for (uint32_t l = 0; l < s.limbs; ++l) {
+        uint32_t v = 0;
+        if (s.kind == RRTL_STIM_RANDOM) v = stim_lane_limb(R.seed, s.param, ca, lane, s.width, l);
+        else if (s.kind == RRTL_STIM_PULSE) v = (l == 0 && ca < s.param) ? 1u : 0u;
+        else if (s.kind == RRTL_STIM_CONST) v = l < 2 ? (uint32_t)(s.param >> (32 * l)) : 0u;
+        else if (s.kind == RRTL_STIM_TRACE)
+          v = live ? R.in_trace[((size_t)c * R.n_trace_cols + s.param + l) * R.lanes + lane] : 0u;
+        if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
+        W.SV(s.sig_off + l) = v;
+      }
+    }
+    W.settle();
+    if (R.n_rec) {
+      unsigned long long h = 0ull;
+      bool diff = false;
+      for (uint32_t k = 0; k < R.n_rec; ++k) {
+        const WordRecDev rc = R.rec[k];
+        for (uint32_t l = 0; l < rc.limbs; ++l) {
+          uint32_t v = W.SV(rc.sig_off + l);
+          if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
+          if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
+          if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
+            // 1-bit signals hash as 32-lane packed words, the gate engine's unit
+            const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
+            if ((threadIdx.x & 31u) == 0 && live) h += hash_term(ca, k, lane >> 5, packed);
+          }
+          if (!live) continue;
+          if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
+          if (R.mode & RRTL_REC_CHECK) {
+            const size_t row = (size_t)c * R.rec_limbs + rc.base + l;
+            const uint32_t idx = R.chk_idx[row];
+            if (idx != 0xFFFFFFFFu) {
+              const uint32_t exp = R.chk_exp[row * R.lanes + lane];
+              if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
+            }
+          }
+          if ((R.mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
+        }
+      }
+      if (R.mode & RRTL_REC_HASH) {
+        for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
+        if ((threadIdx.x & 31u) == 0 && h) atomicAdd(R.out_hash + c, h);
+      }
+      if ((R.mode & RRTL_REC_DETECT) && live && diff && !detected) {
+        detected = true;
+        R.detect[lane] = (uint32_t)ca;
+      }
+    }
+    W.edge();
+  }
+  if (R.final_settle) W.settle();
+}
+
+// ---- per-design compiled kernels
+//
+// A compiled lane keeps its value slots in registers; signal words and the
+// memories listed in WordJitPlace are staged in shared memory for the launch
+// ([word][thread], so any per-lane address is bank-conflict free), the other
+// memories stay word-major in HBM.
+struct JitLaneBase {
+  uint32_t* sv;                     // signal word 0 of this lane
+  size_t svs;                       // signal word stride
+  uint32_t* mb[kJitPlacedMems];     // word 0 of memory k for this lane
+  size_t ms[kJitPlacedMems];        // its word stride
+  uint32_t* gm;                     // R.mems + lane (memories past kJitPlacedMems)
+  size_t LP;                        // lanes_pad
+  __device__ __forceinline__ uint32_t& SV(uint32_t off) const { return sv[(size_t)off * svs]; }
+  __device__ __forceinline__ uint32_t& MK(uint32_t k, size_t w) const { return mb[k][w * ms[k]]; }
+  __device__ __forceinline__ uint32_t& MG(size_t w) const { return gm[w * LP]; }
+};
+
+// Kernel body of a compiled design: stage in, run the cycles, stage out.
+template <class L>
+__device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitPlace& Pl, uint32_t* jsm) {
+  const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t T = blockDim.x;
+  uint32_t* my = jsm + threadIdx.x;
+  L W;
+  W.LP = R.lanes_pad;
+  W.gm = R.mems + lane;
+  if (Pl.sig_smem) {
+    W.sv = my;
+    W.svs = T;
+    for (uint32_t w = 0; w < Pl.n_sig_words; ++w) my[(size_t)w * T] = R.values[(size_t)w * R.lanes_pad + lane];
+  } else {
+    W.sv = R.values + lane;
+    W.svs = R.lanes_pad;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kJitPlacedMems; ++k) {
+    if (k >= Pl.n_mems) break;
+    uint32_t* g = R.mems + (size_t)Pl.mem_off[k] * R.lanes_pad + lane;
+    if (Pl.smem_row[k] != 0xFFFFFFFFu) {
+      uint32_t* s = my + (size_t)Pl.smem_row[k] * T;
+      for (uint32_t w = 0; w < Pl.mem_words[k]; ++w) s[(size_t)w * T] = g[(size_t)w * R.lanes_pad];
+      W.mb[k] = s;
+      W.ms[k] = T;
+    } else {
+      W.mb[k] = g;
+      W.ms[k] = R.lanes_pad;
+    }
+  }
+  word_lane_cycles(R, lane, W);
+  if (Pl.sig_smem)
+    for (uint32_t w = 0; w < Pl.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = my[(size_t)w * T];
+#pragma unroll
+  for (uint32_t k = 0; k < kJitPlacedMems; ++k) {
+    if (k >= Pl.n_mems) break;
+    if (Pl.smem_row[k] == 0xFFFFFFFFu || !Pl.written[k]) continue;
+    uint32_t* g = R.mems + (size_t)Pl.mem_off[k] * R.lanes_pad + lane;
+    const uint32_t* s = my + (size_t)Pl.smem_row[k] * T;
+    for (uint32_t w = 0; w < Pl.mem_words[k]; ++w) g[(size_t)w * R.lanes_pad] = s[(size_t)w * T];
+  }
+}
+
+}  // namespace rrtl

@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "librrtl_gb300.so")
 
 STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE = 0, 1, 2, 3, 4
 REC_TRACE, REC_HASH, REC_DETECT, REC_CHECK = 1, 2, 4, 8
-PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH = 0, 1, 2
+PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH, PATH_WORD_INTERP = 0, 1, 2, 3
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 ENGINE_GATE, ENGINE_WORD = 1, 2
 
@@ -159,6 +159,8 @@ EXPORTS = (
     "rrtl_batch_tile_words",
     "rrtl_batch_last_kernel_ms",
     "rrtl_word_tick_many_noalloc",
+    "rrtl_design_word_jit",
+    "rrtl_word_jit_emit",
 )
 
 _lib = None
@@ -225,6 +227,9 @@ def lib():
         "rrtl_batch_tile_words": [c_void_p, P(c_uint32)],
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
+        "rrtl_design_word_jit": [c_void_p, P(c_uint32), P(c_float)],
+        "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
+                               P(c_uint32), c_char_p, c_size_t],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -331,6 +336,21 @@ def default_context() -> Context:
     return _default_ctx
 
 
+def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] = None):
+    """CUDA source of a design's compiled word kernel, and with `arch` its NVRTC
+    compile (no device needed): (source, cubin bytes, compiler log)."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    n = c_size_t()
+    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), None, None, 0, byref(n), None, None, 0))
+    src = ctypes.create_string_buffer(n.value + 1)
+    logb = ctypes.create_string_buffer(1 << 16)
+    cub = c_uint32()
+    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), arch.encode() if arch else None, src, n.value + 1,
+                                   byref(n), byref(cub), logb, len(logb)))
+    return src.value.decode(), cub.value, logb.value.decode()
+
+
 class CompiledDesign:
     """A design compiled and uploaded once (rrtl_design)."""
 
@@ -363,6 +383,12 @@ class CompiledDesign:
         w, ms = c_uint32(), c_float()
         check(lib().rrtl_design_autotune(self.h, lanes, cycles, byref(w), byref(ms)))
         return w.value, ms.value
+
+    def word_jit(self):
+        """Compile the design's word kernel if not yet tried: (active, compile ms, reason if inactive)."""
+        act, ms = c_uint32(), c_float()
+        check(lib().rrtl_design_word_jit(self.h, byref(act), byref(ms)))
+        return bool(act.value), ms.value, ("" if act.value else lib().rrtl_last_error().decode())
 
     def memory(self, name: str):
         idx, depth, w = c_uint32(), c_uint64(), c_uint32()

@@ -89,7 +89,7 @@ def test_random_designs_match_packed_oracle(engine, seed):
     assert np.array_equal(m, rm)
 
 
-@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN])
+@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN, sim.PATH_WORD_INTERP])
 def test_pipelined_cpu_matches_oracle(engine, path):
     """8-stage pipelined CPU with per-lane random ROMs: PC/accumulator trace,
     register file and data memory bit-exact against PackedSimulator."""

@@ -1,0 +1,62 @@
+"""The compiled word kernel's emitter and its NVRTC compile, on the CPU (no
+device needed): sources compile for sm_103a and hold one statement per word
+instruction of each stream."""
+import pytest
+
+from rrtl_gb300 import sim
+from rrtl_gb300.workloads import counter, pipelined_cpu
+
+from .designs import random_word_design
+
+
+def _compile(d, top):
+    try:
+        return sim.word_jit_emit(d, top, "sm_103a")
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+
+
+def test_counter_source_shape():
+    src, cub, _ = sim.word_jit_emit(counter(), "Counter")
+    assert cub == 0
+    assert 'extern "C" __global__' in src and "rrtl_word_jit" in src
+    assert "JitLane::settle()" in src and "JitLane::edge()" in src
+    # count' = rst ? 0 : (en ? count + 1 : count): one capture, committed after the captures
+    assert src.count("c0 = (uint32_t)t;") == 1
+    assert src.rstrip().endswith("}")
+
+
+@pytest.mark.parametrize("which", ["counter", "cpu", "rand0", "rand1", "rand_mems"])
+def test_sources_compile_for_sm103a(which):
+    if which == "counter":
+        d, top = counter(), "Counter"
+    elif which == "cpu":
+        d, top = pipelined_cpu(), "Cpu8"
+    elif which == "rand_mems":
+        d, meta = random_word_design(501, n_wires=18, n_mems=10)
+        top = meta["top"]
+    else:
+        d, meta = random_word_design(int(which[-1]) + 40)
+        top = meta["top"]
+    src, cub, log = _compile(d, top)
+    assert cub > 0, log
+    assert "error" not in log.lower()
+
+
+def test_wide_values_are_outside_the_word_engine():
+    from rrtl_gb300.builder import Design, uint
+
+    d = Design()
+    m = d.module("Wide")
+    clk = m.input("clk", uint(1))
+    a = m.input("a", uint(100))
+    r = m.reg("r", uint(100))
+    m.clock(r, clk)
+    m.next(r, a)
+    o = m.output("o", uint(100))
+    m.assign(o, r)
+    with pytest.raises(sim.RrtlError) as e:
+        sim.word_jit_emit(d, "Wide")
+    assert e.value.code == "E_WORD_SCOPE" and e.value.status == 7  # RRTL_E_UNSUPPORTED
