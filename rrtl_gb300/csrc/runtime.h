@@ -137,6 +137,8 @@ cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem,
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
+// The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
+const WordJit* word_jit_get(rrtl_design* d);
 cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st);
 cudaError_t word_multi_prepare(size_t smem);
 constexpr uint32_t kWordBlockLanes = 128;

@@ -6,7 +6,9 @@
 // until it finishes) and drives rounds. A round advances every active
 // request by up to `chunk_cycles` cycles: the gate-engine requests together
 // in one launch of the persistent job-queue kernel (one item per tile and
-// chunk), the word-engine requests as one word-kernel launch each. Requests
+// chunk), the word-engine requests as one launch of their compiled kernel
+// each (side by side on a few streams) or, for designs without one,
+// together in one launch of the interpreted multi-job word kernel. Requests
 // that arrive during a round join at the next one, so new work overlaps the
 // requests already on the device. A request's results are those of the same
 // run alone on a fresh batch: every chunk continues from the state the last
@@ -32,6 +34,7 @@ using namespace rrtl;
 namespace {
 
 constexpr uint64_t kMinChunk = 8;  // adaptive chunks never fall below this many cycles
+constexpr int kJitStreams = 4;     // compiled word kernels of a round run side by side on these
 
 uint64_t now_ns() {
   return (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
@@ -57,6 +60,7 @@ struct Request {
   bool gate = false, fused = false;
   GatePrepared gp;
   WordPrepared wp;
+  const WordJit* jit = nullptr;  // the design's compiled word kernel, if any
   uint64_t done_cycles = 0;
   uint64_t chunk = 0;  // cycles of the current round
 };
@@ -88,6 +92,7 @@ struct rrtl_server {
   uint32_t max_active = 0;
   double round_ms = 0;      // target round time (0: fixed chunks)
   double ms_per_cost = 0;   // calibrated device time of one unit of tile-cycle cost
+  double ms_per_wcycle = 0; // calibrated device time of one cycle of a compiled word kernel
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::shared_ptr<Request>> pending;
@@ -103,6 +108,8 @@ struct rrtl_server {
   size_t word_smem_set = 0;
   cudaStream_t word_stream = nullptr;  // word-engine launches overlap the gate queue kernel
   cudaEvent_t staged = nullptr;        // this round's uploads and memsets are done on the context stream
+  cudaStream_t jit_stream[kJitStreams] = {};
+  cudaEvent_t jit_ev[kJitStreams][2] = {};
   // statistics (under mu)
   uint64_t rounds = 0, completed = 0, failed = 0, lane_cycles = 0, busy_ns = 0;
 
@@ -153,6 +160,7 @@ void rrtl_server::admit(std::vector<std::shared_ptr<Request>>& fresh) {
         r.fused = r.gp.fused && r.gp.v->fused_smem <= ctx->max_smem - gate_queue_static_smem();
       } else {
         r.wp = word_prepare(r.batch, r.run, false, false);
+        r.jit = word_jit_get(r.design);  // compiled once per design, on its first request
       }
       active.push_back(rp);
     } catch (const ApiError& e) {
@@ -171,6 +179,8 @@ void rrtl_server::round() {
   std::vector<GateJobDev> jobs;
   std::vector<GateItemDev> items;
   std::vector<WordJobDev> wjobs;
+  std::vector<Request*> jit_reqs;
+  std::vector<WordRunDev> jit_descs;
   uint32_t wblocks = 0;
   size_t smem = 0, wsmem = 0;
   std::vector<std::pair<double, uint32_t>> order;
@@ -208,6 +218,12 @@ void rrtl_server::round() {
         order.push_back({cost, (uint32_t)items.size()});
         items.push_back(GateItemDev{ji, t, (unsigned long long)r.done_cycles, (uint32_t)r.chunk, last ? 1u : 0u});
       }
+    } else if (r.jit) {
+      if (round_ms > 0 && ms_per_wcycle > 0)
+        r.chunk = std::min<uint64_t>(left, std::max<uint64_t>(kMinChunk, (uint64_t)(round_ms / ms_per_wcycle)));
+      const bool lastj = r.done_cycles + r.chunk == r.run.cycles;
+      jit_reqs.push_back(&r);
+      jit_descs.push_back(word_chunk_desc(r.wp, r.done_cycles, r.chunk, lastj));
     } else {
       WordJobDev wj{};
       wj.P = r.design->wdev;
@@ -219,14 +235,32 @@ void rrtl_server::round() {
       wjobs.push_back(wj);
     }
   }
+  if (!jit_reqs.empty() || !wjobs.empty()) cuda_check(cudaEventRecord(staged, st), "event");
+  // compiled word kernels: one launch per request, spread over the side streams
+  uint64_t jit_cycles[kJitStreams] = {};
+  const int n_js = std::min<int>(kJitStreams, (int)jit_reqs.size());
+  for (int k = 0; k < n_js; ++k) {
+    cuda_check(cudaStreamWaitEvent(jit_stream[k], staged, 0), "wait event");
+    cuda_check(cudaEventRecord(jit_ev[k][0], jit_stream[k]), "event");
+  }
+  for (size_t i = 0; i < jit_reqs.size(); ++i) {
+    Request& r = *jit_reqs[i];
+    const int k = (int)(i % kJitStreams);
+    WordJitPlace pl;
+    const size_t jsmem = word_jit_place(r.design->wp, *r.jit, r.design->wdev.n_sig_words, r.wp.R.lanes_pad, r.chunk,
+                                        ctx->sm_count, ctx->max_smem, ctx->max_smem_sm, &pl);
+    cuda_check(launch_word_jit(*r.jit, jit_descs[i], pl, jsmem, jit_stream[k]), "rrtl_word_jit");
+    jit_cycles[k] += r.chunk;
+  }
+  for (int k = 0; k < n_js; ++k) cuda_check(cudaEventRecord(jit_ev[k][1], jit_stream[k]), "event");
   if (!wjobs.empty()) {
-    // one launch for every word-engine request, on the second stream, after this round's staging
+    // one launch for every interpreted word-engine request, on the second stream, after this round's staging
     if (wsmem > word_smem_set) {
       cuda_check(word_multi_prepare(kWordSmemLimit), "word_multi_prepare");
       word_smem_set = kWordSmemLimit;
     }
     upload(d_wjobs, wjobs);
-    cuda_check(cudaEventRecord(staged, st), "event");
+    cuda_check(cudaEventRecord(staged, st), "event");  // after the job table upload
     cuda_check(cudaStreamWaitEvent(word_stream, staged, 0), "wait event");
     cuda_check(launch_word_multi(d_wjobs.as<WordJobDev>(), (uint32_t)wjobs.size(), wblocks, wsmem, word_stream),
                "word_multi_kernel");
@@ -259,6 +293,14 @@ void rrtl_server::round() {
   cuda_check(cudaStreamSynchronize(st), "sync");
   const uint64_t t_gate = now_ns();
   cuda_check(cudaStreamSynchronize(word_stream), "sync");
+  double wcyc = 0;
+  for (int k = 0; k < n_js; ++k) {
+    cuda_check(cudaEventSynchronize(jit_ev[k][1]), "sync");
+    float ms = 0;
+    cuda_check(cudaEventElapsedTime(&ms, jit_ev[k][0], jit_ev[k][1]), "elapsed");
+    if (jit_cycles[k]) wcyc = std::max(wcyc, (double)ms / (double)jit_cycles[k]);
+  }
+  if (wcyc > 0) ms_per_wcycle = ms_per_wcycle > 0 ? 0.7 * ms_per_wcycle + 0.3 * wcyc : wcyc;
   if (crit > 0 && !items.empty()) {
     // calibrate: the round's gate part took about its critical cost
     const double m = (double)(t_gate - t0) / 1e6 / crit;
@@ -297,8 +339,12 @@ void rrtl_server::round() {
 
 void rrtl_server::loop() {
   cudaSetDevice(ctx->device);
-  if (cudaStreamCreateWithFlags(&word_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&staged, cudaEventDisableTiming) != cudaSuccess) {
+  bool streams_ok = cudaStreamCreateWithFlags(&word_stream, cudaStreamNonBlocking) == cudaSuccess &&
+                    cudaEventCreateWithFlags(&staged, cudaEventDisableTiming) == cudaSuccess;
+  for (int k = 0; k < kJitStreams && streams_ok; ++k)
+    streams_ok = cudaStreamCreateWithFlags(&jit_stream[k], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreate(&jit_ev[k][0]) == cudaSuccess && cudaEventCreate(&jit_ev[k][1]) == cudaSuccess;
+  if (!streams_ok) {
     // without its streams the loop cannot run: fail every request as it arrives
     for (;;) {
       std::unique_lock<std::mutex> lk(mu);
@@ -324,6 +370,11 @@ void rrtl_server::loop() {
       lk.unlock();
       cudaEventDestroy(staged);
       cudaStreamDestroy(word_stream);
+      for (int k = 0; k < kJitStreams; ++k) {
+        cudaStreamDestroy(jit_stream[k]);
+        cudaEventDestroy(jit_ev[k][0]);
+        cudaEventDestroy(jit_ev[k][1]);
+      }
       return;
     }
       // admission: first come first served while the device memory budget and the slot count allow

@@ -47,7 +47,11 @@ struct Emitter {
   const WordProgram& wp;
   std::string o;
 
-  explicit Emitter(const WordProgram& w) : wp(w) {}
+  const bool regs;  // signal words as register members s<k>
+
+  explicit Emitter(const WordProgram& w) : wp(w), regs(w.n_sig_words <= kJitRegSignals) {}
+
+  std::string sig(uint32_t off) const { return regs ? "s" + std::to_string(off) : "SV(" + u(off) + ")"; }
 
   static std::string V(uint32_t s) { return "v" + std::to_string(s); }
 
@@ -55,12 +59,12 @@ struct Emitter {
     if (k < kJitPlacedMems) return "MK(" + u(k) + ", " + w + ")";
     return "MG((size_t)" + u(wp.mems[k].offset) + " + " + w + ")";
   }
-  static std::string reset(uint32_t off, bool low) {
-    return std::string("(((SV(") + u(off) + ") & 1u) != 0u) != " + (low ? "true" : "false") + ")";
+  std::string reset(uint32_t off, bool low) const {
+    return "(((" + sig(off) + " & 1u) != 0u) != " + (low ? "true" : "false") + ")";
   }
-  static std::string store(uint32_t off, bool two, const std::string& t) {
-    std::string s = "SV(" + u(off) + ") = (uint32_t)" + t + ";";
-    if (two) s += " SV(" + u(off + 1) + ") = (uint32_t)(" + t + " >> 32);";
+  std::string store(uint32_t off, bool two, const std::string& t) const {
+    std::string s = sig(off) + " = (uint32_t)" + t + ";";
+    if (two) s += " " + sig(off + 1) + " = (uint32_t)(" + t + " >> 32);";
     return s;
   }
 
@@ -70,8 +74,89 @@ struct Emitter {
     o += '\n';
   }
 
+  // Bit width bound of each slot's current value within the block being
+  // emitted (every result is masked to its width, compares give 1 bit).
+  std::vector<uint32_t> vw;
+
+  uint32_t W(uint32_t s) const { return s < vw.size() ? vw[s] : 64u; }
+
+  void define(const WInstr& I) {
+    uint32_t w = 0;
+    switch (I.op) {
+      case W_STORE:
+      case W_ASTORE:
+      case W_CAPTURE:
+      case W_MEMWR: return;
+      case W_EQ:
+      case W_NE:
+      case W_LT:
+      case W_LTS: w = 1; break;
+      case W_MEMRD: w = std::min<uint32_t>(I.width, wp.mems[I.aux].width); break;
+      default: w = I.width; break;
+    }
+    if (I.dst >= vw.size()) vw.resize(I.dst + 1, 64u);
+    vw[I.dst] = std::min<uint32_t>(w, 64u);
+  }
+
+  // 32-bit form of an instruction whose result (and every operand bit it
+  // depends on) fits 32 bits: the low k bits of a sum, difference, product or
+  // bitwise result depend only on the operands' low k bits. Empty when the
+  // 64-bit form is needed.
+  std::string narrow(const WInstr& I) const {
+    if (I.width > 32) return "";
+    const std::string M = hex(wmask(I.width)).substr(0, hex(wmask(I.width)).size() - 3) + "u";
+    auto n = [](uint32_t s) { return "(uint32_t)" + V(s); };
+    const std::string d = V(I.dst) + " = (u64)(uint32_t)(";
+    switch (I.op) {
+      case W_NOT: return d + "~" + n(I.a) + " & " + M + ");";
+      case W_AND: return d + "(" + n(I.a) + " & " + n(I.b) + ") & " + M + ");";
+      case W_OR: return d + "(" + n(I.a) + " | " + n(I.b) + ") & " + M + ");";
+      case W_XOR: return d + "(" + n(I.a) + " ^ " + n(I.b) + ") & " + M + ");";
+      case W_ADD: return d + "(" + n(I.a) + " + " + n(I.b) + ") & " + M + ");";
+      case W_SUB: return d + "(" + n(I.a) + " - " + n(I.b) + ") & " + M + ");";
+      case W_MUL: return d + "(" + n(I.a) + " * " + n(I.b) + ") & " + M + ");";
+      case W_MUX: return d + "((" + n(I.a) + " & 1u) ? " + n(I.b) + " : " + n(I.c) + ") & " + M + ");";
+      case W_MASK: return d + n(I.a) + " & " + M + ");";
+      case W_EQ:
+      case W_NE:
+        if (W(I.a) > 32 || W(I.b) > 32) return "";
+        return d + n(I.a) + (I.op == W_EQ ? " == " : " != ") + n(I.b) + ");";
+      case W_LT: {
+        if (I.aux > 32) return "";
+        const std::string om = hex(wmask(I.aux)).substr(0, hex(wmask(I.aux)).size() - 3) + "u";
+        return d + "(" + n(I.a) + " & " + om + ") < (" + n(I.b) + " & " + om + "));";
+      }
+      case W_LTS: {
+        if (I.aux == 0 || I.aux > 32) return "";
+        const std::string om = hex(wmask(I.aux)).substr(0, hex(wmask(I.aux)).size() - 3) + "u";
+        const std::string sb = u(1u << (I.aux - 1u));
+        return "{ const uint32_t x = " + n(I.a) + " & " + om + ", y = " + n(I.b) + " & " + om +
+               "; const bool xs = (x & " + sb + ") != 0u, ys = (y & " + sb + ") != 0u; " + V(I.dst) +
+               " = (xs != ys) ? (u64)xs : (u64)(x < y); }";
+      }
+      case W_SLICE:
+        if (I.aux >= 64u || I.aux + I.width > 32) return "";
+        return d + "(" + n(I.a) + " >> " + u(I.aux) + ") & " + M + ");";
+      case W_SEXT: {
+        if (I.aux == 0 || I.aux > 32) return "";
+        const unsigned long long wm = wmask(I.aux);
+        const std::string wms = u((uint32_t)wm), nwm = u((uint32_t)~wm);
+        return "{ const uint32_t x = " + n(I.a) + " & " + wms + "; " + V(I.dst) + " = (u64)(uint32_t)((((x >> " +
+               u(I.aux - 1u) + ") & 1u) ? (x | " + nwm + ") : x) & " + M + "); }";
+      }
+      case W_CAT:
+        if (I.aux >= 32u) return d + n(I.b) + " & " + M + ");";
+        return d + "((" + n(I.a) + " << " + u(I.aux) + ") | " + n(I.b) + ") & " + M + ");";
+      default: return "";
+    }
+  }
+
   // Statement for one instruction (empty for opcodes the interpreter skips).
   std::string stmt(const WInstr& I) const {
+    {
+      std::string s = narrow(I);
+      if (!s.empty()) return s;
+    }
     const unsigned long long m = wmask(I.width);
     const std::string M = hex(m);
     const std::string d = V(I.dst), a = V(I.a), b = V(I.b), c = V(I.c);
@@ -79,8 +164,8 @@ struct Emitter {
     switch (I.op) {
       case W_LIT: return d + " = " + hex(wp.lits[I.aux] & m) + ";";
       case W_SIG: {
-        std::string s = "(u64)SV(" + u(I.aux) + ")";
-        if (two) s = "(" + s + " | ((u64)SV(" + u(I.aux + 1) + ") << 32))";
+        std::string s = "(u64)" + sig(I.aux);
+        if (two) s = "(" + s + " | ((u64)" + sig(I.aux + 1) + " << 32))";
         return d + " = " + s + " & " + M + ";";
       }
       case W_NOT: return d + " = ~" + a + " & " + M + ";";
@@ -186,9 +271,11 @@ struct Emitter {
       }
       line(decl + ";");
     }
+    vw.assign(slots.empty() ? 0 : *slots.rbegin() + 1, 64u);
     for (uint32_t pc = b; pc < e; ++pc) {
       std::string s = stmt(wp.code[pc]);
       if (!s.empty()) line(s);
+      define(wp.code[pc]);
     }
     o += "  }\n";
   }
@@ -200,6 +287,25 @@ struct Emitter {
     o += "namespace rrtl {\n";
     o += "typedef unsigned long long u64;\n";
     o += "struct JitLane : JitLaneBase {\n";
+    if (regs && wp.n_sig_words) {
+      const uint32_t n = wp.n_sig_words;
+      o += "  static constexpr bool kRegSignals = true;\n";
+      std::string decl = "  uint32_t";
+      for (uint32_t k = 0; k < n; ++k) decl += (k ? ", s" : " s") + std::to_string(k);
+      o += decl + ";\n";
+      o += "  __device__ __forceinline__ uint32_t get(uint32_t off) const {\n    switch (off) {\n";
+      for (uint32_t k = 0; k < n; ++k) o += "      case " + u(k) + ": return s" + std::to_string(k) + ";\n";
+      o += "      default: return 0u;\n    }\n  }\n";
+      o += "  __device__ __forceinline__ void set(uint32_t off, uint32_t v) {\n    switch (off) {\n";
+      for (uint32_t k = 0; k < n; ++k) o += "      case " + u(k) + ": s" + std::to_string(k) + " = v; break;\n";
+      o += "      default: break;\n    }\n  }\n";
+      o += "  __device__ __forceinline__ void load(const uint32_t* g, size_t lp) {\n";
+      for (uint32_t k = 0; k < n; ++k) o += "    s" + std::to_string(k) + " = g[" + u(k) + " * lp];\n";
+      o += "  }\n";
+      o += "  __device__ __forceinline__ void store(uint32_t* g, size_t lp) const {\n";
+      for (uint32_t k = 0; k < n; ++k) o += "    g[" + u(k) + " * lp] = s" + std::to_string(k) + ";\n";
+      o += "  }\n";
+    }
     o += "  __device__ void settle();\n";
     o += "  __device__ void edge();\n";
     o += "};\n";
@@ -217,7 +323,7 @@ struct Emitter {
     block(wp.commit_b, wp.commit_e, "tick_commit: memory writes");
     for (const WCommitDev& cm : wp.commits)
       for (uint32_t l = 0; l < cm.limbs; ++l)
-        o += "  SV(" + u(cm.sig_off + l) + ") = c" + std::to_string(cm.cap_off + l) + ";\n";
+        o += "  " + sig(cm.sig_off + l) + " = c" + std::to_string(cm.cap_off + l) + ";\n";
     o += "}\n";
     o += "}  // namespace rrtl\n";
     o += "extern \"C\" __global__ void __launch_bounds__(128) rrtl_word_jit(const rrtl::WordRunDev R, "
@@ -318,6 +424,7 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
 void word_jit_build(const WordProgram& wp, int device, WordJit* J) {
   const auto t0 = std::chrono::steady_clock::now();
   J->written.assign(wp.mems.size(), 0);
+  J->reg_signals = wp.n_sig_words <= kJitRegSignals;
   for (const WInstr& I : wp.code)
     if (I.op == W_MEMWR && I.aux < J->written.size()) J->written[I.aux] = 1;
   if (wp.code.size() > kJitMaxInstrs) {
@@ -340,9 +447,13 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J) {
   }
   cudaError_t e = cudaLibraryLoadData(&J->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
   if (e == cudaSuccess) e = cudaLibraryGetKernel(&J->fn, J->lib, "rrtl_word_jit");
-  if (e == cudaSuccess)
+  cudaFuncAttributes fa{};
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(J->fn));
+  if (e == cudaSuccess) {
+    J->static_smem = fa.sharedSizeBytes;
     e = cudaFuncSetAttribute(reinterpret_cast<const void*>(J->fn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)prop.sharedMemPerBlockOptin);
+                             (int)(prop.sharedMemPerBlockOptin - fa.sharedSizeBytes));
+  }
   if (e != cudaSuccess) {
     cudaGetLastError();
     J->error = std::string("loading the compiled kernel: ") + cudaGetErrorString(e);
@@ -363,12 +474,12 @@ size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_wo
   // shared memory between them (one block's rows sit idle otherwise)
   const uint32_t blocks = lanes_pad / kThreads;
   const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(4, (blocks + sm_count - 1) / std::max<uint32_t>(sm_count, 1)));
-  const size_t budget = std::min(max_smem_block, max_smem_sm / per_sm - 1024);
+  const size_t budget = std::min(max_smem_block, max_smem_sm / per_sm - 1024) - J.static_smem;
   // staging costs one pass over the rows at each end of the launch: worth it
   // when the launch runs a few cycles per staged row
   auto worth = [&](uint64_t rows) { return rows <= 64 || rows <= 4 * cycles; };
   size_t used = 0;
-  if (n_sig_words && (size_t)n_sig_words * kRowBytes <= budget && worth(n_sig_words)) {
+  if (!J.reg_signals && n_sig_words && (size_t)n_sig_words * kRowBytes <= budget && worth(n_sig_words)) {
     P.sig_smem = 1;
     used = (size_t)n_sig_words * kRowBytes;
   }

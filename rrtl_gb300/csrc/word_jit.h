@@ -27,12 +27,16 @@ struct WordJit {
   std::string error;     // why there is no compiled kernel (empty when ok)
   double compile_ms = 0; // emit + NVRTC + load
   size_t source_bytes = 0;
+  size_t static_smem = 0;        // the kernel's static shared memory (stimulus/record tables)
+  bool reg_signals = false;      // signal words live in registers (no signal staging)
   std::vector<uint8_t> written;  // per memory: the design writes it
   ~WordJit();
 };
 
 // Largest word program that is compiled (bigger ones run interpreted).
 constexpr size_t kJitMaxInstrs = 20000;
+// Designs with at most this many signal words keep them in registers.
+constexpr uint32_t kJitRegSignals = 256;
 
 // CUDA C++ source of a word program's compiled kernel `rrtl_word_jit`.
 std::string word_jit_source(const WordProgram& wp);

@@ -36,6 +36,8 @@ struct WordLane {
 
   __device__ unsigned long long& V(uint32_t s) const { return vbase[(size_t)s * vstride]; }
   __device__ uint32_t& SV(uint32_t off) const { return sv[(size_t)off * svs]; }
+  __device__ uint32_t get(uint32_t off) const { return SV(off); }
+  __device__ void set(uint32_t off, uint32_t v) const { SV(off) = v; }
 
   __device__ unsigned long long load_sig(uint32_t off, bool two) const {
     unsigned long long v = SV(off);
@@ -164,7 +166,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
              sig_smem ? ssm : R.values + lane, sig_smem ? (size_t)blockDim.x : (size_t)R.lanes_pad};
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) ssm[(size_t)w * blockDim.x] = R.values[(size_t)w * R.lanes_pad + lane];
-  word_lane_cycles(R, lane, W);
+  word_lane_cycles(R, lane, W, R.stim, R.rec);
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = ssm[(size_t)w * blockDim.x];
 }

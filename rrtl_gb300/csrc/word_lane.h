@@ -10,9 +10,12 @@
 // (inputs, settle, check, tick: crates/rrtl-sim-ir/src/lib.rs:9540-9568).
 //
 // An engine type L provides
-//   uint32_t& SV(uint32_t word)  one signal word of the lane
+//   uint32_t get(uint32_t word), set(uint32_t word, uint32_t v)
+//                                one signal word of the lane
 //   void settle()                comb stream, then the async-reset stream
 //   void edge()                  tick_next, tick_commit, register commit
+// and the run's stimulus and record tables come in as ST and RT (R.stim and
+// R.rec, or copies of them in shared memory).
 //
 // The header is also compiled at run time by NVRTC, so it includes only
 // headers that are handed to NVRTC with it.
@@ -28,7 +31,8 @@
 namespace rrtl {
 
 template <class L>
-__device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t lane, L& W) {
+__device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t lane, L& W, const WordStimDev* ST,
+                                                 const WordRecDev* RT) {
   const bool live = lane < R.lanes;
   // a lane detected by an earlier launch of the same run stays detected
   bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
@@ -36,7 +40,7 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
   for (unsigned long long c = 0; c < R.cycles; ++c) {
     const unsigned long long ca = R.cycle_base + c;
     for (uint32_t k = 0; k < R.n_stim; ++k) {
-      const WordStimDev s = R.stim[k];
+      const WordStimDev s = ST[k];
       if (s.kind == RRTL_STIM_HOLD) continue;
       for (uint32_t l = 0; l < s.limbs; ++l) {
         uint32_t v = 0;
@@ -46,7 +50,7 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
         else if (s.kind == RRTL_STIM_TRACE)
           v = live ? R.in_trace[((size_t)c * R.n_trace_cols + s.param + l) * R.lanes + lane] : 0u;
         if (l + 1 == s.limbs && (s.width & 31u)) v &= (1u << (s.width & 31u)) - 1u;
-        W.SV(s.sig_off + l) = v;
+        W.set(s.sig_off + l, v);
       }
     }
     W.settle();
@@ -54,9 +58,9 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
       unsigned long long h = 0ull;
       bool diff = false;
       for (uint32_t k = 0; k < R.n_rec; ++k) {
-        const WordRecDev rc = R.rec[k];
+        const WordRecDev rc = RT[k];
         for (uint32_t l = 0; l < rc.limbs; ++l) {
-          uint32_t v = W.SV(rc.sig_off + l);
+          uint32_t v = W.get(rc.sig_off + l);
           if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
           if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
           if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
@@ -93,32 +97,51 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
 
 // ---- per-design compiled kernels
 //
-// A compiled lane keeps its value slots in registers; signal words and the
-// memories listed in WordJitPlace are staged in shared memory for the launch
-// ([word][thread], so any per-lane address is bank-conflict free), the other
-// memories stay word-major in HBM.
+// A compiled lane keeps its value slots in registers. Its signal words are
+// registers too (kRegSignals: the generated lane type holds them as members
+// and reaches them by a switch when the stimulus or record table names one
+// at run time) or, for designs with many signal words, rows of shared memory
+// or HBM through sv/svs. Memories listed in WordJitPlace are staged in shared
+// memory for the launch ([word][thread], so any per-lane address is bank
+// conflict free); the others stay word-major in HBM.
 struct JitLaneBase {
-  uint32_t* sv;                     // signal word 0 of this lane
+  static constexpr bool kRegSignals = false;
+  uint32_t* sv;                     // signal word 0 of this lane (kRegSignals false)
   size_t svs;                       // signal word stride
   uint32_t* mb[kJitPlacedMems];     // word 0 of memory k for this lane
   size_t ms[kJitPlacedMems];        // its word stride
   uint32_t* gm;                     // R.mems + lane (memories past kJitPlacedMems)
   size_t LP;                        // lanes_pad
   __device__ __forceinline__ uint32_t& SV(uint32_t off) const { return sv[(size_t)off * svs]; }
+  __device__ __forceinline__ uint32_t get(uint32_t off) const { return SV(off); }
+  __device__ __forceinline__ void set(uint32_t off, uint32_t v) const { SV(off) = v; }
   __device__ __forceinline__ uint32_t& MK(uint32_t k, size_t w) const { return mb[k][w * ms[k]]; }
   __device__ __forceinline__ uint32_t& MG(size_t w) const { return gm[w * LP]; }
 };
 
+// Stimulus and record tables of up to this many entries are copied to
+// shared memory for the launch.
+constexpr uint32_t kJitTableEntries = 64;
+
 // Kernel body of a compiled design: stage in, run the cycles, stage out.
 template <class L>
 __device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitPlace& Pl, uint32_t* jsm) {
+  __shared__ WordStimDev s_stim[kJitTableEntries];
+  __shared__ WordRecDev s_rec[kJitTableEntries];
   const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t T = blockDim.x;
   uint32_t* my = jsm + threadIdx.x;
+  const bool st_smem = R.n_stim <= kJitTableEntries, rt_smem = R.n_rec <= kJitTableEntries;
+  if (st_smem)
+    for (uint32_t i = threadIdx.x; i < R.n_stim; i += T) s_stim[i] = R.stim[i];
+  if (rt_smem)
+    for (uint32_t i = threadIdx.x; i < R.n_rec; i += T) s_rec[i] = R.rec[i];
   L W;
   W.LP = R.lanes_pad;
   W.gm = R.mems + lane;
-  if (Pl.sig_smem) {
+  if constexpr (L::kRegSignals) {
+    W.load(R.values + lane, R.lanes_pad);
+  } else if (Pl.sig_smem) {
     W.sv = my;
     W.svs = T;
     for (uint32_t w = 0; w < Pl.n_sig_words; ++w) my[(size_t)w * T] = R.values[(size_t)w * R.lanes_pad + lane];
@@ -140,9 +163,13 @@ __device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitP
       W.ms[k] = R.lanes_pad;
     }
   }
-  word_lane_cycles(R, lane, W);
-  if (Pl.sig_smem)
+  __syncthreads();  // the tables are in place
+  word_lane_cycles(R, lane, W, st_smem ? s_stim : R.stim, rt_smem ? s_rec : R.rec);
+  if constexpr (L::kRegSignals) {
+    W.store(R.values + lane, R.lanes_pad);
+  } else if (Pl.sig_smem) {
     for (uint32_t w = 0; w < Pl.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = my[(size_t)w * T];
+  }
 #pragma unroll
   for (uint32_t k = 0; k < kJitPlacedMems; ++k) {
     if (k >= Pl.n_mems) break;

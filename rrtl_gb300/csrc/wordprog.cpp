@@ -350,6 +350,7 @@ WordProgram build_word_program(const MachineProgram& mp) {
   E.emit_items(E.reference_order(mp.tick_commit), mp.tick_commit);
   wp.commit_e = (uint32_t)wp.code.size();
   wp.total_capture_words = E.cap_words;
+  wp.n_sig_words = (uint32_t)P.total_signal_words;
   if (wp.lits.empty()) wp.lits.push_back(0);
   return wp;
 }

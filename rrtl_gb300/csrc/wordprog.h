@@ -31,6 +31,7 @@ struct WordProgram {
   std::vector<WCommitDev> commits;
   uint32_t n_vslots = 0;
   uint32_t total_capture_words = 0;
+  uint32_t n_sig_words = 0;  // signal value words per lane
   uint64_t source_instrs = 0;
 };
 
