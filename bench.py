@@ -401,7 +401,7 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
     return out
 
 
-def word_configs_leg(ctx, sim):
+def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True):
     """The word-engine configs: the README Counter (1,024 lanes x 10,000
     cycles, full output trace recorded) and the 8-stage pipelined CPU
     (16,384 lanes x 20,000 cycles, per-lane hashed ROMs). The fused path runs
@@ -409,14 +409,14 @@ def word_configs_leg(ctx, sim):
     interpreted word kernel (whole run, one launch) and on the plain
     one-launch-per-cycle path (200 cycles of the same batch shape), and the
     CPU's per-cycle hashes are compared across the three."""
-    from rrtl_gb300.workloads import counter, cpu_rom_hashed, pipelined_cpu
+    from rrtl_gb300.workloads import counter as counter_design, cpu_rom_hashed, pipelined_cpu
 
     out = {}
-    cd = sim.CompiledDesign(counter(), "Counter", ctx)
+    cd = sim.CompiledDesign(counter_design(), "Counter", ctx)
     jit, jit_ms, why = cd.word_jit()
     stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 1)]
     for path, cyc, key in ((sim.PATH_FUSED, 10_000, "value"), (sim.PATH_WORD_INTERP, 10_000, "interpreted"),
-                           (sim.PATH_PLAIN, 200, "plain")):
+                           (sim.PATH_PLAIN, 200, "plain"))[:3 if counter else 0]:
         g = sim.GpuBatchSimulator(cd, lanes=1024)
         g.set_path(path)
         g.run(cyc, seed=1, stim=stim, record=["out"], mode=sim.REC_TRACE)
@@ -432,16 +432,17 @@ def word_configs_leg(ctx, sim):
     stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
     rom = cpu_rom_hashed(16384, seed=3)
     res = {}
-    for path, cyc in ((sim.PATH_FUSED, 20_000), (sim.PATH_WORD_INTERP, 2_000), (sim.PATH_PLAIN, 200)):
+    for path, cyc in ((sim.PATH_FUSED, cpu8_cycles), (sim.PATH_WORD_INTERP, 2_000), (sim.PATH_PLAIN, 200)):
         g = sim.GpuBatchSimulator(cd, lanes=16384)
         g.set_path(path)
         g.set_memory_limbs("rom", rom)
         r = g.run(cyc, stim=stim, record=["out_pc", "out_acc"], mode=sim.REC_HASH)
         res[path] = (1.0e3 * 16384 * cyc / g.last_kernel_ms, r["hash"], g)
     h = res[sim.PATH_FUSED][1]
-    same = bool(np.array_equal(h[:200], res[sim.PATH_PLAIN][1]) and
-                np.array_equal(h[:2000], res[sim.PATH_WORD_INTERP][1]))
-    out["cpu8"] = {"lanes": 16384, "cycles": 20_000, "value": res[sim.PATH_FUSED][0], "unit": "lane-cycles/s",
+    n = min(2000, cpu8_cycles)
+    same = bool(np.array_equal(h[:200], res[sim.PATH_PLAIN][1][:200]) and
+                np.array_equal(h[:n], res[sim.PATH_WORD_INTERP][1][:n]))
+    out["cpu8"] = {"lanes": 16384, "cycles": cpu8_cycles, "value": res[sim.PATH_FUSED][0], "unit": "lane-cycles/s",
                    "interpreted": res[sim.PATH_WORD_INTERP][0], "interpreted_cycles": 2_000,
                    "plain": res[sim.PATH_PLAIN][0], "hash_prefix_equal_all_paths": same, "compiled": jit,
                    "compile_ms": jit_ms,
@@ -507,6 +508,10 @@ def main():
     ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
     ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
+    ap.add_argument("--word-only", action="store_true",
+                    help="profiling case: only the pipelined-CPU word config (its compiled run is the second "
+                         "rrtl_word_jit launch, after the batch's creation settle)")
+    ap.add_argument("--cpu8-cycles", type=int, default=20_000, help="cycles of the pipelined-CPU compiled run")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
     args.warmup = max(args.warmup, 3)
@@ -521,6 +526,11 @@ def main():
 
     from rrtl_gb300 import sim
 
+    if args.word_only:
+        ctx = sim.Context(local)
+        if rank == 0:
+            print(json.dumps({"word_configs": word_configs_leg(ctx, sim, args.cpu8_cycles, counter=False)}))
+        return
     d, meta, js, stim, rec = build_workload()
     ctx = sim.Context(local)
     cd = sim.CompiledDesign(js, meta.top, ctx)
@@ -628,7 +638,7 @@ def main():
         "clocks": clocks.summary(),
     }
     if not args.no_word_configs:
-        out["word_configs"] = word_configs_leg(ctx, sim)
+        out["word_configs"] = word_configs_leg(ctx, sim, args.cpu8_cycles)
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:
