@@ -413,14 +413,19 @@ rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* design, uint32_t* values, u
 rrtl_status rrtl_design_word_jit(rrtl_design* design, uint32_t* active, float* compile_ms);
 
 /* Emit (and, when arch is not NULL, e.g. "sm_103a", compile) the compiled
- * word kernel of a design without a device: for tests and inspection.
+ * word kernel of a design without a device: for tests and inspection. With
+ * run NULL the kernel serves any run; otherwise it is the kernel compiled for
+ * that run's stimulus table, record table and record mode (the fused path
+ * builds one per distinct set of tables, up to 64 per design, and runs with
+ * more than 64 stimulus or record entries use the general one).
  * source: buffer of source_cap bytes for the NUL-terminated CUDA source (may
  * be NULL); *source_len its length. *cubin_bytes the compiled image's size
  * (0 when not compiled); log (may be NULL) the compiler's messages.
  * RRTL_E_UNSUPPORTED when the design is outside the word engine's scope
  * (values over 64 bits) or the compiler fails. */
-rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const char* arch, char* source,
-                               size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log, size_t log_cap);
+rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
+                               char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
+                               size_t log_cap);
 
 #ifdef __cplusplus
 }

@@ -587,6 +587,9 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
           "E_GPU_RECORD: recording needs at least one signal");
   upload(b->d_stim, stim);
   upload(b->d_rec, rec);
+  g.tables.stim = stim;
+  g.tables.rec = rec;
+  g.tables.mode = run.record_mode;
   WordRunDev& R = g.R;
   R.cycles = run.cycles;
   R.seed = run.seed;
@@ -699,6 +702,22 @@ const WordJit* word_jit_get(rrtl_design* d) {
   return d->wjit->ok ? d->wjit.get() : nullptr;
 }
 
+const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t) {
+  const WordJit* any = word_jit_get(d);
+  const char* env = getenv("RRTL_WORD_JIT_RUNS");
+  if (!any || (env && env[0] == '0') || t.stim.size() > kJitRunTableMax || t.rec.size() > kJitRunTableMax) return any;
+  const std::string key = t.key();
+  std::lock_guard<std::mutex> lk(d->wjit_mu);
+  auto it = d->wjit_runs.find(key);
+  if (it == d->wjit_runs.end()) {
+    if (d->wjit_runs.size() >= kJitRunKernelsPerDesign) return any;
+    auto J = std::make_unique<WordJit>();
+    word_jit_build(d->wp, d->ctx->device, J.get(), &t);
+    it = d->wjit_runs.emplace(key, std::move(J)).first;
+  }
+  return it->second->ok ? it->second.get() : any;
+}
+
 void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle,
               const CheckTables* chk = nullptr) {
   rrtl_design* d = b->d;
@@ -708,7 +727,7 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   g.R.final_settle = final_settle;
   const bool per_cycle = (b->path == RRTL_PATH_PLAIN || b->path == RRTL_PATH_PLAIN_GRAPH) && run.cycles > 1;
   // compile before the timed region opens
-  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_get(d) : nullptr;
+  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables) : nullptr;
   Timer tm(b);
   if (per_cycle) {
     // one launch per cycle: the baseline path (captured into a CUDA graph on RRTL_PATH_PLAIN_GRAPH)
@@ -1173,8 +1192,9 @@ rrtl_status rrtl_design_word_jit(rrtl_design* d, uint32_t* active, float* compil
   return st;
 }
 
-rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const char* arch, char* source,
-                               size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log, size_t log_cap) {
+rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
+                               char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
+                               size_t log_cap) {
   return guard([&] {
     REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
     if (cubin_bytes) *cubin_bytes = 0;
@@ -1187,7 +1207,27 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
     } catch (const RrtlError& e) {
       fail(RRTL_E_UNSUPPORTED, e.what());
     }
-    const std::string src = word_jit_source(wp);
+    WordRunTables tabs;
+    if (run) {
+      const PackedProgram& P = mp.source;
+      auto sig = [&](uint32_t i) -> const PackedSignal& {
+        REQUIRE(i < P.signals.size(), RRTL_E_SIGNAL, "E_GPU_SIGNAL: signal index out of range");
+        return P.signals[i];
+      };
+      for (uint32_t i = 0; i < run->n_stim; ++i) {
+        const PackedSignal& ps = sig(run->stim[i].signal);
+        tabs.stim.push_back(WordStimDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, run->stim[i].kind,
+                                        run->stim[i].param});
+      }
+      uint32_t base = 0;
+      for (uint32_t i = 0; i < run->n_record; ++i) {
+        const PackedSignal& ps = sig(run->record[i]);
+        tabs.rec.push_back(WordRecDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, base});
+        base += ps.layout.limbs;
+      }
+      tabs.mode = run->record_mode;
+    }
+    const std::string src = word_jit_source(wp, run ? &tabs : nullptr);
     if (source_len) *source_len = src.size();
     if (source && source_cap) {
       const size_t n = std::min(source_cap - 1, src.size());

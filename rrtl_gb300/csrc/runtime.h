@@ -82,6 +82,7 @@ struct GatePrepared {
 // A word-engine run made ready for chunked launches.
 struct WordPrepared {
   WordRunDev R{};
+  WordRunTables tables;  // host copies of the run's stimulus and record tables
   bool smem_slots = false;
   uint32_t rec_limbs = 0;
   size_t trace_out_bytes = 0, hash_bytes = 0, det_bytes = 0;
@@ -139,6 +140,9 @@ void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
 // The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
 const WordJit* word_jit_get(rrtl_design* d);
+// The kernel compiled for this run's tables (built on first use and kept per
+// design), else the design's general compiled kernel, else nullptr.
+const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t);
 cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st);
 cudaError_t word_multi_prepare(size_t smem);
 constexpr uint32_t kWordBlockLanes = 128;
@@ -179,7 +183,8 @@ struct rrtl_design {
   rrtl::WordProgDev wdev{};
   rrtl::DevBuf d_wcode, d_wcap, d_wlit;
   std::mutex wjit_mu;
-  std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel, built on the first fused run
+  std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel for any run, built on the first fused run
+  std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;  // kernels compiled for one run's tables
 };
 
 struct rrtl_batch {

@@ -45,6 +45,7 @@ std::string u(uint64_t v) { return std::to_string(v) + "u"; }
 
 struct Emitter {
   const WordProgram& wp;
+  const WordRunTables* run = nullptr;
   std::string o;
 
   const bool regs;  // signal words as register members s<k>
@@ -326,10 +327,39 @@ struct Emitter {
         o += "  " + sig(cm.sig_off + l) + " = c" + std::to_string(cm.cap_off + l) + ";\n";
     o += "}\n";
     o += "}  // namespace rrtl\n";
+    if (run) {
+      // this run's tables as compile-time constants
+      o += "namespace rrtl {\n";
+      o += "struct RunSpec {\n";
+      o += "  __device__ __forceinline__ static constexpr uint32_t n_stim() { return " + u(run->stim.size()) + "; }\n";
+      o += "  __device__ __forceinline__ static constexpr WordStimDev stim(uint32_t k) {\n    switch (k) {\n";
+      for (size_t k = 0; k < run->stim.size(); ++k) {
+        const WordStimDev& t = run->stim[k];
+        o += "      case " + u(k) + ": return WordStimDev{" + u(t.sig_off) + ", " + u(t.limbs) + ", " + u(t.width) + ", " +
+             u(t.kind) + ", " + hex(t.param) + "};\n";
+      }
+      o += "      default: return WordStimDev{0u, 0u, 0u, 0u, 0ull};\n    }\n  }\n";
+      o += "  __device__ __forceinline__ static constexpr uint32_t n_rec() { return " + u(run->rec.size()) + "; }\n";
+      o += "  __device__ __forceinline__ static constexpr WordRecDev rec(uint32_t k) {\n    switch (k) {\n";
+      for (size_t k = 0; k < run->rec.size(); ++k) {
+        const WordRecDev& t = run->rec[k];
+        o += "      case " + u(k) + ": return WordRecDev{" + u(t.sig_off) + ", " + u(t.limbs) + ", " + u(t.width) + ", " +
+             u(t.base) + "};\n";
+      }
+      o += "      default: return WordRecDev{0u, 0u, 0u, 0u};\n    }\n  }\n";
+      o += "  __device__ __forceinline__ static constexpr uint32_t mode() { return " + u(run->mode) + "; }\n";
+      o += "};\n}  // namespace rrtl\n";
+    }
     o += "extern \"C\" __global__ void __launch_bounds__(128) rrtl_word_jit(const rrtl::WordRunDev R, "
          "const rrtl::WordJitPlace Pl) {\n";
     o += "  extern __shared__ uint32_t rrtl_jsm[];\n";
-    o += "  rrtl::word_jit_run<rrtl::JitLane>(R, Pl, rrtl_jsm);\n";
+    if (run) {
+      o += "  rrtl::word_jit_run<rrtl::JitLane>(R, Pl, rrtl_jsm, rrtl::RunSpec{});\n";
+    } else {
+      o += "  __shared__ rrtl::JitDynamicRun tables;\n";
+      o += "  const rrtl::WordRunSpec spec = tables.load(R);\n";
+      o += "  rrtl::word_jit_run<rrtl::JitLane>(R, Pl, rrtl_jsm, spec);\n";
+    }
     o += "}\n";
     return o;
   }
@@ -384,7 +414,23 @@ WordJit::~WordJit() {
   if (lib) cudaLibraryUnload(lib);
 }
 
-std::string word_jit_source(const WordProgram& wp) { return Emitter(wp).source(); }
+std::string word_jit_source(const WordProgram& wp, const WordRunTables* run) {
+  Emitter e(wp);
+  e.run = run;
+  return e.source();
+}
+
+std::string WordRunTables::key() const {
+  std::string k = std::to_string(mode) + "|";
+  for (const WordStimDev& t : stim)
+    k += std::to_string(t.sig_off) + "," + std::to_string(t.limbs) + "," + std::to_string(t.width) + "," +
+         std::to_string(t.kind) + "," + std::to_string(t.param) + ";";
+  k += "|";
+  for (const WordRecDev& t : rec)
+    k += std::to_string(t.sig_off) + "," + std::to_string(t.limbs) + "," + std::to_string(t.width) + "," +
+         std::to_string(t.base) + ";";
+  return k;
+}
 
 std::vector<char> word_jit_compile(const std::string& src, const std::string& arch, std::string* log) {
   Nvrtc& N = nvrtc();
@@ -421,7 +467,7 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
   return cubin;
 }
 
-void word_jit_build(const WordProgram& wp, int device, WordJit* J) {
+void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run) {
   const auto t0 = std::chrono::steady_clock::now();
   J->written.assign(wp.mems.size(), 0);
   J->reg_signals = wp.n_sig_words <= kJitRegSignals;
@@ -437,7 +483,7 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J) {
     return;
   }
   const std::string arch = "sm_" + std::to_string(prop.major) + std::to_string(prop.minor) + "a";
-  const std::string src = word_jit_source(wp);
+  const std::string src = word_jit_source(wp, run);
   J->source_bytes = src.size();
   std::string log;
   std::vector<char> cubin = word_jit_compile(src, arch, &log);

@@ -20,6 +20,20 @@
 
 namespace rrtl {
 
+// A run's stimulus table, record table and record mode: what a kernel
+// compiled for one run bakes in.
+struct WordRunTables {
+  std::vector<WordStimDev> stim;
+  std::vector<WordRecDev> rec;
+  uint32_t mode = 0;
+  std::string key() const;
+};
+
+// Runs with more table entries than this use the kernel compiled for any run.
+constexpr size_t kJitRunTableMax = 64;
+// Kernels compiled for specific runs kept per design.
+constexpr size_t kJitRunKernelsPerDesign = 64;
+
 struct WordJit {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
@@ -38,8 +52,9 @@ constexpr size_t kJitMaxInstrs = 20000;
 // Designs with at most this many signal words keep them in registers.
 constexpr uint32_t kJitRegSignals = 256;
 
-// CUDA C++ source of a word program's compiled kernel `rrtl_word_jit`.
-std::string word_jit_source(const WordProgram& wp);
+// CUDA C++ source of a word program's compiled kernel `rrtl_word_jit`: for
+// any run, or with `run` for that run's tables only.
+std::string word_jit_source(const WordProgram& wp, const WordRunTables* run = nullptr);
 
 // Compile `src` for `arch` (e.g. "sm_103a") with NVRTC; returns the cubin,
 // or an empty vector with `log` holding the compiler's messages.
@@ -47,7 +62,7 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
 
 // Emit, compile and load the kernel of `wp` on the current device. Never
 // throws: failures leave ok = false and the reason in error.
-void word_jit_build(const WordProgram& wp, int device, WordJit* out);
+void word_jit_build(const WordProgram& wp, int device, WordJit* out, const WordRunTables* run = nullptr);
 
 // Shared-memory placement for one launch over `lanes_pad` lanes and `cycles`
 // cycles; returns the dynamic shared memory bytes per 128-lane block.

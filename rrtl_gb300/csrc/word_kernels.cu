@@ -166,7 +166,7 @@ __device__ __forceinline__ void word_lane_run(const WordProgDev& P, const WordRu
              sig_smem ? ssm : R.values + lane, sig_smem ? (size_t)blockDim.x : (size_t)R.lanes_pad};
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) ssm[(size_t)w * blockDim.x] = R.values[(size_t)w * R.lanes_pad + lane];
-  word_lane_cycles(R, lane, W, R.stim, R.rec);
+  word_lane_cycles(R, lane, W, WordRunSpec{R.stim, R.rec, R.n_stim, R.n_rec, R.mode});
   if (sig_smem)
     for (uint32_t w = 0; w < P.n_sig_words; ++w) R.values[(size_t)w * R.lanes_pad + lane] = ssm[(size_t)w * blockDim.x];
 }

@@ -14,8 +14,9 @@
 //                                one signal word of the lane
 //   void settle()                comb stream, then the async-reset stream
 //   void edge()                  tick_next, tick_commit, register commit
-// and the run's stimulus and record tables come in as ST and RT (R.stim and
-// R.rec, or copies of them in shared memory).
+// and the run's stimulus table, record table and record mode come in as a
+// spec (WordRunSpec over R.stim and R.rec or copies of them in shared memory,
+// or a generated type holding them as compile-time constants).
 //
 // The header is also compiled at run time by NVRTC, so it includes only
 // headers that are handed to NVRTC with it.
@@ -30,17 +31,32 @@
 
 namespace rrtl {
 
-template <class L>
-__device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t lane, L& W, const WordStimDev* ST,
-                                                 const WordRecDev* RT) {
+// The run's stimulus table, record table and record mode as read at run
+// time (a generated kernel may instead pass a type whose tables are
+// compile-time constants, so the loops below unroll and fold away).
+struct WordRunSpec {
+  const WordStimDev* ST;
+  const WordRecDev* RT;
+  uint32_t ns, nr, md;
+  __device__ __forceinline__ uint32_t n_stim() const { return ns; }
+  __device__ __forceinline__ WordStimDev stim(uint32_t k) const { return ST[k]; }
+  __device__ __forceinline__ uint32_t n_rec() const { return nr; }
+  __device__ __forceinline__ WordRecDev rec(uint32_t k) const { return RT[k]; }
+  __device__ __forceinline__ uint32_t mode() const { return md; }
+};
+
+template <class L, class S>
+__device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t lane, L& W, const S& spec) {
   const bool live = lane < R.lanes;
+  const uint32_t mode = spec.mode();
   // a lane detected by an earlier launch of the same run stays detected
-  bool detected = (R.mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
+  bool detected = (mode & RRTL_REC_DETECT) && live && R.detect[lane] != 0xFFFFFFFFu;
   if (R.start_settle) W.settle();
   for (unsigned long long c = 0; c < R.cycles; ++c) {
     const unsigned long long ca = R.cycle_base + c;
-    for (uint32_t k = 0; k < R.n_stim; ++k) {
-      const WordStimDev s = ST[k];
+#pragma unroll
+    for (uint32_t k = 0; k < spec.n_stim(); ++k) {
+      const WordStimDev s = spec.stim(k);
       if (s.kind == RRTL_STIM_HOLD) continue;
       for (uint32_t l = 0; l < s.limbs; ++l) {
         uint32_t v = 0;
@@ -54,23 +70,24 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
       }
     }
     W.settle();
-    if (R.n_rec) {
+    if (spec.n_rec()) {
       unsigned long long h = 0ull;
       bool diff = false;
-      for (uint32_t k = 0; k < R.n_rec; ++k) {
-        const WordRecDev rc = RT[k];
+#pragma unroll
+      for (uint32_t k = 0; k < spec.n_rec(); ++k) {
+        const WordRecDev rc = spec.rec(k);
         for (uint32_t l = 0; l < rc.limbs; ++l) {
           uint32_t v = W.get(rc.sig_off + l);
           if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
-          if (R.mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
-          if ((R.mode & RRTL_REC_HASH) && rc.width == 1) {
+          if (mode & RRTL_REC_DETECT) diff |= __shfl_sync(0xFFFFFFFFu, v, 0) != v;
+          if ((mode & RRTL_REC_HASH) && rc.width == 1) {
             // 1-bit signals hash as 32-lane packed words, the gate engine's unit
             const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
             if ((threadIdx.x & 31u) == 0 && live) h += hash_term(ca, k, lane >> 5, packed);
           }
           if (!live) continue;
-          if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
-          if (R.mode & RRTL_REC_CHECK) {
+          if (mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
+          if (mode & RRTL_REC_CHECK) {
             const size_t row = (size_t)c * R.rec_limbs + rc.base + l;
             const uint32_t idx = R.chk_idx[row];
             if (idx != 0xFFFFFFFFu) {
@@ -78,14 +95,14 @@ __device__ __forceinline__ void word_lane_cycles(const WordRunDev& R, uint32_t l
               if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
             }
           }
-          if ((R.mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
+          if ((mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
         }
       }
-      if (R.mode & RRTL_REC_HASH) {
+      if (mode & RRTL_REC_HASH) {
         for (int o = 16; o > 0; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
         if ((threadIdx.x & 31u) == 0 && h) atomicAdd(R.out_hash + c, h);
       }
-      if ((R.mode & RRTL_REC_DETECT) && live && diff && !detected) {
+      if ((mode & RRTL_REC_DETECT) && live && diff && !detected) {
         detected = true;
         R.detect[lane] = (uint32_t)ca;
       }
@@ -123,19 +140,29 @@ struct JitLaneBase {
 // shared memory for the launch.
 constexpr uint32_t kJitTableEntries = 64;
 
+// The run tables of a kernel compiled for any run: copied to shared memory
+// for the launch when they are short.
+struct JitDynamicRun {
+  WordStimDev st[kJitTableEntries];
+  WordRecDev rt[kJitTableEntries];
+  __device__ __forceinline__ WordRunSpec load(const WordRunDev& R) {
+    const bool st_smem = R.n_stim <= kJitTableEntries, rt_smem = R.n_rec <= kJitTableEntries;
+    if (st_smem)
+      for (uint32_t i = threadIdx.x; i < R.n_stim; i += blockDim.x) st[i] = R.stim[i];
+    if (rt_smem)
+      for (uint32_t i = threadIdx.x; i < R.n_rec; i += blockDim.x) rt[i] = R.rec[i];
+    return WordRunSpec{st_smem ? st : R.stim, rt_smem ? rt : R.rec, R.n_stim, R.n_rec, R.mode};
+  }
+};
+
 // Kernel body of a compiled design: stage in, run the cycles, stage out.
-template <class L>
-__device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitPlace& Pl, uint32_t* jsm) {
-  __shared__ WordStimDev s_stim[kJitTableEntries];
-  __shared__ WordRecDev s_rec[kJitTableEntries];
+// `spec` is a WordRunSpec over tables that `tables` filled, or a type whose
+// tables are compile-time constants.
+template <class L, class S>
+__device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitPlace& Pl, uint32_t* jsm, const S& spec) {
   const uint32_t lane = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t T = blockDim.x;
   uint32_t* my = jsm + threadIdx.x;
-  const bool st_smem = R.n_stim <= kJitTableEntries, rt_smem = R.n_rec <= kJitTableEntries;
-  if (st_smem)
-    for (uint32_t i = threadIdx.x; i < R.n_stim; i += T) s_stim[i] = R.stim[i];
-  if (rt_smem)
-    for (uint32_t i = threadIdx.x; i < R.n_rec; i += T) s_rec[i] = R.rec[i];
   L W;
   W.LP = R.lanes_pad;
   W.gm = R.mems + lane;
@@ -163,8 +190,8 @@ __device__ __forceinline__ void word_jit_run(const WordRunDev& R, const WordJitP
       W.ms[k] = R.lanes_pad;
     }
   }
-  __syncthreads();  // the tables are in place
-  word_lane_cycles(R, lane, W, st_smem ? s_stim : R.stim, rt_smem ? s_rec : R.rec);
+  __syncthreads();  // shared-memory run tables are in place
+  word_lane_cycles(R, lane, W, spec);
   if constexpr (L::kRegSignals) {
     W.store(R.values + lane, R.lanes_pad);
   } else if (Pl.sig_smem) {

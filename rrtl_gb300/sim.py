@@ -228,7 +228,7 @@ def lib():
         "rrtl_batch_last_kernel_ms": [c_void_p, P(c_float)],
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
         "rrtl_design_word_jit": [c_void_p, P(c_uint32), P(c_float)],
-        "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
+        "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
     }
     for name, args in sigs.items():
@@ -336,18 +336,20 @@ def default_context() -> Context:
     return _default_ctx
 
 
-def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] = None):
-    """CUDA source of a design's compiled word kernel, and with `arch` its NVRTC
-    compile (no device needed): (source, cubin bytes, compiler log)."""
+def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] = None, run: Optional["Run"] = None):
+    """CUDA source of a design's compiled word kernel (for any run, or for the
+    tables of `run`, a Run whose signals are packed indices), and with `arch`
+    its NVRTC compile (no device needed): (source, cubin bytes, compiler log)."""
     text = design.to_json() if isinstance(design, _b.Design) else design
     raw = text.encode()
+    rp = ctypes.cast(byref(run), c_void_p) if run is not None else None
     n = c_size_t()
-    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), None, None, 0, byref(n), None, None, 0))
+    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, None, None, 0, byref(n), None, None, 0))
     src = ctypes.create_string_buffer(n.value + 1)
     logb = ctypes.create_string_buffer(1 << 16)
     cub = c_uint32()
-    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), arch.encode() if arch else None, src, n.value + 1,
-                                   byref(n), byref(cub), logb, len(logb)))
+    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
+                                   n.value + 1, byref(n), byref(cub), logb, len(logb)))
     return src.value.decode(), cub.value, logb.value.decode()
 
 

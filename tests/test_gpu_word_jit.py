@@ -125,3 +125,36 @@ def test_counter_trace_and_detect(engine):
     for k in ("trace", "hash", "detect"):
         assert np.array_equal(out[sim.PATH_FUSED][k], out[sim.PATH_WORD_INTERP][k]), k
     assert (out[sim.PATH_FUSED]["detect"] != 0xFFFFFFFF).any()
+
+
+def test_run_specialised_equals_general_kernel(engine, monkeypatch):
+    """The fused path compiles a kernel for each run's tables; with that off
+    (RRTL_WORD_JIT_RUNS=0) it runs the general compiled kernel. Both equal
+    the interpreter, for every record mode and a multi-limb trace stimulus."""
+    d, meta = random_word_design(777, n_wires=16, depth=3, n_mems=2)
+    js = d.to_json()
+    lanes, cycles = 200, 30
+    rng = np.random.default_rng(5)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 2)]
+    stim += [(n, sim.STIM_RANDOM, i + 3) for i, (n, w) in enumerate(meta["inputs"][1:])]
+    name0, w0 = meta["inputs"][0]
+    limbs0 = max(1, (w0 + 31) // 32)
+    trace = rng.integers(0, 2**32, size=(cycles, limbs0, lanes), dtype=np.uint64).astype(np.uint32)
+    if w0 % 32:
+        trace[:, -1, :] &= np.uint32((1 << (w0 % 32)) - 1)
+    stim += [(name0, sim.STIM_TRACE, 0)]
+    rec = [n for n, w in meta["outputs"]]
+    mode = sim.REC_TRACE | sim.REC_HASH | sim.REC_DETECT
+    out = {}
+    for key, path, env in (("spec", sim.PATH_FUSED, "1"), ("general", sim.PATH_FUSED, "0"),
+                           ("interp", sim.PATH_WORD_INTERP, "1")):
+        monkeypatch.setenv("RRTL_WORD_JIT_RUNS", env)
+        g = sim.GpuBatchSimulator(js, meta["top"], lanes)
+        g.set_path(path)
+        res = g.run(cycles, seed=11, stim=stim, record=rec, mode=mode, input_trace=trace)
+        out[key] = (res, g.snapshot_storage())
+    for key in ("general", "interp"):
+        for k in ("trace", "hash", "detect"):
+            assert np.array_equal(out["spec"][0][k], out[key][0][k]), (key, k)
+        assert np.array_equal(out["spec"][1][0], out[key][1][0])
+        assert np.array_equal(out["spec"][1][1], out[key][1][1])

@@ -60,3 +60,48 @@ def test_wide_values_are_outside_the_word_engine():
     with pytest.raises(sim.RrtlError) as e:
         sim.word_jit_emit(d, "Wide")
     assert e.value.code == "E_WORD_SCOPE" and e.value.status == 7  # RRTL_E_UNSUPPORTED
+
+
+def _run_for(design, top, stim, record, mode):
+    """A Run naming packed signal indices (looked up through the oracle's lowering)."""
+    import ctypes
+
+    from oracle import binding as ob
+
+    od = ob.OracleDesign(design.to_json(), top)
+    st = (sim.Stim * max(1, len(stim)))(*[sim.Stim(od.signal(n), k, p) for n, k, p in stim])
+    rec = (ctypes.c_uint32 * max(1, len(record)))(*[od.signal(n) for n in record])
+    r = sim.Run()
+    r.n_stim, r.stim = len(stim), st
+    r.n_record, r.record = len(record), rec
+    r.record_mode = mode
+    r._keep = (st, rec)
+    return r
+
+
+@pytest.mark.parametrize("which", ["counter", "cpu"])
+def test_run_specialised_sources_compile(which):
+    """The kernel compiled for one run's tables holds them as constants."""
+    if which == "counter":
+        d, top = counter(), "Counter"
+        stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 0)]
+        rec = ["out"]
+    else:
+        d, top = pipelined_cpu(), "Cpu8"
+        stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
+        rec = ["out_pc", "out_acc"]
+    run = _run_for(d, top, stim, rec, sim.REC_TRACE | sim.REC_HASH | sim.REC_DETECT)
+    src, cub, log = sim.word_jit_emit(d, top, None, run)
+    assert "struct RunSpec" in src and f"n_stim() {{ return {len(stim)}u; }}" in src
+    assert "JitDynamicRun" not in src
+    src, cub, log = _compile_run(d, top, run)
+    assert cub > 0, log
+
+
+def _compile_run(d, top, run):
+    try:
+        return sim.word_jit_emit(d, top, "sm_103a", run)
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
