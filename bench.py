@@ -451,6 +451,41 @@ def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True):
     return out
 
 
+def instance_fold_leg(ctx, sim, cycles=2000):
+    """Instance folding: a wrapper of 64 independent 32-bit datapaths,
+    flattened (one program with 64 copies, `base` lanes) against folded (the
+    datapath once, 64 x `base` lanes), in datapath-cycles/s (instances x base
+    lanes x cycles per second, the same total work both ways), at the base
+    lane counts of the reference's table (docs/rrtl-optimizations.md:544-572).
+    Outputs of every instance are compared between the two."""
+    from rrtl_gb300.workloads import replicated_datapath
+
+    n = 64
+    js = replicated_datapath(n).to_json()
+    flat_d = sim.CompiledDesign(js, "Top", ctx)
+    plan = sim.instance_fold_plan(js, "Top")
+    fold_d = sim.CompiledDesign(js, plan["child"], ctx)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 2)]
+    rows = []
+    for base in (64, 1024, 4096):
+        rng = np.random.default_rng(base)
+        din = rng.integers(0, 2**32, size=(cycles, n, base), dtype=np.uint64).astype(np.uint32)
+        gf = sim.GpuBatchSimulator(flat_d, lanes=base)
+        rf = gf.run(cycles, stim=stim + [(f"din{i}", sim.STIM_TRACE, i) for i in range(n)],
+                    record=[f"o{i}" for i in range(n)], mode=sim.REC_TRACE, input_trace=din)
+        flat_ms = gf.last_kernel_ms
+        gc = sim.GpuBatchSimulator(fold_d, lanes=n * base)
+        rc = gc.run(cycles, stim=stim + [("din", sim.STIM_TRACE, 0)], record=["o"], mode=sim.REC_TRACE,
+                    input_trace=din.reshape(cycles, 1, n * base))
+        fold_ms = gc.last_kernel_ms
+        same = bool(np.array_equal(rc["trace"][:, 0, :].reshape(cycles, n, base), rf["trace"]))
+        work = n * base * cycles
+        rows.append({"base_lanes": base, "flattened": work / (flat_ms / 1e3), "folded": work / (fold_ms / 1e3),
+                     "speedup": flat_ms / fold_ms, "bitexact": same})
+    return {"instances": n, "cycles": cycles, "unit": "datapath-cycles/s",
+            "program_instrs": {"flattened": flat_d.info.n_gates, "folded": fold_d.info.n_gates}, "rows": rows}
+
+
 def run_reference(args, ws, rank):
     """The reference's CPU implementation of the path on the host cores: the
     AOT bit-parallel engine restated (see cpu_baseline), each step a bounded
@@ -512,6 +547,8 @@ def main():
                     help="profiling case: only the pipelined-CPU word config (its compiled run is the second "
                          "rrtl_word_jit launch, after the batch's creation settle)")
     ap.add_argument("--cpu8-cycles", type=int, default=20_000, help="cycles of the pipelined-CPU compiled run")
+    ap.add_argument("--no-fold", action="store_true", help="skip the instance-folding leg")
+    ap.add_argument("--fold-only", action="store_true", help="only the instance-folding leg")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
     args.warmup = max(args.warmup, 3)
@@ -530,6 +567,11 @@ def main():
         ctx = sim.Context(local)
         if rank == 0:
             print(json.dumps({"word_configs": word_configs_leg(ctx, sim, args.cpu8_cycles, counter=False)}))
+        return
+    if args.fold_only:
+        ctx = sim.Context(local)
+        if rank == 0:
+            print(json.dumps({"instance_fold": instance_fold_leg(ctx, sim)}))
         return
     d, meta, js, stim, rec = build_workload()
     ctx = sim.Context(local)
@@ -639,6 +681,8 @@ def main():
     }
     if not args.no_word_configs:
         out["word_configs"] = word_configs_leg(ctx, sim, args.cpu8_cycles)
+    if not args.no_fold:
+        out["instance_fold"] = instance_fold_leg(ctx, sim)
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:

@@ -427,6 +427,23 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
                                size_t log_cap);
 
+/* ---- instance folding ------------------------------------------------------
+ * A top that is a flat wrapper of N >= 2 independent instances of one module
+ * (no logic of its own, no instance output feeding an instance input, no
+ * signal driven by two instances; shared inputs such as a clock allowed)
+ * simulates as that child module over N x L lanes, instance i on lanes
+ * [i*L, (i+1)*L): load the design with the child as top
+ * (rrtl_design_load_json(ctx, json, len, child, ...)) and create a batch of
+ * N x L lanes. This replaces analyze_instance_fold
+ * (crates/rrtl-sim-ir/src/instance_fold.rs:42-97) and the plan side of
+ * InstanceFoldPlan (crates/rrtl-gpu-sim/src/instance_fold.rs). No device is
+ * needed. plan: buffer of cap bytes for the NUL-terminated JSON plan
+ * {"child", "instances": [names], "connections": [[top_signal, instance,
+ * port, "in"|"out"], ...]}; *plan_len its length. RRTL_E_UNSUPPORTED
+ * (E_INSTANCE_FOLD: reason) when the design does not fold. */
+rrtl_status rrtl_instance_fold_plan(const char* json, size_t len, const char* top, char* plan, size_t cap,
+                                    size_t* plan_len);
+
 #ifdef __cplusplus
 }
 #endif

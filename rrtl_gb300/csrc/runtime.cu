@@ -2,6 +2,7 @@
 // lane batches and runs. All device memory is owned here; caller buffers are
 // only touched during a call.
 #include "runtime.h"
+#include "instance_fold.h"
 
 #include <algorithm>
 #include <cmath>
@@ -617,8 +618,6 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
     R.chk_cap = chk->cap;
   }
   g.smem_slots = word_smem_slots(d);
-  REQUIRE(g.smem_slots, RRTL_E_UNSUPPORTED,
-          "E_WORD_SCOPE: design needs " + std::to_string(d->wdev.n_vslots) + " live value slots, more than shared memory holds");
   g.rec_limbs = rec_limbs;
   size_t trace_in_bytes = (size_t)run.cycles * run.n_trace_cols * b->lanes * 4;
   g.trace_out_bytes = (size_t)run.cycles * rec_limbs * b->lanes * 4;
@@ -657,6 +656,14 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   if (g.want_hash) cuda_check(cudaMemsetAsync(R.out_hash, 0, g.hash_bytes, st), "memset hash");
   if (g.want_det) cuda_check(cudaMemsetAsync(R.detect, 0xFF, g.det_bytes, st), "memset detect");
   return g;
+}
+
+// The interpreted word kernel keeps a block's value slots in shared memory
+// (the compiled kernel keeps them in registers and has no such limit).
+void word_require_interp(const rrtl_design* d, const WordPrepared& g) {
+  REQUIRE(g.smem_slots, RRTL_E_UNSUPPORTED,
+          "E_WORD_SCOPE: design needs " + std::to_string(d->wdev.n_vslots) +
+              " live value slots, more than the interpreted word kernel holds in shared memory");
 }
 
 // Launch cycles [c0, c0 + n) of a prepared word run (one kernel; the settle
@@ -728,6 +735,7 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   const bool per_cycle = (b->path == RRTL_PATH_PLAIN || b->path == RRTL_PATH_PLAIN_GRAPH) && run.cycles > 1;
   // compile before the timed region opens
   const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables) : nullptr;
+  if (!J) word_require_interp(d, g);
   Timer tm(b);
   if (per_cycle) {
     // one launch per cycle: the baseline path (captured into a CUDA graph on RRTL_PATH_PLAIN_GRAPH)
@@ -1244,6 +1252,24 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
     }
     REQUIRE(!cubin.empty(), RRTL_E_UNSUPPORTED, "E_WORD_JIT: " + lg.substr(0, 400));
     if (cubin_bytes) *cubin_bytes = (uint32_t)cubin.size();
+  });
+}
+
+rrtl_status rrtl_instance_fold_plan(const char* json, size_t len, const char* top, char* plan, size_t cap,
+                                    size_t* plan_len) {
+  return guard([&] {
+    REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
+    Design dz = design_from_json(json, len);
+    std::string why;
+    auto f = analyze_instance_fold(dz, top, &why);
+    REQUIRE(f.has_value(), RRTL_E_UNSUPPORTED, "E_INSTANCE_FOLD: " + why);
+    const std::string js = instance_fold_json(*f);
+    if (plan_len) *plan_len = js.size();
+    if (plan && cap) {
+      const size_t n = std::min(cap - 1, js.size());
+      memcpy(plan, js.data(), n);
+      plan[n] = 0;
+    }
   });
 }
 

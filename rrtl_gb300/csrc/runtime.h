@@ -138,6 +138,8 @@ cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem,
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
+// Throws E_WORD_SCOPE when the interpreted word kernel cannot hold the design's value slots.
+void word_require_interp(const rrtl_design* d, const WordPrepared& g);
 // The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
 const WordJit* word_jit_get(rrtl_design* d);
 // The kernel compiled for this run's tables (built on first use and kept per

@@ -161,6 +161,7 @@ void rrtl_server::admit(std::vector<std::shared_ptr<Request>>& fresh) {
       } else {
         r.wp = word_prepare(r.batch, r.run, false, false);
         r.jit = word_jit_for_run(r.design, r.wp.tables);  // compiled once per design and run tables
+        if (!r.jit) word_require_interp(r.design, r.wp);
       }
       active.push_back(rp);
     } catch (const ApiError& e) {

@@ -9,6 +9,7 @@ loading fails loudly when the library is missing.
 from __future__ import annotations
 
 import ctypes
+import json
 import os
 from ctypes import POINTER, byref, c_char_p, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
 from typing import Iterable, Optional, Sequence, Union
@@ -161,6 +162,7 @@ EXPORTS = (
     "rrtl_word_tick_many_noalloc",
     "rrtl_design_word_jit",
     "rrtl_word_jit_emit",
+    "rrtl_instance_fold_plan",
 )
 
 _lib = None
@@ -230,6 +232,7 @@ def lib():
         "rrtl_design_word_jit": [c_void_p, P(c_uint32), P(c_float)],
         "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
+        "rrtl_instance_fold_plan": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -770,3 +773,80 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def instance_fold_plan(design: Union[_b.Design, str], top: str) -> dict:
+    """The instance-fold plan of `top` (no device needed); raises RrtlError
+    (code E_INSTANCE_FOLD) when the design does not fold."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    n = c_size_t()
+    check(lib().rrtl_instance_fold_plan(raw, len(raw), top.encode(), None, 0, byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    check(lib().rrtl_instance_fold_plan(raw, len(raw), top.encode(), buf, n.value + 1, byref(n)))
+    return json.loads(buf.value.decode())
+
+
+class InstanceFoldSimulator:
+    """N independent instances of one module folded into the lane axis: the
+    child module simulated over N x base_lanes lanes, instance i on lanes
+    [i*base_lanes, (i+1)*base_lanes). Mirrors InstanceFoldSimulator
+    (crates/rrtl-gpu-sim/src/instance_fold.rs): set_port / get_port address
+    the child's ports over all lanes; set_top_input / get_top_output address
+    the wrapper's own signals over base_lanes lanes, demultiplexed by lane
+    block through the plan's connections."""
+
+    def __init__(self, design: Union[_b.Design, str], top: str, base_lanes: int, ctx: Optional[Context] = None):
+        text = design.to_json() if isinstance(design, _b.Design) else design
+        self.plan = instance_fold_plan(text, top)
+        self.n = len(self.plan["instances"])
+        self.base_lanes = base_lanes
+        self.sim = GpuBatchSimulator(text, self.plan["child"], self.n * base_lanes, ctx)
+        self._in, self._out = {}, {}
+        for tsig, inst, port, d in self.plan["connections"]:
+            (self._out if d == "out" else self._in).setdefault(tsig, []).append((inst, port))
+
+    @property
+    def num_instances(self) -> int:
+        return self.n
+
+    @property
+    def total_lanes(self) -> int:
+        return self.n * self.base_lanes
+
+    def instance_lane(self, inst: int, local: int) -> int:
+        return inst * self.base_lanes + local
+
+    def set_port(self, port: str, limbs_by_lane: np.ndarray):
+        """A child port over all lanes: [limbs][total_lanes]."""
+        self.sim.set_input_limbs(port, limbs_by_lane)
+
+    def get_port(self, port: str) -> np.ndarray:
+        return self.sim.get_signal_limbs(port)
+
+    def set_top_input(self, name: str, limbs_by_lane: np.ndarray):
+        """A wrapper input over base_lanes lanes ([limbs][base_lanes]), written to
+        the lane block of every instance port it drives."""
+        vals = np.atleast_2d(np.asarray(limbs_by_lane, dtype=np.uint32))
+        by_port = {}
+        for inst, port in self._in.get(name, []):
+            by_port.setdefault(port, []).append(inst)
+        for port, insts in by_port.items():
+            cur = self.get_port(port)
+            for i in insts:
+                cur[:, i * self.base_lanes:(i + 1) * self.base_lanes] = vals
+            self.set_port(port, cur)
+
+    def get_top_output(self, name: str) -> np.ndarray:
+        """A wrapper signal driven by an instance output: [limbs][base_lanes]."""
+        (inst, port), = self._out[name]
+        return self.get_port(port)[:, inst * self.base_lanes:(inst + 1) * self.base_lanes]
+
+    def tick(self):
+        self.sim.tick()
+
+    def tick_many(self, steps: int):
+        self.sim.tick_many(steps)
+
+    def eval_combinational(self):
+        self.sim.eval_combinational()

@@ -418,3 +418,39 @@ def job_faults(meta: NetlistMeta, lanes: int, seed: int):
     rng = Rng(seed ^ 0xFA17)
     sites = meta.gate_names + meta.regs + meta.outputs
     return [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]
+
+
+# ------------------------------------------------------- instance folding --
+def replicated_datapath(n_instances: int, top: str = "Top", child: str = "Lane") -> Design:
+    """A flat wrapper of `n_instances` independent copies of one 32-bit
+    datapath (the shape the reference folds into the lane axis: shared clk
+    and reset, a data input and an output per instance). The datapath: a
+    multiply-accumulate register, a rotate-xor mixer and a small history of
+    its inputs, reset synchronously."""
+    d = Design()
+    m = d.module(child)
+    clk = m.input("clk", uint(1))
+    rst = m.input("rst", uint(1))
+    din = m.input("din", uint(32))
+    acc = m.reg("acc", uint(32))
+    mix = m.reg("mix", uint(32))
+    h0 = m.reg("h0", uint(32))
+    h1 = m.reg("h1", uint(32))
+    for r in (acc, mix, h0, h1):
+        m.clock(r, clk)
+        m.reset(r, rst, 0)
+    m.next(acc, acc * lit_u(0x9E3779B9, 32) + din)
+    rot = concat([mix.slice(0, 7), mix.slice(7, 25)])
+    m.next(mix, (rot ^ acc) + (h0 ^ h1))
+    m.next(h0, din)
+    m.next(h1, h0 + lit_u(0x7F4A7C15, 32))
+    o = m.output("o", uint(32))
+    m.assign(o, mix ^ acc)
+    t = d.module(top)
+    tclk = t.input("clk", uint(1))
+    trst = t.input("rst", uint(1))
+    for i in range(n_instances):
+        di = t.input(f"din{i}", uint(32))
+        oi = t.output(f"o{i}", uint(32))
+        t.instance(f"u{i}", child, [("clk", tclk), ("rst", trst), ("din", di), ("o", oi)])
+    return d

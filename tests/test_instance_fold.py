@@ -1,0 +1,134 @@
+"""Instance folding on the CPU: the structural analysis (the reference's own
+accept/reject cases, crates/rrtl-sim-ir/src/instance_fold.rs:99-156, plus
+the other rules), and the semantic claim checked with the oracle: the child
+module over N x L lanes equals the flattened wrapper over L lanes, instance
+by instance and cycle by cycle."""
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from rrtl_gb300 import sim
+from rrtl_gb300.builder import Design, lit_u, uint
+from rrtl_gb300.workloads import Rng, replicated_datapath
+
+
+def _child(d):
+    m = d.module("M")
+    clk = m.input("clk", uint(1))
+    din = m.input("din", uint(32))
+    acc = m.reg("acc", uint(32))
+    m.clock(acc, clk)
+    m.next(acc, acc * lit_u(3, 32) + din)
+    o = m.output("o", uint(32))
+    m.assign(o, acc)
+
+
+def _plan_error(d, top="Top"):
+    with pytest.raises(sim.RrtlError) as e:
+        sim.instance_fold_plan(d, top)
+    assert e.value.code == "E_INSTANCE_FOLD"
+    return str(e.value)
+
+
+def test_detects_independent_instances():
+    d = Design()
+    _child(d)
+    m = d.module("Top")
+    clk = m.input("clk", uint(1))
+    for i in range(4):
+        din = m.input(f"din{i}", uint(32))
+        o = m.output(f"o{i}", uint(32))
+        m.instance(f"u{i}", "M", [("clk", clk), ("din", din), ("o", o)])
+    plan = sim.instance_fold_plan(d, "Top")
+    assert plan["child"] == "M" and plan["instances"] == ["u0", "u1", "u2", "u3"]
+    assert ["clk", 2, "clk", "in"] in plan["connections"] and ["o3", 3, "o", "out"] in plan["connections"]
+
+
+def test_rejects_inter_instance_dataflow():
+    d = Design()
+    _child(d)
+    m = d.module("Top")
+    clk = m.input("clk", uint(1))
+    din = m.input("din", uint(32))
+    mid = m.wire("mid", uint(32))
+    o = m.output("o", uint(32))
+    m.instance("u0", "M", [("clk", clk), ("din", din), ("o", mid)])
+    m.instance("u1", "M", [("clk", clk), ("din", mid), ("o", o)])
+    assert "feeds" in _plan_error(d)
+
+
+def test_rejects_shared_driver_top_logic_and_mixed_modules():
+    d = Design()
+    _child(d)
+    m = d.module("Top")
+    clk = m.input("clk", uint(1))
+    din = m.input("din", uint(32))
+    o = m.output("o", uint(32))
+    m.instance("u0", "M", [("clk", clk), ("din", din), ("o", o)])
+    m.instance("u1", "M", [("clk", clk), ("din", din), ("o", o)])
+    assert "two instance outputs" in _plan_error(d)
+
+    d = replicated_datapath(3)
+    t = [m for m in d._modules if m.name == "Top"][0]
+    from rrtl_gb300.builder import ModuleBuilder
+
+    tb = ModuleBuilder(d, t)
+    w = tb.wire("extra", uint(32))
+    tb.assign(w, lit_u(5, 32))
+    assert "logic of its own" in _plan_error(d)
+
+    d = Design()
+    _child(d)
+    m2 = d.module("M2")
+    clk2 = m2.input("clk", uint(1))
+    din2 = m2.input("din", uint(32))
+    o2 = m2.output("o", uint(32))
+    m2.assign(o2, din2)
+    m = d.module("Top")
+    clk = m.input("clk", uint(1))
+    a, b = m.input("a", uint(32)), m.input("b", uint(32))
+    oa, ob_ = m.output("oa", uint(32)), m.output("ob", uint(32))
+    m.instance("u0", "M", [("clk", clk), ("din", a), ("o", oa)])
+    m.instance("u1", "M2", [("clk", clk), ("din", b), ("o", ob_)])
+    assert "different modules" in _plan_error(d)
+
+    d = Design()
+    _child(d)
+    m = d.module("Top")
+    clk = m.input("clk", uint(1))
+    din = m.input("din", uint(32))
+    o = m.output("o", uint(32))
+    m.instance("u0", "M", [("clk", clk), ("din", din), ("o", o)])
+    assert "fewer than two" in _plan_error(d)
+
+
+def test_fold_equals_flattened_on_the_oracle():
+    """The packed oracle on the flattened wrapper (L lanes) and on the child
+    (N x L lanes, inputs demultiplexed by lane block) agree on every
+    instance output for 25 cycles."""
+    n, base, cycles = 5, 7, 25
+    d = replicated_datapath(n)
+    js = d.to_json()
+    plan = sim.instance_fold_plan(d, "Top")
+    flat = ob.OracleDesign(js, "Top")
+    child = ob.OracleDesign(js, plan["child"])
+    pf = ob.PackedSim(flat, base)
+    pc = ob.PackedSim(child, n * base)
+    rng = Rng(9)
+    for c in range(cycles):
+        rst = 1 if c < 2 else 0
+        pf.set_signal(flat.signal("clk"), np.ones((1, base), np.uint32))
+        pf.set_signal(flat.signal("rst"), np.full((1, base), rst, np.uint32))
+        pc.set_signal(child.signal("clk"), np.ones((1, n * base), np.uint32))
+        pc.set_signal(child.signal("rst"), np.full((1, n * base), rst, np.uint32))
+        allin = np.zeros((1, n * base), np.uint32)
+        for i in range(n):
+            v = np.array([[rng.next() & 0xFFFFFFFF for _ in range(base)]], np.uint32)
+            pf.set_signal(flat.signal(f"din{i}"), v)
+            allin[:, i * base:(i + 1) * base] = v
+        pc.set_signal(child.signal("din"), allin)
+        pf.tick()
+        pc.tick()
+        o = pc.get_signal(child.signal("o"))
+        for i in range(n):
+            assert np.array_equal(pf.get_signal(flat.signal(f"o{i}")), o[:, i * base:(i + 1) * base]), (c, i)
