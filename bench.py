@@ -451,6 +451,53 @@ def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True):
     return out
 
 
+def crc32_netlist():
+    """The reference's crc32 gate netlist (bench/sv/crc32_gates.json), from the
+    committed compact fixture."""
+    from rrtl_gb300.netlist import import_yosys_netlist
+
+    c = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                    "crc32_gates.compact.json")))
+    y = {"modules": {c["top"]: {
+        "ports": {k: {"direction": d, "bits": b} for k, (d, b) in c["ports"].items()},
+        "cells": {f"c{i:04d}": {"type": t, "connections": conns} for i, (t, conns) in enumerate(c["cells"])}}}}
+    return import_yosys_netlist(y, c["top"])
+
+
+def crc32_leg(ctx, sim, cycles=2000):
+    """The reference's headline GPU workload: its per-design compiled gate
+    kernel on the crc32 netlist (docs/rrtl-optimizations.md:1725-1734, M3 /
+    OpenCL: 4,182 / 4,719 / 19,315 / 17,129 M lane-cycles/s at 16K / 65K /
+    256K / 1M lanes). Random din per lane per cycle, reset on cycle 0; the
+    compiled gate kernel with no per-cycle recording (state only, like the
+    reference's run) and with a per-cycle hash of the 32 crc outputs, the
+    fused kernel (tile width 8) beside it; per-cycle hashes compared."""
+    cd = sim.CompiledDesign(crc32_netlist(), "crc32", ctx)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)] + [(f"din_{i}", sim.STIM_RANDOM, i) for i in range(8)]
+    rec = [f"crc_{i}" for i in range(32)]
+    rows = []
+    for lanes in (16384, 65536, 262144, 1048576):
+        row = {"lanes": lanes}
+        hashes = {}
+        for key, words, mode in (("compiled", 0, 0), ("compiled_hash", 0, sim.REC_HASH), ("fused_hash", 8, sim.REC_HASH)):
+            g = sim.GpuBatchSimulator(cd, lanes=lanes)
+            if words:
+                g.set_tile_words(words)
+            g.run(10, stim=stim, record=rec, mode=mode)
+            best = float("inf")
+            for _ in range(3):
+                r = g.run(cycles, stim=stim, record=rec, mode=mode)
+                best = min(best, g.last_kernel_ms)
+            row[key] = lanes * cycles / (best / 1e3)
+            if mode:
+                hashes[key] = r["hash"]
+        row["hash_equal"] = bool(np.array_equal(hashes["compiled_hash"], hashes["fused_hash"]))
+        rows.append(row)
+    return {"cycles": cycles, "unit": "lane-cycles/s", "cells": cd.info.n_gates, "rows": rows,
+            "reference_m3_opencl": {"16384": 4.182e9, "65536": 4.719e9, "262144": 1.9315e10, "1048576": 1.7129e10,
+                                    "note": "published Apple M3 numbers, unavailable on this box (OpenCL.framework)"}}
+
+
 def instance_fold_leg(ctx, sim, cycles=2000):
     """Instance folding: a wrapper of 64 independent 32-bit datapaths,
     flattened (one program with 64 copies, `base` lanes) against folded (the
@@ -548,6 +595,8 @@ def main():
                          "rrtl_word_jit launch, after the batch's creation settle)")
     ap.add_argument("--cpu8-cycles", type=int, default=20_000, help="cycles of the pipelined-CPU compiled run")
     ap.add_argument("--no-fold", action="store_true", help="skip the instance-folding leg")
+    ap.add_argument("--no-crc32", action="store_true", help="skip the crc32 compiled-gate-kernel leg")
+    ap.add_argument("--crc32-only", action="store_true", help="only the crc32 leg")
     ap.add_argument("--fold-only", action="store_true", help="only the instance-folding leg")
     args = ap.parse_args()
     globals()["LANES"], globals()["CYCLES"] = args.lanes, args.cycles
@@ -572,6 +621,11 @@ def main():
         ctx = sim.Context(local)
         if rank == 0:
             print(json.dumps({"instance_fold": instance_fold_leg(ctx, sim)}))
+        return
+    if args.crc32_only:
+        ctx = sim.Context(local)
+        if rank == 0:
+            print(json.dumps({"crc32": crc32_leg(ctx, sim)}))
         return
     d, meta, js, stim, rec = build_workload()
     ctx = sim.Context(local)
@@ -683,6 +737,8 @@ def main():
         out["word_configs"] = word_configs_leg(ctx, sim, args.cpu8_cycles)
     if not args.no_fold:
         out["instance_fold"] = instance_fold_leg(ctx, sim)
+    if not args.no_crc32:
+        out["crc32"] = crc32_leg(ctx, sim)
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:

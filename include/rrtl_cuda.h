@@ -427,6 +427,22 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
                                size_t log_cap);
 
+/* ---- per-design compiled gate kernels ---------------------------------------
+ * A gate-engine run on the fused path without stuck-at forces, with an
+ * automatic tile width, on a design of up to 8,192 cells, runs a gate kernel
+ * compiled for the design and the run's tables: one thread per 32-lane word,
+ * every net a register, one LOP3 per cell (the reference's per-design
+ * compiled kernel, crates/rrtl-sim-ir/src/gpu_codegen.rs:503-557). Designs
+ * of up to 1,024 cells use it unless the autotuner measured a tile width
+ * faster for the lane count; rrtl_design_autotune times it as a candidate and
+ * reports it as best_words = 0. rrtl_batch_tile_words reads 0 after such a
+ * run. This call emits (and with arch compiles) that kernel without a device,
+ * like rrtl_word_jit_emit; run is required (its signals are packed indices).
+ * RRTL_E_UNSUPPORTED when the design is outside the gate engine. */
+rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
+                               char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
+                               size_t log_cap);
+
 /* ---- instance folding ------------------------------------------------------
  * A top that is a flat wrapper of N >= 2 independent instances of one module
  * (no logic of its own, no instance output feeding an instance input, no

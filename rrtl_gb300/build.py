@@ -45,6 +45,8 @@ JIT_HEADERS = [
     ("word_dev.h", "word_dev.h"),
     ("stim.h", "stim.h"),
     ("check_log.h", "check_log.h"),
+    ("gate_dev.h", "gate_dev.h"),
+    ("gate_common.h", "gate_common.h"),
     ("../../include/rrtl_cuda.h", os.path.join("..", "..", "include", "rrtl_cuda.h")),
 ]
 JIT_STUBS = [

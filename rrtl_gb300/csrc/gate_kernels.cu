@@ -22,6 +22,7 @@
 
 #include "../../include/rrtl_cuda.h"
 #include "check_log.h"
+#include "gate_common.h"
 #include "gate_dev.h"
 #include "lut_classes.h"
 #include "stim.h"
@@ -77,13 +78,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
-template <int L>
-__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
-  uint32_t d;
-  asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(L));
-  return d;
-}
-
 // Runtime truth table: Shannon expansion on a, then b, then c.
 __device__ __forceinline__ uint32_t lut_eval(uint32_t t, uint32_t a, uint32_t b, uint32_t c) {
   uint32_t m0 = 0u - (t & 1u), m1 = 0u - ((t >> 1) & 1u), m2 = 0u - ((t >> 2) & 1u), m3 = 0u - ((t >> 3) & 1u);
@@ -92,39 +86,6 @@ __device__ __forceinline__ uint32_t lut_eval(uint32_t t, uint32_t a, uint32_t b,
   uint32_t u2 = (c & m5) | (~c & m4), u3 = (c & m7) | (~c & m6);
   uint32_t f0 = (b & u1) | (~b & u0), f1 = (b & u3) | (~b & u2);
   return (a & f1) | (~a & f0);
-}
-
-__device__ __forceinline__ uint32_t valid_mask(uint32_t gw, uint32_t lanes) {
-  uint32_t base = gw * 32u;
-  if (base >= lanes) return 0u;
-  uint32_t n = lanes - base;
-  return n >= 32u ? 0xFFFFFFFFu : ((1u << n) - 1u);
-}
-
-__device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateRunDev& R, uint64_t c, uint32_t gw,
-                                               uint32_t cur) {
-  switch (s.kind) {
-    case RRTL_STIM_RANDOM: return stim_word(R.seed, s.param, c, gw);
-    case RRTL_STIM_PULSE: return c < s.param ? 0xFFFFFFFFu : 0u;
-    case RRTL_STIM_CONST: return (s.param & 1u) ? 0xFFFFFFFFu : 0u;
-    case RRTL_STIM_TRACE:
-      return gw < R.words ? R.in_trace[((size_t)c * R.n_trace_cols + s.param) * R.words + gw] : 0u;
-    default: return cur;
-  }
-}
-
-// Trace check of recorded net k on 32-lane word gw at cycle c: every lane
-// whose bit differs from the expected word is logged (limb 0).
-__device__ __forceinline__ void check_word(const GateRunDev& R, uint64_t c, uint32_t k, uint32_t gw, uint32_t v) {
-  const uint32_t idx = R.chk_idx[(size_t)c * R.n_rec + k];
-  if (idx == 0xFFFFFFFFu) return;
-  const uint32_t exp = R.chk_exp[((size_t)c * R.n_rec + k) * R.words + gw];
-  uint32_t mm = (v ^ exp) & valid_mask(gw, R.lanes);
-  while (mm) {
-    const uint32_t b = __ffs(mm) - 1u;
-    log_mismatch(R.chk_log, R.chk_cap, c, idx, gw * 32u + b, 0u, (exp >> b) & 1u, (v >> b) & 1u);
-    mm &= mm - 1u;
-  }
 }
 
 // Bytes of the fused kernel's slot array, rounded so the tables behind it

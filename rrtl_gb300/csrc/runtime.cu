@@ -267,7 +267,7 @@ uint32_t lane_bucket(uint32_t words) {
 
 uint32_t choose_tile_words(rrtl_design* d, uint32_t words) {
   auto tuned = d->tuned_w.find(lane_bucket(words));
-  if (tuned != d->tuned_w.end()) return tuned->second;
+  if (tuned != d->tuned_w.end() && tuned->second != kTunedCompiled) return tuned->second;
   constexpr double kBarrierSteps = 4.0;
   constexpr double kStepCost[4] = {1.45, 1.25, 1.1, 1.0};
   const GateProgram& gp = d->gp();
@@ -431,6 +431,9 @@ GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   REQUIRE(run.cycles < (1ull << 32), RRTL_E_ARG, "E_GPU_STEPS: cycle count exceeds 2^32");
   upload(b->d_stim, stim);
   upload(b->d_rec, rec);
+  g.tables.stim = stim;
+  g.tables.rec = rec;
+  g.tables.mode = run.record_mode;
 
   GateRunDev& R = g.R;
   R.cycles = run.cycles;
@@ -539,12 +542,44 @@ void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st
   cuda_check(e, "cudaGraphLaunch");
 }
 
-void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckTables* chk = nullptr) {
+const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
+  const char* env = getenv("RRTL_GATE_JIT");
+  if ((env && env[0] == '0') || d->gp().n_real_cells > kGateJitMaxCells || t.stim.size() > kJitRunTableMax ||
+      t.rec.size() > kJitRunTableMax)
+    return nullptr;
+  const std::string key = t.key();
+  std::lock_guard<std::mutex> lk(d->wjit_mu);
+  auto it = d->gjit_runs.find(key);
+  if (it == d->gjit_runs.end()) {
+    if (d->gjit_runs.size() >= kJitRunKernelsPerDesign) return nullptr;
+    auto J = std::make_unique<WordJit>();
+    gate_jit_build(d->gp(), t, d->ctx->device, J.get());
+    it = d->gjit_runs.emplace(key, std::move(J)).first;
+  }
+  return it->second->ok ? it->second.get() : nullptr;
+}
+
+bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
+  auto tuned = d->tuned_w.find(lane_bucket(words));
+  if (tuned != d->tuned_w.end()) return tuned->second == kTunedCompiled;
+  return d->gp().n_real_cells <= kGateJitAutoCells;
+}
+
+void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckTables* chk = nullptr,
+              bool force_compiled = false) {
   rrtl_design* d = b->d;
   cudaStream_t st = d->ctx->stream;
   GatePrepared g = gate_prepare(b, run, device_ptrs, b->path == RRTL_PATH_FUSED, chk);
+  // the compiled gate kernel: automatic tile width, no stuck-at forces; built before the timed region
+  const WordJit* J = nullptr;
+  if (b->path == RRTL_PATH_FUSED && !g.R.has_forces && (force_compiled || (b->tile_words == 0 && gate_jit_preferred(d, b->words))))
+    J = gate_jit_for_run(d, g.tables);
   Timer tm(b);
-  if (g.fused) {
+  if (J) {
+    g.R.cycle_base = 0;
+    cuda_check(launch_gate_jit(*J, g.R, st), "rrtl_gate_jit");
+    g.W = 0;
+  } else if (g.fused) {
     uint32_t grid = std::min<uint32_t>(g.R.n_tiles, d->ctx->sm_count * g.v->fused_ctas);
     cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
   } else {
@@ -1255,6 +1290,51 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
   });
 }
 
+rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
+                               char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
+                               size_t log_cap) {
+  return guard([&] {
+    REQUIRE(json && top && run, RRTL_E_ARG, "E_ARG: null argument");
+    if (cubin_bytes) *cubin_bytes = 0;
+    if (log && log_cap) log[0] = 0;
+    Design dz = design_from_json(json, len);
+    MachineProgram mp = lower_to_machine_program(lower_to_packed_program(dz, top));
+    GateProgram gp;
+    try {
+      gp = build_gate_program(mp, 8);
+    } catch (const RrtlError& e) {
+      fail(RRTL_E_UNSUPPORTED, e.what());
+    }
+    GateRunTables tabs;
+    for (uint32_t i = 0; i < run->n_stim; ++i) {
+      REQUIRE(run->stim[i].signal < gp.n_signals, RRTL_E_SIGNAL, "E_GPU_SIGNAL: signal index out of range");
+      tabs.stim.push_back(GateStimDev{0u, gp.signal_net[run->stim[i].signal], run->stim[i].kind, 0u, run->stim[i].param});
+    }
+    for (uint32_t i = 0; i < run->n_record; ++i) {
+      REQUIRE(run->record[i] < gp.n_signals, RRTL_E_SIGNAL, "E_GPU_SIGNAL: signal index out of range");
+      tabs.rec.push_back(GateRecDev{0u, gp.signal_net[run->record[i]]});
+    }
+    tabs.mode = run->record_mode;
+    const std::string src = gate_jit_source(gp, tabs);
+    if (source_len) *source_len = src.size();
+    if (source && source_cap) {
+      const size_t n = std::min(source_cap - 1, src.size());
+      memcpy(source, src.data(), n);
+      source[n] = 0;
+    }
+    if (!arch) return;
+    std::string lg;
+    std::vector<char> cubin = word_jit_compile(src, arch, &lg);
+    if (log && log_cap) {
+      const size_t n = std::min(log_cap - 1, lg.size());
+      memcpy(log, lg.data(), n);
+      log[n] = 0;
+    }
+    REQUIRE(!cubin.empty(), RRTL_E_UNSUPPORTED, "E_GATE_JIT: " + lg.substr(0, 400));
+    if (cubin_bytes) *cubin_bytes = (uint32_t)cubin.size();
+  });
+}
+
 rrtl_status rrtl_instance_fold_plan(const char* json, size_t len, const char* top, char* plan, size_t cap,
                                     size_t* plan_len) {
   return guard([&] {
@@ -1863,8 +1943,29 @@ rrtl_status rrtl_design_autotune(rrtl_design* d, uint32_t lanes, uint32_t cycles
         best = W;
       }
     }
+    // the compiled gate kernel, when the design qualifies
+    if (d->gp().n_real_cells <= kGateJitMaxCells) {
+      rrtl_batch* b = nullptr;
+      rrtl_status st = rrtl_batch_create(d, lanes, &b);
+      if (st) fail(st, g_last_error);
+      float t = INFINITY;
+      try {
+        for (int rep = 0; rep < 3; ++rep) {
+          gate_run(b, run, false, nullptr, true);
+          if (rep && b->last_tile_words == 0) t = std::min(t, b->last_ms);
+        }
+      } catch (...) {
+        rrtl_batch_destroy(b);
+        throw;
+      }
+      rrtl_batch_destroy(b);
+      if (t < best_t) {
+        best_t = t;
+        best = kTunedCompiled;
+      }
+    }
     d->tuned_w[lane_bucket(words)] = best;
-    if (best_words) *best_words = best;
+    if (best_words) *best_words = best == kTunedCompiled ? 0u : best;
     if (best_ms) *best_ms = best_t;
   });
 }

@@ -12,6 +12,7 @@
 
 #include "../../include/rrtl_cuda.h"
 #include "gate_dev.h"
+#include "gate_jit.h"
 #include "gateprog.h"
 #include "lower.h"
 #include "word_dev.h"
@@ -73,6 +74,7 @@ struct ForceTable {
 struct GatePrepared {
   GateVariant* v = nullptr;
   GateRunDev R{};
+  GateRunTables tables;  // host copies of the run's stimulus and record tables
   bool fused = false;
   uint32_t W = 0;
   size_t trace_out_bytes = 0, hash_bytes = 0, det_bytes = 0;
@@ -138,6 +140,15 @@ cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem,
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
 void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
+// The compiled gate kernel for this run's tables (built on first use and
+// kept per design), or nullptr when the design or run does not qualify.
+const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t);
+// Whether a fused-path run of `words` 32-lane words should use the compiled
+// gate kernel: the autotuner's choice for the lane bucket, else small designs.
+bool gate_jit_preferred(rrtl_design* d, uint32_t words);
+constexpr uint32_t kTunedCompiled = 0xFFFFFFFFu;
+// Designs of at most this many cells use the compiled gate kernel unless tuned otherwise.
+constexpr uint32_t kGateJitAutoCells = 1024;
 // Throws E_WORD_SCOPE when the interpreted word kernel cannot hold the design's value slots.
 void word_require_interp(const rrtl_design* d, const WordPrepared& g);
 // The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
@@ -178,7 +189,8 @@ struct rrtl_design {
   std::unique_ptr<rrtl::GateVariant> gvar[4];
   uint32_t gate_base = 3;   // log2 W of the variant built at load time
   uint32_t gate_w_max = 0;  // widest W whose slots fit on chip, 0 if none
-  std::map<uint32_t, uint32_t> tuned_w;  // measured best W by lane bucket (ceil log2 of 32-lane words)
+  std::map<uint32_t, uint32_t> tuned_w;  // measured best W by lane bucket (ceil log2 of 32-lane words);
+                                         // rrtl::kTunedCompiled: the compiled gate kernel
   const rrtl::GateProgram& gp() const { return gvar[gate_base]->gp; }
   // word engine
   rrtl::WordProgram wp;
@@ -187,6 +199,7 @@ struct rrtl_design {
   std::mutex wjit_mu;
   std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel for any run, built on the first fused run
   std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;  // kernels compiled for one run's tables
+  std::map<std::string, std::unique_ptr<rrtl::WordJit>> gjit_runs;  // compiled gate kernels, per run tables
 };
 
 struct rrtl_batch {

@@ -467,23 +467,14 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
   return cubin;
 }
 
-void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run) {
+void jit_build_kernel(const std::string& src, int device, const char* name, WordJit* J) {
   const auto t0 = std::chrono::steady_clock::now();
-  J->written.assign(wp.mems.size(), 0);
-  J->reg_signals = wp.n_sig_words <= kJitRegSignals;
-  for (const WInstr& I : wp.code)
-    if (I.op == W_MEMWR && I.aux < J->written.size()) J->written[I.aux] = 1;
-  if (wp.code.size() > kJitMaxInstrs) {
-    J->error = "word program of " + std::to_string(wp.code.size()) + " instructions runs interpreted";
-    return;
-  }
   cudaDeviceProp prop{};
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
     J->error = "cudaGetDeviceProperties failed";
     return;
   }
   const std::string arch = "sm_" + std::to_string(prop.major) + std::to_string(prop.minor) + "a";
-  const std::string src = word_jit_source(wp, run);
   J->source_bytes = src.size();
   std::string log;
   std::vector<char> cubin = word_jit_compile(src, arch, &log);
@@ -492,7 +483,7 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRun
     return;
   }
   cudaError_t e = cudaLibraryLoadData(&J->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-  if (e == cudaSuccess) e = cudaLibraryGetKernel(&J->fn, J->lib, "rrtl_word_jit");
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&J->fn, J->lib, name);
   cudaFuncAttributes fa{};
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(J->fn));
   if (e == cudaSuccess) {
@@ -507,6 +498,18 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRun
   }
   J->ok = true;
   J->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run) {
+  J->written.assign(wp.mems.size(), 0);
+  J->reg_signals = wp.n_sig_words <= kJitRegSignals;
+  for (const WInstr& I : wp.code)
+    if (I.op == W_MEMWR && I.aux < J->written.size()) J->written[I.aux] = 1;
+  if (wp.code.size() > kJitMaxInstrs) {
+    J->error = "word program of " + std::to_string(wp.code.size()) + " instructions runs interpreted";
+    return;
+  }
+  jit_build_kernel(word_jit_source(wp, run), device, "rrtl_word_jit", J);
 }
 
 size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad, uint64_t cycles,

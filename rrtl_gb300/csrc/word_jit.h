@@ -60,6 +60,11 @@ std::string word_jit_source(const WordProgram& wp, const WordRunTables* run = nu
 // or an empty vector with `log` holding the compiler's messages.
 std::vector<char> word_jit_compile(const std::string& src, const std::string& arch, std::string* log);
 
+// Compile CUDA source `src` with NVRTC for `device` and load its kernel
+// `name` into J. Never throws: failures leave ok = false and the reason in
+// error.
+void jit_build_kernel(const std::string& src, int device, const char* name, WordJit* J);
+
 // Emit, compile and load the kernel of `wp` on the current device. Never
 // throws: failures leave ok = false and the reason in error.
 void word_jit_build(const WordProgram& wp, int device, WordJit* out, const WordRunTables* run = nullptr);

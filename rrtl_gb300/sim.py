@@ -163,6 +163,7 @@ EXPORTS = (
     "rrtl_design_word_jit",
     "rrtl_word_jit_emit",
     "rrtl_instance_fold_plan",
+    "rrtl_gate_jit_emit",
 )
 
 _lib = None
@@ -233,6 +234,8 @@ def lib():
         "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
         "rrtl_instance_fold_plan": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
+        "rrtl_gate_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
+                               P(c_uint32), c_char_p, c_size_t],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -352,6 +355,23 @@ def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] =
     logb = ctypes.create_string_buffer(1 << 16)
     cub = c_uint32()
     check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
+                                   n.value + 1, byref(n), byref(cub), logb, len(logb)))
+    return src.value.decode(), cub.value, logb.value.decode()
+
+
+def gate_jit_emit(design: Union[_b.Design, str], top: str, run: "Run", arch: Optional[str] = None):
+    """CUDA source of the compiled gate kernel for `run`'s tables (a Run whose
+    signals are packed indices), and with `arch` its NVRTC compile (no device
+    needed): (source, cubin bytes, compiler log)."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    rp = ctypes.cast(byref(run), c_void_p)
+    n = c_size_t()
+    check(lib().rrtl_gate_jit_emit(raw, len(raw), top.encode(), rp, None, None, 0, byref(n), None, None, 0))
+    src = ctypes.create_string_buffer(n.value + 1)
+    logb = ctypes.create_string_buffer(1 << 16)
+    cub = c_uint32()
+    check(lib().rrtl_gate_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
                                    n.value + 1, byref(n), byref(cub), logb, len(logb)))
     return src.value.decode(), cub.value, logb.value.decode()
 

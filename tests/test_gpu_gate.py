@@ -209,7 +209,7 @@ def test_autotune_picks_a_measured_width(small_netlist):
     d, meta, cd, od = small_netlist
     stim, rec = netlist_run_spec(meta)
     best, ms = cd.autotune(4096, cycles=8)
-    assert best in (1, 2, 4, 8) and ms > 0
+    assert best in (0, 1, 2, 4, 8) and ms > 0  # 0: the compiled gate kernel
     g = sim.GpuBatchSimulator(cd, lanes=4000)  # same lane bucket
     res = g.run(9, seed=3, stim=stim, record=rec, mode=sim.REC_HASH)
     assert g.tile_words == best

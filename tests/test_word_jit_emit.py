@@ -105,3 +105,32 @@ def _compile_run(d, top, run):
         if "NVRTC not found" in str(e):
             pytest.skip("NVRTC is not installed")
         raise
+
+
+@pytest.mark.parametrize("which", ["crc32", "netlist"])
+def test_compiled_gate_kernel_sources_compile(which):
+    """The compiled gate kernel (one thread per 32-lane word, one LOP3 per
+    cell) for the reference's crc32 netlist and a generated netlist."""
+    from rrtl_gb300.workloads import gate_netlist, netlist_run_spec
+
+    from .helpers import crc32_netlist_json
+
+    if which == "crc32":
+        d, top = crc32_netlist_json(), "crc32"
+        stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)] + [(f"din_{i}", sim.STIM_RANDOM, i)
+                                                                           for i in range(8)]
+        rec = [f"crc_{i}" for i in range(32)]
+    else:
+        d, meta = gate_netlist(n_gates=900, n_ff=40, n_pi=8, n_po=8, depth=8, seed=3)
+        top = meta.top
+        stim, rec = netlist_run_spec(meta)
+    run = _run_for(d, top, stim, rec, sim.REC_TRACE | sim.REC_HASH | sim.REC_DETECT)
+    src, _, _ = sim.gate_jit_emit(d, top, run)
+    assert src.count("lop3<") >= 2 * 100  # the cells, in the cycle body and the closing settle
+    try:
+        src, cub, log = sim.gate_jit_emit(d, top, run, "sm_103a")
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+    assert cub > 0, log
