@@ -443,6 +443,21 @@ rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, co
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
                                size_t log_cap);
 
+/* ---- bit-sliced multi-bit designs --------------------------------------------
+ * The reference's BitSliceSimulator (crates/rrtl-sim-ir/src/bitslice.rs:1-402)
+ * keeps a W-bit signal as W bit-planes across lanes. rrtl_design_load_bitslice
+ * rewrites a design's flattened packed program into 1-bit plane signals
+ * ("<signal>[p]", plane p = bit p of every lane) whose per-plane operations
+ * (bitwise, mux, ripple add/sub, xor/OR-reduce eq/ne, borrow-chain lt,
+ * plane reindexing for slice/concat/extension) run on the bit-sliced gate
+ * engine, 32 lanes per u32 word. Scope: no memories, no multiply, no
+ * asynchronous reset (E_BITSLICE, RRTL_E_UNSUPPORTED). Inputs and outputs
+ * are the planes: set and read them with the 1-bit signal calls (lane bits
+ * packed 32 per word). rrtl_bitslice_json returns the plane design as
+ * design JSON without a device (for inspection and the oracle). */
+rrtl_status rrtl_design_load_bitslice(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out);
+rrtl_status rrtl_bitslice_json(const char* json, size_t len, const char* top, char* out, size_t cap, size_t* out_len);
+
 /* ---- instance folding ------------------------------------------------------
  * A top that is a flat wrapper of N >= 2 independent instances of one module
  * (no logic of its own, no instance output feeding an instance input, no

@@ -2,6 +2,7 @@
 // lane batches and runs. All device memory is owned here; caller buffers are
 // only touched during a call.
 #include "runtime.h"
+#include "bitslice.h"
 #include "instance_fold.h"
 
 #include <algorithm>
@@ -1179,13 +1180,60 @@ rrtl_status rrtl_ctx_synchronize(rrtl_ctx* ctx) {
   });
 }
 
+static void load_design(rrtl_ctx* ctx, Design design, const std::string& top, rrtl_design** out);
+
 rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out) {
   return guard([&] {
     REQUIRE(ctx && json && top && out, RRTL_E_ARG, "E_ARG: null argument");
     set_device(ctx);
+    load_design(ctx, design_from_json(json, len), top, out);
+  });
+}
+
+rrtl_status rrtl_design_load_bitslice(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out) {
+  return guard([&] {
+    REQUIRE(ctx && json && top && out, RRTL_E_ARG, "E_ARG: null argument");
+    set_device(ctx);
+    Design planes;
+    try {
+      planes = bitslice_design(lower_to_packed_program(design_from_json(json, len), top));
+    } catch (const RrtlError& e) {
+      if (e.code == "E_BITSLICE") fail(RRTL_E_UNSUPPORTED, e.what());
+      throw;
+    }
+    load_design(ctx, std::move(planes), top, out);
+    if ((*out)->engine != RRTL_ENGINE_GATE) {
+      rrtl_design_destroy(*out);
+      *out = nullptr;
+      fail(RRTL_E_UNSUPPORTED, "E_BITSLICE: the plane design is outside the gate engine");
+    }
+  });
+}
+
+rrtl_status rrtl_bitslice_json(const char* json, size_t len, const char* top, char* out, size_t cap, size_t* out_len) {
+  return guard([&] {
+    REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
+    std::string js;
+    try {
+      js = design_to_json(bitslice_design(lower_to_packed_program(design_from_json(json, len), top)));
+    } catch (const RrtlError& e) {
+      if (e.code == "E_BITSLICE") fail(RRTL_E_UNSUPPORTED, e.what());
+      throw;
+    }
+    if (out_len) *out_len = js.size();
+    if (out && cap) {
+      const size_t n = std::min(cap - 1, js.size());
+      memcpy(out, js.data(), n);
+      out[n] = 0;
+    }
+  });
+}
+
+static void load_design(rrtl_ctx* ctx, Design design, const std::string& top, rrtl_design** out) {
+  {
     auto d = std::make_unique<rrtl_design>();
     d->ctx = ctx;
-    d->design = design_from_json(json, len);
+    d->design = std::move(design);
     d->top = top;
     PackedProgram pp = lower_to_packed_program(d->design, top);
     d->mp = lower_to_machine_program(pp);
@@ -1205,7 +1253,7 @@ rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, c
     }
     ctx->refs++;
     *out = d.release();
-  });
+  }
 }
 
 rrtl_status rrtl_design_destroy(rrtl_design* d) {

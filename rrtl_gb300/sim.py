@@ -164,6 +164,8 @@ EXPORTS = (
     "rrtl_word_jit_emit",
     "rrtl_instance_fold_plan",
     "rrtl_gate_jit_emit",
+    "rrtl_design_load_bitslice",
+    "rrtl_bitslice_json",
 )
 
 _lib = None
@@ -234,6 +236,8 @@ def lib():
         "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
         "rrtl_instance_fold_plan": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
+        "rrtl_design_load_bitslice": [c_void_p, c_char_p, c_size_t, c_char_p, P(c_void_p)],
+        "rrtl_bitslice_json": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
         "rrtl_gate_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
     }
@@ -379,12 +383,13 @@ def gate_jit_emit(design: Union[_b.Design, str], top: str, run: "Run", arch: Opt
 class CompiledDesign:
     """A design compiled and uploaded once (rrtl_design)."""
 
-    def __init__(self, design: Union[_b.Design, str], top: str, ctx: Optional[Context] = None):
+    def __init__(self, design: Union[_b.Design, str], top: str, ctx: Optional[Context] = None, bitslice: bool = False):
         self.ctx = ctx or default_context()
         text = design.to_json() if isinstance(design, _b.Design) else design
         raw = text.encode()
         self.h = c_void_p()
-        check(lib().rrtl_design_load_json(self.ctx.h, raw, len(raw), top.encode(), byref(self.h)))
+        load = lib().rrtl_design_load_bitslice if bitslice else lib().rrtl_design_load_json
+        check(load(self.ctx.h, raw, len(raw), top.encode(), byref(self.h)))
         self.top = top
         self._cache = {}
 
@@ -870,3 +875,73 @@ class InstanceFoldSimulator:
 
     def eval_combinational(self):
         self.sim.eval_combinational()
+
+
+def bitslice_json(design: Union[_b.Design, str], top: str) -> str:
+    """The plane design (1-bit signals "<signal>[p]") of a multi-bit design,
+    as design JSON (no device needed)."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    n = c_size_t()
+    check(lib().rrtl_bitslice_json(raw, len(raw), top.encode(), None, 0, byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    check(lib().rrtl_bitslice_json(raw, len(raw), top.encode(), buf, n.value + 1, byref(n)))
+    return buf.value.decode()
+
+
+class BitSliceSimulator:
+    """A multi-bit design simulated bit-sliced on the gate engine (the
+    reference's BitSliceSimulator, crates/rrtl-sim-ir/src/bitslice.rs): a
+    W-bit signal is W plane signals "<name>[p]"; set_signal / get_signal move
+    per-lane values (Python ints, up to any width) in and out of the planes."""
+
+    def __init__(self, design: Union[_b.Design, str], top: str, lanes: int, ctx: Optional[Context] = None):
+        self.design = CompiledDesign(design, top, ctx, bitslice=True)
+        self.sim = GpuBatchSimulator(self.design, lanes=lanes)
+        self.lanes = lanes
+        self._width = {}
+
+    def width(self, name: str) -> int:
+        if name not in self._width:
+            w = 0
+            while True:
+                try:
+                    self.design.signal(f"{name}[{w}]")
+                except RrtlError:
+                    break
+                w += 1
+            if w == 0:
+                raise RrtlError(3, f"E_GPU_SIGNAL: no signal `{name}`")
+            self._width[name] = w
+        return self._width[name]
+
+    def planes(self, name: str):
+        return [f"{name}[{p}]" for p in range(self.width(name))]
+
+    def set_signal(self, name: str, lane_values: Sequence[int]):
+        vals = [int(v) for v in lane_values]
+        words = (self.lanes + 31) // 32
+        for p, plane in enumerate(self.planes(name)):
+            bits = np.array([(v >> p) & 1 for v in vals], dtype=np.uint32)
+            packed = np.zeros(words, dtype=np.uint32)
+            idx = np.nonzero(bits)[0]
+            np.bitwise_or.at(packed, idx // 32, (np.uint32(1) << (idx % 32).astype(np.uint32)))
+            self.sim.set_input_bits(plane, packed)
+
+    def get_signal(self, name: str) -> list:
+        out = [0] * self.lanes
+        for p, plane in enumerate(self.planes(name)):
+            words = self.sim.get_signal_bits(plane)
+            bits = (words[np.arange(self.lanes) // 32] >> (np.arange(self.lanes) % 32).astype(np.uint32)) & 1
+            for l in np.nonzero(bits)[0]:
+                out[l] |= 1 << p
+        return out
+
+    def eval_combinational(self):
+        self.sim.eval_combinational()
+
+    def tick(self):
+        self.sim.tick()
+
+    def tick_many(self, steps: int):
+        self.sim.tick_many(steps)

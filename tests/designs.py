@@ -13,7 +13,7 @@ from rrtl_gb300.workloads import Rng
 
 
 def random_word_design(seed, n_inputs=4, n_regs=5, n_wires=14, n_mems=1, max_width=64, depth=3,
-                       wire_every_node=False, async_resets=True, top="Rand"):
+                       wire_every_node=False, async_resets=True, top="Rand", no_mul=False):
     rng = Rng(seed)
     d = Design()
     m = d.module(top)
@@ -85,7 +85,7 @@ def random_word_design(seed, n_inputs=4, n_regs=5, n_wires=14, n_mems=1, max_wid
             e = a & b if k == 1 else a | b if k == 2 else a ^ b
         elif k in (4, 5, 6):
             a, b = expr(w, dep - 1), expr(w, dep - 1)
-            e = a + b if k == 4 else a - b if k == 5 else a * b
+            e = a + b if k == 4 else a - b if k == 5 else (a ^ b if no_mul else a * b)
         elif k == 7 and w == 1:
             v = widths[rng.below(len(widths))]
             a, b = expr(v, dep - 1), expr(v, dep - 1)
