@@ -498,6 +498,36 @@ def crc32_leg(ctx, sim, cycles=2000):
                                     "note": "published Apple M3 numbers, unavailable on this box (OpenCL.framework)"}}
 
 
+def bitslice_leg(ctx, sim, cycles=1000):
+    """Bit-sliced multi-bit evaluation: a 16-bit ALU datapath (add, sub, xor,
+    compare, mux; no multiply or memory) run as bit-planes on the gate engine
+    against the word engine's compiled kernel, random inputs, no recording."""
+    from rrtl_gb300.workloads import narrow_alu
+
+    js = narrow_alu(16).to_json()
+    planes = sim.CompiledDesign(js, "Alu", ctx, bitslice=True)
+    words = sim.CompiledDesign(js, "Alu", ctx)
+    rows = []
+    for lanes in (65536, 1048576):
+        row = {"lanes": lanes}
+        for key, cd, stim in (
+                ("bitsliced", planes, [("__bitslice_clk", sim.STIM_CONST, 1), ("rst[0]", sim.STIM_PULSE, 1)] +
+                 [(f"din[{p}]", sim.STIM_RANDOM, p) for p in range(16)] + [(f"sel[{p}]", sim.STIM_RANDOM, 20 + p)
+                                                                          for p in range(2)]),
+                ("word", words, [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("din", sim.STIM_RANDOM, 1),
+                                 ("sel", sim.STIM_RANDOM, 2)])):
+            g = sim.GpuBatchSimulator(cd, lanes=lanes)
+            g.run(10, stim=stim)
+            best = float("inf")
+            for _ in range(3):
+                g.run(cycles, stim=stim)
+                best = min(best, g.last_kernel_ms)
+            row[key] = lanes * cycles / (best / 1e3)
+        rows.append(row)
+    return {"design": "16-bit ALU datapath", "cycles": cycles, "unit": "lane-cycles/s",
+            "plane_cells": planes.info.n_gates, "word_instrs": words.info.n_gates, "rows": rows}
+
+
 def instance_fold_leg(ctx, sim, cycles=2000):
     """Instance folding: a wrapper of 64 independent 32-bit datapaths,
     flattened (one program with 64 copies, `base` lanes) against folded (the
@@ -596,6 +626,7 @@ def main():
     ap.add_argument("--cpu8-cycles", type=int, default=20_000, help="cycles of the pipelined-CPU compiled run")
     ap.add_argument("--no-fold", action="store_true", help="skip the instance-folding leg")
     ap.add_argument("--no-crc32", action="store_true", help="skip the crc32 compiled-gate-kernel leg")
+    ap.add_argument("--no-bitslice", action="store_true", help="skip the bit-slice leg")
     ap.add_argument("--crc32-only", action="store_true", help="only the crc32 leg")
     ap.add_argument("--fold-only", action="store_true", help="only the instance-folding leg")
     args = ap.parse_args()
@@ -625,7 +656,7 @@ def main():
     if args.crc32_only:
         ctx = sim.Context(local)
         if rank == 0:
-            print(json.dumps({"crc32": crc32_leg(ctx, sim)}))
+            print(json.dumps({"crc32": crc32_leg(ctx, sim), "bitslice": bitslice_leg(ctx, sim)}))
         return
     d, meta, js, stim, rec = build_workload()
     ctx = sim.Context(local)
@@ -739,6 +770,8 @@ def main():
         out["instance_fold"] = instance_fold_leg(ctx, sim)
     if not args.no_crc32:
         out["crc32"] = crc32_leg(ctx, sim)
+    if not args.no_bitslice:
+        out["bitslice"] = bitslice_leg(ctx, sim)
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:

@@ -454,3 +454,32 @@ def replicated_datapath(n_instances: int, top: str = "Top", child: str = "Lane")
         oi = t.output(f"o{i}", uint(32))
         t.instance(f"u{i}", child, [("clk", tclk), ("rst", trst), ("din", di), ("o", oi)])
     return d
+
+
+def narrow_alu(width: int = 16, top: str = "Alu") -> Design:
+    """A small multi-bit datapath inside the bit-slice scope (no memory, no
+    multiply): two operand registers loaded from inputs, an accumulator that
+    adds, subtracts, xors or keeps the larger operand by a 2-bit select, and
+    a flag output; synchronous reset."""
+    d = Design()
+    m = d.module(top)
+    clk = m.input("clk", uint(1))
+    rst = m.input("rst", uint(1))
+    din = m.input("din", uint(width))
+    sel = m.input("sel", uint(2))
+    a = m.reg("a", uint(width))
+    b = m.reg("b", uint(width))
+    acc = m.reg("acc", uint(width))
+    for r in (a, b, acc):
+        m.clock(r, clk)
+        m.reset(r, rst, 0)
+    m.next(a, din)
+    m.next(b, a ^ acc)
+    s0, s1 = sel.slice(0, 1), sel.slice(1, 1)
+    larger = mux(a.lt_expr(b), b, a)
+    m.next(acc, mux(s1, mux(s0, acc + a, acc - b), mux(s0, acc ^ larger, acc + larger)))
+    flag = m.output("flag", uint(1))
+    m.assign(flag, acc.eq_expr(a))
+    out = m.output("out", uint(width))
+    m.assign(out, acc)
+    return d

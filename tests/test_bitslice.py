@@ -74,6 +74,10 @@ def test_counter_and_adder_chain():
     o = m.output("o", uint(1))
     m.assign(o, acc.eq_expr(a))
     compare_on_oracle(d.to_json(), "Acc", [("clk", 1), ("rst", 1), ("a", 100), ("b", 100)], [("acc", 100), ("o", 1)])
+    from rrtl_gb300.workloads import narrow_alu
+
+    compare_on_oracle(narrow_alu(16).to_json(), "Alu", [("clk", 1), ("rst", 1), ("din", 16), ("sel", 2)],
+                      [("acc", 16), ("out", 16), ("flag", 1), ("b", 16)])
 
 
 def test_out_of_scope_designs_are_rejected():
