@@ -191,6 +191,15 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
     aot.run(lanes, cycles, SEED)
     dt = time.perf_counter() - t
     value = lanes * cycles / dt
+    # one core, on a quarter of the budget
+    l1 = 64 * 8
+    t = time.perf_counter()
+    aot.run(l1, 8, SEED, threads=1)
+    d1 = max(time.perf_counter() - t, 1e-3)
+    c1 = max(8, int(budget_s / 4 / d1 * 8))
+    t = time.perf_counter()
+    aot.run(l1, c1, SEED, threads=1)
+    one_core = l1 * c1 / (time.perf_counter() - t)
     # the interpreter on a shorter sample
     ilanes, icycles = 64 * threads * 4, 4
     run = ob.make_run(icycles, SEED, stim_idx, rec_idx, 2, out_hash=np.zeros(icycles, dtype=np.uint64))
@@ -201,6 +210,7 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
             "sample": f"{lanes} lanes x {cycles} cycles of the same netlist and stimulus (bit-parallel AOT: "
                       f"emitted C, gcc -O2, {threads} threads)", "seconds": round(dt, 3),
             "compile_s": round(compile_s, 1),
+            "one_core": {"value": one_core, "sample": f"{l1} lanes x {c1} cycles, 1 thread"},
             "interpreter": {"value": ilanes * icycles / idt, "sample": f"{ilanes} lanes x {icycles} cycles"}}
 
 
