@@ -630,6 +630,7 @@ def main():
     ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
     ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
+    ap.add_argument("--serve-round-us", type=int, default=10_000, help="serving loop target round time")
     ap.add_argument("--word-only", action="store_true",
                     help="profiling case: only the pipelined-CPU word config (its compiled run is the second "
                          "rrtl_word_jit launch, after the batch's creation settle)")
@@ -786,7 +787,8 @@ def main():
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
     if args.serve_rates:
         rates = [float(x) for x in args.serve_rates.split(",") if x]
-        out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), rates, args.serve_seconds)
+        out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), rates, args.serve_seconds,
+                                     round_us=args.serve_round_us)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import binding as ob
 

@@ -121,6 +121,7 @@ uint32_t log2_words(uint32_t W) { return W == 8 ? 3u : W == 4 ? 2u : W == 2 ? 1u
 // 512 groups) and shrink until the tables fit too.
 GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
   uint32_t li = log2_words(W);
+  std::lock_guard<std::mutex> lk(d->gvar_mu);
   if (d->gvar[li]) return d->gvar[li].get();
   auto v = std::make_unique<GateVariant>();
   v->W = W;
@@ -759,6 +760,27 @@ const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t) {
     it = d->wjit_runs.emplace(key, std::move(J)).first;
   }
   return it->second->ok ? it->second.get() : any;
+}
+
+void design_warm_for_run(rrtl_design* d, uint32_t lanes, const rrtl_run& run) {
+  set_device(d->ctx);
+  if (d->engine == RRTL_ENGINE_GATE) {
+    if (d->gate_w_max) gate_variant(d, choose_tile_words(d, (lanes + 31) / 32));
+    return;
+  }
+  WordRunTables t;
+  uint32_t base = 0;
+  for (uint32_t i = 0; i < run.n_stim; ++i) {
+    const PackedSignal& ps = signal_of(d, run.stim[i].signal);
+    t.stim.push_back(WordStimDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, run.stim[i].kind, run.stim[i].param});
+  }
+  for (uint32_t i = 0; i < run.n_record; ++i) {
+    const PackedSignal& ps = signal_of(d, run.record[i]);
+    t.rec.push_back(WordRecDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, base});
+    base += ps.layout.limbs;
+  }
+  t.mode = run.record_mode;
+  word_jit_for_run(d, t);
 }
 
 void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle,

@@ -149,6 +149,10 @@ bool gate_jit_preferred(rrtl_design* d, uint32_t words);
 constexpr uint32_t kTunedCompiled = 0xFFFFFFFFu;
 // Designs of at most this many cells use the compiled gate kernel unless tuned otherwise.
 constexpr uint32_t kGateJitAutoCells = 1024;
+// Host-side preparation a run of `lanes` lanes will need (the gate
+// program variant of its tile width, or the word kernel compiled for its
+// tables), done ahead so that the serving loop's admission finds it built.
+void design_warm_for_run(rrtl_design* d, uint32_t lanes, const rrtl_run& run);
 // Throws E_WORD_SCOPE when the interpreted word kernel cannot hold the design's value slots.
 void word_require_interp(const rrtl_design* d, const WordPrepared& g);
 // The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
@@ -196,6 +200,7 @@ struct rrtl_design {
   rrtl::WordProgram wp;
   rrtl::WordProgDev wdev{};
   rrtl::DevBuf d_wcode, d_wcap, d_wlit;
+  std::mutex gvar_mu;  // builds of gvar entries (serving producers prepare designs concurrently)
   std::mutex wjit_mu;
   std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel for any run, built on the first fused run
   std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;  // kernels compiled for one run's tables

@@ -430,6 +430,9 @@ rrtl_status rrtl_server_create(rrtl_ctx* ctx, const rrtl_server_opts* opts, rrtl
     s->chunk = opts && opts->chunk_cycles ? opts->chunk_cycles : 256;
     s->max_active = opts ? opts->max_active : 0;
     s->round_ms = opts ? opts->round_us / 1000.0 : 0.0;
+    // the first NVRTC compile of a process pays for loading the compiler;
+    // pay it here rather than in the first word request's admission
+    jit_warm();
     ctx->refs++;
     rrtl_server* raw = s.release();
     raw->owner = std::thread([raw] { raw->loop(); });
@@ -462,6 +465,13 @@ rrtl_status rrtl_server_submit(rrtl_server* s, const rrtl_request* req, uint64_t
     r->run.record = r->record.data();
     r->bytes = request_bytes(*r);
     r->t_submit = now_ns();
+    // build what admission will need (a tile-width variant, a compiled word
+    // kernel) on the submitting thread, so the device loop never stalls on it;
+    // a failure here surfaces again at admission
+    try {
+      design_warm_for_run(r->design, r->lanes, r->run);
+    } catch (...) {
+    }
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (s->stop) fail(RRTL_E_ARG, "E_SERVER: the server is shutting down");

@@ -467,6 +467,14 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
   return cubin;
 }
 
+void jit_warm() {
+  static std::once_flag once;
+  std::call_once(once, [] {
+    std::string log;
+    word_jit_compile("extern \"C\" __global__ void rrtl_warm() {}\n", "sm_103a", &log);
+  });
+}
+
 void jit_build_kernel(const std::string& src, int device, const char* name, WordJit* J) {
   const auto t0 = std::chrono::steady_clock::now();
   cudaDeviceProp prop{};

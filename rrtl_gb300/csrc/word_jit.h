@@ -60,6 +60,10 @@ std::string word_jit_source(const WordProgram& wp, const WordRunTables* run = nu
 // or an empty vector with `log` holding the compiler's messages.
 std::vector<char> word_jit_compile(const std::string& src, const std::string& arch, std::string* log);
 
+// Load and exercise NVRTC once (a trivial compile) so later compiles skip
+// its start-up cost; a no-op when NVRTC is absent.
+void jit_warm();
+
 // Compile CUDA source `src` with NVRTC for `device` and load its kernel
 // `name` into J. Never throws: failures leave ok = false and the reason in
 // error.
