@@ -324,7 +324,7 @@ def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
     return out
 
 
-def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000), round_us=10_000):
+def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000), round_us=5_000):
     """Serving loop (the C5 shape): Poisson arrivals over three resident
     designs (the 50k-gate netlist, the 8-stage CPU, a 500k-gate / 20k-FF
     netlist of the same family); lanes log-uniform 64-16,384, cycles
@@ -630,7 +630,7 @@ def main():
     ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
     ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
-    ap.add_argument("--serve-round-us", type=int, default=10_000, help="serving loop target round time")
+    ap.add_argument("--serve-round-us", type=int, default=5_000, help="serving loop target round time")
     ap.add_argument("--word-only", action="store_true",
                     help="profiling case: only the pipelined-CPU word config (its compiled run is the second "
                          "rrtl_word_jit launch, after the batch's creation settle)")
