@@ -433,8 +433,9 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
  * compiled for the design and the run's tables: one thread per 32-lane word,
  * every net a register, one LOP3 per cell (the reference's per-design
  * compiled kernel, crates/rrtl-sim-ir/src/gpu_codegen.rs:503-557). Designs
- * of up to 1,024 cells use it unless the autotuner measured a tile width
- * faster for the lane count; rrtl_design_autotune times it as a candidate and
+ * whose live nets fit in registers (at most 192 at once) use it unless the
+ * autotuner measured a tile width faster for the lane count (larger designs
+ * spill and run faster on the fused kernel); rrtl_design_autotune times it as a candidate and
  * reports it as best_words = 0. rrtl_batch_tile_words reads 0 after such a
  * run. This call emits (and with arch compiles) that kernel without a device,
  * like rrtl_word_jit_emit; run is required (its signals are packed indices).

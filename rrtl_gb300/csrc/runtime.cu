@@ -562,9 +562,11 @@ const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
 }
 
 bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
+  const char* env = getenv("RRTL_GATE_JIT");
+  if (env && env[0] == '2') return true;  // A/B switch: every design within the compiled kernel's size limit
   auto tuned = d->tuned_w.find(lane_bucket(words));
   if (tuned != d->tuned_w.end()) return tuned->second == kTunedCompiled;
-  return d->gp().n_real_cells <= kGateJitAutoCells;
+  return d->gp().n_slots <= kGateJitAutoSlots && d->gp().n_real_cells <= kGateJitMaxCells;
 }
 
 void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckTables* chk = nullptr,

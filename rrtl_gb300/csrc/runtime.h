@@ -144,11 +144,14 @@ WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool 
 // kept per design), or nullptr when the design or run does not qualify.
 const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t);
 // Whether a fused-path run of `words` 32-lane words should use the compiled
-// gate kernel: the autotuner's choice for the lane bucket, else small designs.
+// gate kernel: the autotuner's choice for the lane bucket, else designs whose
+// live nets fit in registers.
 bool gate_jit_preferred(rrtl_design* d, uint32_t words);
 constexpr uint32_t kTunedCompiled = 0xFFFFFFFFu;
-// Designs of at most this many cells use the compiled gate kernel unless tuned otherwise.
-constexpr uint32_t kGateJitAutoCells = 1024;
+// Designs whose peak of live nets (the fused program's slot count) is at
+// most this use the compiled gate kernel unless tuned otherwise: beyond it
+// the nets no longer fit the registers of one thread and spill.
+constexpr uint32_t kGateJitAutoSlots = 192;
 // Host-side preparation a run of `lanes` lanes will need (the gate
 // program variant of its tile width, or the word kernel compiled for its
 // tables), done ahead so that the serving loop's admission finds it built.

@@ -1,9 +1,8 @@
 """The per-design compiled gate kernel against the fused and plain gate
 kernels and the bit-parallel oracle.
 
-Small netlists (up to 1,024 cells) run the compiled kernel on the default
-path, so the crc32 and small-netlist oracle tests elsewhere already check
-it; these tests pin that it is the kernel that runs and that it equals the
+Netlists whose live nets fit in registers (crc32) run the compiled kernel
+on the default path, so the crc32 oracle tests elsewhere already check it; these tests pin that it is the kernel that runs and that it equals the
 other paths under every record mode and stimulus kind."""
 import numpy as np
 import pytest
@@ -47,7 +46,10 @@ def test_crc32_compiled_equals_fused_and_plain(engine, lanes):
 
 
 @pytest.mark.parametrize("seed", range(4))
-def test_small_netlists_compiled_match_oracle(engine, seed):
+def test_small_netlists_compiled_match_oracle(engine, seed, monkeypatch):
+    # these netlists have more live nets than the automatic choice puts in
+    # registers: force the compiled kernel
+    monkeypatch.setenv("RRTL_GATE_JIT", "2")
     d, meta = gate_netlist(n_gates=300 + 150 * seed, n_ff=24 + 8 * seed, n_pi=12, n_po=16, depth=6 + seed, seed=70 + seed)
     js = d.to_json()
     cd = sim.CompiledDesign(js, meta.top)
