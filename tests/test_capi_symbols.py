@@ -24,8 +24,11 @@ def test_library_exports_every_declared_symbol():
     assert set(names) == set(sim.EXPORTS)
 
 
-def test_last_error_is_empty_before_any_call():
+def test_last_error_is_empty_after_a_successful_call():
+    from rrtl_gb300.workloads import counter
+
     build.build()
+    sim.word_jit_emit(counter(), "Counter")  # no device needed
     assert sim.lib().rrtl_last_error() == b""
 
 
