@@ -566,7 +566,9 @@ bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
   if (env && env[0] == '2') return true;  // A/B switch: every design within the compiled kernel's size limit
   auto tuned = d->tuned_w.find(lane_bucket(words));
   if (tuned != d->tuned_w.end()) return tuned->second == kTunedCompiled;
-  return d->gp().n_slots <= kGateJitAutoSlots && d->gp().n_real_cells <= kGateJitMaxCells;
+  const GateProgram& gp = d->gp();
+  if (gp.n_real_cells > kGateJitMaxCells) return false;
+  return gp.n_slots <= kGateJitAutoSlots || gp.n_real_cells < (uint64_t)kGateJitNarrowLevel * std::max(1u, gp.n_levels);
 }
 
 void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckTables* chk = nullptr,

@@ -152,6 +152,10 @@ constexpr uint32_t kTunedCompiled = 0xFFFFFFFFu;
 // most this use the compiled gate kernel unless tuned otherwise: beyond it
 // the nets no longer fit the registers of one thread and spill.
 constexpr uint32_t kGateJitAutoSlots = 192;
+// Designs of narrow levels (fewer cells per level on average than this) use
+// it too: the fused kernel's per-level barrier then dominates and most of its
+// warps idle, which costs more than spilled nets.
+constexpr uint32_t kGateJitNarrowLevel = 48;
 // Host-side preparation a run of `lanes` lanes will need (the gate
 // program variant of its tile width, or the word kernel compiled for its
 // tables), done ahead so that the serving loop's admission finds it built.
