@@ -102,8 +102,11 @@ def test_word_engine_replay_matches_oracle_and_logs_planted_mismatches(engine):
     assert n3 == len(planted) and len(log3) == 3 and set(log3) <= planted
 
 
-@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN])
-def test_gate_engine_replay_matches_oracle(engine, path):
+@pytest.mark.parametrize("path", [sim.PATH_FUSED, sim.PATH_PLAIN, "compiled"])
+def test_gate_engine_replay_matches_oracle(engine, path, monkeypatch):
+    if path == "compiled":  # the compiled gate kernel's check stage
+        monkeypatch.setenv("RRTL_GATE_JIT", "2")
+        path = sim.PATH_FUSED
     d, meta = gate_netlist(n_gates=1500, n_ff=80, n_pi=12, n_po=16, depth=8, seed=44)
     js = d.to_json()
     od = ob.OracleDesign(js, meta.top)
