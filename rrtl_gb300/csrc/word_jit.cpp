@@ -531,7 +531,9 @@ size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_wo
   // shared memory between them (one block's rows sit idle otherwise)
   const uint32_t blocks = lanes_pad / kThreads;
   const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(4, (blocks + sm_count - 1) / std::max<uint32_t>(sm_count, 1)));
-  const size_t budget = std::min(max_smem_block, max_smem_sm / per_sm - 1024) - J.static_smem;
+  const size_t share = std::min(max_smem_block, max_smem_sm / per_sm);
+  const size_t reserve = 1024 + J.static_smem;
+  const size_t budget = share > reserve ? share - reserve : 0;
   // staging costs one pass over the rows at each end of the launch: worth it
   // when the launch runs a few cycles per staged row
   auto worth = [&](uint64_t rows) { return rows <= 64 || rows <= 4 * cycles; };
