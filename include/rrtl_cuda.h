@@ -425,7 +425,15 @@ rrtl_status rrtl_design_word_jit(rrtl_design* design, uint32_t* active, float* c
  * (values over 64 bits) or the compiler fails. */
 rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
-                               size_t log_cap);
+                               size_t log_cap, uint32_t flags);
+/* flags bit 0 (RRTL_JIT_SPLIT): with run, the two-warp form (two warps per 32
+ * lanes, each evaluating the cones of its share of the registers and memory
+ * writes, registers exchanged through shared memory at the clock edge), which
+ * the fused path runs when the environment sets RRTL_WORD_JIT_SPLIT=2 (it
+ * measured slower than one warp per 32 lanes); RRTL_E_UNSUPPORTED when the
+ * design does not split
+ * (asynchronous resets, combinational feedback, very uneven cones). */
+enum { RRTL_JIT_SPLIT = 1 };
 
 /* ---- per-design compiled gate kernels ---------------------------------------
  * A gate-engine run on the fused path without stuck-at forces, with an

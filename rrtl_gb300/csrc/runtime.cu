@@ -750,10 +750,28 @@ const WordJit* word_jit_get(rrtl_design* d) {
   return d->wjit->ok ? d->wjit.get() : nullptr;
 }
 
-const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t) {
+const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad) {
   const WordJit* any = word_jit_get(d);
   const char* env = getenv("RRTL_WORD_JIT_RUNS");
   if (!any || (env && env[0] == '0') || t.stim.size() > kJitRunTableMax || t.rec.size() > kJitRunTableMax) return any;
+  // two warps per 32 lanes on request only (RRTL_WORD_JIT_SPLIT=2): measured
+  // slower than one warp on the pipelined CPU even at 4,096 lanes
+  const char* senv = getenv("RRTL_WORD_JIT_SPLIT");
+  const bool want_split = lanes_pad && senv && senv[0] == '2';
+  if (want_split) {
+    const std::string skey = t.key() + "|split";
+    std::lock_guard<std::mutex> lk(d->wjit_mu);
+    auto it = d->wjit_runs.find(skey);
+    if (it == d->wjit_runs.end() && d->wjit_runs.size() < kJitRunKernelsPerDesign) {
+      auto J = std::make_unique<WordJit>();
+      WordSplitPlan plan;
+      std::string why;
+      if (word_split_plan(d->wp, t, &plan, &why)) word_jit_build(d->wp, d->ctx->device, J.get(), &t, &plan);
+      else J->error = "no split: " + why;
+      it = d->wjit_runs.emplace(skey, std::move(J)).first;
+    }
+    if (it != d->wjit_runs.end() && it->second->ok) return it->second.get();
+  }
   const std::string key = t.key();
   std::lock_guard<std::mutex> lk(d->wjit_mu);
   auto it = d->wjit_runs.find(key);
@@ -784,7 +802,7 @@ void design_warm_for_run(rrtl_design* d, uint32_t lanes, const rrtl_run& run) {
     base += ps.layout.limbs;
   }
   t.mode = run.record_mode;
-  word_jit_for_run(d, t);
+  word_jit_for_run(d, t, (lanes + 127) / 128 * 128);
 }
 
 void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_settle, bool final_settle,
@@ -796,7 +814,7 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   g.R.final_settle = final_settle;
   const bool per_cycle = (b->path == RRTL_PATH_PLAIN || b->path == RRTL_PATH_PLAIN_GRAPH) && run.cycles > 1;
   // compile before the timed region opens
-  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables) : nullptr;
+  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables, b->lanes_pad) : nullptr;
   if (!J) word_require_interp(d, g);
   Timer tm(b);
   if (per_cycle) {
@@ -1311,7 +1329,7 @@ rrtl_status rrtl_design_word_jit(rrtl_design* d, uint32_t* active, float* compil
 
 rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
-                               size_t log_cap) {
+                               size_t log_cap, uint32_t flags) {
   return guard([&] {
     REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
     if (cubin_bytes) *cubin_bytes = 0;
@@ -1344,7 +1362,13 @@ rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, co
       }
       tabs.mode = run->record_mode;
     }
-    const std::string src = word_jit_source(wp, run ? &tabs : nullptr);
+    WordSplitPlan plan;
+    const bool split = run && (flags & RRTL_JIT_SPLIT);
+    if (split) {
+      std::string why;
+      REQUIRE(word_split_plan(wp, tabs, &plan, &why), RRTL_E_UNSUPPORTED, "E_WORD_JIT_SPLIT: " + why);
+    }
+    const std::string src = word_jit_source(wp, run ? &tabs : nullptr, split ? &plan : nullptr);
     if (source_len) *source_len = src.size();
     if (source && source_cap) {
       const size_t n = std::min(source_cap - 1, src.size());

@@ -166,7 +166,8 @@ void word_require_interp(const rrtl_design* d, const WordPrepared& g);
 const WordJit* word_jit_get(rrtl_design* d);
 // The kernel compiled for this run's tables (built on first use and kept per
 // design), else the design's general compiled kernel, else nullptr.
-const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t);
+// lanes_pad: the batch's padded lanes (0: no two-warp split).
+const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad = 0);
 cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st);
 cudaError_t word_multi_prepare(size_t smem);
 constexpr uint32_t kWordBlockLanes = 128;

@@ -160,7 +160,7 @@ void rrtl_server::admit(std::vector<std::shared_ptr<Request>>& fresh) {
         r.fused = r.gp.fused && r.gp.v->fused_smem <= ctx->max_smem - gate_queue_static_smem();
       } else {
         r.wp = word_prepare(r.batch, r.run, false, false);
-        r.jit = word_jit_for_run(r.design, r.wp.tables);  // compiled once per design and run tables
+        r.jit = word_jit_for_run(r.design, r.wp.tables, r.wp.R.lanes_pad);  // compiled once per design and run tables
         if (!r.jit) word_require_interp(r.design, r.wp);
       }
       active.push_back(rp);

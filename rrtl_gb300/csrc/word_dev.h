@@ -103,7 +103,7 @@ struct WordJitPlace {
   uint32_t sig_smem;      // 1: signal words staged from row 0
   uint32_t n_sig_words;
   uint32_t n_mems;        // memories with an entry below (min(memories, kJitPlacedMems))
-  uint32_t pad;
+  uint32_t x_row;         // split kernels: first row of the register exchange area
   uint32_t mem_off[kJitPlacedMems];    // first word of memory k in a lane's memory block
   uint32_t mem_words[kJitPlacedMems];  // depth x limbs
   uint32_t smem_row[kJitPlacedMems];   // first shared-memory row, ~0 = stays in HBM

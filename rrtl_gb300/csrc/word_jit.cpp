@@ -20,6 +20,8 @@
 #include <cstdio>
 #include <mutex>
 #include <set>
+#include <unordered_map>
+#include <unordered_set>
 
 // kJitHeaderCount, kJitHeaderNames, kJitHeaderTexts: the headers the
 // generated source includes, embedded at build time.
@@ -46,6 +48,7 @@ std::string u(uint64_t v) { return std::to_string(v) + "u"; }
 struct Emitter {
   const WordProgram& wp;
   const WordRunTables* run = nullptr;
+  const WordSplitPlan* split = nullptr;
   std::string o;
 
   const bool regs;  // signal words as register members s<k>
@@ -256,10 +259,11 @@ struct Emitter {
   }
 
   // One stream in its own scope with its own slot locals.
-  void block(uint32_t b, uint32_t e, const char* what) {
+  void block(uint32_t b, uint32_t e, const char* what, const std::vector<uint8_t>* mask = nullptr) {
     if (b == e) return;
     std::set<uint32_t> slots;
-    for (uint32_t pc = b; pc < e; ++pc) uses(wp.code[pc], slots);
+    for (uint32_t pc = b; pc < e; ++pc)
+      if (!mask || (*mask)[pc]) uses(wp.code[pc], slots);
     o += "  {  // ";
     o += what;
     o += '\n';
@@ -274,6 +278,7 @@ struct Emitter {
     }
     vw.assign(slots.empty() ? 0 : *slots.rbegin() + 1, 64u);
     for (uint32_t pc = b; pc < e; ++pc) {
+      if (mask && !(*mask)[pc]) continue;
       std::string s = stmt(wp.code[pc]);
       if (!s.empty()) line(s);
       define(wp.code[pc]);
@@ -309,6 +314,28 @@ struct Emitter {
     }
     o += "  __device__ void settle();\n";
     o += "  __device__ void edge();\n";
+    if (split) {
+      o += "  __device__ void settle_part(uint32_t p);\n";
+      o += "  __device__ void edge_part(uint32_t p);\n";
+      for (const char* fn : {"xout", "xin"}) {
+        o += std::string("  __device__ __forceinline__ void ") + fn + "(uint32_t p, uint32_t* X, uint32_t lid) {\n";
+        for (int q = 0; q < 2; ++q) {
+          o += std::string(q ? "    else {\n" : "    if (p == 0u) {\n");
+          for (size_t x = 0; x < split->xwords.size(); ++x) {
+            const std::string cell = "X[" + u(x) + " * 32u + lid]";
+            const std::string sv = "s" + std::to_string(split->xwords[x]);
+            if (fn[1] == 'o' && split->owner[x] == q) o += "      " + cell + " = " + sv + ";\n";
+            if (fn[1] == 'i' && split->need[q][x]) o += "      " + sv + " = " + cell + ";\n";
+          }
+          o += "    }\n";
+        }
+        o += "  }\n";
+      }
+      o += "  __device__ __forceinline__ void xin_all(uint32_t* X, uint32_t lid) {\n";
+      for (size_t x = 0; x < split->xwords.size(); ++x)
+        if (split->owner[x] != 0) o += "    s" + std::to_string(split->xwords[x]) + " = X[" + u(x) + " * 32u + lid];\n";
+      o += "  }\n";
+    }
     o += "};\n";
     o += std::string(big ? "__device__ __noinline__" : "__device__ __forceinline__") + " void JitLane::settle() {\n";
     block(wp.comb_b, wp.comb_e, "comb");
@@ -326,6 +353,34 @@ struct Emitter {
       for (uint32_t l = 0; l < cm.limbs; ++l)
         o += "  " + sig(cm.sig_off + l) + " = c" + std::to_string(cm.cap_off + l) + ";\n";
     o += "}\n";
+    if (split) {
+      o += "__device__ __forceinline__ void JitLane::settle_part(uint32_t p) {\n";
+      for (int q = 0; q < 2; ++q) {
+        o += std::string(q ? "  else {\n" : "  if (p == 0u) {\n");
+        block(wp.comb_b, wp.comb_e, "comb, this warp's cones", &split->in[q]);
+        o += "  }\n";
+      }
+      o += "}\n";
+      o += "__device__ __forceinline__ void JitLane::edge_part(uint32_t p) {\n";
+      for (int q = 0; q < 2; ++q) {
+        o += std::string(q ? "  else {\n" : "  if (p == 0u) {\n");
+        if (wp.total_capture_words) {
+          std::string decl = "  uint32_t";
+          for (uint32_t k = 0; k < wp.total_capture_words; ++k) decl += (k ? ", c" : " c") + std::to_string(k) + " = 0u";
+          o += decl + ";\n";
+        }
+        block(wp.next_b, wp.next_e, "tick_next: this warp's captures", &split->in[q]);
+        block(wp.commit_b, wp.commit_e, "tick_commit: this warp's memory writes", &split->in[q]);
+        for (size_t k = 0; k < wp.commits.size(); ++k) {
+          if (split->commit_owner[k] != q) continue;
+          const WCommitDev& cm = wp.commits[k];
+          for (uint32_t l = 0; l < cm.limbs; ++l)
+            o += "  " + sig(cm.sig_off + l) + " = c" + std::to_string(cm.cap_off + l) + ";\n";
+        }
+        o += "  }\n";
+      }
+      o += "}\n";
+    }
     o += "}  // namespace rrtl\n";
     if (run) {
       // this run's tables as compile-time constants
@@ -350,10 +405,13 @@ struct Emitter {
       o += "  __device__ __forceinline__ static constexpr uint32_t mode() { return " + u(run->mode) + "; }\n";
       o += "};\n}  // namespace rrtl\n";
     }
-    o += "extern \"C\" __global__ void __launch_bounds__(128) rrtl_word_jit(const rrtl::WordRunDev R, "
+    o += std::string("extern \"C\" __global__ void __launch_bounds__(") + (split ? "64" : "128") +
+         ") rrtl_word_jit(const rrtl::WordRunDev R, "
          "const rrtl::WordJitPlace Pl) {\n";
     o += "  extern __shared__ uint32_t rrtl_jsm[];\n";
-    if (run) {
+    if (run && split) {
+      o += "  rrtl::word_jit_run_split<rrtl::JitLane>(R, Pl, rrtl_jsm, rrtl::RunSpec{});\n";
+    } else if (run) {
       o += "  rrtl::word_jit_run<rrtl::JitLane>(R, Pl, rrtl_jsm, rrtl::RunSpec{});\n";
     } else {
       o += "  __shared__ rrtl::JitDynamicRun tables;\n";
@@ -414,10 +472,156 @@ WordJit::~WordJit() {
   if (lib) cudaLibraryUnload(lib);
 }
 
-std::string word_jit_source(const WordProgram& wp, const WordRunTables* run) {
+std::string word_jit_source(const WordProgram& wp, const WordRunTables* run, const WordSplitPlan* split) {
   Emitter e(wp);
   e.run = run;
+  e.split = run ? split : nullptr;
   return e.source();
+}
+
+bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitPlan* sp, std::string* why) {
+  auto no = [&](const char* w) {
+    if (why) *why = w;
+    return false;
+  };
+  if (wp.async_b != wp.async_e) return no("asynchronous resets");
+  if (wp.n_sig_words > kJitRegSignals || wp.code.size() > kJitMaxInstrs) return no("too large");
+  const size_t N = wp.code.size();
+  std::vector<std::vector<uint32_t>> dep(N);
+  std::unordered_map<uint32_t, uint32_t> sig_def;  // signal word -> the comb store that defines it this cycle
+  std::unordered_set<uint32_t> read_before_store;
+  auto walk = [&](uint32_t b, uint32_t e, bool comb) {
+    std::unordered_map<uint32_t, uint32_t> slot_def;
+    for (uint32_t pc = b; pc < e; ++pc) {
+      const WInstr& I = wp.code[pc];
+      auto use = [&](uint32_t sl) {
+        auto it = slot_def.find(sl);
+        if (it != slot_def.end()) dep[pc].push_back(it->second);
+      };
+      auto usesig = [&](uint32_t off) {
+        auto it = sig_def.find(off);
+        if (it != sig_def.end()) dep[pc].push_back(it->second);
+        else if (comb) read_before_store.insert(off);
+      };
+      switch (I.op) {
+        case W_LIT: break;
+        case W_SIG: usesig(I.aux); if (I.flags & 1) usesig(I.aux + 1); break;
+        case W_NOT: case W_SLICE: case W_MASK: case W_SEXT: case W_MEMRD: use(I.a); break;
+        case W_MUX: use(I.a); use(I.b); use(I.c); break;
+        case W_STORE: use(I.a); break;
+        case W_ASTORE: use(I.a); usesig(I.aux2); break;
+        case W_CAPTURE: use(I.a); if (I.flags & 2) usesig(I.aux2); break;
+        case W_MEMWR: use(I.a); use(I.b); use(I.c); break;
+        default: use(I.a); use(I.b); break;
+      }
+      if (I.op == W_STORE) {
+        // a word the cycle reads before it stores it feeds back: not split
+        if (read_before_store.count(I.aux) || ((I.flags & 1) && read_before_store.count(I.aux + 1))) {
+          sig_def.clear();
+          read_before_store.insert(0xFFFFFFFFu);
+        }
+        sig_def[I.aux] = pc;
+        if (I.flags & 1) sig_def[I.aux + 1] = pc;
+      } else if (I.op != W_CAPTURE && I.op != W_MEMWR && I.op != W_ASTORE) {
+        slot_def[I.dst] = pc;
+      }
+    }
+  };
+  walk(wp.comb_b, wp.comb_e, true);
+  if (read_before_store.count(0xFFFFFFFFu)) return no("combinational feedback");
+  walk(wp.next_b, wp.next_e, false);
+  walk(wp.commit_b, wp.commit_e, false);
+  auto cone = [&](uint32_t root) {
+    std::vector<uint32_t> out, st{root};
+    std::vector<uint8_t> seen(N, 0);
+    while (!st.empty()) {
+      const uint32_t x = st.back();
+      st.pop_back();
+      if (seen[x]) continue;
+      seen[x] = 1;
+      out.push_back(x);
+      for (uint32_t y : dep[x]) st.push_back(y);
+    }
+    return out;
+  };
+  sp->in[0].assign(N, 0);
+  sp->in[1].assign(N, 0);
+  size_t size[2] = {0, 0};
+  auto add = [&](int p, const std::vector<uint32_t>& c) {
+    for (uint32_t x : c)
+      if (!sp->in[p][x]) {
+        sp->in[p][x] = 1;
+        ++size[p];
+      }
+  };
+  // what the record stage reads is computed by warp 0
+  for (const WordRecDev& r : run.rec)
+    for (uint32_t l = 0; l < r.limbs; ++l) {
+      auto it = sig_def.find(r.sig_off + l);
+      if (it != sig_def.end()) add(0, cone(it->second));
+    }
+  std::vector<std::pair<size_t, uint32_t>> sinks;
+  std::vector<std::vector<uint32_t>> cones(N);
+  for (uint32_t pc = wp.next_b; pc < wp.commit_e; ++pc)
+    if (wp.code[pc].op == W_CAPTURE || wp.code[pc].op == W_MEMWR) {
+      cones[pc] = cone(pc);
+      sinks.push_back({cones[pc].size(), pc});
+    }
+  std::sort(sinks.begin(), sinks.end(), [](const std::pair<size_t, uint32_t>& a, const std::pair<size_t, uint32_t>& b) {
+    return a.first != b.first ? a.first > b.first : a.second < b.second;
+  });
+  std::vector<int8_t> sink_part(N, -1);
+  for (auto& sk : sinks) {
+    size_t grow[2] = {0, 0};
+    for (int p = 0; p < 2; ++p)
+      for (uint32_t x : cones[sk.second]) grow[p] += !sp->in[p][x];
+    const int p = size[0] + grow[0] <= size[1] + grow[1] ? 0 : 1;
+    add(p, cones[sk.second]);
+    sink_part[sk.second] = (int8_t)p;
+  }
+  const size_t total = (wp.comb_e - wp.comb_b) + (wp.commit_e - wp.next_b);
+  sp->sizes[0] = size[0];
+  sp->sizes[1] = size[1];
+  if (size[1] == 0 || (double)std::max(size[0], size[1]) > 0.75 * (double)total) return no("unbalanced");
+  // register words: owned by the warp that captures them
+  std::unordered_map<uint32_t, uint32_t> cap_instr;
+  for (uint32_t pc = wp.next_b; pc < wp.next_e; ++pc)
+    if (wp.code[pc].op == W_CAPTURE) {
+      cap_instr[wp.code[pc].aux] = pc;
+      if (wp.code[pc].flags & 1) cap_instr[wp.code[pc].aux + 1] = pc;
+    }
+  std::unordered_map<uint32_t, uint32_t> xindex;
+  sp->commit_owner.clear();
+  for (const WCommitDev& cm : wp.commits) {
+    auto it = cap_instr.find(cm.cap_off);
+    if (it == cap_instr.end() || sink_part[it->second] < 0) return no("register without a capture");
+    const uint8_t own = (uint8_t)sink_part[it->second];
+    sp->commit_owner.push_back(own);
+    for (uint32_t l = 0; l < cm.limbs; ++l) {
+      xindex[cm.sig_off + l] = (uint32_t)sp->xwords.size();
+      sp->xwords.push_back(cm.sig_off + l);
+      sp->owner.push_back(own);
+    }
+  }
+  sp->need[0].assign(sp->xwords.size(), 0);
+  sp->need[1].assign(sp->xwords.size(), 0);
+  auto needs = [&](int p, uint32_t word) {
+    auto it = xindex.find(word);
+    if (it != xindex.end() && sp->owner[it->second] != p) sp->need[p][it->second] = 1;
+  };
+  for (int p = 0; p < 2; ++p)
+    for (uint32_t pc = 0; pc < N; ++pc) {
+      if (!sp->in[p][pc]) continue;
+      const WInstr& I = wp.code[pc];
+      if (I.op == W_SIG) {
+        needs(p, I.aux);
+        if (I.flags & 1) needs(p, I.aux + 1);
+      }
+      if ((I.op == W_CAPTURE && (I.flags & 2)) || I.op == W_ASTORE) needs(p, I.aux2);
+    }
+  for (const WordRecDev& r : run.rec)
+    for (uint32_t l = 0; l < r.limbs; ++l) needs(0, r.sig_off + l);
+  return true;
 }
 
 std::string WordRunTables::key() const {
@@ -508,7 +712,8 @@ void jit_build_kernel(const std::string& src, int device, const char* name, Word
   J->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run) {
+void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run,
+                    const WordSplitPlan* split) {
   J->written.assign(wp.mems.size(), 0);
   J->reg_signals = wp.n_sig_words <= kJitRegSignals;
   for (const WInstr& I : wp.code)
@@ -517,22 +722,28 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRun
     J->error = "word program of " + std::to_string(wp.code.size()) + " instructions runs interpreted";
     return;
   }
-  jit_build_kernel(word_jit_source(wp, run), device, "rrtl_word_jit", J);
+  if (split) {
+    J->split = true;
+    J->n_xwords = (uint32_t)split->xwords.size();
+  }
+  jit_build_kernel(word_jit_source(wp, run, split), device, "rrtl_word_jit", J);
 }
 
 size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad, uint64_t cycles,
                       uint32_t sm_count, size_t max_smem_block, size_t max_smem_sm, WordJitPlace* out) {
-  constexpr uint32_t kThreads = 128;
-  constexpr size_t kRowBytes = (size_t)kThreads * 4u;
+  // a row holds one word of every lane of a block: 128 lanes, 32 for a split kernel
+  const uint32_t kThreads = J.split ? 32u : 128u;
+  const size_t kRowBytes = (size_t)kThreads * 4u;
   WordJitPlace P{};
   P.n_sig_words = n_sig_words;
   P.n_mems = (uint32_t)std::min<size_t>(wp.mems.size(), kJitPlacedMems);
   // several blocks per SM when there are lanes for them: split the SM's
   // shared memory between them (one block's rows sit idle otherwise)
   const uint32_t blocks = lanes_pad / kThreads;
-  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(4, (blocks + sm_count - 1) / std::max<uint32_t>(sm_count, 1)));
+  const uint32_t per_sm = std::max<uint32_t>(
+      1, std::min<uint32_t>(J.split ? 16u : 4u, (blocks + sm_count - 1) / std::max<uint32_t>(sm_count, 1)));
   const size_t share = std::min(max_smem_block, max_smem_sm / per_sm);
-  const size_t reserve = 1024 + J.static_smem;
+  const size_t reserve = 1024 + J.static_smem + (size_t)J.n_xwords * kRowBytes;
   const size_t budget = share > reserve ? share - reserve : 0;
   // staging costs one pass over the rows at each end of the launch: worth it
   // when the launch runs a few cycles per staged row
@@ -558,6 +769,9 @@ size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_wo
       used += bytes;
     }
   }
+  // the split kernel's register exchange rows follow the staged rows
+  P.x_row = (uint32_t)(used / kRowBytes);
+  used += (size_t)J.n_xwords * kRowBytes;
   *out = P;
   return used;
 }
@@ -566,6 +780,8 @@ cudaError_t launch_word_jit(const WordJit& J, const WordRunDev& R, const WordJit
   WordRunDev r = R;
   WordJitPlace p = Pl;
   void* args[] = {&r, &p};
+  if (J.split)  // 32 lanes per block on two warps
+    return cudaLaunchKernel(reinterpret_cast<const void*>(J.fn), dim3(R.lanes_pad / 32u), dim3(64), args, smem, st);
   return cudaLaunchKernel(reinterpret_cast<const void*>(J.fn), dim3(R.lanes_pad / 128u), dim3(128), args, smem, st);
 }
 

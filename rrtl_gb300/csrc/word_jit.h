@@ -34,6 +34,24 @@ constexpr size_t kJitRunTableMax = 64;
 // Kernels compiled for specific runs kept per design.
 constexpr size_t kJitRunKernelsPerDesign = 64;
 
+// Two-warp split of a run's compiled kernel: which instructions each warp
+// evaluates (the cones of its register captures and memory writes; warp 0
+// also what the record stage reads), and the register words the warps
+// exchange at the clock edge.
+struct WordSplitPlan {
+  std::vector<uint8_t> in[2];        // per instruction: evaluated by warp p
+  std::vector<uint32_t> xwords;      // register signal words, in exchange-row order
+  std::vector<uint8_t> owner;        // per exchange word: the warp that captures it
+  std::vector<uint8_t> need[2];      // per exchange word: warp p reads it from the other warp
+  std::vector<uint8_t> commit_owner; // per commit entry
+  size_t sizes[2] = {0, 0};
+};
+
+// Split plan of `wp` for `run`; false (with the reason) when the design does
+// not split: asynchronous resets, combinational feedback, signals beyond the
+// register limit, or partitions too uneven to gain.
+bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitPlan* sp, std::string* why);
+
 struct WordJit {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
@@ -43,6 +61,8 @@ struct WordJit {
   size_t source_bytes = 0;
   size_t static_smem = 0;        // the kernel's static shared memory (stimulus/record tables)
   bool reg_signals = false;      // signal words live in registers (no signal staging)
+  bool split = false;            // two warps per 32 lanes (word_jit_run_split)
+  uint32_t n_xwords = 0;         // register words exchanged between the two warps
   std::vector<uint8_t> written;  // per memory: the design writes it
   ~WordJit();
 };
@@ -54,7 +74,8 @@ constexpr uint32_t kJitRegSignals = 256;
 
 // CUDA C++ source of a word program's compiled kernel `rrtl_word_jit`: for
 // any run, or with `run` for that run's tables only.
-std::string word_jit_source(const WordProgram& wp, const WordRunTables* run = nullptr);
+std::string word_jit_source(const WordProgram& wp, const WordRunTables* run = nullptr,
+                            const WordSplitPlan* split = nullptr);
 
 // Compile `src` for `arch` (e.g. "sm_103a") with NVRTC; returns the cubin,
 // or an empty vector with `log` holding the compiler's messages.
@@ -71,7 +92,8 @@ void jit_build_kernel(const std::string& src, int device, const char* name, Word
 
 // Emit, compile and load the kernel of `wp` on the current device. Never
 // throws: failures leave ok = false and the reason in error.
-void word_jit_build(const WordProgram& wp, int device, WordJit* out, const WordRunTables* run = nullptr);
+void word_jit_build(const WordProgram& wp, int device, WordJit* out, const WordRunTables* run = nullptr,
+                    const WordSplitPlan* split = nullptr);
 
 // Shared-memory placement for one launch over `lanes_pad` lanes and `cycles`
 // cycles; returns the dynamic shared memory bytes per 128-lane block.

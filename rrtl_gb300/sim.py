@@ -234,7 +234,7 @@ def lib():
         "rrtl_word_tick_many_noalloc": [c_void_p, c_void_p, c_void_p, c_uint32, c_uint64],
         "rrtl_design_word_jit": [c_void_p, P(c_uint32), P(c_float)],
         "rrtl_word_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
-                               P(c_uint32), c_char_p, c_size_t],
+                               P(c_uint32), c_char_p, c_size_t, c_uint32],
         "rrtl_instance_fold_plan": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
         "rrtl_design_load_bitslice": [c_void_p, c_char_p, c_size_t, c_char_p, P(c_void_p)],
         "rrtl_bitslice_json": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
@@ -346,7 +346,8 @@ def default_context() -> Context:
     return _default_ctx
 
 
-def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] = None, run: Optional["Run"] = None):
+def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] = None, run: Optional["Run"] = None,
+                  split: bool = False):
     """CUDA source of a design's compiled word kernel (for any run, or for the
     tables of `run`, a Run whose signals are packed indices), and with `arch`
     its NVRTC compile (no device needed): (source, cubin bytes, compiler log)."""
@@ -354,12 +355,13 @@ def word_jit_emit(design: Union[_b.Design, str], top: str, arch: Optional[str] =
     raw = text.encode()
     rp = ctypes.cast(byref(run), c_void_p) if run is not None else None
     n = c_size_t()
-    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, None, None, 0, byref(n), None, None, 0))
+    fl = 1 if split else 0
+    check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, None, None, 0, byref(n), None, None, 0, fl))
     src = ctypes.create_string_buffer(n.value + 1)
     logb = ctypes.create_string_buffer(1 << 16)
     cub = c_uint32()
     check(lib().rrtl_word_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
-                                   n.value + 1, byref(n), byref(cub), logb, len(logb)))
+                                   n.value + 1, byref(n), byref(cub), logb, len(logb), fl))
     return src.value.decode(), cub.value, logb.value.decode()
 
 

@@ -158,3 +158,40 @@ def test_run_specialised_equals_general_kernel(engine, monkeypatch):
             assert np.array_equal(out["spec"][0][k], out[key][0][k]), (key, k)
         assert np.array_equal(out["spec"][1][0], out[key][1][0])
         assert np.array_equal(out["spec"][1][1], out[key][1][1])
+
+
+def _split_vs_unsplit(monkeypatch, js, top, lanes, cycles, stim, rec, mode, setup=None, input_trace=None):
+    out = {}
+    for key, env in (("split", "2"), ("unsplit", "0")):
+        monkeypatch.setenv("RRTL_WORD_JIT_SPLIT", env)
+        g = sim.GpuBatchSimulator(js, top, lanes)
+        if setup:
+            setup(g)
+        res = g.run(cycles, seed=4, stim=stim, record=rec, mode=mode, input_trace=input_trace)
+        out[key] = (res, g.snapshot_storage())
+    for k in ("trace", "hash", "detect"):
+        if out["split"][0][k] is not None:
+            assert np.array_equal(out["split"][0][k], out["unsplit"][0][k]), k
+    assert np.array_equal(out["split"][1][0], out["unsplit"][1][0])
+    assert np.array_equal(out["split"][1][1], out["unsplit"][1][1])
+
+
+@pytest.mark.parametrize("lanes,cycles", [(64, 200), (2048, 300), (16384, 40)])
+def test_cpu_two_warp_split_equals_one_warp(engine, monkeypatch, lanes, cycles):
+    """Two warps per 32 lanes (each the cones of its share of the registers and
+    memory writes, registers exchanged at the edge) against one warp per 32
+    lanes, on the pipelined CPU: hashes, register file, data memory, state."""
+    js = pipelined_cpu().to_json()
+    rom = cpu_rom(lanes, seed=lanes + 1)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
+    _split_vs_unsplit(monkeypatch, js, "Cpu8", lanes, cycles, stim, ["out_pc", "out_acc"],
+                      sim.REC_HASH | sim.REC_TRACE | sim.REC_DETECT, setup=lambda g: g.set_memory_limbs("rom", rom))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_designs_two_warp_split(engine, monkeypatch, seed):
+    d, meta = random_word_design(900 + seed, n_wires=20, depth=3, n_mems=2, async_resets=False)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 2)]
+    stim += [(n, sim.STIM_RANDOM, i + 7) for i, (n, w) in enumerate(meta["inputs"])]
+    rec = [n for n, w in meta["outputs"]]
+    _split_vs_unsplit(monkeypatch, d.to_json(), meta["top"], 100, 30, stim, rec, sim.REC_TRACE | sim.REC_HASH)

@@ -134,3 +134,26 @@ def test_compiled_gate_kernel_sources_compile(which):
             pytest.skip("NVRTC is not installed")
         raise
     assert cub > 0, log
+
+
+def test_two_warp_split_source_compiles():
+    """The two-warp form of the pipelined CPU's run kernel: both halves, the
+    register exchange and the split run protocol compile for sm_103a; a design
+    with a single register does not split."""
+    d, top = pipelined_cpu(), "Cpu8"
+    run = _run_for(d, top, [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)], ["out_pc", "out_acc"],
+                   sim.REC_HASH)
+    src, _, _ = sim.word_jit_emit(d, top, None, run, split=True)
+    assert "word_jit_run_split" in src and "settle_part" in src and "xin_all" in src
+    try:
+        src, cub, log = sim.word_jit_emit(d, top, "sm_103a", run, split=True)
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+    assert cub > 0, log
+    c = counter()
+    run = _run_for(c, "Counter", [("clk", sim.STIM_CONST, 1)], ["out"], sim.REC_HASH)
+    with pytest.raises(sim.RrtlError) as e:
+        sim.word_jit_emit(c, "Counter", None, run, split=True)
+    assert e.value.code == "E_WORD_JIT_SPLIT"
