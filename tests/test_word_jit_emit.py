@@ -139,7 +139,7 @@ def test_compiled_gate_kernel_sources_compile(which):
 def test_two_warp_split_source_compiles():
     """The two-warp form of the pipelined CPU's run kernel: both halves, the
     register exchange and the split run protocol compile for sm_103a; a design
-    with a single register does not split."""
+    with an asynchronous reset does not split."""
     d, top = pipelined_cpu(), "Cpu8"
     run = _run_for(d, top, [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)], ["out_pc", "out_acc"],
                    sim.REC_HASH)
@@ -152,8 +152,18 @@ def test_two_warp_split_source_compiles():
             pytest.skip("NVRTC is not installed")
         raise
     assert cub > 0, log
-    c = counter()
-    run = _run_for(c, "Counter", [("clk", sim.STIM_CONST, 1)], ["out"], sim.REC_HASH)
+    from rrtl_gb300.builder import Design, lit_u, uint
+
+    a = Design()
+    m = a.module("A")
+    clk, rst = m.input("clk", uint(1)), m.input("rst", uint(1))
+    r = m.reg("r", uint(8))
+    m.clock(r, clk)
+    m.async_reset(r, rst, 3)
+    m.next(r, r + lit_u(1, 8))
+    o = m.output("o", uint(8))
+    m.assign(o, r)
+    run = _run_for(a, "A", [("clk", sim.STIM_CONST, 1)], ["o"], sim.REC_HASH)
     with pytest.raises(sim.RrtlError) as e:
-        sim.word_jit_emit(c, "Counter", None, run, split=True)
+        sim.word_jit_emit(a, "A", None, run, split=True)
     assert e.value.code == "E_WORD_JIT_SPLIT"
