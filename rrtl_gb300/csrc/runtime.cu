@@ -544,21 +544,36 @@ void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st
   cuda_check(e, "cudaGraphLaunch");
 }
 
+// A per-design kernel cache entry is built once, outside the lock: a thread
+// that finds an entry another thread is still building gets nullptr and
+// falls back (general kernel, interpreter or fused kernel) instead of waiting,
+// so a compile on one thread never stalls another (the serving loop).
+template <class Build>
+const WordJit* jit_cache_get(std::mutex& mu, std::map<std::string, std::unique_ptr<WordJit>>& cache,
+                             const std::string& key, Build build) {
+  WordJit* J = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      WordJit* e = it->second.get();
+      return e->ready.load(std::memory_order_acquire) && e->ok ? e : nullptr;
+    }
+    if (cache.size() >= kJitRunKernelsPerDesign) return nullptr;
+    J = cache.emplace(key, std::make_unique<WordJit>()).first->second.get();
+  }
+  build(J);
+  J->ready.store(true, std::memory_order_release);
+  return J->ok ? J : nullptr;
+}
+
 const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
   const char* env = getenv("RRTL_GATE_JIT");
   if ((env && env[0] == '0') || d->gp().n_real_cells > kGateJitMaxCells || t.stim.size() > kJitRunTableMax ||
       t.rec.size() > kJitRunTableMax)
     return nullptr;
-  const std::string key = t.key();
-  std::lock_guard<std::mutex> lk(d->wjit_mu);
-  auto it = d->gjit_runs.find(key);
-  if (it == d->gjit_runs.end()) {
-    if (d->gjit_runs.size() >= kJitRunKernelsPerDesign) return nullptr;
-    auto J = std::make_unique<WordJit>();
-    gate_jit_build(d->gp(), t, d->ctx->device, J.get());
-    it = d->gjit_runs.emplace(key, std::move(J)).first;
-  }
-  return it->second->ok ? it->second.get() : nullptr;
+  return jit_cache_get(d->wjit_mu, d->gjit_runs, t.key(),
+                       [&](WordJit* J) { gate_jit_build(d->gp(), t, d->ctx->device, J); });
 }
 
 bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
@@ -737,17 +752,14 @@ void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {
   if (g.want_det) cuda_check(cudaMemcpyAsync(run.detect, g.R.detect, g.det_bytes, cudaMemcpyDeviceToHost, st), "d2h detect");
 }
 
-// The design's compiled word kernel, built on first use (nullptr when the
-// design runs interpreted; the reason stays in d->wjit->error).
+// The design's compiled word kernel for any run, built on first use (nullptr
+// when the design runs interpreted; the reason stays in the "general" cache
+// entry's error).
 const WordJit* word_jit_get(rrtl_design* d) {
-  std::lock_guard<std::mutex> lk(d->wjit_mu);
-  if (!d->wjit) {
-    d->wjit = std::make_unique<WordJit>();
-    const char* env = getenv("RRTL_WORD_JIT");
-    if (env && env[0] == '0') d->wjit->error = "compiled word kernels are off (RRTL_WORD_JIT=0)";
-    else word_jit_build(d->wp, d->ctx->device, d->wjit.get());
-  }
-  return d->wjit->ok ? d->wjit.get() : nullptr;
+  const char* env = getenv("RRTL_WORD_JIT");
+  if (env && env[0] == '0') return nullptr;
+  return jit_cache_get(d->wjit_mu, d->wjit_runs, "general",
+                       [&](WordJit* J) { word_jit_build(d->wp, d->ctx->device, J); });
 }
 
 const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad) {
@@ -757,31 +769,18 @@ const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t
   // two warps per 32 lanes on request only (RRTL_WORD_JIT_SPLIT=2): measured
   // slower than one warp on the pipelined CPU even at 4,096 lanes
   const char* senv = getenv("RRTL_WORD_JIT_SPLIT");
-  const bool want_split = lanes_pad && senv && senv[0] == '2';
-  if (want_split) {
-    const std::string skey = t.key() + "|split";
-    std::lock_guard<std::mutex> lk(d->wjit_mu);
-    auto it = d->wjit_runs.find(skey);
-    if (it == d->wjit_runs.end() && d->wjit_runs.size() < kJitRunKernelsPerDesign) {
-      auto J = std::make_unique<WordJit>();
+  if (lanes_pad && senv && senv[0] == '2') {
+    const WordJit* S = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key() + "|split", [&](WordJit* J) {
       WordSplitPlan plan;
       std::string why;
-      if (word_split_plan(d->wp, t, &plan, &why)) word_jit_build(d->wp, d->ctx->device, J.get(), &t, &plan);
+      if (word_split_plan(d->wp, t, &plan, &why)) word_jit_build(d->wp, d->ctx->device, J, &t, &plan);
       else J->error = "no split: " + why;
-      it = d->wjit_runs.emplace(skey, std::move(J)).first;
-    }
-    if (it != d->wjit_runs.end() && it->second->ok) return it->second.get();
+    });
+    if (S) return S;
   }
-  const std::string key = t.key();
-  std::lock_guard<std::mutex> lk(d->wjit_mu);
-  auto it = d->wjit_runs.find(key);
-  if (it == d->wjit_runs.end()) {
-    if (d->wjit_runs.size() >= kJitRunKernelsPerDesign) return any;
-    auto J = std::make_unique<WordJit>();
-    word_jit_build(d->wp, d->ctx->device, J.get(), &t);
-    it = d->wjit_runs.emplace(key, std::move(J)).first;
-  }
-  return it->second->ok ? it->second.get() : any;
+  const WordJit* R = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key(),
+                                   [&](WordJit* J) { word_jit_build(d->wp, d->ctx->device, J, &t); });
+  return R ? R : any;
 }
 
 void design_warm_for_run(rrtl_design* d, uint32_t lanes, const rrtl_run& run) {
@@ -1319,9 +1318,12 @@ rrtl_status rrtl_design_word_jit(rrtl_design* d, uint32_t* active, float* compil
     }
     set_device(d->ctx);
     const WordJit* J = word_jit_get(d);
-    if (compile_ms) *compile_ms = (float)d->wjit->compile_ms;
     *active = J ? 1u : 0u;
-    if (!J) why = d->wjit->error;
+    std::lock_guard<std::mutex> lk(d->wjit_mu);
+    auto it = d->wjit_runs.find("general");
+    const WordJit* E = it != d->wjit_runs.end() && it->second->ready.load() ? it->second.get() : nullptr;
+    if (compile_ms && E) *compile_ms = (float)E->compile_ms;
+    if (!J) why = E ? E->error : std::string("compiled word kernels are off (RRTL_WORD_JIT=0) or still building");
   });
   if (st == RRTL_OK && !why.empty()) g_last_error = why;
   return st;

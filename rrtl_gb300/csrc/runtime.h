@@ -210,8 +210,9 @@ struct rrtl_design {
   rrtl::DevBuf d_wcode, d_wcap, d_wlit;
   std::mutex gvar_mu;  // builds of gvar entries (serving producers prepare designs concurrently)
   std::mutex wjit_mu;
-  std::unique_ptr<rrtl::WordJit> wjit;  // compiled kernel for any run, built on the first fused run
-  std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;  // kernels compiled for one run's tables
+  // compiled word kernels: "general" (any run, built on the first fused run)
+  // and one per run tables
+  std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;
   std::map<std::string, std::unique_ptr<rrtl::WordJit>> gjit_runs;  // compiled gate kernels, per run tables
 };
 

@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -55,6 +56,7 @@ bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitP
 struct WordJit {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
+  std::atomic<bool> ready{false};  // the build finished (the fields below are final)
   bool ok = false;
   std::string error;     // why there is no compiled kernel (empty when ok)
   double compile_ms = 0; // emit + NVRTC + load
