@@ -93,9 +93,15 @@ std::string gate_jit_source(const GateProgram& gp, const GateRunTables& run) {
     if (detect) o += "      uint32_t diff = 0u;\n";
     for (size_t k = 0; k < run.rec.size(); ++k) {
       const std::string kk = u(k);
+      if (hash && k % 32 == 0)  // the cycle's hash salts, one per lane of the warp, shared by shuffles
+        o += "      const unsigned long long salt" + std::to_string(k / 32) + " = hash_salt(c, " + u(k) +
+             " + (threadIdx.x & 31u));\n";
+      if (hash)
+        o += "      const unsigned long long sk" + kk + " = __shfl_sync(0xFFFFFFFFu, salt" + std::to_string(k / 32) +
+             ", " + u(k % 32) + ");\n";
       o += "      { const uint32_t v = " + n(run.rec[k].net) + " & vm; if (w < R.words) {";
       if (trace) o += " R.out_trace[((size_t)c * " + u(run.rec.size()) + " + " + kk + ") * R.words + w] = v;";
-      if (hash) o += " h += hash_term(c, " + kk + ", w, v);";
+      if (hash) o += " h += hash_term_salted(sk" + kk + ", w, v);";
       if (detect) o += " diff |= v ^ (0u - (v & 1u));";
       if (check) o += " check_word(R, c, " + kk + ", w, v);";
       o += " } }\n";

@@ -46,9 +46,14 @@ RRTL_HD uint32_t stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, 
 // 1-bit recorded signals (value = the packed word, lanes past the batch end
 // cleared) and lane*limbs+limb for wider ones; the per-cycle hash is the
 // wrapping sum of all terms, so any evaluation order and either engine agree.
-RRTL_HD uint64_t hash_term(uint64_t cycle, uint32_t rec, uint64_t idx, uint32_t value) {
-  uint64_t salt = smix64((cycle << 20) ^ (uint64_t)rec ^ 0x5851F42D4C957F2Dull);
+RRTL_HD uint64_t hash_salt(uint64_t cycle, uint32_t rec) {
+  return smix64((cycle << 20) ^ (uint64_t)rec ^ 0x5851F42D4C957F2Dull);
+}
+RRTL_HD uint64_t hash_term_salted(uint64_t salt, uint64_t idx, uint32_t value) {
   return smix64((uint64_t)value ^ (idx << 32) ^ salt);
+}
+RRTL_HD uint64_t hash_term(uint64_t cycle, uint32_t rec, uint64_t idx, uint32_t value) {
+  return hash_term_salted(hash_salt(cycle, rec), idx, value);
 }
 
 }  // namespace rrtl
