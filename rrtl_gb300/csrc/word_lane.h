@@ -75,9 +75,15 @@ __device__ __forceinline__ void word_record(const WordRunDev& R, uint32_t lane, 
   const uint32_t mode = spec.mode();
   unsigned long long h = 0ull;
   bool diff = false;
+  unsigned long long salts = 0ull;  // hash salt of record (k & ~31) + this lane's index in the warp
 #pragma unroll
   for (uint32_t k = 0; k < spec.n_rec(); ++k) {
     const WordRecDev rc = spec.rec(k);
+    if (mode & RRTL_REC_HASH) {
+      // one salt per lane of the warp, shared by shuffles (the whole warp runs this loop)
+      if ((k & 31u) == 0) salts = hash_salt(ca, k + (threadIdx.x & 31u));
+    }
+    const unsigned long long salt = (mode & RRTL_REC_HASH) ? __shfl_sync(0xFFFFFFFFu, salts, k & 31u) : 0ull;
     for (uint32_t l = 0; l < rc.limbs; ++l) {
       uint32_t v = W.get(rc.sig_off + l);
       if (l + 1 == rc.limbs && (rc.width & 31u)) v &= (1u << (rc.width & 31u)) - 1u;
@@ -85,7 +91,7 @@ __device__ __forceinline__ void word_record(const WordRunDev& R, uint32_t lane, 
       if ((mode & RRTL_REC_HASH) && rc.width == 1) {
         // 1-bit signals hash as 32-lane packed words, the gate engine's unit
         const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
-        if ((threadIdx.x & 31u) == 0 && live) h += hash_term(ca, k, lane >> 5, packed);
+        if ((threadIdx.x & 31u) == 0 && live) h += hash_term_salted(salt, lane >> 5, packed);
       }
       if (!live) continue;
       if (mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
@@ -97,7 +103,7 @@ __device__ __forceinline__ void word_record(const WordRunDev& R, uint32_t lane, 
           if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
         }
       }
-      if ((mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term(ca, k, (uint64_t)lane * rc.limbs + l, v);
+      if ((mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term_salted(salt, (uint64_t)lane * rc.limbs + l, v);
     }
   }
   if (mode & RRTL_REC_HASH) {
