@@ -188,3 +188,33 @@ def test_run_kernels_of_random_designs_compile(seed):
         raise
     assert cub > 0, log
     assert "struct RunSpec" in src
+
+
+def test_compiled_gate_kernel_of_a_plane_design_compiles():
+    """A bit-sliced design's plane netlist (deep, narrow levels: the compiled
+    gate kernel's case) compiles; its cells are one LOP3 each."""
+    from rrtl_gb300.workloads import narrow_alu
+
+    planes = sim.bitslice_json(narrow_alu(16), "Alu")
+    stim = [("__bitslice_clk", sim.STIM_CONST, 1), ("rst[0]", sim.STIM_PULSE, 1)]
+    stim += [(f"din[{p}]", sim.STIM_RANDOM, p) for p in range(16)]
+    rec = [f"out[{p}]" for p in range(16)] + ["flag[0]"]
+    from oracle import binding as ob
+
+    od = ob.OracleDesign(planes, "Alu")
+    import ctypes
+
+    st = (sim.Stim * len(stim))(*[sim.Stim(od.signal(n), k, p) for n, k, p in stim])
+    rc = (ctypes.c_uint32 * len(rec))(*[od.signal(n) for n in rec])
+    run = sim.Run()
+    run.n_stim, run.stim = len(stim), st
+    run.n_record, run.record = len(rec), rc
+    run.record_mode = sim.REC_HASH | sim.REC_TRACE
+    try:
+        src, cub, log = sim.gate_jit_emit(planes, "Alu", run, "sm_103a")
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+    assert cub > 0, log
+    assert src.count("lop3<") >= 2 * 500
