@@ -583,6 +583,20 @@ bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitP
   sp->sizes[0] = size[0];
   sp->sizes[1] = size[1];
   if (size[1] == 0 || (double)std::max(size[0], size[1]) > 0.75 * (double)total) return no("unbalanced");
+  // memory reads in the register or commit stream run after the first
+  // barrier, beside the other warp's memory writes: a memory read there by
+  // one warp must not be written by the other (the single warp reads first)
+  std::vector<uint8_t> writer(wp.mems.size(), 0);  // bit p: warp p writes memory k
+  for (uint32_t pc = wp.commit_b; pc < wp.commit_e; ++pc)
+    if (wp.code[pc].op == W_MEMWR && wp.code[pc].aux < writer.size())
+      for (int p = 0; p < 2; ++p)
+        if (sp->in[p][pc]) writer[wp.code[pc].aux] |= (uint8_t)(1u << p);
+  for (uint32_t pc = wp.next_b; pc < wp.commit_e; ++pc) {
+    const WInstr& I = wp.code[pc];
+    if (I.op != W_MEMRD || I.aux >= writer.size()) continue;
+    for (int p = 0; p < 2; ++p)
+      if (sp->in[p][pc] && (writer[I.aux] & (1u << (1 - p)))) return no("a register-stream memory read races the other warp's write");
+  }
   // register words: owned by the warp that captures them
   std::unordered_map<uint32_t, uint32_t> cap_instr;
   for (uint32_t pc = wp.next_b; pc < wp.next_e; ++pc)
