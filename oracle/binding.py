@@ -73,6 +73,12 @@ def lib():
         L.orc_hash_term.restype = c_uint64
         L.orc_packed_new.argtypes = [c_void_p, c_uint32]
         L.orc_packed_new.restype = c_void_p
+        L.orc_bs_new.argtypes = [c_void_p, c_uint32]
+        L.orc_bs_new.restype = c_void_p
+        L.orc_bs_free.argtypes = [c_void_p]
+        L.orc_bs_set_signal.argtypes = [c_void_p, c_uint32, c_void_p]
+        L.orc_bs_get_signal.argtypes = [c_void_p, c_uint32, c_void_p]
+        L.orc_bs_tick.argtypes = [c_void_p]
         L.orc_packed_free.argtypes = [c_void_p]
         L.orc_packed_set_signal.argtypes = [c_void_p, c_uint32, POINTER(c_uint32), c_int]
         L.orc_packed_get_signal.argtypes = [c_void_p, c_uint32, POINTER(c_uint32)]
@@ -265,6 +271,39 @@ class PackedSim:
         rc = lib().orc_packed_run(self.h, ctypes.byref(run))
         if rc:
             raise OracleError(lib().orc_last_error().decode())
+
+
+class BitSlice:
+    """Restated `BitSliceSimulator` (multi-bit signals as bit-planes, 64 lanes
+    per u64; crates/rrtl-sim-ir/src/bitslice.rs). Signals move as
+    [limbs][lanes] u32, like PackedSim."""
+
+    def __init__(self, design: OracleDesign, lanes: int):
+        self.d = design
+        self.lanes = lanes
+        self.h = lib().orc_bs_new(design.h, lanes)
+        if not self.h:
+            raise OracleError(lib().orc_last_error().decode())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_bs_free(self.h)
+            self.h = None
+
+    def _limbs(self, sig):
+        return max(1, (lib().orc_signal_width(self.d.h, sig) + 31) // 32)
+
+    def set_signal(self, sig: int, values):
+        a = np.ascontiguousarray(np.asarray(values, dtype=np.uint32).reshape(self._limbs(sig), self.lanes))
+        lib().orc_bs_set_signal(self.h, sig, a.ctypes.data)
+
+    def get_signal(self, sig: int) -> np.ndarray:
+        out = np.zeros((self._limbs(sig), self.lanes), dtype=np.uint32)
+        lib().orc_bs_get_signal(self.h, sig, out.ctypes.data)
+        return out
+
+    def tick(self):
+        lib().orc_bs_tick(self.h)
 
 
 class BitParallel:

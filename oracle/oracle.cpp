@@ -7,6 +7,7 @@
 //                                      limb helpers :12942-13196
 //   BitParallel  <- BitParallelSimulator crates/rrtl-sim-ir/src/bitparallel.rs:32-347
 //   ScalarSim    <- rrtl_core::Simulator crates/rrtl-core/src/lib.rs:5820-6470
+//   BitSlice     <- BitSliceSimulator crates/rrtl-sim-ir/src/bitslice.rs:26-402
 // The packed/machine programs come from the lowering in rrtl_gb300/csrc
 // (itself a restatement of lower_to_packed_program / lower_to_machine_program);
 // ScalarSim works on the unlowered design, so it checks that lowering.
@@ -486,6 +487,218 @@ struct BitParallel {
   }
 };
 
+// ---------------------------------------------------------------- BitSlice --
+// BitSliceSimulator (crates/rrtl-sim-ir/src/bitslice.rs:26-402): a W-bit signal is
+// W bit-planes of 64 lanes per u64. Bitwise ops and muxes per plane (the mux on
+// plane 0 of the condition), add/sub as a ripple carry (sub as a + ~b + 1),
+// eq/ne as xor planes OR-reduced over the wider operand, slice / zext / trunc /
+// cast / sext (repeating the top plane) / MSB-first concat as plane
+// reindexing; operand planes past an operand's width read 0. Settle runs the
+// async-reset stream, then comb, storing per packet; tick settles, captures
+// every register (reset select per plane) and commits, then settles.
+// Scope as the reference's (:37-80): no memories, no multiply, no compare.
+struct BitSlice {
+  const MachineProgram* M;
+  uint32_t lanes, words;
+  std::vector<size_t> sig_base;
+  std::vector<uint32_t> widths;
+  std::vector<uint64_t> state;  // [(sig_base[s] + p) * words + k]
+
+  BitSlice(const OracleDesign* od, uint32_t n) : M(&od->machine), lanes(n) {
+    if (!M->source.memories.empty()) throw RrtlError("E_BITSLICE", "bit-slice does not support memories");
+    for (const Block* b : {&M->async_reset_comb, &M->comb, &M->tick_next, &M->tick_commit})
+      for (auto& p : b->packets)
+        for (auto& in : p.instrs)
+          if (in.kind == IK::Mul || in.kind == IK::Lt || in.kind == IK::MemRead)
+            throw RrtlError("E_BITSLICE", "op outside the bit-slice scope");
+    words = std::max<uint32_t>(1, (lanes + 63) / 64);
+    size_t total = 0;
+    for (auto& s : M->source.signals) {
+      sig_base.push_back(total);
+      widths.push_back(s.layout.width);
+      total += s.layout.width;
+    }
+    state.assign(total * words, 0);
+  }
+
+  struct Work {
+    std::vector<size_t> base;
+    std::vector<uint32_t> width;
+    std::vector<uint64_t> ws;
+  };
+  uint64_t rd(const Work& W, uint32_t v, size_t p, uint32_t k) const {
+    return p < W.width[v] ? W.ws[(W.base[v] + p) * words + k] : 0ull;
+  }
+  Work eval(const Block& b) const {
+    Work W;
+    W.width.assign(b.num_values, 0);
+    for (uint32_t v = 0; v < b.num_values && v < b.value_width.size(); ++v) W.width[v] = b.value_width[v];
+    W.base.assign(b.num_values, 0);
+    size_t total = 0;
+    for (uint32_t v = 0; v < b.num_values; ++v) {
+      W.base[v] = total;
+      total += W.width[v];
+    }
+    W.ws.assign(total * words, 0);
+    for (auto& pk : b.packets)
+      for (auto& in : pk.instrs) {
+        const size_t db = W.base[in.dst];
+        const uint32_t dw = W.width[in.dst];
+        uint64_t* D = &W.ws[db * words];
+        auto put = [&](size_t p, uint32_t k, uint64_t v) { D[p * words + k] = v; };
+        switch (in.kind) {
+          case IK::Signal:
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k)
+                put(p, k, p < widths[in.index] ? state[(sig_base[in.index] + p) * words + k] : 0ull);
+            break;
+          case IK::Lit:
+            for (size_t p = 0; p < dw; ++p) {
+              const uint32_t limb = (uint32_t)(p / 32);
+              const bool bit = limb < in.lit.size() && ((in.lit[limb] >> (p % 32)) & 1u);
+              for (uint32_t k = 0; k < words; ++k) put(p, k, bit ? ~0ull : 0ull);
+            }
+            break;
+          case IK::Not:
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k) put(p, k, ~rd(W, in.ops[0], p, k));
+            break;
+          case IK::And: case IK::Or: case IK::Xor:
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k) {
+                const uint64_t a = rd(W, in.ops[0], p, k), c = rd(W, in.ops[1], p, k);
+                put(p, k, in.kind == IK::And ? (a & c) : in.kind == IK::Or ? (a | c) : (a ^ c));
+              }
+            break;
+          case IK::Mux:
+            for (uint32_t k = 0; k < words; ++k) {
+              const uint64_t c = rd(W, in.ops[0], 0, k);
+              for (size_t p = 0; p < dw; ++p) put(p, k, (c & rd(W, in.ops[1], p, k)) | (~c & rd(W, in.ops[2], p, k)));
+            }
+            break;
+          case IK::Eq: case IK::Ne: {
+            const size_t wmax = std::max(W.width[in.ops[0]], W.width[in.ops[1]]);
+            for (uint32_t k = 0; k < words; ++k) {
+              uint64_t diff = 0;
+              for (size_t p = 0; p < wmax; ++p) diff |= rd(W, in.ops[0], p, k) ^ rd(W, in.ops[1], p, k);
+              put(0, k, in.kind == IK::Eq ? ~diff : diff);
+              for (size_t p = 1; p < dw; ++p) put(p, k, 0ull);
+            }
+            break;
+          }
+          case IK::Add: case IK::Sub: {
+            const bool sub = in.kind == IK::Sub;
+            for (uint32_t k = 0; k < words; ++k) {
+              uint64_t carry = sub ? ~0ull : 0ull;
+              for (size_t p = 0; p < dw; ++p) {
+                const uint64_t a = rd(W, in.ops[0], p, k);
+                const uint64_t c = sub ? ~rd(W, in.ops[1], p, k) : rd(W, in.ops[1], p, k);
+                const uint64_t x = a ^ c;
+                put(p, k, x ^ carry);
+                carry = (a & c) | (carry & x);
+              }
+            }
+            break;
+          }
+          case IK::Slice:
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k) put(p, k, rd(W, in.ops[0], p + in.lsb, k));
+            break;
+          case IK::Zext: case IK::Trunc: case IK::Cast:
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k) put(p, k, rd(W, in.ops[0], p, k));
+            break;
+          case IK::Sext: {
+            const size_t sw = W.width[in.ops[0]];
+            for (size_t p = 0; p < dw; ++p)
+              for (uint32_t k = 0; k < words; ++k) put(p, k, sw ? rd(W, in.ops[0], p < sw ? p : sw - 1, k) : 0ull);
+            break;
+          }
+          case IK::Concat: {
+            size_t off = 0;
+            for (size_t q = in.ops.size(); q-- > 0;) {
+              const uint32_t pw = W.width[in.ops[q]];
+              for (size_t p = 0; p < pw && off + p < dw; ++p)
+                for (uint32_t k = 0; k < words; ++k) put(off + p, k, rd(W, in.ops[q], p, k));
+              off += pw;
+            }
+            break;
+          }
+          default: break;
+        }
+      }
+    return W;
+  }
+  void asserted(const PackedReset& r, std::vector<uint64_t>& out) const {
+    for (uint32_t k = 0; k < words; ++k) {
+      const uint64_t b = state[sig_base[r.signal] * words + k];  // plane 0 of the reset signal
+      out[k] = r.active_low ? ~b : b;
+    }
+  }
+  void store(uint32_t dst, const Work& W, uint32_t v, const PackedReset* r) {
+    std::vector<uint64_t> as(words, 0);
+    if (r) asserted(*r, as);
+    for (size_t p = 0; p < widths[dst]; ++p) {
+      const uint32_t limb = (uint32_t)(p / 32);
+      const bool rb = r && limb < r->value.size() && ((r->value[limb] >> (p % 32)) & 1u);
+      for (uint32_t k = 0; k < words; ++k) {
+        const uint64_t nv = rd(W, v, p, k);
+        state[(sig_base[dst] + p) * words + k] = r ? ((as[k] & (rb ? ~0ull : 0ull)) | (~as[k] & nv)) : nv;
+      }
+    }
+  }
+  void settle() {
+    for (const Block* b : {&M->async_reset_comb, &M->comb}) {
+      const Work W = eval(*b);
+      for (auto& pk : b->packets)
+        for (auto& e : pk.effects) {
+          if (e.kind == EffK::StoreSignal) store(e.dst, W, e.value, nullptr);
+          else if (e.kind == EffK::CaptureReg && e.has_reset) store(e.dst, W, e.value, &e.reset);
+        }
+    }
+  }
+  void tick() {
+    settle();
+    const Work W = eval(M->tick_next);
+    // every capture reads the pre-commit state; all commit together
+    std::vector<std::pair<uint32_t, std::vector<uint64_t>>> next;
+    std::vector<uint64_t> as(words, 0);
+    for (auto& pk : M->tick_next.packets)
+      for (auto& e : pk.effects) {
+        if (e.kind != EffK::CaptureReg) continue;
+        if (e.has_reset) asserted(e.reset, as);
+        std::vector<uint64_t> planes((size_t)widths[e.dst] * words);
+        for (size_t p = 0; p < widths[e.dst]; ++p) {
+          const uint32_t limb = (uint32_t)(p / 32);
+          const bool rb = e.has_reset && limb < e.reset.value.size() && ((e.reset.value[limb] >> (p % 32)) & 1u);
+          for (uint32_t k = 0; k < words; ++k) {
+            const uint64_t nv = rd(W, e.value, p, k);
+            planes[p * words + k] = e.has_reset ? ((as[k] & (rb ? ~0ull : 0ull)) | (~as[k] & nv)) : nv;
+          }
+        }
+        next.emplace_back(e.dst, std::move(planes));
+      }
+    for (auto& n : next) std::copy(n.second.begin(), n.second.end(), &state[sig_base[n.first] * words]);
+    settle();
+  }
+  void set_lanes(uint32_t sig, const uint32_t* data) {  // [limbs][lanes]
+    const uint32_t limbs = std::max<uint32_t>(1, (widths[sig] + 31) / 32);
+    for (size_t p = 0; p < widths[sig]; ++p)
+      for (uint32_t k = 0; k < words; ++k) state[(sig_base[sig] + p) * words + k] = 0;
+    for (uint32_t l = 0; l < lanes; ++l)
+      for (size_t p = 0; p < widths[sig]; ++p)
+        if ((p / 32) < limbs && ((data[(p / 32) * lanes + l] >> (p % 32)) & 1u))
+          state[(sig_base[sig] + p) * words + l / 64] |= 1ull << (l % 64);
+  }
+  void get_lanes(uint32_t sig, uint32_t* out) const {  // [limbs][lanes]
+    const uint32_t limbs = std::max<uint32_t>(1, (widths[sig] + 31) / 32);
+    std::fill(out, out + (size_t)limbs * lanes, 0u);
+    for (uint32_t l = 0; l < lanes; ++l)
+      for (size_t p = 0; p < widths[sig]; ++p)
+        if ((state[(sig_base[sig] + p) * words + l / 64] >> (l % 64)) & 1ull) out[(p / 32) * lanes + l] |= 1u << (p % 32);
+  }
+};
+
 // ---------------------------------------------------------------- ScalarSim --
 // rrtl_core::Simulator: hierarchical, unmasked u128 intermediates, fixpoint settle.
 u128 mask128(uint32_t w) { return w >= 128 ? ~(u128)0 : (((u128)1 << w) - 1); }
@@ -858,6 +1071,15 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
   s->eval_combinational();
   return 0;
 }
+
+// ---- BitSlice
+void* orc_bs_new(void* dp, uint32_t lanes) {
+  try { return new BitSlice((OracleDesign*)dp, lanes); } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
+void orc_bs_free(void* s) { delete (BitSlice*)s; }
+void orc_bs_set_signal(void* s, uint32_t sig, const uint32_t* data) { ((BitSlice*)s)->set_lanes(sig, data); }
+void orc_bs_get_signal(void* s, uint32_t sig, uint32_t* out) { ((BitSlice*)s)->get_lanes(sig, out); }
+void orc_bs_tick(void* s) { ((BitSlice*)s)->tick(); }
 
 // ---- BitParallel
 void* orc_bp_new(void* dp, uint32_t lanes) {
