@@ -227,9 +227,33 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
     pdt = max(packed_run(pcyc), 1e-4)
     pcyc = max(16, int(budget_s / 4 / pdt * pcyc))
     packed = plane * pcyc / packed_run(pcyc)
+    # the bit-slice engine restated (planes of 64 lanes, one core) on the
+    # 16-bit ALU of the bit-slice leg without its compare (outside the
+    # reference engine's scope)
+    bitslice = None
+    try:
+        from rrtl_gb300.workloads import narrow_alu
+
+        aod = ob.OracleDesign(narrow_alu(16, compare=False).to_json(), "Alu")
+        blanes = 64 * 64
+        bsim = ob.BitSlice(aod, blanes)
+        rng = np.random.default_rng(1)
+        t0 = time.perf_counter()
+        bcyc = 0
+        while time.perf_counter() - t0 < budget_s / 8:
+            for name, w in (("din", 16), ("sel", 2)):
+                bsim.set_signal(aod.signal(name), rng.integers(0, 1 << w, size=(1, blanes), dtype=np.uint32))
+            bsim.tick()
+            bcyc += 1
+        bitslice = {"value": blanes * bcyc / (time.perf_counter() - t0), "cores": 1,
+                    "sample": f"16-bit ALU without compare, {blanes} lanes x {bcyc} cycles, bit-slice engine "
+                              "restated, 1 thread"}
+    except Exception as e:  # the baseline is reported, not required
+        bitslice = {"unavailable": str(e)[:200]}
     return {"value": value, "unit": "lane-cycles/s", "cores": threads, "kind": "port",
             "packed_cpu8": {"value": packed, "cores": 1, "sample": f"pipelined CPU, {plane} lanes x {pcyc} cycles, "
                                                                    "packed simulator restated, 1 thread"},
+            "bitslice_alu16": bitslice,
             "sample": f"{lanes} lanes x {cycles} cycles of the same netlist and stimulus (bit-parallel AOT: "
                       f"emitted C, gcc -O2, {threads} threads)", "seconds": round(dt, 3),
             "compile_s": round(compile_s, 1),

@@ -456,11 +456,12 @@ def replicated_datapath(n_instances: int, top: str = "Top", child: str = "Lane")
     return d
 
 
-def narrow_alu(width: int = 16, top: str = "Alu") -> Design:
+def narrow_alu(width: int = 16, top: str = "Alu", compare: bool = True) -> Design:
     """A small multi-bit datapath inside the bit-slice scope (no memory, no
     multiply): two operand registers loaded from inputs, an accumulator that
     adds, subtracts, xors or keeps the larger operand by a 2-bit select, and
-    a flag output; synchronous reset."""
+    a flag output; synchronous reset. With compare=False the larger operand
+    becomes their xor (the reference's bit-slice engine has no compare)."""
     d = Design()
     m = d.module(top)
     clk = m.input("clk", uint(1))
@@ -476,7 +477,7 @@ def narrow_alu(width: int = 16, top: str = "Alu") -> Design:
     m.next(a, din)
     m.next(b, a ^ acc)
     s0, s1 = sel.slice(0, 1), sel.slice(1, 1)
-    larger = mux(a.lt_expr(b), b, a)
+    larger = mux(a.lt_expr(b), b, a) if compare else a ^ b
     m.next(acc, mux(s1, mux(s0, acc + a, acc - b), mux(s0, acc ^ larger, acc + larger)))
     flag = m.output("flag", uint(1))
     m.assign(flag, acc.eq_expr(a))
