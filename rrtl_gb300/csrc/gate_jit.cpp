@@ -147,7 +147,7 @@ std::string gate_jit_source(const GateProgram& gp, const GateRunTables& run) {
   return o;
 }
 
-void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device, WordJit* J) {
+void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device, JitKernel* J) {
   if (gp.n_real_cells > kGateJitMaxCells) {
     J->error = "gate program of " + std::to_string(gp.n_real_cells) + " cells runs on the fused kernel";
     return;
@@ -155,7 +155,7 @@ void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device,
   jit_build_kernel(gate_jit_source(gp, run), device, "rrtl_gate_jit", J);
 }
 
-cudaError_t launch_gate_jit(const WordJit& J, const GateRunDev& R, cudaStream_t st) {
+cudaError_t launch_gate_jit(const JitKernel& J, const GateRunDev& R, cudaStream_t st) {
   GateRunDev r = R;
   void* args[] = {&r};
   const uint32_t grid = (R.words_pad + kGateJitThreads - 1) / kGateJitThreads;

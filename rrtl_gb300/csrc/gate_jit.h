@@ -38,8 +38,8 @@ struct GateRunTables {
 std::string gate_jit_source(const GateProgram& gp, const GateRunTables& run);
 
 // Emit, compile and load; never throws (failures leave ok = false).
-void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device, WordJit* J);
+void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device, JitKernel* J);
 
-cudaError_t launch_gate_jit(const WordJit& J, const GateRunDev& R, cudaStream_t st);
+cudaError_t launch_gate_jit(const JitKernel& J, const GateRunDev& R, cudaStream_t st);
 
 }  // namespace rrtl

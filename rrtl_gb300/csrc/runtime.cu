@@ -549,31 +549,31 @@ void gate_plain_launches(const GatePrepared& g, uint64_t cycles, cudaStream_t st
 // falls back (general kernel, interpreter or fused kernel) instead of waiting,
 // so a compile on one thread never stalls another (the serving loop).
 template <class Build>
-const WordJit* jit_cache_get(std::mutex& mu, std::map<std::string, std::unique_ptr<WordJit>>& cache,
+const JitKernel* jit_cache_get(std::mutex& mu, std::map<std::string, std::unique_ptr<JitKernel>>& cache,
                              const std::string& key, Build build) {
-  WordJit* J = nullptr;
+  JitKernel* J = nullptr;
   {
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) {
-      WordJit* e = it->second.get();
+      JitKernel* e = it->second.get();
       return e->ready.load(std::memory_order_acquire) && e->ok ? e : nullptr;
     }
     if (cache.size() >= kJitRunKernelsPerDesign) return nullptr;
-    J = cache.emplace(key, std::make_unique<WordJit>()).first->second.get();
+    J = cache.emplace(key, std::make_unique<JitKernel>()).first->second.get();
   }
   build(J);
   J->ready.store(true, std::memory_order_release);
   return J->ok ? J : nullptr;
 }
 
-const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
+const JitKernel* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
   const char* env = getenv("RRTL_GATE_JIT");
   if ((env && env[0] == '0') || d->gp().n_real_cells > kGateJitMaxCells || t.stim.size() > kJitRunTableMax ||
       t.rec.size() > kJitRunTableMax)
     return nullptr;
   return jit_cache_get(d->wjit_mu, d->gjit_runs, t.key(),
-                       [&](WordJit* J) { gate_jit_build(d->gp(), t, d->ctx->device, J); });
+                       [&](JitKernel* J) { gate_jit_build(d->gp(), t, d->ctx->device, J); });
 }
 
 bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
@@ -592,7 +592,7 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckT
   cudaStream_t st = d->ctx->stream;
   GatePrepared g = gate_prepare(b, run, device_ptrs, b->path == RRTL_PATH_FUSED, chk);
   // the compiled gate kernel: automatic tile width, no stuck-at forces; built before the timed region
-  const WordJit* J = nullptr;
+  const JitKernel* J = nullptr;
   if (b->path == RRTL_PATH_FUSED && !g.R.has_forces && (force_compiled || (b->tile_words == 0 && gate_jit_preferred(d, b->words))))
     J = gate_jit_for_run(d, g.tables);
   Timer tm(b);
@@ -755,22 +755,22 @@ void word_copy_out(rrtl_batch* b, const WordPrepared& g, const rrtl_run& run) {
 // The design's compiled word kernel for any run, built on first use (nullptr
 // when the design runs interpreted; the reason stays in the "general" cache
 // entry's error).
-const WordJit* word_jit_get(rrtl_design* d) {
+const JitKernel* word_jit_get(rrtl_design* d) {
   const char* env = getenv("RRTL_WORD_JIT");
   if (env && env[0] == '0') return nullptr;
   return jit_cache_get(d->wjit_mu, d->wjit_runs, "general",
-                       [&](WordJit* J) { word_jit_build(d->wp, d->ctx->device, J); });
+                       [&](JitKernel* J) { word_jit_build(d->wp, d->ctx->device, J); });
 }
 
-const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad) {
-  const WordJit* any = word_jit_get(d);
+const JitKernel* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad) {
+  const JitKernel* any = word_jit_get(d);
   const char* env = getenv("RRTL_WORD_JIT_RUNS");
   if (!any || (env && env[0] == '0') || t.stim.size() > kJitRunTableMax || t.rec.size() > kJitRunTableMax) return any;
   // two warps per 32 lanes on request only (RRTL_WORD_JIT_SPLIT=2): measured
   // slower than one warp on the pipelined CPU even at 4,096 lanes
   const char* senv = getenv("RRTL_WORD_JIT_SPLIT");
   if (lanes_pad && senv && senv[0] == '2') {
-    const WordJit* S = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key() + "|split", [&](WordJit* J) {
+    const JitKernel* S = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key() + "|split", [&](JitKernel* J) {
       WordSplitPlan plan;
       std::string why;
       if (word_split_plan(d->wp, t, &plan, &why)) word_jit_build(d->wp, d->ctx->device, J, &t, &plan);
@@ -778,8 +778,8 @@ const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t
     });
     if (S) return S;
   }
-  const WordJit* R = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key(),
-                                   [&](WordJit* J) { word_jit_build(d->wp, d->ctx->device, J, &t); });
+  const JitKernel* R = jit_cache_get(d->wjit_mu, d->wjit_runs, t.key(),
+                                   [&](JitKernel* J) { word_jit_build(d->wp, d->ctx->device, J, &t); });
   return R ? R : any;
 }
 
@@ -813,7 +813,7 @@ void word_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, bool start_s
   g.R.final_settle = final_settle;
   const bool per_cycle = (b->path == RRTL_PATH_PLAIN || b->path == RRTL_PATH_PLAIN_GRAPH) && run.cycles > 1;
   // compile before the timed region opens
-  const WordJit* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables, b->lanes_pad) : nullptr;
+  const JitKernel* J = !per_cycle && b->path == RRTL_PATH_FUSED ? word_jit_for_run(d, g.tables, b->lanes_pad) : nullptr;
   if (!J) word_require_interp(d, g);
   Timer tm(b);
   if (per_cycle) {
@@ -1317,11 +1317,11 @@ rrtl_status rrtl_design_word_jit(rrtl_design* d, uint32_t* active, float* compil
       return;
     }
     set_device(d->ctx);
-    const WordJit* J = word_jit_get(d);
+    const JitKernel* J = word_jit_get(d);
     *active = J ? 1u : 0u;
     std::lock_guard<std::mutex> lk(d->wjit_mu);
     auto it = d->wjit_runs.find("general");
-    const WordJit* E = it != d->wjit_runs.end() && it->second->ready.load() ? it->second.get() : nullptr;
+    const JitKernel* E = it != d->wjit_runs.end() && it->second->ready.load() ? it->second.get() : nullptr;
     if (compile_ms && E) *compile_ms = (float)E->compile_ms;
     if (!J) why = E ? E->error : std::string("compiled word kernels are off (RRTL_WORD_JIT=0) or still building");
   });

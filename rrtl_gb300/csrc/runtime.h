@@ -142,7 +142,7 @@ void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
 // The compiled gate kernel for this run's tables (built on first use and
 // kept per design), or nullptr when the design or run does not qualify.
-const WordJit* gate_jit_for_run(rrtl_design* d, const GateRunTables& t);
+const JitKernel* gate_jit_for_run(rrtl_design* d, const GateRunTables& t);
 // Whether a fused-path run of `words` 32-lane words should use the compiled
 // gate kernel: the autotuner's choice for the lane bucket, else designs whose
 // live nets fit in registers.
@@ -163,11 +163,11 @@ void design_warm_for_run(rrtl_design* d, uint32_t lanes, const rrtl_run& run);
 // Throws E_WORD_SCOPE when the interpreted word kernel cannot hold the design's value slots.
 void word_require_interp(const rrtl_design* d, const WordPrepared& g);
 // The design's compiled word kernel, built on first use; nullptr when the design runs interpreted.
-const WordJit* word_jit_get(rrtl_design* d);
+const JitKernel* word_jit_get(rrtl_design* d);
 // The kernel compiled for this run's tables (built on first use and kept per
 // design), else the design's general compiled kernel, else nullptr.
 // lanes_pad: the batch's padded lanes (0: no two-warp split).
-const WordJit* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad = 0);
+const JitKernel* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad = 0);
 cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st);
 cudaError_t word_multi_prepare(size_t smem);
 constexpr uint32_t kWordBlockLanes = 128;
@@ -212,8 +212,8 @@ struct rrtl_design {
   std::mutex wjit_mu;
   // compiled word kernels: "general" (any run, built on the first fused run)
   // and one per run tables
-  std::map<std::string, std::unique_ptr<rrtl::WordJit>> wjit_runs;
-  std::map<std::string, std::unique_ptr<rrtl::WordJit>> gjit_runs;  // compiled gate kernels, per run tables
+  std::map<std::string, std::unique_ptr<rrtl::JitKernel>> wjit_runs;
+  std::map<std::string, std::unique_ptr<rrtl::JitKernel>> gjit_runs;  // compiled gate kernels, per run tables
 };
 
 struct rrtl_batch {

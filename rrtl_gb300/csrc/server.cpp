@@ -60,7 +60,7 @@ struct Request {
   bool gate = false, fused = false;
   GatePrepared gp;
   WordPrepared wp;
-  const WordJit* jit = nullptr;  // the design's compiled word kernel, if any
+  const JitKernel* jit = nullptr;  // the design's compiled word kernel, if any
   uint64_t done_cycles = 0;
   uint64_t chunk = 0;  // cycles of the current round
 };

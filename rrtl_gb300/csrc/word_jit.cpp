@@ -468,7 +468,7 @@ Nvrtc& nvrtc() {
 
 }  // namespace
 
-WordJit::~WordJit() {
+JitKernel::~JitKernel() {
   if (lib) cudaLibraryUnload(lib);
 }
 
@@ -693,7 +693,7 @@ void jit_warm() {
   });
 }
 
-void jit_build_kernel(const std::string& src, int device, const char* name, WordJit* J) {
+void jit_build_kernel(const std::string& src, int device, const char* name, JitKernel* J) {
   const auto t0 = std::chrono::steady_clock::now();
   cudaDeviceProp prop{};
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
@@ -726,7 +726,7 @@ void jit_build_kernel(const std::string& src, int device, const char* name, Word
   J->compile_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRunTables* run,
+void word_jit_build(const WordProgram& wp, int device, JitKernel* J, const WordRunTables* run,
                     const WordSplitPlan* split) {
   J->written.assign(wp.mems.size(), 0);
   J->reg_signals = wp.n_sig_words <= kJitRegSignals;
@@ -743,7 +743,7 @@ void word_jit_build(const WordProgram& wp, int device, WordJit* J, const WordRun
   jit_build_kernel(word_jit_source(wp, run, split), device, "rrtl_word_jit", J);
 }
 
-size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad, uint64_t cycles,
+size_t word_jit_place(const WordProgram& wp, const JitKernel& J, uint32_t n_sig_words, uint32_t lanes_pad, uint64_t cycles,
                       uint32_t sm_count, size_t max_smem_block, size_t max_smem_sm, WordJitPlace* out) {
   // a row holds one word of every lane of a block: 128 lanes, 32 for a split kernel
   const uint32_t kThreads = J.split ? 32u : 128u;
@@ -790,7 +790,7 @@ size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_wo
   return used;
 }
 
-cudaError_t launch_word_jit(const WordJit& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem, cudaStream_t st) {
+cudaError_t launch_word_jit(const JitKernel& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem, cudaStream_t st) {
   WordRunDev r = R;
   WordJitPlace p = Pl;
   void* args[] = {&r, &p};

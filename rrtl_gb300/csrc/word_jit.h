@@ -53,7 +53,9 @@ struct WordSplitPlan {
 // register limit, or partitions too uneven to gain.
 bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitPlan* sp, std::string* why);
 
-struct WordJit {
+// One NVRTC-compiled kernel (a compiled word or gate kernel) loaded as a
+// library; destroyed with the design that owns it.
+struct JitKernel {
   cudaLibrary_t lib = nullptr;
   cudaKernel_t fn = nullptr;
   std::atomic<bool> ready{false};  // the build finished (the fields below are final)
@@ -66,7 +68,7 @@ struct WordJit {
   bool split = false;            // two warps per 32 lanes (word_jit_run_split)
   uint32_t n_xwords = 0;         // register words exchanged between the two warps
   std::vector<uint8_t> written;  // per memory: the design writes it
-  ~WordJit();
+  ~JitKernel();
 };
 
 // Largest word program that is compiled (bigger ones run interpreted).
@@ -90,20 +92,20 @@ void jit_warm();
 // Compile CUDA source `src` with NVRTC for `device` and load its kernel
 // `name` into J. Never throws: failures leave ok = false and the reason in
 // error.
-void jit_build_kernel(const std::string& src, int device, const char* name, WordJit* J);
+void jit_build_kernel(const std::string& src, int device, const char* name, JitKernel* J);
 
 // Emit, compile and load the kernel of `wp` on the current device. Never
 // throws: failures leave ok = false and the reason in error.
-void word_jit_build(const WordProgram& wp, int device, WordJit* out, const WordRunTables* run = nullptr,
+void word_jit_build(const WordProgram& wp, int device, JitKernel* out, const WordRunTables* run = nullptr,
                     const WordSplitPlan* split = nullptr);
 
 // Shared-memory placement for one launch over `lanes_pad` lanes and `cycles`
 // cycles; returns the dynamic shared memory bytes per 128-lane block.
-size_t word_jit_place(const WordProgram& wp, const WordJit& J, uint32_t n_sig_words, uint32_t lanes_pad,
+size_t word_jit_place(const WordProgram& wp, const JitKernel& J, uint32_t n_sig_words, uint32_t lanes_pad,
                       uint64_t cycles, uint32_t sm_count, size_t max_smem_block, size_t max_smem_sm,
                       WordJitPlace* out);
 
-cudaError_t launch_word_jit(const WordJit& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem,
+cudaError_t launch_word_jit(const JitKernel& J, const WordRunDev& R, const WordJitPlace& Pl, size_t smem,
                             cudaStream_t st);
 
 }  // namespace rrtl
