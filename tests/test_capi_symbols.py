@@ -38,3 +38,19 @@ def test_null_arguments_fail_with_codes_not_crashes():
     assert L.rrtl_ctx_create(0, None) == 1  # RRTL_E_ARG: out is null
     assert b"E_ARG" in L.rrtl_last_error()
     assert L.rrtl_batch_eval(None) == 1
+
+
+def test_every_entry_point_rejects_null_arguments():
+    """Each rrtl_status call made with every argument NULL (or 0) returns
+    RRTL_E_ARG before touching a device; destroying NULL is a no-op."""
+    lib = ctypes.CDLL(build.build())  # fresh function objects, no argtypes
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    protos = re.findall(r"^rrtl_status\s+(rrtl_[a-z_0-9]+)\s*\(([^)]*)\)\s*;", text, re.M)
+    assert len(protos) >= 50
+    for name, params in protos:
+        n = len([p for p in params.split(",") if p.strip() and p.strip() != "void"])
+        st = getattr(lib, name)(*([None] * n))
+        if name.endswith("_destroy"):
+            assert st == 0, name
+        else:
+            assert st == 1, (name, st, sim.lib().rrtl_last_error())
