@@ -844,6 +844,20 @@ class InstanceFoldSimulator:
     def instance_lane(self, inst: int, local: int) -> int:
         return inst * self.base_lanes + local
 
+    def port_offset(self, port: str) -> Optional[int]:
+        """Handle of a child input or output port (its packed signal index, what
+        the C ABI's signal calls take), None when the child has no such port
+        (InstanceFoldPlan::port_offset, crates/rrtl-gpu-sim/src/instance_fold.rs:45-55,
+        which returns the storage offset the reference's own calls take)."""
+        try:
+            idx, _, kind = self.sim.design.signal(port)
+        except RrtlError:
+            return None
+        return idx if kind in (0, 1) else None
+
+    def synchronize(self):
+        self.sim.synchronize()
+
     def set_port(self, port: str, limbs_by_lane: np.ndarray):
         """A child port over all lanes: [limbs][total_lanes]."""
         self.sim.set_input_limbs(port, limbs_by_lane)

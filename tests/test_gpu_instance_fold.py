@@ -41,6 +41,9 @@ def test_fold_port_demux_stepwise(engine):
     js = d.to_json()
     flat = sim.GpuBatchSimulator(js, "Top", base)
     fold = sim.InstanceFoldSimulator(js, "Top", base)
+    assert fold.port_offset("din") == fold.sim.design.signal("din")[0]
+    assert fold.port_offset("no_such_port") is None
+    assert fold.port_offset("acc") is None  # a register, not a port
     rng = Rng(4)
     for c in range(12):
         for name, v in (("clk", 1), ("rst", 1 if c == 0 else 0)):
@@ -52,5 +55,6 @@ def test_fold_port_demux_stepwise(engine):
             fold.set_top_input(f"din{i}", v)
         flat.tick()
         fold.tick()
+        fold.synchronize()
         for i in range(n):
             assert np.array_equal(fold.get_top_output(f"o{i}"), flat.get_signal_limbs(f"o{i}")), (c, i)
