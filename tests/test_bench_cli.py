@@ -28,3 +28,20 @@ def test_net_streaming_byte_model_of_the_headline_netlist():
     bpl = bench.net_stream_bytes_per_lane_cycle(bench.gate_fanins(js), bench.FFS, bench.PIS, bench.POS)
     assert 19_000 < bpl < 19_600
     json.dumps({"bytes_per_lane_cycle": bpl})
+
+
+def test_reference_arm_prints_one_contract_line():
+    """`bench.py --impl reference` times the CPU restatement of the path on
+    the host (no GPU) and prints one JSON line with the arm's keys."""
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, cwd=ROOT, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    r = json.loads(lines[0])
+    assert r["impl"] == "reference" and r["unit"] == "lane-cycles/s" and r["higher_is_better"] is True
+    assert r["steps"] == 1 and r["warmup"] == 3 and r["n_gpus"] == 1
+    assert r["value"] > 0 and r["cpu_baseline"]["value"] == r["value"]
+    assert r["cpu_baseline"]["kind"] in ("port", "reference") and r["cpu_baseline"]["cores"] >= 1
+    assert r["e2e"] == {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "workload" in r["config"]
