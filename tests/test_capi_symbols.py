@@ -54,3 +54,25 @@ def test_every_entry_point_rejects_null_arguments():
             assert st == 0, name
         else:
             assert st == 1, (name, st, sim.lib().rrtl_last_error())
+
+
+def test_last_error_is_per_thread():
+    """A failure on one thread leaves another thread's message untouched."""
+    import threading
+
+    build.build()
+    L = sim.lib()
+    assert L.rrtl_batch_eval(None) == 1
+    before = L.rrtl_last_error()
+    seen = {}
+
+    def other():
+        seen["start"] = L.rrtl_last_error()
+        L.rrtl_ctx_create(0, None)
+        seen["after"] = L.rrtl_last_error()
+
+    t = threading.Thread(target=other)
+    t.start()
+    t.join()
+    assert seen["start"] == b"" and b"out is null" in seen["after"]
+    assert L.rrtl_last_error() == before
