@@ -63,10 +63,11 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
       : "memory");
 }
 
-// Bounded wait for the mbarrier phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for the mbarrier phase with the given parity; false after
+// `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit) {
   uint32_t addr = smem_u32(bar);
-  for (uint32_t it = 0; it < kSpinLimit; ++it) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -740,6 +741,27 @@ cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem,
 
 cudaError_t launch_gate_plain(const GateProgDev& P, const GateRunDev& R, uint64_t c, int phase, cudaStream_t st) {
   gate_plain_kernel<<<R.n_tiles, kPlainThreads, 0, st>>>(P, R, c, phase);
+  return cudaGetLastError();
+}
+
+// Self-check of the bounded wait the fused and queue kernels use: one thread
+// waits `limit` polls on an mbarrier that nothing arrives on, so the wait
+// must give up; then it arrives once and waits again with the kernels' own
+// limit, which must complete at once. out[0]: RRTL_E_TIMEOUT when the first
+// wait gave up (RRTL_OK if it did not); out[1]: 1 when the second wait
+// completed. No copy is ever in flight.
+__global__ void mbar_wait_check_kernel(uint32_t limit, uint32_t* out) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  out[0] = mbar_wait(&bar, 0, limit) ? (uint32_t)RRTL_OK : (uint32_t)RRTL_E_TIMEOUT;
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bar)) : "memory");
+  out[1] = mbar_wait(&bar, 0) ? 1u : 0u;
+}
+
+cudaError_t launch_mbar_wait_check(uint32_t limit, uint32_t* out, cudaStream_t st) {
+  mbar_wait_check_kernel<<<1, 32, 0, st>>>(limit, out);
   return cudaGetLastError();
 }
 

@@ -1223,6 +1223,23 @@ rrtl_status rrtl_ctx_synchronize(rrtl_ctx* ctx) {
   });
 }
 
+rrtl_status rrtl_ctx_check_wait_timeout(rrtl_ctx* ctx, uint32_t polls, uint32_t* wait_status, uint32_t* completed) {
+  return guard([&] {
+    REQUIRE(ctx && wait_status && completed, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(polls >= 1 && polls <= (1u << 22), RRTL_E_ARG, "E_ARG: polls must be in 1..2^22");
+    set_device(ctx);
+    DevBuf out;
+    out.reserve(16);
+    cuda_check(cudaMemsetAsync(out.p, 0xFF, 16, ctx->stream), "memset");
+    cuda_check(launch_mbar_wait_check(polls, out.as<uint32_t>(), ctx->stream), "wait check launch");
+    uint32_t h[2] = {0, 0};
+    cuda_check(cudaMemcpyAsync(h, out.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream), "d2h wait check");
+    cuda_check(cudaStreamSynchronize(ctx->stream), "sync");
+    *wait_status = h[0];
+    *completed = h[1];
+  });
+}
+
 static void load_design(rrtl_ctx* ctx, Design design, const std::string& top, rrtl_design** out);
 
 rrtl_status rrtl_design_load_json(rrtl_ctx* ctx, const char* json, size_t len, const char* top, rrtl_design** out) {

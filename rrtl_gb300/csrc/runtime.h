@@ -138,6 +138,7 @@ size_t gate_queue_static_smem();
 cudaError_t gate_queue_prepare(size_t smem);
 cudaError_t launch_gate_queue(const GateQueueDev& Q, uint32_t grid, size_t smem, cudaStream_t st);
 cudaError_t launch_gate_fused(const GateProgDev& P, const GateRunDev& R, uint32_t grid, size_t smem, cudaStream_t st);
+cudaError_t launch_mbar_wait_check(uint32_t limit, uint32_t* out, cudaStream_t st);
 void set_last_error(const std::string& msg);
 WordRunDev word_chunk_desc(const WordPrepared& g, uint64_t c0, uint64_t n, bool last);
 // The compiled gate kernel for this run's tables (built on first use and

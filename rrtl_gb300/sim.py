@@ -116,6 +116,7 @@ EXPORTS = (
     "rrtl_ctx_event_record",
     "rrtl_ctx_event_elapsed",
     "rrtl_ctx_synchronize",
+    "rrtl_ctx_check_wait_timeout",
     "rrtl_design_load_json",
     "rrtl_design_destroy",
     "rrtl_design_info_get",
@@ -188,6 +189,7 @@ def lib():
         "rrtl_ctx_event_record": [c_void_p, c_uint32],
         "rrtl_ctx_event_elapsed": [c_void_p, c_uint32, c_uint32, P(c_float)],
         "rrtl_ctx_synchronize": [c_void_p],
+        "rrtl_ctx_check_wait_timeout": [c_void_p, c_uint32, P(c_uint32), P(c_uint32)],
         "rrtl_design_load_json": [c_void_p, c_char_p, c_size_t, c_char_p, P(c_void_p)],
         "rrtl_design_destroy": [c_void_p],
         "rrtl_design_info_get": [c_void_p, P(DesignInfo)],
@@ -281,6 +283,14 @@ class Context:
 
     def synchronize(self):
         check(lib().rrtl_ctx_synchronize(self.h))
+
+    def check_wait_timeout(self, polls: int = 256):
+        """Run the bounded-wait self-check: (status of a wait on an mbarrier
+        nothing arrives on -- RRTL_E_TIMEOUT is the expected answer --, whether
+        the wait after one arrival completed)."""
+        st, done = c_uint32(), c_uint32()
+        check(lib().rrtl_ctx_check_wait_timeout(self.h, polls, byref(st), byref(done)))
+        return st.value, bool(done.value)
 
     # -- device job queue (rrtl_queue_*)
     def submit(self, batch: "GpuBatchSimulator", cycles: int, seed: int = 0, stim: Iterable = (),
