@@ -117,6 +117,30 @@ def test_crc32_fault_sim_known_answer(oracle_lib):
     assert round(sum(lat) / len(lat), 1) == 2.1
 
 
+def test_crc32_atpg_vector_confirmed_on_the_bit_parallel_engine(oracle_lib):
+    """The reference's symbolic ATPG test for crc_5 stuck-at-0 (din = 0x01,
+    initial state 0), confirmed concretely: lane 0 golden, lane 1 faulted,
+    one tick gives golden 0x690ce0ee and faulty 0x690ce0ce
+    (crates/rrtl-sim-ir/examples/symbolic_exec.rs:192-212;
+    docs/rrtl-optimizations.md:1931-1934)."""
+    d = crc32_netlist_json()
+    od = ob.OracleDesign(d.to_json(), "crc32")
+    bp = ob.BitParallel(od, 2)
+    din, state = 0x01, 0
+    for l in range(2):
+        bp.set(od.signal("clk"), l, 1)
+        bp.set(od.signal("rst"), l, 0)
+        for i in range(8):
+            bp.set(od.signal(f"din_{i}"), l, (din >> i) & 1)
+        for k in range(32):
+            bp.set(od.signal(f"crc_{k}"), l, (state >> k) & 1)
+    bp.set_force(od.signal("crc_5"), 1, 0)
+    bp.tick()
+    golden, faulty = (sum(bp.get(od.signal(f"crc_{i}"), l) << i for i in range(32)) for l in range(2))
+    assert (golden, faulty) == (0x690CE0EE, 0x690CE0CE)
+    assert golden == ob.crc_step(state, din)
+
+
 def test_stuck_at_force_clamps_and_isolates_lanes(oracle_lib):
     """crates/rrtl-sim-ir/src/bitparallel.rs:582-628."""
     d = Design()
