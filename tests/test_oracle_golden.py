@@ -5,7 +5,7 @@ from oracle import binding as ob
 from rrtl_gb300.builder import Design, lit_u, mux, uint
 from rrtl_gb300.workloads import Rng, smix64, stim_word
 
-from .helpers import crc32_netlist_json
+from .helpers import crc32_netlist_json, oracle_bp_run
 
 
 def _counter():
@@ -139,6 +139,15 @@ def test_crc32_atpg_vector_confirmed_on_the_bit_parallel_engine(oracle_lib):
     golden, faulty = (sum(bp.get(od.signal(f"crc_{i}"), l) << i for i in range(32)) for l in range(2))
     assert (golden, faulty) == (0x690CE0EE, 0x690CE0CE)
     assert golden == ob.crc_step(state, din)
+    # the same vector through the run protocol the GPU engines follow:
+    # constant stimulus; a cycle records before its clock edge, so the second
+    # cycle's row holds the state after one edge
+    stim = [(od.signal("clk"), 3, 1), (od.signal("rst"), 3, 0)]
+    stim += [(od.signal(f"din_{i}"), 3, (din >> i) & 1) for i in range(8)]
+    tr = oracle_bp_run(od, 2, 2, 0, stim, [od.signal(f"crc_{i}") for i in range(32)], 1,
+                       faults=[(1, od.signal("crc_5"), 0)])["trace"]
+    row = [[sum(((int(tr[c, i, 0]) >> l) & 1) << i for i in range(32)) for l in range(2)] for c in range(2)]
+    assert row == [[0, 0], [0x690CE0EE, 0x690CE0CE]]
 
 
 def test_stuck_at_force_clamps_and_isolates_lanes(oracle_lib):
