@@ -150,6 +150,42 @@ def test_crc32_atpg_vector_confirmed_on_the_bit_parallel_engine(oracle_lib):
     assert row == [[0, 0], [0x690CE0EE, 0x690CE0CE]]
 
 
+def test_reconvergent_cone_fault_answers(oracle_lib):
+    """The reference's ATPG answers on y = (a&b) | (a&~b), confirmed
+    exhaustively on the concrete engine (comb-wire forces clamp on store):
+    nb stuck-at-1 is untestable, nb stuck-at-0 is detected only by a=1,b=0,
+    w stuck-at-0 only by a=1,b=1, v stuck-at-1 by a=0
+    (crates/rrtl-sim-ir/examples/symbolic_exec.rs:76-135;
+    docs/rrtl-optimizations.md:1926-1929). One 32-lane word per fault, lanes
+    1-4 of it take the four input pairs, through the engines' run protocol."""
+    d = Design()
+    m = d.module("Redund")
+    a, b = m.input("a", uint(1)), m.input("b", uint(1))
+    nb, w, v = m.wire("nb", uint(1)), m.wire("w", uint(1)), m.wire("v", uint(1))
+    y = m.output("y", uint(1))
+    m.assign(nb, ~b)
+    m.assign(w, a & b)
+    m.assign(v, a & nb)
+    m.assign(y, w | v)
+    od = ob.OracleDesign(d.to_json(), "Redund")
+    faults = [("nb", 1), ("nb", 0), ("w", 0), ("v", 1)]
+    pairs = [(0, 0), (0, 1), (1, 0), (1, 1)]
+    trace = np.zeros((1, 2, len(faults)), np.uint32)
+    for f in range(len(faults)):
+        for k, (av, bv) in enumerate(pairs):
+            trace[0, 0, f] |= av << (k + 1)
+            trace[0, 1, f] |= bv << (k + 1)
+    stim = [(od.signal("a"), 4, 0), (od.signal("b"), 4, 1)]
+    placed = [(32 * f + k + 1, od.signal(n), val) for f, (n, val) in enumerate(faults) for k in range(4)]
+    tr = oracle_bp_run(od, 32 * len(faults), 1, 0, stim, [od.signal("y")], 1, faults=placed,
+                       input_trace=trace)["trace"]
+    detected = {}
+    for f, fault in enumerate(faults):
+        ys = [(int(tr[0, 0, f]) >> (k + 1)) & 1 for k in range(4)]
+        detected[fault] = [pairs[k] for k in range(4) if ys[k] != pairs[k][0]]  # golden y = a
+    assert detected == {("nb", 1): [], ("nb", 0): [(1, 0)], ("w", 0): [(1, 1)], ("v", 1): [(0, 0), (0, 1)]}
+
+
 def test_stuck_at_force_clamps_and_isolates_lanes(oracle_lib):
     """crates/rrtl-sim-ir/src/bitparallel.rs:582-628."""
     d = Design()
