@@ -554,6 +554,12 @@ class GpuBatchSimulator:
     def eval_combinational(self):
         check(lib().rrtl_batch_eval(self.h))
 
+    def eval_combinational_many(self, iterations: int):
+        """`iterations` settles in a row (GpuBatchSimulator::eval_combinational_many,
+        crates/rrtl-gpu-sim/src/lib.rs:958-964); 0 does nothing."""
+        for _ in range(iterations):
+            check(lib().rrtl_batch_eval(self.h))
+
     def tick(self):
         check(lib().rrtl_batch_tick(self.h))
 

@@ -65,6 +65,8 @@ def test_combinational_only_design(engine, lanes):
     g.eval_combinational()
     a, b, c = vals["a"], vals["b"], vals["c"]
     assert np.array_equal(g.get_signal("y"), np.where(a == 1, b, c) ^ (a & b))
+    g.eval_combinational_many(2)  # settling again changes nothing
+    assert np.array_equal(g.get_signal("y"), np.where(a == 1, b, c) ^ (a & b))
 
 
 def test_register_only_design_shifts(engine):
