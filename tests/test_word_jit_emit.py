@@ -136,6 +136,23 @@ def test_compiled_gate_kernel_sources_compile(which):
     assert cub > 0, log
 
 
+@pytest.mark.parametrize("n_ff,mode", [(0, sim.REC_TRACE | sim.REC_HASH | sim.REC_DETECT), (40, 0)])
+def test_compiled_gate_kernel_edge_shapes_compile(n_ff, mode):
+    """A netlist without registers, and a run that records nothing."""
+    from rrtl_gb300.workloads import gate_netlist, netlist_run_spec
+
+    d, meta = gate_netlist(n_gates=200, n_ff=n_ff, n_pi=4, n_po=4, depth=5, seed=11)
+    stim, rec = netlist_run_spec(meta)
+    run = _run_for(d, meta.top, stim, rec if mode else [], mode)
+    try:
+        src, cub, log = sim.gate_jit_emit(d, meta.top, run, "sm_103a")
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+    assert cub > 0, log
+
+
 def test_two_warp_split_source_compiles():
     """The two-warp form of the pipelined CPU's run kernel: both halves, the
     register exchange and the split run protocol compile for sm_103a; a design
