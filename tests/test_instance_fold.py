@@ -132,3 +132,67 @@ def test_fold_equals_flattened_on_the_oracle():
         o = pc.get_signal(child.signal("o"))
         for i in range(n):
             assert np.array_equal(pf.get_signal(flat.signal(f"o{i}")), o[:, i * base:(i + 1) * base]), (c, i)
+
+
+def _limbs(vals, w):
+    n = max(1, (w + 31) // 32)
+    return np.array([[(v >> (32 * l)) & 0xFFFFFFFF for v in vals] for l in range(n)], dtype=np.uint32)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_children_with_shared_and_private_inputs_fold(seed):
+    """Random child modules (registers with every reset kind, a memory,
+    inputs and outputs of many widths) wrapped N = 3 times, each child input
+    tied either to one shared wrapper input or to a private one per
+    instance: the product's fold plan, used to demultiplex lane blocks, makes
+    the child over N x L lanes equal the flattened wrapper on the oracle."""
+    from .designs import random_word_design
+
+    n, base, cycles = 3, 5, 12
+    d, meta = random_word_design(seed, n_wires=10, depth=3, n_mems=1, top="Cell")
+    rng = Rng(seed * 7 + 1)
+    m = d.module("Wrap")
+    clk, rst = m.input("clk", uint(1)), m.input("rst", uint(1))
+    shared, wrap_in = {}, []
+    for name, w in meta["inputs"]:
+        if rng.below(3) == 0:
+            shared[name] = m.input(f"sh_{name}", uint(w))
+            wrap_in.append((f"sh_{name}", w))
+    for i in range(n):
+        conns = [("clk", clk), ("rst", rst)]
+        for name, w in meta["inputs"]:
+            if name in shared:
+                conns.append((name, shared[name]))
+            else:
+                wrap_in.append((f"{name}_{i}", w))
+                conns.append((name, m.input(f"{name}_{i}", uint(w))))
+        conns += [(name, m.output(f"{name}_{i}", uint(w))) for name, w in meta["outputs"]]
+        m.instance(f"u{i}", "Cell", conns)
+    js = d.to_json()
+    plan = sim.instance_fold_plan(js, "Wrap")
+    assert plan["child"] == "Cell" and len(plan["instances"]) == n
+    drives = {}
+    for tsig, inst, port, direction in plan["connections"]:
+        if direction == "in":
+            drives.setdefault(port, {})[inst] = tsig
+    flat, child = ob.OracleDesign(js, "Wrap"), ob.OracleDesign(js, "Cell")
+    pf, pc = ob.PackedSim(flat, base), ob.PackedSim(child, n * base)
+    compared = 0
+    for c in range(cycles):
+        vals = {"clk": [1] * base, "rst": [1 if c < 2 else 0] * base}
+        for name, w in wrap_in:
+            vals[name] = [rng.next() & ((1 << w) - 1) if w < 64 else rng.next() for _ in range(base)]
+        for name, w in [("clk", 1), ("rst", 1)] + wrap_in:
+            pf.set_signal(flat.signal(name), _limbs(vals[name], w), settle=False)
+        for port, w in [("clk", 1), ("rst", 1)] + list(meta["inputs"]):
+            lanes = sum((vals[drives[port][i]] for i in range(n)), [])
+            pc.set_signal(child.signal(port), _limbs(lanes, w), settle=False)
+        pf.tick()
+        pc.tick()
+        for name, w in meta["outputs"]:
+            co = pc.get_signal(child.signal(name))
+            for i in range(n):
+                assert np.array_equal(pf.get_signal(flat.signal(f"{name}_{i}")), co[:, i * base:(i + 1) * base]), \
+                    (c, name, i)
+                compared += 1
+    assert compared >= cycles * n
