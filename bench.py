@@ -43,13 +43,20 @@ METRIC = "lane-cycles/s (gate-evals/s) batched vs plain CUDA on 1 GB300; p99 job
 
 
 def dist_setup():
+    """Host-side process group over gloo: it only carries barriers and the
+    max of the ranks' timings (lanes shard with no data-path exchange). A
+    rank that fails or never arrives makes the others' next collective fail
+    within RRTL_DIST_TIMEOUT_S seconds (default 600) instead of hanging."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
+        from datetime import timedelta
+
         import torch.distributed as dist
 
-        dist.init_process_group("gloo", init_method="env://")
+        timeout = timedelta(seconds=float(os.environ.get("RRTL_DIST_TIMEOUT_S", "600")))
+        dist.init_process_group("gloo", init_method="env://", timeout=timeout)
         return ws, rank, local, dist
     return 1, 0, 0, None
 

@@ -43,3 +43,36 @@ def test_two_rank_lane_shards_and_max_time():
     assert (f0, l0, f1, l1) == (0, 4096, 4096, 8192)  # disjoint, covering, contiguous
     assert ms0 == ms1 == 15.0  # max over ranks
     assert v0 == v1 == pytest.approx(2 * 4096 * 100 * 5 / 0.015)
+
+
+def _failing_rank(rank, ws, port, out):
+    """Rank 1 fails between steps (raises, then its process exits); rank 0
+    learns of it at its next collective, which errors instead of hanging."""
+    import time
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank), RRTL_DIST_TIMEOUT_S="20")
+    _, _, _, d = bench.dist_setup()
+    bench.reduce_max(d, 1.0)  # one step that both ranks finish
+    if rank == 1:
+        raise SystemExit(3)  # a failure on the host between steps
+    t0 = time.time()
+    try:
+        bench.reduce_max(d, 2.0)
+        out.put(("no error", time.time() - t0))
+    except Exception as e:  # the collective reports the missing peer
+        out.put((type(e).__name__, time.time() - t0))
+
+
+def test_a_failed_rank_is_detected_at_the_next_collective():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 31500 + os.getpid() % 2000
+    procs = [ctx.Process(target=_failing_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    kind, secs = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+    assert procs[1].exitcode == 3
+    assert kind != "no error" and secs < 60
