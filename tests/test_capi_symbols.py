@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from rrtl_gb300 import build, sim
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "rrtl_cuda.h")
@@ -76,3 +78,20 @@ def test_last_error_is_per_thread():
     t.join()
     assert seen["start"] == b"" and b"out is null" in seen["after"]
     assert L.rrtl_last_error() == before
+
+
+def test_without_a_device_the_context_fails_with_a_code():
+    """On a host without a usable GPU the engine refuses at context creation
+    with RRTL_E_DEVICE and the CUDA error text; it has no CPU fallback."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    build.build()
+    L = sim.lib()
+    out = ctypes.c_void_p()
+    assert L.rrtl_ctx_create(0, ctypes.byref(out)) == 4  # RRTL_E_DEVICE
+    assert L.rrtl_last_error().startswith(b"E_DEVICE") and out.value is None
+    with pytest.raises(sim.RrtlError) as e:
+        sim.Context(0)
+    assert e.value.status == 4
