@@ -95,3 +95,14 @@ def test_without_a_device_the_context_fails_with_a_code():
     with pytest.raises(sim.RrtlError) as e:
         sim.Context(0)
     assert e.value.status == 4
+
+
+def test_a_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """The Python mirror has no fallback: without the built library every
+    entry raises."""
+    monkeypatch.setattr(sim, "LIB_PATH", str(tmp_path / "librrtl_gb300.so"))
+    monkeypatch.setattr(sim, "_lib", None)
+    with pytest.raises(RuntimeError, match="is missing"):
+        sim.lib()
+    with pytest.raises(RuntimeError, match="is missing"):
+        sim.bitslice_json("{}", "Top")
