@@ -73,11 +73,11 @@ rrtl_status rrtl_ctx_event_elapsed(rrtl_ctx* ctx, uint32_t a, uint32_t b, float*
 rrtl_status rrtl_ctx_synchronize(rrtl_ctx* ctx);
 /* Failure-detection self-check of the bounded device wait that the fused and
  * queue kernels use for their copies (no reference counterpart). One CTA
- * waits `polls` polls
- * (1..2^22) on an mbarrier that nothing arrives on: *wait_status is
- * RRTL_E_TIMEOUT when that wait gave up, as it must (RRTL_OK would mean it
- * did not). It then arrives once and waits again: *completed is 1 when that
- * wait finished. No copy is in flight; the context stays usable. */
+ * waits `polls` polls (1..2^22) on an mbarrier that nothing arrives on:
+ * *wait_status is RRTL_E_TIMEOUT when that wait gave up, as it must (RRTL_OK
+ * would mean it did not). It then arrives once and waits again: *completed
+ * is 1 when that wait finished. No copy is in flight; the context stays
+ * usable. */
 rrtl_status rrtl_ctx_check_wait_timeout(rrtl_ctx* ctx, uint32_t polls, uint32_t* wait_status, uint32_t* completed);
 
 /* ---- compiled design ---------------------------------------------------- */
