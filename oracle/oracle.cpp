@@ -16,7 +16,12 @@
 // answer [1,0,2,2] (crates/rrtl-gpu-sim/src/lib.rs:5763-5787), the crc32 gate
 // netlist against the CRC-32 algorithm (crates/rrtl-sim-ir/examples/netlist_crc32.rs)
 // and the stuck-at fault-sim coverage 64/64 with latency 1/6/2.1
-// (crates/rrtl-sim-ir/examples/fault_sim.rs; docs/rrtl-optimizations.md:1411-1416).
+// (crates/rrtl-sim-ir/examples/fault_sim.rs; docs/rrtl-optimizations.md:1411-1416),
+// the ATPG answers confirmed concretely (crc_5 stuck-at-0: golden 0x690ce0ee,
+// faulty 0x690ce0ce; the reconvergent cone's testable and untestable faults;
+// crates/rrtl-sim-ir/examples/symbolic_exec.rs:76-212). BitSlice is pinned by
+// the reference's own bit-slice test (tests/test_bitslice.py,
+// crates/rrtl-sim-ir/src/bitslice.rs:727-778).
 #include <algorithm>
 #include <functional>
 #include <cstring>
