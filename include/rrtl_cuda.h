@@ -395,12 +395,19 @@ rrtl_status rrtl_server_destroy(rrtl_server* s);
  * lives in a fixed device array of 2^20 u32 words that the library defines,
  * so total capture words (one per register limb) x lanes_pad may not exceed
  * 2^20; larger requests fail with RRTL_E_ARG (E_NOALLOC_SIZE). Every GPU that
- * loads the library holds that array until the process exits. The first call
- * on a device looks up the array's device address; make that first call
- * before any stream capture begins. All calls share the array and it keeps
- * the previous call's contents, which every call overwrites before reading;
- * calls whose work overlaps on the GPU race on it. Runs on the design's
- * context stream and returns after the work finishes. */
+ * loads the library holds that array until the process exits. rrtl_ctx_create
+ * looks up the array's device address (with the context's device current)
+ * and the context keeps it, so this call does no set-up of its own.
+ * `values` and `memories` must be device (or managed) memory of the design's
+ * device: other pointers (host memory, another device's memory) fail with
+ * RRTL_E_ARG before anything is launched. The call runs on the context's
+ * stream, which does not wait for the legacy default stream or for the
+ * caller's streams: finish every write to `values` and `memories` (for
+ * example with a stream or device synchronise) before calling. All calls
+ * share the array and it keeps the previous call's contents, which every call
+ * overwrites before reading; calls whose work overlaps on the GPU race on it.
+ * steps == 0 returns without launching anything. Returns after the work
+ * finishes. */
 rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* design, uint32_t* values, uint32_t* memories, uint32_t lanes,
                                         uint64_t steps);
 

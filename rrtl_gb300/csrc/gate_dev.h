@@ -127,7 +127,8 @@ struct GateQueueDev {
   const GateJobDev* jobs;
   const GateItemDev* items;
   uint32_t n_items;
-  uint32_t* next;  // atomic item counter (zeroed before the launch)
+  uint32_t* next;  // [0] atomic item counter, [1] launch status (both zeroed before the launch): a CTA
+                   // that could not drain its copies at exit fails every job of the launch
 };
 
 }  // namespace rrtl

@@ -309,11 +309,14 @@ __device__ __forceinline__ void fused_cta_init(FusedCta& cta, uint8_t* smem) {
 }
 
 // After an abort, let every copy still in flight land before the CTA's shared
-// memory is released.
-__device__ __forceinline__ void fused_cta_drain(const FusedCta& cta) {
+// memory is released. A drain wait that gives up leaves a copy in flight into
+// shared memory the next CTA on this SM may reuse, possibly for another job:
+// it is recorded in `err`, which covers every run the launch serves.
+__device__ __forceinline__ void fused_cta_drain(const FusedCta& cta, uint32_t* err) {
   if (cta.aborted && threadIdx.x == 0)
     for (uint64_t k = cta.q; k < cta.issued; ++k)
-      (void)mbar_wait(&cta.bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u);
+      if (!mbar_wait(&cta.bars[(uint32_t)k & (kRing - 1u)], ((uint32_t)k >> 2) & 1u))
+        atomicExch(err, (uint32_t)RRTL_E_TIMEOUT);
 }
 
 // Cycles [c0, c0 + ncyc) of one tile (W words) of a run, then the closing
@@ -535,7 +538,7 @@ __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused
   fused_cta_init(cta, smem);
   for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !cta.aborted; tile += gridDim.x)
     fused_tile<W>(P, R, tile, R.cycle_base, R.cycles, R.final_settle != 0, cta);
-  fused_cta_drain(cta);
+  fused_cta_drain(cta, R.err);
 }
 
 // Persistent job-queue kernel: CTAs take (job, tile, cycle range) items from
@@ -568,7 +571,7 @@ __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_queue
     }
     if (cta.aborted) break;
   }
-  fused_cta_drain(cta);
+  fused_cta_drain(cta, Q.next + 1);
 }
 
 // ------------------------------------------------------------ plain path --

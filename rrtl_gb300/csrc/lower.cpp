@@ -367,17 +367,48 @@ std::vector<std::vector<PackedOp>> schedule_assignments(const std::vector<std::p
   }
   std::vector<int64_t> memo(as.size(), -1);
   std::vector<char> visiting(as.size(), 0);
-  // Iterative DFS with the reference's cycle rule: a node re-entered while on
-  // the stack contributes level 0 and is not memoised on that path.
-  std::function<int64_t(size_t)> level = [&](size_t i) -> int64_t {
-    if (memo[i] >= 0) return memo[i];
-    if (visiting[i]) return 0;
-    visiting[i] = 1;
-    int64_t lv = 0;
-    for (uint32_t d : deps[i]) lv = std::max(lv, level(d) + 1);
-    visiting[i] = 0;
-    memo[i] = lv;
-    return lv;
+  // The reference's recursive assignment_level restated as a DFS over an
+  // explicit stack (a 100k-deep chain of wires must not recurse 100k frames
+  // deep on the host stack). Same visiting order and cycle rule: a node
+  // re-entered while on the stack contributes level 0, and every node is
+  // memoised when its own visit ends.
+  struct Frame {
+    size_t node;
+    size_t next_dep;
+    int64_t lv;
+  };
+  std::vector<Frame> stack;
+  auto level = [&](size_t root) -> int64_t {
+    if (memo[root] >= 0) return memo[root];
+    int64_t result = 0;
+    visiting[root] = 1;
+    stack.push_back(Frame{root, 0, 0});
+    while (!stack.empty()) {
+      const size_t top = stack.size() - 1;
+      const size_t node = stack[top].node;
+      if (stack[top].next_dep < deps[node].size()) {
+        const uint32_t d = deps[node][stack[top].next_dep++];
+        int64_t child;
+        if (memo[d] >= 0) {
+          child = memo[d];
+        } else if (visiting[d]) {
+          child = 0;
+        } else {
+          visiting[d] = 1;
+          stack.push_back(Frame{d, 0, 0});
+          continue;
+        }
+        stack[top].lv = std::max(stack[top].lv, child + 1);
+        continue;
+      }
+      const int64_t lv = stack[top].lv;
+      visiting[node] = 0;
+      memo[node] = lv;
+      stack.pop_back();
+      if (stack.empty()) result = lv;
+      else stack.back().lv = std::max(stack.back().lv, lv + 1);
+    }
+    return result;
   };
   std::vector<std::vector<PackedOp>> levels;
   for (size_t i = 0; i < as.size(); ++i) {

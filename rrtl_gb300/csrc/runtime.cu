@@ -869,6 +869,10 @@ JobQueue& queue_of(rrtl_ctx* c) {
 // status. Called once the stream has passed the launches' end.
 void queue_finish(rrtl_ctx* c) {
   JobQueue& Q = queue_of(c);
+  // launch status: a CTA that could not drain its copies fails every job of the launch
+  uint32_t launch_err = 0;
+  if (Q.d_next.p && cudaMemcpy(&launch_err, Q.d_next.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    launch_err = RRTL_E_DEVICE;
   std::vector<QueueJob> keep;
   for (QueueJob& j : Q.jobs) {
     if (j.status != RRTL_JOB_RUNNING) {
@@ -876,8 +880,8 @@ void queue_finish(rrtl_ctx* c) {
       continue;
     }
     rrtl_batch* b = j.batch;
-    uint32_t e = 0;
-    cudaError_t ce = cudaMemcpy(&e, b->d_err.p, 4, cudaMemcpyDeviceToHost);
+    uint32_t e = launch_err;
+    cudaError_t ce = e ? cudaSuccess : cudaMemcpy(&e, b->d_err.p, 4, cudaMemcpyDeviceToHost);
     if (ce == cudaSuccess && e == 0) {
       try {
         gate_copy_out(b, j.prep, j.run);
@@ -887,7 +891,7 @@ void queue_finish(rrtl_ctx* c) {
         j.status = RRTL_JOB_FAILED;
       }
     } else {
-      if (e) cudaMemset(b->d_err.p, 0, 4);
+      cudaMemset(b->d_err.p, 0, 4);
       j.status = RRTL_JOB_FAILED;
     }
     b->queued = false;
@@ -972,7 +976,7 @@ void queue_launch(rrtl_ctx* c) {
     upload(Q.d_jobs, jobs);
     upload(Q.d_items, flat);
     Q.d_next.reserve(16);
-    cuda_check(cudaMemsetAsync(Q.d_next.p, 0, 4, st), "memset queue");
+    cuda_check(cudaMemsetAsync(Q.d_next.p, 0, 8, st), "memset queue");
     if (!Q.smem_set) {
       // the limit is per kernel: allow every job this queue can take
       cuda_check(gate_queue_prepare(qmax), "gate_queue_prepare");
@@ -1156,6 +1160,7 @@ rrtl_status rrtl_ctx_create(int32_t device, rrtl_ctx** out) {
       c->max_smem = (size_t)smem;
       c->max_smem_sm = (size_t)smem_sm;
       for (auto& e : c->events) cuda_check(cudaEventCreate(&e), "event");
+      cuda_check(noalloc_scratch_lookup(&c->noalloc_scratch), "noalloc scratch lookup");
     } catch (...) {
       delete c;
       throw;

@@ -171,6 +171,9 @@ const JitKernel* word_jit_get(rrtl_design* d);
 const JitKernel* word_jit_for_run(rrtl_design* d, const WordRunTables& t, uint32_t lanes_pad = 0);
 cudaError_t launch_word_multi(const WordJobDev* jobs, uint32_t n_jobs, uint32_t blocks, size_t smem, cudaStream_t st);
 cudaError_t word_multi_prepare(size_t smem);
+// Device address of the allocation-free entry point's scratch array for the
+// current device (cudaGetSymbolAddress; the device must be current).
+cudaError_t noalloc_scratch_lookup(uint32_t** out);
 constexpr uint32_t kWordBlockLanes = 128;
 constexpr size_t kWordSmemLimit = 96 * 1024;
 
@@ -188,6 +191,10 @@ struct rrtl_ctx {
   size_t max_smem_sm = 0;   // shared memory per SM
   cudaEvent_t events[8] = {};
   std::unique_ptr<rrtl::JobQueue> queue;
+  // device address of the allocation-free entry point's fixed scratch array,
+  // looked up when the context is created (with its device current), so it
+  // lives and dies with the context
+  uint32_t* noalloc_scratch = nullptr;
 };
 
 struct rrtl_design {

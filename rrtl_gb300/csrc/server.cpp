@@ -286,7 +286,7 @@ void rrtl_server::round() {
     upload(d_jobs, jobs);
     upload(d_items, sorted);
     d_next.reserve(16);
-    cuda_check(cudaMemsetAsync(d_next.p, 0, 4, st), "memset queue");
+    cuda_check(cudaMemsetAsync(d_next.p, 0, 8, st), "memset queue");
     GateQueueDev QD{d_jobs.as<GateJobDev>(), d_items.as<GateItemDev>(), (uint32_t)sorted.size(), d_next.as<uint32_t>()};
     cuda_check(launch_gate_queue(QD, std::min<uint32_t>((uint32_t)sorted.size(), ctx->sm_count), smem, st),
                "gate_queue_kernel");
@@ -312,9 +312,18 @@ void rrtl_server::round() {
     ++rounds;
     busy_ns += now_ns() - t0;
   }
+  // launch status of the queue kernel: a CTA that could not drain its copies
+  // fails every request the launch served
+  uint32_t launch_err = 0;
+  if (!items.empty() && cudaMemcpy(&launch_err, d_next.as<uint32_t>() + 1, 4, cudaMemcpyDeviceToHost) != cudaSuccess)
+    launch_err = RRTL_E_DEVICE;
   std::vector<std::shared_ptr<Request>> keep;
   for (auto& rp : active) {
     Request& r = *rp;
+    if (launch_err && r.gate && r.fused) {
+      finish(r, RRTL_JOB_FAILED, "E_TIMEOUT: a bounded device wait of the round's queue launch gave up");
+      continue;
+    }
     r.done_cycles += r.chunk;
     if (r.done_cycles < r.run.cycles) {
       keep.push_back(rp);

@@ -253,23 +253,31 @@ static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords
 
 void set_last_error(const std::string& msg);
 
-namespace {
-std::mutex g_noalloc_mu;
-uint32_t* g_noalloc_ptr[64] = {};  // per-device address of g_noalloc_scratch
-
-// Host code cannot use the array's name as a device address; look the address
-// up once per device, with that device current.
-cudaError_t noalloc_scratch(int device, uint32_t** out) {
-  if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_ptr[device] = static_cast<uint32_t*>(p);
-  }
-  *out = g_noalloc_ptr[device];
+// Host code cannot use the array's name as a device address: the name is a
+// host-side stand-in. rrtl_ctx_create calls this once per context, with the
+// context's device current, and keeps the address in the context, so the
+// address is never used past the context (and the device context) it was
+// looked up in.
+cudaError_t noalloc_scratch_lookup(uint32_t** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return e;
+  *out = static_cast<uint32_t*>(p);
   return cudaSuccess;
+}
+
+namespace {
+// Whether p is memory the design's device can dereference as ordinary device
+// memory (a cudaMalloc or managed allocation of that device).
+bool device_pointer_of(const void* p, int device) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();  // clear the (non-sticky) error an unknown pointer leaves
+    return false;
+  }
+  if (a.type == cudaMemoryTypeDevice) return a.device == device;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return false;
 }
 }  // namespace
 
@@ -289,16 +297,25 @@ extern "C" rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* d, uint32_t* val
   if (d->mp.source.total_memory_words_per_lane > 0 && !memories) return fail_with(RRTL_E_ARG, "E_ARG: memories is null");
   if ((size_t)d->wdev.n_vslots * 128u * 8u > 96u * 1024u)
     return fail_with(RRTL_E_UNSUPPORTED, "E_WORD_SCOPE: design needs more live value slots than shared memory holds");
-  const uint32_t lanes_pad = (lanes + 127u) / 128u * 128u;
-  const size_t cap_words = (size_t)d->wp.total_capture_words * lanes_pad;
+  // padded in 64 bits: lanes near 2^32 must not wrap to a zero-sized request
+  const uint64_t lanes_pad = ((uint64_t)lanes + 127u) / 128u * 128u;
+  if (lanes_pad > 0xFFFFFF80ull)
+    return fail_with(RRTL_E_LANES, "E_GPU_LANES: " + std::to_string(lanes) + " lanes exceed the padded-lane limit");
+  const uint64_t cap_words = (uint64_t)d->wp.total_capture_words * lanes_pad;
   if (cap_words > kNoAllocScratchWords)
     return fail_with(RRTL_E_ARG, "E_NOALLOC_SIZE: " + std::to_string(d->wp.total_capture_words) + " capture words x " +
                                      std::to_string(lanes_pad) + " padded lanes exceed the fixed scratch of " +
                                      std::to_string(kNoAllocScratchWords) + " words");
   cudaError_t e = cudaSetDevice(d->ctx->device);
-  uint32_t* scratch = nullptr;
-  if (e == cudaSuccess) e = noalloc_scratch(d->ctx->device, &scratch);
-  if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: scratch lookup: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail_with(RRTL_E_DEVICE, std::string("E_DEVICE: ") + cudaGetErrorString(e));
+  // the kernel dereferences these: host memory or another device's memory is
+  // refused before anything is launched
+  if (!device_pointer_of(values, d->ctx->device))
+    return fail_with(RRTL_E_ARG, "E_ARG: values is not device memory of the design's device");
+  if (memories && !device_pointer_of(memories, d->ctx->device))
+    return fail_with(RRTL_E_ARG, "E_ARG: memories is not device memory of the design's device");
+  uint32_t* scratch = d->ctx->noalloc_scratch;
+  if (!scratch) return fail_with(RRTL_E_DEVICE, "E_DEVICE: the context has no scratch address");
   uint32_t* status = scratch + kNoAllocScratchWords;
   cudaStream_t st = d->ctx->stream;
   e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st);
@@ -306,7 +323,7 @@ extern "C" rrtl_status rrtl_word_tick_many_noalloc(rrtl_design* d, uint32_t* val
   WordRunDev R{};
   R.cycles = steps;
   R.lanes = lanes;
-  R.lanes_pad = lanes_pad;
+  R.lanes_pad = (uint32_t)lanes_pad;
   R.values = values;
   R.mems = memories;
   R.caps = scratch;

@@ -6,8 +6,8 @@ bench/sv/crc32.sv, 195 cells). The fixture keeps only what the netlist
 importer reads (port bit lists, cell types and connections), with cells
 renamed to their index in key order so the file stays small.
 
-Run inside the development container (the reference tree is mounted there):
-    python tests/golden/make_crc32_fixture.py /root/reference/bench/sv/crc32_gates.json
+Usage (the argument is the netlist inside a checkout of the reference):
+    python tests/golden/make_crc32_fixture.py <reference>/bench/sv/crc32_gates.json
 """
 import json
 import os
@@ -29,4 +29,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/bench/sv/crc32_gates.json")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_crc32_fixture.py <reference>/bench/sv/crc32_gates.json")
+    main(sys.argv[1])

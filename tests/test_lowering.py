@@ -156,3 +156,26 @@ def test_lut_class_list_is_the_permutation_representatives():
     hdr = open(os.path.join(os.path.dirname(__file__), "..", "rrtl_gb300", "csrc", "lut_classes.h")).read()
     listed = sorted(int(x) for x in re.findall(r"X\((\d+)\)", hdr.split("#define RRTL_LUT_CLASSES(X)")[1]))
     assert listed == canon and len(canon) == 80
+
+
+def test_levelization_of_a_200k_deep_wire_chain(oracle_lib):
+    """A comb chain 200,000 assignments deep levelizes without recursing that
+    deep on the host stack: level k holds wire k, and the chain's output is
+    the input plus the chain length (mod 2^16) after one settle."""
+    n = 200_000
+    d = Design()
+    m = d.module("Chain")
+    a = m.input("a", uint(16))
+    y = m.output("y", uint(16))
+    prev = a.value()
+    for i in range(n):
+        w = m.wire(f"w{i}", uint(16))
+        m.assign(w, (prev + lit_u(1, 16)).trunc(16))
+        prev = w.value()
+    m.assign(y, prev)
+    od = ob.OracleDesign(d.to_json(), "Chain")
+    assert od.num_levels == n + 1
+    ps = ob.PackedSim(od, 2)
+    ps.set_signal(od.signal("a"), np.array([[7, 65535]], dtype=np.uint32))
+    got = ps.get_signal(od.signal("y"))
+    assert list(got[0]) == [(7 + n) & 0xFFFF, (65535 + n) & 0xFFFF]

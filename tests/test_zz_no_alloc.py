@@ -40,9 +40,12 @@ def _from_device_layout(v, m, tsw, tmw, lanes):
     return values, memories
 
 
-def test_noalloc_tick_many_matches_batch_tick_many(engine):
+@pytest.mark.parametrize("seed,n_mems", [(1234, 2), (4321, 0)])
+def test_noalloc_tick_many_matches_batch_tick_many(engine, seed, n_mems):
+    """Two calls in a row (and a zero-step call between them) equal the
+    regular batch; the memory-free design passes memories=None."""
     torch = pytest.importorskip("torch")
-    d, meta = random_word_design(1234, n_wires=14, n_mems=2, depth=3)
+    d, meta = random_word_design(seed, n_wires=14, n_mems=n_mems, depth=3)
     js = d.to_json()
     lanes = 300
     g = sim.GpuBatchSimulator(js, meta["top"], lanes)
@@ -70,9 +73,10 @@ def test_noalloc_tick_many_matches_batch_tick_many(engine):
     dm = torch.from_numpy(hm.view(np.int32)).to(dev)
     torch.cuda.synchronize()
     fn = sim.lib().rrtl_word_tick_many_noalloc
-    for steps in (17, 5):  # two calls in a row, each compared with the regular path
+    mem_arg = ctypes.c_void_p(dm.data_ptr()) if tmw else None
+    for steps in (17, 0, 5):  # calls in a row, each compared with the regular path (0: no launch)
         g.tick_many(steps)
-        sim.check(fn(cd.h, ctypes.c_void_p(dv.data_ptr()), ctypes.c_void_p(dm.data_ptr()), lanes, steps))
+        sim.check(fn(cd.h, ctypes.c_void_p(dv.data_ptr()), mem_arg, lanes, steps))
         want_v, want_m = g.snapshot_storage()
         got_v, got_m = _from_device_layout(dv.cpu().numpy().view(np.uint32), dm.cpu().numpy().view(np.uint32),
                                            tsw, tmw, lanes)
@@ -89,3 +93,18 @@ def test_noalloc_rejects_requests_beyond_its_scratch(engine):
     rc = fn(g.design.h, dummy, dummy, 1 << 30, 1)
     assert rc == 1
     assert b"E_NOALLOC_SIZE" in sim.lib().rrtl_last_error()
+
+
+def test_noalloc_rejects_host_memory_before_launching(engine):
+    """Host buffers would be dereferenced by the kernel: they are refused on
+    the host, before any launch, with RRTL_E_ARG."""
+    d, meta = random_word_design(99, n_mems=1)
+    g = sim.GpuBatchSimulator(d.to_json(), meta["top"], 64)
+    info = g.design.info
+    host_v = np.zeros((info.total_signal_words, 128), dtype=np.uint32)
+    host_m = np.zeros((max(info.total_memory_words_per_lane, 1), 128), dtype=np.uint32)
+    fn = sim.lib().rrtl_word_tick_many_noalloc
+    rc = fn(g.design.h, host_v.ctypes.data_as(ctypes.c_void_p), host_m.ctypes.data_as(ctypes.c_void_p), 64, 3)
+    assert rc == 1
+    assert b"not device memory" in sim.lib().rrtl_last_error()
+    assert not host_v.any()  # nothing ran on it
