@@ -77,10 +77,32 @@ def throughput(ws: int, lanes_per_rank: int, cycles: int, steps: int, ms: float)
     return ws * lanes_per_rank * cycles * steps / (ms / 1000.0)
 
 
-def lane_shard(total_lanes: int, rank: int, ws: int):
+def lane_shard(total_lanes: int, rank: int, ws: int, align: int = 1):
     """Global lane range [first, last) of a rank: contiguous, disjoint shards
-    (the reference's shard plan, crates/rrtl-runtime/src/lib.rs:168-175)."""
-    return total_lanes * rank // ws, total_lanes * (rank + 1) // ws
+    (the reference's shard plan, crates/rrtl-runtime/src/lib.rs:168-175),
+    each starting on a multiple of `align` lanes (32: a whole 32-lane word,
+    the unit the engines key stimulus and hashes on)."""
+    units = (total_lanes + align - 1) // align
+
+    def edge(r):
+        return min(total_lanes, units * r // ws * align)
+
+    return edge(rank), edge(rank + 1)
+
+
+def sum_hashes(dist, h):
+    """Per-cycle hashes of every rank's lane shard added up (wrapping u64), on
+    every rank: the shards' hashes compose into the hash of the whole run.
+    Identity when single-process."""
+    h = np.asarray(h, dtype=np.uint64)
+    if not dist:
+        return h
+    parts = [None] * dist.get_world_size()
+    dist.all_gather_object(parts, h)
+    total = np.zeros_like(h)
+    for p in parts:
+        total += p
+    return total
 
 
 def net_stream_bytes_per_lane_cycle(meta_fanins, n_ff, n_pi, n_po):

@@ -161,10 +161,14 @@ rrtl_status rrtl_batch_synchronize(rrtl_batch* b);
  * a final tick would leave. */
 enum {
   RRTL_STIM_HOLD = 0,   /* keep the current value */
-  RRTL_STIM_RANDOM = 1, /* uniform bits from the counter hash (param = stream id) */
+  RRTL_STIM_RANDOM = 1, /* uniform bits from the counter hash (param = stream id), drawn per global lane */
   RRTL_STIM_PULSE = 2,  /* 1 for cycles < param, then 0 (a reset pulse) */
   RRTL_STIM_CONST = 3,  /* constant param on every lane */
-  RRTL_STIM_TRACE = 4   /* from input_trace column `param` */
+  RRTL_STIM_TRACE = 4,  /* from input_trace column `param` */
+  RRTL_STIM_RANDOM_UNIFORM = 5 /* uniform bits from the counter hash keyed on (seed, param, cycle) only: the
+                                  same value on every lane, namely the value RANDOM gives global lane 0. This
+                                  is fault simulation's stimulus: the golden lane and every faulted lane see
+                                  one input sequence (set_signal_all, crates/rrtl-sim-ir/examples/fault_sim.rs:66-76) */
 };
 
 typedef struct {
@@ -190,6 +194,12 @@ typedef struct {
   uint64_t* out_hash;          /* [cycle] per-cycle output hash */
   uint32_t* detect;            /* [lanes] first cycle a lane's recorded signals differ from lane 0 of its
                                   32-lane word; 0xFFFFFFFF if never (gate engine only) */
+  uint64_t lane_base;          /* global index of the batch's lane 0, a multiple of 32: RANDOM stimulus and the
+                                  hash terms are keyed on global lanes (words), so batches at lane_base 0, L,
+                                  2L, ... of one seed are shards of one run of their total lanes, and their
+                                  per-cycle hashes add up (wrapping) to that run's (the reference's shard plan,
+                                  RuntimeShardInfo::start_lane, crates/rrtl-runtime/src/lib.rs:168-175).
+                                  Traces, input traces and detect stay indexed by the batch's own lanes. */
 } rrtl_run;
 
 /* Runs on the device. Host pointers in `run` are copied in and out inside the

@@ -35,6 +35,7 @@ class Run(ctypes.Structure):
         ("out_trace", POINTER(c_uint32)),
         ("out_hash", POINTER(c_uint64)),
         ("detect", POINTER(c_uint32)),
+        ("lane_base", c_uint64),
     ]
 
 
@@ -192,7 +193,7 @@ class OracleDesign:
 
 
 def make_run(cycles, seed, stim, record, mode, input_trace=None, n_trace_cols=0, out_trace=None, out_hash=None,
-             detect=None):
+             detect=None, lane_base=0):
     """Build an rrtl_run structure; keeps the numpy buffers alive on the object."""
     st = (Stim * max(1, len(stim)))(*[Stim(s, k, p) for (s, k, p) in stim])
     rec = np.asarray(record, dtype=np.uint32)
@@ -209,6 +210,7 @@ def make_run(cycles, seed, stim, record, mode, input_trace=None, n_trace_cols=0,
     r.out_trace = _u32p(out_trace) if out_trace is not None else None
     r.out_hash = _u64p(out_hash) if out_hash is not None else None
     r.detect = _u32p(detect) if detect is not None else None
+    r.lane_base = lane_base
     r._keep = (st, rec, input_trace, out_trace, out_hash, detect)
     return r
 
@@ -421,7 +423,7 @@ class BitParallelAot:
     (tick_many_parallel, :513-523). Stimulus and output hash follow this
     library's run protocol, so its per-cycle hash equals the GPU engines'."""
 
-    def __init__(self, design: "OracleDesign", stim, record, cc: str = "gcc", opt: str = "-O3"):
+    def __init__(self, design: "OracleDesign", stim, record, cc: str = "gcc", opt: str = "-O3", native: bool = False):
         import hashlib
         import subprocess
 
@@ -435,7 +437,15 @@ class BitParallelAot:
         if lib().orc_bp_emit_c(design.h, st, len(stim), rp, len(rec), buf, need.value, ctypes.byref(need)):
             raise OracleError(lib().orc_last_error().decode())
         src = buf.value
-        tag = hashlib.sha1(src + opt.encode()).hexdigest()[:16]
+        flags = [opt]
+        if native:
+            # tuned for the host it runs on (the emitted C is built where it runs, like the reference's
+            # clang -O3 build of its AOT source)
+            import platform
+
+            flags.append("-mcpu=native" if platform.machine() in ("aarch64", "arm64") else "-march=native")
+        self.flags = flags
+        tag = hashlib.sha1(src + " ".join(flags).encode()).hexdigest()[:16]
         d = os.path.join(_HERE, "_build", "aot")
         os.makedirs(d, exist_ok=True)
         so = os.path.join(d, f"bp_{tag}.so")
@@ -449,8 +459,8 @@ class BitParallelAot:
                     f.write(part)
                 obj = cpath[:-2] + f".{os.getpid()}.o"
                 objs.append(obj)
-                procs.append(subprocess.Popen([cc, opt, "-fPIC", "-c", "-o", obj, cpath], stdout=subprocess.PIPE,
-                                              stderr=subprocess.PIPE))
+                procs.append(subprocess.Popen([cc] + flags + ["-fPIC", "-c", "-o", obj, cpath],
+                                              stdout=subprocess.PIPE, stderr=subprocess.PIPE))
             for p in procs:
                 _, err = p.communicate()
                 if p.returncode:
@@ -468,29 +478,41 @@ class BitParallelAot:
         self.lib.run_bp.restype = None
         self.ns = design.num_signals
 
-    def run(self, lanes: int, cycles: int, seed: int, threads: int = 0):
+    def run(self, lanes: int, cycles: int, seed: int, threads: int = 0, lane_base: int = 0, signals=None):
         """`cycles` cycles of `lanes` lanes (a multiple of 64) from the zero
-        state; returns the per-cycle hash summed over all lanes."""
+        state, global lanes [lane_base, lane_base + lanes) (lane_base a
+        multiple of 64); returns the per-cycle hash summed over all lanes, and
+        with `signals` (signal indices) also their final values as 32-lane
+        words [len(signals)][lanes / 32] (bit k of word w = lane 32w + k)."""
         from concurrent.futures import ThreadPoolExecutor
 
-        assert lanes % 64 == 0
+        assert lanes % 64 == 0 and lane_base % 64 == 0
         groups = lanes // 64
         threads = threads or (os.cpu_count() or 1)
         chunks = max(1, min(groups, threads * 4))
         bounds = [groups * i // chunks for i in range(chunks + 1)]
         hashes = [np.zeros(cycles, dtype=np.uint64) for _ in range(chunks)]
+        sig = None if signals is None else np.asarray(signals, dtype=np.int64)
+        final = None if sig is None else np.zeros((len(sig), groups), dtype=np.uint64)
 
         def work(i):
             g0, g1 = bounds[i], bounds[i + 1]
             if g1 == g0:
                 return
             st = np.zeros((g1 - g0) * self.ns, dtype=np.uint64)
-            self.lib.run_bp(st.ctypes.data_as(POINTER(ctypes.c_uint64)), g1 - g0, g0, 0, cycles, seed,
-                            hashes[i].ctypes.data_as(POINTER(ctypes.c_uint64)))
+            self.lib.run_bp(st.ctypes.data_as(POINTER(ctypes.c_uint64)), g1 - g0, lane_base // 64 + g0, 0, cycles,
+                            seed, hashes[i].ctypes.data_as(POINTER(ctypes.c_uint64)))
+            if final is not None:
+                final[:, g0:g1] = st.reshape(g1 - g0, self.ns)[:, sig].T
 
         with ThreadPoolExecutor(max_workers=threads) as ex:
             list(ex.map(work, range(chunks)))
         total = np.zeros(cycles, dtype=np.uint64)
         for h in hashes:
             total += h
-        return total
+        if final is None:
+            return total
+        words = np.zeros((len(sig), 2 * groups), dtype=np.uint32)
+        words[:, 0::2] = (final & 0xFFFFFFFF).astype(np.uint32)
+        words[:, 1::2] = (final >> 32).astype(np.uint32)
+        return total, words

@@ -55,8 +55,8 @@ uint32_t o_stim_word(uint64_t seed, uint64_t stream, uint64_t cycle, uint64_t id
   uint64_t k = o_smix(seed ^ (stream * 0xD6E8FEB86659FD93ull));
   return (uint32_t)o_smix(k ^ (cycle * 0xA0761D6478BD642Full) ^ (idx * 0xE7037ED1A0B428DBull));
 }
-uint32_t o_stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, uint32_t lane, uint32_t width, uint32_t limb) {
-  if (width == 1) return (o_stim_word(seed, stream, cycle, lane / 32) >> (lane % 32)) & 1u;
+uint32_t o_stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, uint64_t lane, uint32_t width, uint32_t limb) {
+  if (width == 1) return (o_stim_word(seed, stream, cycle, lane / 32) >> (uint32_t)(lane % 32)) & 1u;
   uint32_t v = o_stim_word(seed, stream ^ ((uint64_t)limb << 40), cycle, lane);
   uint32_t nl = (width + 31) / 32;
   if (limb + 1 == nl && width % 32) v &= (1u << (width % 32)) - 1u;
@@ -1033,7 +1033,8 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
       for (uint32_t lane = 0; lane < lanes; ++lane) {
         Limbs v(L.limbs, 0);
         for (uint32_t i = 0; i < L.limbs; ++i) {
-          if (st.kind == RRTL_STIM_RANDOM) v[i] = o_stim_lane_limb(r->seed, st.param, c, lane, L.width, i);
+          if (st.kind == RRTL_STIM_RANDOM) v[i] = o_stim_lane_limb(r->seed, st.param, c, r->lane_base + lane, L.width, i);
+          else if (st.kind == RRTL_STIM_RANDOM_UNIFORM) v[i] = o_stim_lane_limb(r->seed, st.param, c, 0, L.width, i);
           else if (st.kind == RRTL_STIM_PULSE) v[i] = (i == 0 && c < st.param) ? 1u : 0u;
           else if (st.kind == RRTL_STIM_CONST) v[i] = i < 2 ? (uint32_t)(st.param >> (32 * i)) : 0u;
           else if (st.kind == RRTL_STIM_TRACE) v[i] = r->input_trace[(c * r->n_trace_cols + st.param + i) * lanes + lane];
@@ -1050,7 +1051,7 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
         for (uint32_t w = 0; w < words; ++w) {
           uint32_t packed = 0;
           for (uint32_t b = 0; b < 32 && w * 32 + b < lanes; ++b) packed |= (s->values[s->vidx(L.offset, 0, w * 32 + b)] & 1u) << b;
-          if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, w, packed);
+          if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, r->lane_base / 32 + w, packed);
         }
       }
       {
@@ -1066,7 +1067,8 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
               for (uint32_t q2 = 0; q2 < r->n_record; ++q2) total += (size_t)P.signals[r->record[q2]].layout.limbs;
               r->out_trace[(c * total + base + i) * lanes + lane] = v;
             }
-            if ((r->record_mode & RRTL_REC_HASH) && L.width != 1) h += o_hash_term(c, q, (uint64_t)lane * L.limbs + i, v);
+            if ((r->record_mode & RRTL_REC_HASH) && L.width != 1)
+              h += o_hash_term(c, q, (r->lane_base + lane) * L.limbs + i, v);
           }
       }
     }
@@ -1143,7 +1145,8 @@ int orc_bp_run(void* sp, const rrtl_run* r) {
       if (st.kind == RRTL_STIM_HOLD) continue;
       for (uint32_t w = 0; w < words32; ++w) {
         uint32_t v = 0;
-        if (st.kind == RRTL_STIM_RANDOM) v = o_stim_word(r->seed, st.param, c, w);
+        if (st.kind == RRTL_STIM_RANDOM) v = o_stim_word(r->seed, st.param, c, r->lane_base / 32 + w);
+        else if (st.kind == RRTL_STIM_RANDOM_UNIFORM) v = (o_stim_word(r->seed, st.param, c, 0) & 1u) ? 0xFFFFFFFFu : 0u;
         else if (st.kind == RRTL_STIM_PULSE) v = c < st.param ? 0xFFFFFFFFu : 0u;
         else if (st.kind == RRTL_STIM_CONST) v = (st.param & 1) ? 0xFFFFFFFFu : 0u;
         else if (st.kind == RRTL_STIM_TRACE) v = r->input_trace[(c * r->n_trace_cols + st.param) * words32 + w];
@@ -1158,7 +1161,7 @@ int orc_bp_run(void* sp, const rrtl_run* r) {
       orc_bp_get_bits(s, r->record[q], col.data());
       for (uint32_t w = 0; w < words32; ++w) {
         if (r->record_mode & RRTL_REC_TRACE) r->out_trace[(c * r->n_record + q) * words32 + w] = col[w];
-        if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, w, col[w]);
+        if (r->record_mode & RRTL_REC_HASH) h += o_hash_term(c, q, r->lane_base / 32 + w, col[w]);
         if (r->record_mode & RRTL_REC_DETECT) diff[w] |= col[w] ^ ((col[w] & 1u) ? 0xFFFFFFFFu : 0u);
       }
     }
@@ -1175,7 +1178,7 @@ int orc_bp_run(void* sp, const rrtl_run* r) {
 
 // Lane-parallel CPU baseline: `threads` independent BitParallel engines over
 // disjoint 64-lane groups, each running the same protocol on its lanes. Only
-// RANDOM / PULSE / CONST stimuli (they are functions of the global lane).
+// RANDOM / RANDOM_UNIFORM / PULSE / CONST stimuli (functions of the global lane).
 // Returns the per-cycle hash (sum over all engines) in r->out_hash.
 int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t threads) {
   auto* d = (OracleDesign*)dp;
@@ -1191,7 +1194,7 @@ int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t th
       uint32_t my = (g1 - g0) * 64;
       if (!my) return;
       BitParallel bp(d, my);
-      uint32_t w32 = my / 32, wbase = g0 * 2;
+      const uint64_t w32 = my / 32, wbase = r->lane_base / 32 + (uint64_t)g0 * 2;
       std::vector<uint32_t> col(w32);
       for (uint64_t c = 0; c < r->cycles; ++c) {
         for (uint32_t k = 0; k < r->n_stim; ++k) {
@@ -1200,6 +1203,7 @@ int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t th
           for (uint32_t w = 0; w < w32; ++w) {
             uint32_t v = 0;
             if (st.kind == RRTL_STIM_RANDOM) v = o_stim_word(r->seed, st.param, c, wbase + w);
+            else if (st.kind == RRTL_STIM_RANDOM_UNIFORM) v = (o_stim_word(r->seed, st.param, c, 0) & 1u) ? 0xFFFFFFFFu : 0u;
             else if (st.kind == RRTL_STIM_PULSE) v = c < st.param ? 0xFFFFFFFFu : 0u;
             else if (st.kind == RRTL_STIM_CONST) v = (st.param & 1) ? 0xFFFFFFFFu : 0u;
             col[w] = v;
@@ -1237,7 +1241,7 @@ int orc_bp_run_parallel(void* dp, uint32_t lanes, const rrtl_run* r, uint32_t th
 // is cut into functions of about kAotChunk instructions (see AotEmitter),
 // which keeps the C compiler's time linear in the design size. To be comparable with the other engines it also runs this
 // library's run protocol per cycle: stimulus from the counter hash
-// (RANDOM / PULSE / CONST), settle, per-cycle output hash, capture/commit.
+// (RANDOM / RANDOM_UNIFORM / PULSE / CONST), settle, per-cycle output hash, capture/commit.
 // Entry: run_bp(st, groups, g_base, c0, cycles, seed, hash) with st the
 // [group][signal] state of `groups` groups starting at global group g_base.
 // The source comes as translation units separated by "//@@PART@@" lines.
@@ -1365,6 +1369,8 @@ int orc_bp_emit_c(void* dp, const rrtl_stim* stim, uint32_t n_stim, const uint32
       if (t.kind == RRTL_STIM_RANDOM)
         v = "((u64)sw(seed, " + std::to_string(t.param) + "ull, c, w0) | ((u64)sw(seed, " + std::to_string(t.param) +
             "ull, c, w0 + 1) << 32))";
+      else if (t.kind == RRTL_STIM_RANDOM_UNIFORM)
+        v = "((sw(seed, " + std::to_string(t.param) + "ull, c, 0) & 1u) ? ~0ull : 0ull)";
       else if (t.kind == RRTL_STIM_PULSE) v = "((u64)c < " + std::to_string(t.param) + "ull ? ~0ull : 0ull)";
       else if (t.kind == RRTL_STIM_CONST) v = (t.param & 1) ? "~0ull" : "0ull";
       else continue;

@@ -32,7 +32,8 @@ __device__ __forceinline__ uint32_t valid_mask(uint32_t gw, uint32_t lanes) {
 __device__ __forceinline__ uint32_t stim_value(const GateStimDev& s, const GateRunDev& R, uint64_t c, uint32_t gw,
                                                uint32_t cur) {
   switch (s.kind) {
-    case RRTL_STIM_RANDOM: return stim_word(R.seed, s.param, c, gw);
+    case RRTL_STIM_RANDOM: return stim_word(R.seed, s.param, c, R.word_base + gw);
+    case RRTL_STIM_RANDOM_UNIFORM: return stim_uniform_word(R.seed, s.param, c);
     case RRTL_STIM_PULSE: return c < s.param ? 0xFFFFFFFFu : 0u;
     case RRTL_STIM_CONST: return (s.param & 1u) ? 0xFFFFFFFFu : 0u;
     case RRTL_STIM_TRACE:

@@ -101,6 +101,7 @@ struct GateRunDev {
   uint32_t* nets;             // [rows][words_pad]
   uint32_t* err;              // device status word
   unsigned long long cycle_base;  // absolute cycle of the launch's first cycle (stimulus, records)
+  unsigned long long word_base;   // global 32-lane word of the batch's word 0 (RANDOM stimulus, hash terms)
   // trace checks (RRTL_REC_CHECK): per cycle and recorded net, the check index
   // (~0: none) and the expected words; mismatches go to an atomic log
   const uint32_t* chk_idx;    // [cycle][rec]

@@ -101,7 +101,7 @@ std::string gate_jit_source(const GateProgram& gp, const GateRunTables& run) {
              ", " + u(k % 32) + ");\n";
       o += "      { const uint32_t v = " + n(run.rec[k].net) + " & vm; if (w < R.words) {";
       if (trace) o += " R.out_trace[((size_t)c * " + u(run.rec.size()) + " + " + kk + ") * R.words + w] = v;";
-      if (hash) o += " h += hash_term_salted(sk" + kk + ", w, v);";
+      if (hash) o += " h += hash_term_salted(sk" + kk + ", R.word_base + w, v);";
       if (detect) o += " diff |= v ^ (0u - (v & 1u));";
       if (check) o += " check_word(R, c, " + kk + ", w, v);";
       o += " } }\n";

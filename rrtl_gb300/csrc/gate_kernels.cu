@@ -473,7 +473,7 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
         uint32_t v = S[R.rec[k].slot * W + ww] & valid_mask(gw, R.lanes);
         if (gw < R.words) {
           if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
-          if (R.mode & RRTL_REC_HASH) hs += hash_term(c, k, gw, v);
+          if (R.mode & RRTL_REC_HASH) hs += hash_term(c, k, R.word_base + gw, v);
           if (R.mode & RRTL_REC_DETECT) atomicOr(&dstate[ww], v ^ (0u - (v & 1u)));
           if (R.mode & RRTL_REC_CHECK) check_word(R, c, k, gw, v);
         }
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(kPlainThreads) gate_plain_kernel(GateProgDev P
       uint32_t v = G[(size_t)R.rec[k].net * wp + gw] & valid_mask(gw, R.lanes);
       if (gw < R.words) {
         if (R.mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.n_rec + k) * R.words + gw] = v;
-        if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, gw, v);
+        if (R.mode & RRTL_REC_HASH) h += hash_term(c, k, R.word_base + gw, v);
         if (R.mode & RRTL_REC_DETECT) atomicOr(&diff[ww], v ^ (0u - (v & 1u)));
         if (R.mode & RRTL_REC_CHECK) check_word(R, c, k, gw, v);
       }

@@ -412,7 +412,7 @@ GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
     signal_of(d, s.signal);
     uint32_t net = gp.signal_net[s.signal];
     REQUIRE(gp.net_is_source[net], RRTL_E_ARG, "E_GPU_STIM: stimulus targets a combinationally driven signal");
-    REQUIRE(s.kind <= RRTL_STIM_TRACE, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
+    REQUIRE(s.kind <= RRTL_STIM_RANDOM_UNIFORM, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
     if (s.kind == RRTL_STIM_TRACE)
       REQUIRE(s.param < run.n_trace_cols && run.input_trace, RRTL_E_ARG, "E_GPU_STIM: trace column out of range");
     stim.push_back(GateStimDev{0u, net, s.kind, 0, s.param});
@@ -459,6 +459,9 @@ GatePrepared gate_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   R.nets = b->d_nets.as<uint32_t>();
   R.err = b->d_err.as<uint32_t>();
   R.cycle_base = 0;
+  REQUIRE(run.lane_base % 32 == 0 && run.lane_base < (1ull << 40), RRTL_E_ARG,
+          "E_GPU_LANE_BASE: lane_base must be a multiple of 32 below 2^40");
+  R.word_base = run.lane_base / 32;
   REQUIRE(!(run.record_mode & RRTL_REC_CHECK) || chk, RRTL_E_ARG, "E_GPU_RECORD: checks are for trace replay");
   if (chk) {
     R.chk_idx = chk->idx;
@@ -628,7 +631,7 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   for (uint32_t i = 0; i < run.n_stim; ++i) {
     const rrtl_stim& s = run.stim[i];
     const PackedSignal& ps = signal_of(d, s.signal);
-    REQUIRE(s.kind <= RRTL_STIM_TRACE, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
+    REQUIRE(s.kind <= RRTL_STIM_RANDOM_UNIFORM, RRTL_E_ARG, "E_GPU_STIM: unknown stimulus kind");
     if (s.kind == RRTL_STIM_TRACE)
       REQUIRE(s.param < run.n_trace_cols && run.input_trace, RRTL_E_ARG, "E_GPU_STIM: trace column out of range");
     stim.push_back(WordStimDev{ps.layout.offset, ps.layout.limbs, ps.layout.width, s.kind, s.param});
@@ -666,6 +669,9 @@ WordPrepared word_prepare(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, 
   R.start_settle = start_settle;
   R.err = b->d_err.as<uint32_t>();
   R.vspill = nullptr;
+  REQUIRE(run.lane_base % 32 == 0 && run.lane_base < (1ull << 40), RRTL_E_ARG,
+          "E_GPU_LANE_BASE: lane_base must be a multiple of 32 below 2^40");
+  R.lane_base = run.lane_base;
   REQUIRE(!(run.record_mode & RRTL_REC_CHECK) || chk, RRTL_E_ARG, "E_GPU_RECORD: checks are for trace replay");
   if (chk) {
     R.chk_idx = chk->idx;

@@ -30,16 +30,23 @@ RRTL_HD uint32_t stim_word(uint64_t seed, uint64_t stream, uint64_t cycle, uint6
   return (uint32_t)smix64(k ^ (cycle * 0xA0761D6478BD642Full) ^ (idx * 0xE7037ED1A0B428DBull));
 }
 
-// Value of limb `limb` of a RANDOM input of `width` bits on `lane`:
-// 1-bit inputs take bit (lane % 32) of the word for lane/32, so a bit-sliced
-// engine draws one word per 32 lanes; wider inputs draw one word per limb.
-RRTL_HD uint32_t stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, uint32_t lane, uint32_t width,
+// Value of limb `limb` of a RANDOM input of `width` bits on global lane
+// `lane`: 1-bit inputs take bit (lane % 32) of the word for lane/32, so a
+// bit-sliced engine draws one word per 32 lanes; wider inputs draw one word
+// per limb. RANDOM_UNIFORM gives every lane the value of global lane 0.
+RRTL_HD uint32_t stim_lane_limb(uint64_t seed, uint64_t stream, uint64_t cycle, uint64_t lane, uint32_t width,
                                 uint32_t limb) {
-  if (width == 1) return (stim_word(seed, stream, cycle, lane >> 5) >> (lane & 31)) & 1u;
+  if (width == 1) return (stim_word(seed, stream, cycle, lane >> 5) >> (uint32_t)(lane & 31u)) & 1u;
   uint32_t v = stim_word(seed, stream ^ ((uint64_t)limb << 40), cycle, lane);
   uint32_t nl = (width + 31) / 32;
   if (limb + 1 == nl && (width & 31)) v &= (1u << (width & 31)) - 1u;
   return v;
+}
+
+// The 32-lane word of a 1-bit RANDOM_UNIFORM input: every lane takes the bit
+// global lane 0 would take under RANDOM.
+RRTL_HD uint32_t stim_uniform_word(uint64_t seed, uint64_t stream, uint64_t cycle) {
+  return (stim_word(seed, stream, cycle, 0) & 1u) ? 0xFFFFFFFFu : 0u;
 }
 
 // One term of the per-cycle output hash. `idx` is the 32-lane word index for

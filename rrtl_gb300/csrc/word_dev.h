@@ -87,6 +87,7 @@ struct WordRunDev {
   uint32_t start_settle;      // settle before the first cycle (eval)
   unsigned long long cycle_base;  // absolute index of this launch's first cycle (stimulus, hash, detect);
                                   // buffers are indexed from the launch's first cycle
+  unsigned long long lane_base;   // global lane of the batch's lane 0 (RANDOM stimulus, hash terms)
   uint32_t* err;
   // trace checks (RRTL_REC_CHECK), per cycle and recorded limb row
   const uint32_t* chk_idx;    // [cycle][rec limb rows], ~0 = no check

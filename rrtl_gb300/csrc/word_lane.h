@@ -55,7 +55,8 @@ __device__ __forceinline__ void word_stimulus(const WordRunDev& R, uint32_t lane
     if (s.kind == RRTL_STIM_HOLD) continue;
     for (uint32_t l = 0; l < s.limbs; ++l) {
       uint32_t v = 0;
-      if (s.kind == RRTL_STIM_RANDOM) v = stim_lane_limb(R.seed, s.param, ca, lane, s.width, l);
+      if (s.kind == RRTL_STIM_RANDOM) v = stim_lane_limb(R.seed, s.param, ca, R.lane_base + lane, s.width, l);
+      else if (s.kind == RRTL_STIM_RANDOM_UNIFORM) v = stim_lane_limb(R.seed, s.param, ca, 0ull, s.width, l);
       else if (s.kind == RRTL_STIM_PULSE) v = (l == 0 && ca < s.param) ? 1u : 0u;
       else if (s.kind == RRTL_STIM_CONST) v = l < 2 ? (uint32_t)(s.param >> (32 * l)) : 0u;
       else if (s.kind == RRTL_STIM_TRACE)
@@ -91,7 +92,7 @@ __device__ __forceinline__ void word_record(const WordRunDev& R, uint32_t lane, 
       if ((mode & RRTL_REC_HASH) && rc.width == 1) {
         // 1-bit signals hash as 32-lane packed words, the gate engine's unit
         const uint32_t packed = __ballot_sync(0xFFFFFFFFu, live && (v & 1u));
-        if ((threadIdx.x & 31u) == 0 && live) h += hash_term_salted(salt, lane >> 5, packed);
+        if ((threadIdx.x & 31u) == 0 && live) h += hash_term_salted(salt, (R.lane_base + lane) >> 5, packed);
       }
       if (!live) continue;
       if (mode & RRTL_REC_TRACE) R.out_trace[((size_t)c * R.rec_limbs + rc.base + l) * R.lanes + lane] = v;
@@ -103,7 +104,8 @@ __device__ __forceinline__ void word_record(const WordRunDev& R, uint32_t lane, 
           if (exp != v) log_mismatch(R.chk_log, R.chk_cap, ca, idx, lane, l, exp, v);
         }
       }
-      if ((mode & RRTL_REC_HASH) && rc.width != 1) h += hash_term_salted(salt, (uint64_t)lane * rc.limbs + l, v);
+      if ((mode & RRTL_REC_HASH) && rc.width != 1)
+        h += hash_term_salted(salt, (R.lane_base + lane) * rc.limbs + l, v);
     }
   }
   if (mode & RRTL_REC_HASH) {

@@ -21,7 +21,7 @@ from . import builder as _b
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "librrtl_gb300.so")
 
-STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE = 0, 1, 2, 3, 4
+STIM_HOLD, STIM_RANDOM, STIM_PULSE, STIM_CONST, STIM_TRACE, STIM_RANDOM_UNIFORM = 0, 1, 2, 3, 4, 5
 REC_TRACE, REC_HASH, REC_DETECT, REC_CHECK = 1, 2, 4, 8
 PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH, PATH_WORD_INTERP = 0, 1, 2, 3
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
@@ -66,6 +66,7 @@ class Run(ctypes.Structure):
         ("out_trace", POINTER(c_uint32)),
         ("out_hash", POINTER(c_uint64)),
         ("detect", POINTER(c_uint32)),
+        ("lane_base", c_uint64),
     ]
 
 
@@ -294,10 +295,12 @@ class Context:
 
     # -- device job queue (rrtl_queue_*)
     def submit(self, batch: "GpuBatchSimulator", cycles: int, seed: int = 0, stim: Iterable = (),
-               record: Iterable = (), mode: int = 0, input_trace: Optional[np.ndarray] = None) -> "QueuedJob":
+               record: Iterable = (), mode: int = 0, input_trace: Optional[np.ndarray] = None,
+               lane_base: int = 0) -> "QueuedJob":
         """Queue a run on `batch`; its outputs fill the returned job's arrays once it finishes."""
         out = batch.alloc_outputs(cycles, list(record), mode)
-        r = batch.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
+        r = batch.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"],
+                           lane_base)
         j = Job()
         j.batch = batch.h
         j.run = r
@@ -595,7 +598,8 @@ class GpuBatchSimulator:
 
     # -- per-cycle runs
     def make_run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
-                 input_trace: Optional[np.ndarray] = None, out_trace=None, out_hash=None, detect=None) -> Run:
+                 input_trace: Optional[np.ndarray] = None, out_trace=None, out_hash=None, detect=None,
+                 lane_base: int = 0) -> Run:
         st = [(self._sig(s), k, p) for (s, k, p) in stim]
         arr = (Stim * max(1, len(st)))(*[Stim(a, b, c) for a, b, c in st])
         rec = np.asarray([self._sig(r) for r in record], dtype=np.uint32)
@@ -614,6 +618,7 @@ class GpuBatchSimulator:
         r.out_trace = _u32p(out_trace) if out_trace is not None else None
         r.out_hash = out_hash.ctypes.data_as(POINTER(c_uint64)) if out_hash is not None else None
         r.detect = _u32p(detect) if detect is not None else None
+        r.lane_base = lane_base
         r._keep = (arr, rec, input_trace, out_trace, out_hash, detect)
         return r
 
@@ -635,11 +640,14 @@ class GpuBatchSimulator:
         return {"trace": out_trace, "hash": out_hash, "detect": detect}
 
     def run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
-            input_trace: Optional[np.ndarray] = None):
-        """Run `cycles` cycles; returns dict(trace=..., hash=..., detect=...) for the requested records."""
+            input_trace: Optional[np.ndarray] = None, lane_base: int = 0):
+        """Run `cycles` cycles; returns dict(trace=..., hash=..., detect=...) for the requested records.
+        lane_base: global index of this batch's lane 0 (a multiple of 32) when the batch is one shard of a
+        larger run (random stimulus and hash terms follow global lanes)."""
         record = list(record)
         out = self.alloc_outputs(cycles, record, mode)
-        r = self.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"])
+        r = self.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"], out["detect"],
+                          lane_base)
         check(lib().rrtl_batch_run(self.h, byref(r)))
         return out
 

@@ -175,14 +175,20 @@ def gate_netlist(n_gates: int = 50_000, n_ff: int = 2048, n_pi: int = 64, n_po: 
     return d, meta
 
 
-def netlist_run_spec(meta: NetlistMeta, reset_cycles: int = 1):
+def netlist_run_spec(meta: NetlistMeta, reset_cycles: int = 1, uniform: bool = False):
     """Stimulus for a netlist run: rst pulses for `reset_cycles`, every
     primary input takes fresh uniform bits each cycle (stream = input index),
-    clk is held at 1. Returns (stim, record) in name form."""
-    from .sim import STIM_CONST, STIM_PULSE, STIM_RANDOM
+    clk is held at 1. Returns (stim, record) in name form.
 
+    uniform: every lane sees the same input sequence (RANDOM_UNIFORM), the
+    fault-simulation protocol of the reference (set_signal_all before each
+    tick, crates/rrtl-sim-ir/examples/fault_sim.rs:66-76): lanes then differ
+    only through their injected faults."""
+    from .sim import STIM_CONST, STIM_PULSE, STIM_RANDOM, STIM_RANDOM_UNIFORM
+
+    kind = STIM_RANDOM_UNIFORM if uniform else STIM_RANDOM
     stim = [(meta.clk, STIM_CONST, 1), (meta.rst, STIM_PULSE, reset_cycles)]
-    stim += [(p, STIM_RANDOM, i) for i, p in enumerate(meta.inputs)]
+    stim += [(p, kind, i) for i, p in enumerate(meta.inputs)]
     return stim, list(meta.outputs)
 
 
@@ -414,7 +420,10 @@ def job_stream(n_jobs: int, n_designs: int, lanes_lo: int = 32, lanes_hi: int = 
 
 def job_faults(meta: NetlistMeta, lanes: int, seed: int):
     """One stuck-at fault per lane at a seeded random net (wires, flops,
-    outputs); lane 0 of every 32-lane word stays fault-free as the reference."""
+    outputs); lane 0 of every 32-lane word stays fault-free as the reference.
+    Run fault jobs with lane-uniform stimulus (netlist_run_spec(uniform=True)):
+    every fault-free lane then equals the reference's golden lane 0, so the
+    per-word comparison is the reference's comparison with lane 0."""
     rng = Rng(seed ^ 0xFA17)
     sites = meta.gate_names + meta.regs + meta.outputs
     return [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]

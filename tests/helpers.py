@@ -24,7 +24,7 @@ def crc32_netlist_json():
     return import_yosys_netlist(y, c["top"])
 
 
-def oracle_bp_run(od, lanes, cycles, seed, stim, record, mode, faults=(), input_trace=None):
+def oracle_bp_run(od, lanes, cycles, seed, stim, record, mode, faults=(), input_trace=None, lane_base=0):
     """Run the bit-parallel oracle; stim/record use packed indices."""
     bp = ob.BitParallel(od, lanes)
     for lane, sig, v in faults:
@@ -37,7 +37,7 @@ def oracle_bp_run(od, lanes, cycles, seed, stim, record, mode, faults=(), input_
     if input_trace is not None:
         input_trace = np.ascontiguousarray(input_trace, dtype=np.uint32)
         cols = input_trace.shape[1]
-    r = ob.make_run(cycles, seed, stim, record, mode, input_trace, cols, out_trace, out_hash, detect)
+    r = ob.make_run(cycles, seed, stim, record, mode, input_trace, cols, out_trace, out_hash, detect, lane_base)
     bp.run(r)
     return {"trace": out_trace, "hash": out_hash, "detect": detect, "sim": bp}
 

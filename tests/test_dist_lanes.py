@@ -76,3 +76,49 @@ def test_a_failed_rank_is_detected_at_the_next_collective():
         p.join(timeout=60)
     assert procs[1].exitcode == 3
     assert kind != "no error" and secs < 60
+
+
+def _shard_rank(rank, ws, port, out):
+    """Rank r simulates global lanes lane_shard(total, r, ws) of one run on the
+    oracle (lane_base = its first lane); rank 0 sums the ranks' per-cycle
+    hashes, the host-side gather the multi-GPU bench does."""
+    import numpy as np
+
+    from oracle import binding as ob
+    from rrtl_gb300.workloads import gate_netlist, netlist_run_spec
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        d, meta = gate_netlist(n_gates=800, n_ff=40, n_pi=10, n_po=10, depth=8, seed=71)
+        od = ob.OracleDesign(d.to_json(), meta.top)
+        stim, rec = netlist_run_spec(meta)
+        si = [(od.signal(n), k, p) for n, k, p in stim]
+        ri = [od.signal(r) for r in rec]
+        total, cycles = 384, 12
+        first, last = bench.lane_shard(total, rank, ws, align=32)
+        h = np.zeros(cycles, dtype=np.uint64)
+        ob.BitParallel(od, last - first).run(ob.make_run(cycles, 3, si, ri, 2, out_hash=h, lane_base=first))
+        got = bench.sum_hashes(dist, h)
+        if rank == 0:
+            full = np.zeros(cycles, dtype=np.uint64)
+            ob.BitParallel(od, total).run(ob.make_run(cycles, 3, si, ri, 2, out_hash=full))
+            out.put((first, last, bool(np.array_equal(got, full)), bool(full.any())))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_rank_shards_compose_into_one_run(oracle_lib):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 33500 + os.getpid() % 2000
+    procs = [ctx.Process(target=_shard_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    first, last, equal, nonzero = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert (first, last) == (0, 192)
+    assert equal and nonzero

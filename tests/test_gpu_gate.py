@@ -180,7 +180,7 @@ def test_netlist_faults_tile_widths_match_oracle(small_netlist, words):
     rng = Rng(91 + words)
     sites = meta.gate_names + meta.regs + meta.outputs
     faults = [(l, sites[rng.below(len(sites))], rng.below(2)) for l in range(lanes) if l % 32]
-    stim, rec = netlist_run_spec(meta)
+    stim, rec = netlist_run_spec(meta, uniform=True)  # one input sequence for every lane (fault simulation)
     g = sim.GpuBatchSimulator(cd, lanes=lanes)
     g.set_tile_words(words)
     g.set_faults(faults)
@@ -189,6 +189,8 @@ def test_netlist_faults_tile_widths_match_oracle(small_netlist, words):
                         [od.signal(r) for r in rec], 6, faults=[(l, od.signal(s), v) for l, s, v in faults])
     assert np.array_equal(res["hash"], ref["hash"])
     assert np.array_equal(res["detect"], ref["detect"])
+    n_det = int((res["detect"] != 0xFFFFFFFF).sum())
+    assert 0 < n_det < len(faults)  # detected faults and latent ones, not stimulus noise
 
 
 def test_auto_tile_width_is_a_valid_width(small_netlist):

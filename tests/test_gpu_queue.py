@@ -58,7 +58,7 @@ def test_queue_jobs_match_runs_alone(designs):
     queued = []
     for spec in specs:
         meta = designs[spec["design"]][0]
-        stim, rec = netlist_run_spec(meta)
+        stim, rec = netlist_run_spec(meta, uniform=spec["faults"])
         g = _make_batch(designs, spec)
         job = ctx.submit(g, spec["cycles"], seed=spec["seed"], stim=stim, record=rec, mode=_mode(spec))
         assert job.status == sim.JOB_QUEUED
@@ -69,7 +69,7 @@ def test_queue_jobs_match_runs_alone(designs):
     for spec, g, job in queued:
         assert job.status == sim.JOB_DONE
         meta = designs[spec["design"]][0]
-        stim, rec = netlist_run_spec(meta)
+        stim, rec = netlist_run_spec(meta, uniform=spec["faults"])
         alone = _make_batch(designs, spec)
         ref = alone.run(spec["cycles"], seed=spec["seed"], stim=stim, record=rec, mode=_mode(spec))
         for k in ("trace", "hash", "detect"):
@@ -96,6 +96,31 @@ def test_queue_job_matches_oracle(designs):
                             [od.signal(r) for r in rec], 3)
         assert np.array_equal(job.outputs["trace"], ref["trace"])
         assert np.array_equal(job.outputs["hash"], ref["hash"])
+
+
+def test_queue_fault_job_detection_matches_oracle(designs):
+    """A fault-simulation job (one stuck-at fault per lane, lane-uniform
+    stimulus, lane 0 of each word fault-free) on the persistent queue: its
+    detection vector equals the bit-parallel oracle's with the same forces."""
+    from rrtl_gb300.workloads import job_faults
+
+    meta, cd, js = designs[1]
+    od = ob.OracleDesign(js, meta.top)
+    stim, rec = netlist_run_spec(meta, uniform=True)
+    lanes, cycles, seed = 600, 40, 12
+    faults = job_faults(meta, lanes, seed)
+    ctx = sim.default_context()
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    g.set_faults(faults)
+    job = ctx.submit(g, cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH | sim.REC_DETECT)
+    ctx.launch()
+    ctx.wait()
+    ref = oracle_bp_run(od, lanes, cycles, seed, [(od.signal(n), k, p) for n, k, p in stim],
+                        [od.signal(r) for r in rec], 6, faults=[(l, od.signal(s), v) for l, s, v in faults])
+    assert np.array_equal(job.outputs["detect"], ref["detect"])
+    assert np.array_equal(job.outputs["hash"], ref["hash"])
+    n_det = int((ref["detect"] != 0xFFFFFFFF).sum())
+    assert 0 < n_det < len(faults)
 
 
 def test_queue_status_and_errors(designs):
