@@ -74,6 +74,8 @@ def lib():
         L.orc_hash_term.restype = c_uint64
         L.orc_packed_new.argtypes = [c_void_p, c_uint32]
         L.orc_packed_new.restype = c_void_p
+        L.orc_simd_new.argtypes = [c_void_p, c_uint32]
+        L.orc_simd_new.restype = c_void_p
         L.orc_bs_new.argtypes = [c_void_p, c_uint32]
         L.orc_bs_new.restype = c_void_p
         L.orc_bs_free.argtypes = [c_void_p]
@@ -273,6 +275,68 @@ class PackedSim:
         rc = lib().orc_packed_run(self.h, ctypes.byref(run))
         if rc:
             raise OracleError(lib().orc_last_error().decode())
+
+
+class SimdSim(PackedSim):
+    """Restated `SimdCpuSimulator` (crates/rrtl-sim-ir/src/lib.rs:5375-7457):
+    PackedSim's cycle evaluated instruction by instruction across all lanes
+    on u64 lanes (designs whose values are at most 64 bits). Same storage and
+    entry points as PackedSim."""
+
+    def __init__(self, design: OracleDesign, lanes: int):
+        self.d = design
+        self.lanes = lanes
+        self.h = lib().orc_simd_new(design.h, lanes)
+        if not self.h:
+            raise OracleError(lib().orc_last_error().decode())
+
+
+def simd_run_parallel(design: OracleDesign, lanes: int, cycles: int, seed: int, stim, record, mode: int = 2,
+                      memories=None, threads: int = 0, snapshot: bool = False):
+    """The SIMD engine over `lanes` lanes split into disjoint lane ranges, one
+    engine per host thread (lanes never interact; the reference's parallel
+    CPU engines split the same way). Each range runs with lane_base = its
+    first lane, so per-cycle hashes add up to the whole batch's.
+    memories: {memory index: [addr][limb][lanes] array}. Returns the per-cycle
+    hash (mode & 2), and with `snapshot` the final PackedSimulatorStorage
+    (values [word][lanes], memories [lanes][word] flattened)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    threads = threads or (os.cpu_count() or 1)
+    chunks = max(1, min(threads, (lanes + 31) // 32))
+    unit = ((lanes + 31) // 32 + chunks - 1) // chunks * 32  # lane ranges start on 32-lane words
+    bounds = [min(lanes, i * unit) for i in range(chunks + 1)]
+    bounds[-1] = lanes
+    hashes = [np.zeros(max(cycles, 1), dtype=np.uint64) for _ in range(chunks)]
+    tsw, tmw = design.total_signal_words, design.total_memory_words
+    vals = np.zeros((tsw, lanes), dtype=np.uint32) if snapshot else None
+    mems = np.zeros((lanes, tmw), dtype=np.uint32) if snapshot else None
+
+    def work(i):
+        a, b = bounds[i], bounds[i + 1]
+        if b <= a:
+            return
+        s = SimdSim(design, b - a)
+        for mi, data in (memories or {}).items():
+            s.set_memory(mi, np.ascontiguousarray(np.asarray(data)[:, :, a:b]), settle=False)
+        s.eval()
+        r = make_run(cycles, seed, stim, record, mode, out_hash=hashes[i] if mode & 2 else None, lane_base=a)
+        s.run(r)
+        if snapshot:
+            v, m = s.snapshot()
+            vals[:, a:b] = v.reshape(tsw, b - a)
+            if tmw:
+                mems[a:b, :] = m.reshape(b - a, tmw)
+
+    with ThreadPoolExecutor(max_workers=chunks) as ex:
+        list(ex.map(work, range(chunks)))
+    total = np.zeros(max(cycles, 1), dtype=np.uint64)
+    for h in hashes:
+        total += h
+    total = total[:cycles]
+    if snapshot:
+        return total, vals.reshape(-1), mems.reshape(-1)
+    return total
 
 
 class BitSlice:

@@ -26,6 +26,7 @@
 #include <functional>
 #include <cstring>
 #include <map>
+#include <stdexcept>
 #include <memory>
 #include <string>
 #include <thread>
@@ -213,8 +214,9 @@ struct PackedSim {
   PackedSim(const OracleDesign* od, uint32_t n) : d(od), P(&od->packed), M(&od->machine), lanes(n) {
     values.assign(P->total_signal_words * lanes, 0);
     memories.assign(P->total_memory_words_per_lane * lanes, 0);
-    eval_combinational();  // PackedSimulator::new settles once (lib.rs:3058)
+    PackedSim::eval_combinational();  // PackedSimulator::new settles once (lib.rs:3058)
   }
+  virtual ~PackedSim() = default;
 
   size_t vidx(uint32_t off, uint32_t limb, uint32_t lane) const { return ((size_t)off + limb) * lanes + lane; }
   size_t midx(const PackedMemory& m, uint32_t lane, uint64_t addr, uint32_t limb) const {
@@ -329,7 +331,7 @@ struct PackedSim {
     }
   }
 
-  void eval_combinational() {  // lib.rs:9278-9281: comb, then async-reset comb
+  virtual void eval_combinational() {  // lib.rs:9278-9281: comb, then async-reset comb
     execute_block(M->comb);
     execute_block(M->async_reset_comb);
   }
@@ -363,7 +365,7 @@ struct PackedSim {
         std::copy(c.vals.begin() + (size_t)i * lanes, c.vals.begin() + (size_t)(i + 1) * lanes, values.begin() + vidx(L.offset, i, 0));
     }
   }
-  void tick_from_evaluated_no_post_eval() {  // lib.rs:9289-9293
+  virtual void tick_from_evaluated_no_post_eval() {  // lib.rs:9289-9293
     capture_registers();
     execute_block(M->tick_commit);
     commit_registers();
@@ -373,6 +375,230 @@ struct PackedSim {
     if (!n) return;
     eval_combinational();
     for (uint64_t i = 0; i < n; ++i) { tick_from_evaluated_no_post_eval(); eval_combinational(); }
+  }
+};
+
+// ---------------------------------------------------------------- SimdSim --
+// SimdCpuSimulator restated (crates/rrtl-sim-ir/src/lib.rs:5375-7457, its
+// tick_many at :5784): the packed simulator's cycle, evaluated instruction by
+// instruction across every lane of the batch (eval_simd_instr_into, :6109),
+// with the reference's one- and two-limb fast paths as one u64 per lane: it
+// takes designs whose values, signals and memory words are all at most 64
+// bits wide. Storage, streams and effects are PackedSim's, so every
+// PackedSim entry point (signals, memories, snapshots, the run protocol)
+// works on it unchanged. The lane loops are plain arrays the host compiler
+// vectorises; a caller runs disjoint lane ranges on several threads (lanes
+// never interact), as the reference's parallel engines do.
+struct SimdSim : PackedSim {
+  std::vector<uint64_t> wv;    // [value][lane] of the current block
+  std::vector<uint64_t> caps;  // [capture][lane]
+  std::vector<uint32_t> cap_sig;
+
+  static uint64_t m64(uint32_t w) { return w >= 64 ? ~0ull : ((1ull << w) - 1ull); }
+  static uint64_t lit64(const std::vector<uint32_t>& l) {
+    return (l.empty() ? 0ull : l[0]) | (l.size() > 1 ? (uint64_t)l[1] << 32 : 0ull);
+  }
+  static void check_block(const Block& b) {
+    for (uint32_t w : b.value_width)
+      if (w > 64) throw std::runtime_error("E_UNSUPPORTED: the SIMD engine takes values of at most 64 bits");
+  }
+
+  SimdSim(const OracleDesign* od, uint32_t n) : PackedSim(od, n) {
+    for (const PackedSignal& sg : P->signals)
+      if (sg.layout.width > 64) throw std::runtime_error("E_UNSUPPORTED: the SIMD engine takes signals of at most 64 bits");
+    for (const PackedMemory& m : P->memories)
+      if (m.data_layout.width > 64) throw std::runtime_error("E_UNSUPPORTED: the SIMD engine takes memory words of at most 64 bits");
+    check_block(M->comb);
+    check_block(M->async_reset_comb);
+    check_block(M->tick_next);
+    check_block(M->tick_commit);
+  }
+
+  uint64_t* V(uint32_t v) { return wv.data() + (size_t)v * lanes; }
+  void load_signal(const ValueLayout& L, uint64_t m, uint64_t* o) const {
+    const uint32_t* lo = values.data() + (size_t)L.offset * lanes;
+    if (L.limbs == 1) {
+      for (uint32_t l = 0; l < lanes; ++l) o[l] = lo[l] & m;
+    } else {
+      const uint32_t* hi = lo + lanes;
+      for (uint32_t l = 0; l < lanes; ++l) o[l] = ((uint64_t)lo[l] | ((uint64_t)hi[l] << 32)) & m;
+    }
+  }
+  void store_signal(const ValueLayout& L, const uint64_t* v) {
+    const uint64_t m = m64(L.width);
+    uint32_t* lo = values.data() + (size_t)L.offset * lanes;
+    if (L.limbs == 1) {
+      for (uint32_t l = 0; l < lanes; ++l) lo[l] = (uint32_t)(v[l] & m);
+    } else {
+      uint32_t* hi = lo + lanes;
+      for (uint32_t l = 0; l < lanes; ++l) {
+        const uint64_t x = v[l] & m;
+        lo[l] = (uint32_t)x;
+        hi[l] = (uint32_t)(x >> 32);
+      }
+    }
+  }
+  bool reset_on(const PackedReset& r, uint32_t lane) const {
+    const bool v = values[(size_t)P->signals[r.signal].layout.offset * lanes + lane] & 1u;
+    return r.active_low ? !v : v;
+  }
+  uint64_t mem_load(const PackedMemory& m, uint32_t lane, uint64_t a) const {
+    const uint32_t* p = memories.data() + (size_t)lane * P->total_memory_words_per_lane + m.offset +
+                        a * m.data_layout.limbs;
+    const uint64_t x = m.data_layout.limbs == 1 ? p[0] : ((uint64_t)p[0] | ((uint64_t)p[1] << 32));
+    return x & m64(m.data_layout.width);
+  }
+
+  // eval_machine_instr_lane's semantics (lib.rs:9796-9907) on u64 lanes; every
+  // result is masked to its width as fit_limbs does.
+  void eval(const Instr& in, const Block& b) {
+    uint64_t* o = V(in.dst);
+    const uint64_t m = m64(in.ty.width);
+    const uint32_t n = lanes;
+    auto A = [&](uint32_t k) { return (const uint64_t*)V(in.ops[k]); };
+    auto Wd = [&](uint32_t k) { return b.value_width[in.ops[k]]; };
+    switch (in.kind) {
+      case IK::Lit: {
+        const uint64_t v = lit64(in.lit) & m;
+        for (uint32_t l = 0; l < n; ++l) o[l] = v;
+        break;
+      }
+      case IK::Signal: load_signal(P->signals[in.index].layout, m, o); break;
+      case IK::Not: { const uint64_t* a = A(0); for (uint32_t l = 0; l < n; ++l) o[l] = ~a[l] & m; break; }
+      case IK::And: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] & c[l]) & m; break; }
+      case IK::Or: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] | c[l]) & m; break; }
+      case IK::Xor: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] ^ c[l]) & m; break; }
+      case IK::Add: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] + c[l]) & m; break; }
+      case IK::Sub: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] - c[l]) & m; break; }
+      case IK::Mul: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] * c[l]) & m; break; }
+      case IK::Eq: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = a[l] == c[l]; break; }
+      case IK::Ne: { const uint64_t *a = A(0), *c = A(1); for (uint32_t l = 0; l < n; ++l) o[l] = a[l] != c[l]; break; }
+      case IK::Lt: {
+        // at the left operand's width (lt_values): the right operand's higher bits are dropped
+        const uint64_t *a = A(0), *c = A(1);
+        const uint32_t w = Wd(0);
+        const uint64_t mw = m64(w);
+        if (in.is_signed) {
+          const uint32_t sh = 64 - w;
+          for (uint32_t l = 0; l < n; ++l)
+            o[l] = (int64_t)((a[l] & mw) << sh) < (int64_t)((c[l] & mw) << sh);
+        } else {
+          for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] & mw) < (c[l] & mw);
+        }
+        break;
+      }
+      case IK::Mux: {
+        const uint64_t *c = A(0), *t = A(1), *e = A(2);
+        for (uint32_t l = 0; l < n; ++l) o[l] = ((c[l] & 1u) ? t[l] : e[l]) & m;
+        break;
+      }
+      case IK::Slice: {
+        const uint64_t* a = A(0);
+        if (in.lsb >= 64) { for (uint32_t l = 0; l < n; ++l) o[l] = 0; break; }
+        for (uint32_t l = 0; l < n; ++l) o[l] = (a[l] >> in.lsb) & m;
+        break;
+      }
+      case IK::Zext: case IK::Trunc: case IK::Cast: { const uint64_t* a = A(0); for (uint32_t l = 0; l < n; ++l) o[l] = a[l] & m; break; }
+      case IK::Sext: {
+        const uint64_t* a = A(0);
+        const uint32_t w = Wd(0);
+        const uint64_t mw = m64(w);
+        for (uint32_t l = 0; l < n; ++l) {
+          const uint64_t x = a[l] & mw;
+          o[l] = (((x >> (w - 1)) & 1u) ? (x | ~mw) : x) & m;
+        }
+        break;
+      }
+      case IK::Concat: {
+        // MSB-first parts (concat_limbs): the last part takes the low bits
+        for (uint32_t l = 0; l < n; ++l) o[l] = 0;
+        uint32_t off = 0;
+        for (size_t k = in.ops.size(); k-- > 0;) {
+          const uint64_t* a = A((uint32_t)k);
+          const uint32_t w = Wd((uint32_t)k);
+          if (off < 64) {
+            const uint64_t mw = m64(w);
+            for (uint32_t l = 0; l < n; ++l) o[l] |= (a[l] & mw) << off;
+          }
+          off += w;
+        }
+        for (uint32_t l = 0; l < n; ++l) o[l] &= m;
+        break;
+      }
+      case IK::MemRead: {
+        const PackedMemory& mem = P->memories[in.index];
+        const uint64_t* a = A(0);
+        for (uint32_t l = 0; l < n; ++l) o[l] = a[l] < mem.depth ? mem_load(mem, l, a[l]) & m : 0ull;
+        break;
+      }
+    }
+  }
+
+  // execute_machine_block + execute_machine_effect (lib.rs:9700-9777).
+  void exec(const Block& b) {
+    if (b.packets.empty()) return;
+    wv.resize((size_t)b.num_values * lanes);
+    for (auto& pkt : b.packets) {
+      for (auto& in : pkt.instrs) eval(in, b);
+      for (auto& ef : pkt.effects) {
+        const uint64_t* v = V(ef.value);
+        if (ef.kind == EffK::StoreSignal) {
+          store_signal(P->signals[ef.dst].layout, v);
+        } else if (ef.kind == EffK::CaptureReg) {
+          if (!ef.has_reset || !ef.reset.async) continue;
+          const ValueLayout& L = P->signals[ef.dst].layout;
+          for (uint32_t lane = 0; lane < lanes; ++lane)
+            if (reset_on(ef.reset, lane)) {
+              Limbs x{(uint32_t)v[lane], (uint32_t)(v[lane] >> 32)};
+              store_layout(L, lane, x);
+            }
+        } else {
+          const PackedMemory& mem = P->memories[ef.dst];
+          const uint64_t *en = V(ef.enable), *ad = V(ef.addr);
+          const uint64_t dm = m64(mem.data_layout.width);
+          for (uint32_t lane = 0; lane < lanes; ++lane) {
+            if (!(en[lane] & 1u) || ad[lane] >= mem.depth) continue;
+            uint32_t* p = memories.data() + (size_t)lane * P->total_memory_words_per_lane + mem.offset +
+                          ad[lane] * mem.data_layout.limbs;
+            const uint64_t x = v[lane] & dm;
+            p[0] = (uint32_t)x;
+            if (mem.data_layout.limbs > 1) p[1] = (uint32_t)(x >> 32);
+          }
+        }
+      }
+    }
+  }
+
+  void eval_combinational() override {
+    exec(M->comb);
+    exec(M->async_reset_comb);
+  }
+  // capture_register_stream / capture_register_value (lib.rs:9614-9686),
+  // memory writes, then the commit of every capture (:9688-9699).
+  void tick_from_evaluated_no_post_eval() override {
+    const Block& b = M->tick_next;
+    size_t k = 0;
+    if (!b.packets.empty()) {
+      wv.resize((size_t)b.num_values * lanes);
+      for (auto& pkt : b.packets) {
+        for (auto& in : pkt.instrs) eval(in, b);
+        for (auto& ef : pkt.effects) {
+          if (ef.kind != EffK::CaptureReg) continue;
+          const ValueLayout& L = P->signals[ef.dst].layout;
+          if (caps.size() < (k + 1) * lanes) caps.resize((k + 1) * lanes);
+          if (cap_sig.size() <= k) cap_sig.resize(k + 1);
+          cap_sig[k] = ef.dst;
+          uint64_t* c = caps.data() + k * lanes;
+          const uint64_t* v = V(ef.value);
+          const uint64_t rv = lit64(ef.reset.value) & m64(L.width);
+          for (uint32_t lane = 0; lane < lanes; ++lane)
+            c[lane] = (ef.has_reset && reset_on(ef.reset, lane)) ? rv : v[lane];
+          ++k;
+        }
+      }
+    }
+    exec(M->tick_commit);
+    for (size_t i = 0; i < k; ++i) store_signal(P->signals[cap_sig[i]].layout, caps.data() + i * lanes);
   }
 };
 
@@ -966,6 +1192,11 @@ void* orc_packed_new(void* dp, uint32_t lanes) {
   try { return new PackedSim((OracleDesign*)dp, lanes); } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
 }
 void orc_packed_free(void* s) { delete (PackedSim*)s; }
+// SimdSim: a PackedSim whose cycle runs on u64 lanes (every orc_packed_* call applies).
+void* orc_simd_new(void* dp, uint32_t lanes) {
+  if (!lanes) { g_err = "E_SIM_IR_LANES: packed simulator requires at least one lane"; return nullptr; }
+  try { return static_cast<PackedSim*>(new SimdSim((OracleDesign*)dp, lanes)); } catch (const std::exception& e) { g_err = e.what(); return nullptr; }
+}
 // set_signal_limbs re-settles (lib.rs:9911-9944); `settle`=0 gives the raw store.
 void orc_packed_set_signal(void* sp, uint32_t sig, const uint32_t* data, int settle) {
   auto* s = (PackedSim*)sp;
@@ -1030,16 +1261,23 @@ int orc_packed_run(void* sp, const rrtl_run* r) {
       const rrtl_stim& st = r->stim[k];
       const ValueLayout& L = P.signals[st.signal].layout;
       if (st.kind == RRTL_STIM_HOLD) continue;
-      for (uint32_t lane = 0; lane < lanes; ++lane) {
-        Limbs v(L.limbs, 0);
-        for (uint32_t i = 0; i < L.limbs; ++i) {
-          if (st.kind == RRTL_STIM_RANDOM) v[i] = o_stim_lane_limb(r->seed, st.param, c, r->lane_base + lane, L.width, i);
-          else if (st.kind == RRTL_STIM_RANDOM_UNIFORM) v[i] = o_stim_lane_limb(r->seed, st.param, c, 0, L.width, i);
-          else if (st.kind == RRTL_STIM_PULSE) v[i] = (i == 0 && c < st.param) ? 1u : 0u;
-          else if (st.kind == RRTL_STIM_CONST) v[i] = i < 2 ? (uint32_t)(st.param >> (32 * i)) : 0u;
-          else if (st.kind == RRTL_STIM_TRACE) v[i] = r->input_trace[(c * r->n_trace_cols + st.param + i) * lanes + lane];
+      // limb i of every lane, masked to the width like store_layout (fit_limbs)
+      for (uint32_t i = 0; i < L.limbs; ++i) {
+        const uint32_t m = i + 1 == L.limbs ? top_mask(L.width) : 0xFFFFFFFFu;
+        uint32_t* dst = s->values.data() + s->vidx(L.offset, i, 0);
+        if (st.kind == RRTL_STIM_RANDOM) {
+          for (uint32_t lane = 0; lane < lanes; ++lane)
+            dst[lane] = o_stim_lane_limb(r->seed, st.param, c, r->lane_base + lane, L.width, i) & m;
+        } else if (st.kind == RRTL_STIM_TRACE) {
+          for (uint32_t lane = 0; lane < lanes; ++lane)
+            dst[lane] = r->input_trace[(c * r->n_trace_cols + st.param + i) * lanes + lane] & m;
+        } else {
+          uint32_t v = 0;  // lane-uniform kinds
+          if (st.kind == RRTL_STIM_RANDOM_UNIFORM) v = o_stim_lane_limb(r->seed, st.param, c, 0, L.width, i);
+          else if (st.kind == RRTL_STIM_PULSE) v = (i == 0 && c < st.param) ? 1u : 0u;
+          else if (st.kind == RRTL_STIM_CONST) v = i < 2 ? (uint32_t)(st.param >> (32 * i)) : 0u;
+          for (uint32_t lane = 0; lane < lanes; ++lane) dst[lane] = v & m;
         }
-        s->store_layout(L, lane, v);
       }
     }
     s->eval_combinational();

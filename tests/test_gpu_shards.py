@@ -68,7 +68,7 @@ def test_word_shards_compose(engine):
         g = sim.GpuBatchSimulator(cd, lanes=half)
         g.set_memory_limbs("rom", rom[:, :, base:base + half])
         hs.append(g.run(cycles, stim=stim, record=rec, mode=sim.REC_HASH, lane_base=base)["hash"])
-        assert np.array_equal(g.get_signal("acc"), full.get_signal("acc")[:, base:base + half])
+        assert np.array_equal(g.get_signal_limbs("acc"), full.get_signal_limbs("acc")[:, base:base + half])
     assert np.array_equal(hs[0] + hs[1], rf["hash"])
 
 
