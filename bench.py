@@ -178,6 +178,24 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def profiled_issue(name):
+    """Issue-slot figures of the top kernel from a committed ncu summary
+    (lines 'issue_<key>: value')."""
+    p = os.path.join(ROOT, "profiles", name)
+    out = {}
+    if os.path.exists(p):
+        with open(p) as f:
+            for line in f:
+                ln = line.strip()
+                if ln.startswith("issue_") and ":" in ln:
+                    k, v = ln.split(":", 1)
+                    try:
+                        out[k[len("issue_"):]] = float(v)
+                    except ValueError:
+                        out[k[len("issue_"):]] = v.strip()
+    return out or None
+
+
 def profiled_traffic(name):
     """Per-launch DRAM bytes from a committed ncu summary (line 'traffic_bytes_per_launch: N')."""
     p = os.path.join(ROOT, "profiles", name)
@@ -197,19 +215,18 @@ def profiled_traffic(name):
     return traffic, lanes
 
 
-def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
+def cpu_baseline(od, aot, compile_s, stim_idx, rec_idx, budget_s=12.0):
     """The reference's fastest CPU engine for this path restated: the AOT
     bit-parallel engine (BitParallelAot, crates/rrtl-sim-ir/src/bitparallel.rs:348-528:
-    the design as straight-line u64 C, compiled with -O2, 64 lanes per word,
-    group ranges over all host threads), on a bounded sample of the same
-    netlist and stimulus. The bit-parallel interpreter is timed beside it."""
+    the design as straight-line u64 C, compiled -O3 for the host, 64 lanes per
+    word, group ranges over all host threads), on a bounded sample of the same
+    netlist and stimulus. The bit-parallel interpreter is timed beside it, and
+    for the word-level configuration the SIMD-shaped packed engine
+    (SimdCpuSimulator restated) on all threads and the scalar packed
+    simulator on one."""
     from oracle import binding as ob
 
-    od = ob.OracleDesign(js, top)
     threads = os.cpu_count() or 1
-    t = time.perf_counter()
-    aot = ob.BitParallelAot(od, stim_idx, rec_idx, opt="-O2")
-    compile_s = time.perf_counter() - t
     lanes = 64 * threads * 8
     aot.run(lanes, 2, SEED)
     t = time.perf_counter()
@@ -235,26 +252,37 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
     t = time.perf_counter()
     ob.bp_run_parallel(od, ilanes, run, threads)
     idt = time.perf_counter() - t
-    # the word-level configuration: the reference's packed simulator restated
-    # (scalar, one core) on the pipelined CPU with per-lane hashed ROMs
+    # the word-level configuration: the SIMD-shaped packed engine (all host
+    # threads) and the scalar packed simulator (one thread) on the pipelined
+    # CPU with per-lane hashed ROMs
     from rrtl_gb300 import sim as _sim
     from rrtl_gb300.workloads import cpu_rom_hashed, pipelined_cpu
 
     cod = ob.OracleDesign(pipelined_cpu().to_json(), "Cpu8")
-    plane, pcyc = 64, 16
     cstim = [(cod.signal("clk"), _sim.STIM_CONST, 1), (cod.signal("rst"), _sim.STIM_PULSE, 1)]
     crec = [cod.signal("out_pc"), cod.signal("out_acc")]
+    rom_mi = cod.memory("rom")
+    slanes = 512 * threads
+    srom = cpu_rom_hashed(slanes, seed=3)
+    t = time.perf_counter()
+    ob.simd_run_parallel(cod, slanes, 50, 0, cstim, crec, 2, memories={rom_mi: srom}, threads=threads)
+    sdt = max(time.perf_counter() - t, 1e-3)
+    scyc = max(50, int(budget_s / 3 / sdt * 50))
+    t = time.perf_counter()
+    ob.simd_run_parallel(cod, slanes, scyc, 0, cstim, crec, 2, memories={rom_mi: srom}, threads=threads)
+    simd = slanes * scyc / (time.perf_counter() - t)
+    plane, pcyc = 64, 16
 
     def packed_run(cycles):
         ps = ob.PackedSim(cod, plane)
-        ps.set_memory(cod.memory("rom"), cpu_rom_hashed(plane, seed=3))
+        ps.set_memory(rom_mi, cpu_rom_hashed(plane, seed=3))
         r = ob.make_run(cycles, 0, cstim, crec, 2, out_hash=np.zeros(cycles, dtype=np.uint64))
         t0 = time.perf_counter()
         ps.run(r)
         return time.perf_counter() - t0
 
     pdt = max(packed_run(pcyc), 1e-4)
-    pcyc = max(16, int(budget_s / 4 / pdt * pcyc))
+    pcyc = max(16, int(budget_s / 8 / pdt * pcyc))
     packed = plane * pcyc / packed_run(pcyc)
     # the bit-slice engine restated (planes of 64 lanes, one core) on the
     # 16-bit ALU of the bit-slice leg without its compare (outside the
@@ -280,14 +308,54 @@ def cpu_baseline(js, top, stim_idx, rec_idx, budget_s=12.0):
     except Exception as e:  # the baseline is reported, not required
         bitslice = {"unavailable": str(e)[:200]}
     return {"value": value, "unit": "lane-cycles/s", "cores": threads, "kind": "port",
-            "packed_cpu8": {"value": packed, "cores": 1, "sample": f"pipelined CPU, {plane} lanes x {pcyc} cycles, "
-                                                                   "packed simulator restated, 1 thread"},
+            "packed_cpu8": {"value": simd, "cores": threads,
+                            "sample": f"pipelined CPU, {slanes} lanes x {scyc} cycles, SIMD-shaped packed engine "
+                                      f"(SimdCpuSimulator restated), {threads} threads"},
+            "packed_cpu8_scalar": {"value": packed, "cores": 1,
+                                   "sample": f"pipelined CPU, {plane} lanes x {pcyc} cycles, scalar packed "
+                                             "simulator restated, 1 thread"},
             "bitslice_alu16": bitslice,
             "sample": f"{lanes} lanes x {cycles} cycles of the same netlist and stimulus (bit-parallel AOT: "
-                      f"emitted C, gcc -O2, {threads} threads)", "seconds": round(dt, 3),
+                      f"emitted C, gcc {' '.join(aot.flags)}, {threads} threads)", "seconds": round(dt, 3),
             "compile_s": round(compile_s, 1),
             "one_core": {"value": one_core, "sample": f"{l1} lanes x {c1} cycles, 1 thread"},
             "interpreter": {"value": ilanes * icycles / idt, "sample": f"{ilanes} lanes x {icycles} cycles"}}
+
+
+AOT_OPT = "-O3"  # the emitted C is built where it runs, tuned for that host (the reference builds with clang -O3)
+
+
+def aot_engine(od, stim_idx, rec_idx):
+    """The bit-parallel AOT engine (oracle) for the headline netlist and run."""
+    from oracle import binding as ob
+
+    t = time.perf_counter()
+    aot = ob.BitParallelAot(od, stim_idx, rec_idx, opt=AOT_OPT, native=True)
+    return aot, time.perf_counter() - t
+
+
+def c2_parity(sim, cd, meta, stim, rec, aot, od, lanes, cycles, lane_base):
+    """The headline run at its full size against the oracle: a fresh batch of
+    `lanes` lanes (global lanes from lane_base) runs `cycles` cycles from reset
+    on the default fused path; its per-cycle output hash and final flip-flop
+    state must equal the bit-parallel AOT engine's (emitted C on every host
+    thread) on the same seed and lanes."""
+    g = sim.GpuBatchSimulator(cd, lanes=lanes)
+    r = g.run(cycles, seed=SEED, stim=stim, record=rec, mode=sim.REC_HASH, lane_base=lane_base)
+    q_gpu = g.get_signals_bits(meta.regs)
+    tile_words = g.tile_words
+    del g
+    t = time.perf_counter()
+    h_or, q_or = aot.run(lanes, cycles, SEED, lane_base=lane_base, signals=[od.signal(q) for q in meta.regs])
+    dt = time.perf_counter() - t
+    hash_ok = bool(np.array_equal(r["hash"], h_or))
+    state_ok = bool(np.array_equal(q_gpu, q_or[:, : q_gpu.shape[1]]))
+    return {"equal": hash_ok and state_ok, "hash_equal": hash_ok, "state_equal": state_ok, "lanes": lanes,
+            "cycles": cycles, "lane_base": lane_base, "tile_words": tile_words,
+            "checked": f"per-cycle output hash ({cycles} cycles) and final state of {len(meta.regs)} flip-flops "
+                       f"on all {lanes} lanes",
+            "oracle": f"bit-parallel AOT engine (emitted C, {AOT_OPT} host-tuned), {os.cpu_count()} host threads",
+            "oracle_s": round(dt, 2)}
 
 
 def build_workload():
@@ -296,10 +364,6 @@ def build_workload():
     d, meta = gate_netlist(n_gates=GATES, n_ff=FFS, n_pi=PIS, n_po=POS, depth=DEPTH, window=WINDOW, seed=SEED)
     js = d.to_json()
     stim, rec = netlist_run_spec(meta)
-    # fanin counts per gate type for the net-streaming byte model
-    fanins = []
-    for name in meta.gate_names:
-        pass
     return d, meta, js, stim, rec
 
 
@@ -321,23 +385,28 @@ def gate_fanins(js):
     return out
 
 
-def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
-    """Uneven job stream (the C4 shape, scaled): jobs on netlists of 5k-200k
-    gates, lanes log-uniform 32-65,536, cycles log-uniform 10-5,000 (the C4
-    range 100-50,000 divided by 10 so the plain paths finish in the run), 30%
-    fault jobs. Persistent job queue vs the plain one-launch-per-cycle path
-    on the whole stream, and the plain path with each run's launches captured
-    as a CUDA graph on the first `graph_jobs` jobs; every job's hash and
-    detection vector must agree across the paths."""
+def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, plain_jobs=24, graph_jobs=8, cycles=(100, 50_000)):
+    """Uneven job stream (C4): `n_jobs` jobs on netlists of the 50k-gate
+    family with gate counts log-uniform 5k-200k (a pool of `n_designs`
+    netlists of distinct seeds; each job takes one at random), lanes
+    log-uniform 32-65,536, cycles log-uniform 100-50,000, 30% fault jobs
+    (one stuck-at fault per lane, lane-uniform stimulus so every fault-free
+    lane equals the golden lane). All jobs run in one launch of the
+    persistent job-queue kernel. The plain one-launch-per-cycle path runs a
+    seeded subset of `plain_jobs` jobs (every n/plain_jobs-th), which also
+    runs alone on the persistent queue, so the speed-up compares the same
+    jobs; the subset's hashes and detection vectors must equal the full
+    stream's. Graph capture of the plain path is timed on `graph_jobs` of them."""
     from rrtl_gb300.workloads import job_faults, job_stream, job_stream_designs, netlist_run_spec
 
     t0 = time.perf_counter()
     designs = job_stream_designs(n_designs)
     cds = []
     for d, meta in designs:
-        stim, rec = netlist_run_spec(meta)
-        cds.append((meta, sim.CompiledDesign(d.to_json(), meta.top, ctx), stim, rec))
-    jobs = job_stream(n_jobs, len(cds), cycles_lo=10, cycles_hi=5000)
+        cds.append((meta, sim.CompiledDesign(d.to_json(), meta.top, ctx), netlist_run_spec(meta),
+                    netlist_run_spec(meta, uniform=True)))
+    del designs
+    jobs = job_stream(n_jobs, len(cds), cycles_lo=cycles[0], cycles_hi=cycles[1])
     setup_s = time.perf_counter() - t0
 
     def make(j, path):
@@ -348,54 +417,83 @@ def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, graph_jobs=24):
             g.set_faults(job_faults(meta, j.lanes, j.seed))
         return g
 
-    def mode(j):
-        return sim.REC_HASH | (sim.REC_DETECT if j.fault else 0)
+    def spec(j):
+        stim, rec = cds[j.design][3] if j.fault else cds[j.design][2]
+        return stim, rec, sim.REC_HASH | (sim.REC_DETECT if j.fault else 0)
+
+    def queue_run(sub):
+        batches = [make(j, sim.PATH_FUSED) for j in sub]
+        ctx.synchronize()
+        t = time.perf_counter()
+        q = []
+        for g, j in zip(batches, sub):
+            stim, rec, mode = spec(j)
+            q.append(ctx.submit(g, j.cycles, seed=j.seed, stim=stim, record=rec, mode=mode))
+        ctx.launch()
+        ctx.wait()
+        wall = time.perf_counter() - t
+        outs = [jq.outputs for jq in q]
+        widths = sorted({g.tile_words for g in batches})
+        return wall, ctx.queue_ms, outs, widths
 
     lane_cycles = sum(j.lanes * j.cycles for j in jobs)
     gate_evals = sum(j.lanes * j.cycles * cds[j.design][1].info.n_gates for j in jobs)
-    # persistent queue: one launch drains every job
-    batches = [make(j, sim.PATH_FUSED) for j in jobs]
-    ctx.synchronize()
-    t0 = time.perf_counter()
-    q = [ctx.submit(g, j.cycles, seed=j.seed, stim=cds[j.design][2], record=cds[j.design][3], mode=mode(j))
-         for g, j in zip(batches, jobs)]
-    ctx.launch()
-    ctx.wait()
-    persist_s = time.perf_counter() - t0
-    persist_dev_ms = ctx.queue_ms
-    results = [jq.outputs for jq in q]
-    widths = sorted({g.tile_words for g in batches})
-    del batches, q
-    out = {"jobs": n_jobs, "designs_gates": [m.n_gates for m, _, _, _ in cds],
+    persist_s, persist_dev_ms, results, widths = queue_run(jobs)
+    # fault coverage: faulted lanes (all but lane 0 of each word) that detected
+    fl = fd = 0
+    for j, r in zip(jobs, results):
+        if j.fault:
+            det = r["detect"]
+            faulted = np.arange(j.lanes) % 32 != 0
+            fl += int(faulted.sum())
+            fd += int((det[faulted] != 0xFFFFFFFF).sum())
+    fault_free_quiet = all((r["detect"][::32] == 0xFFFFFFFF).all() for j, r in zip(jobs, results) if j.fault)
+    out = {"jobs": n_jobs, "design_pool": n_designs, "designs_gates": [m.n_gates for m, _, _, _ in cds],
            "fault_jobs": sum(j.fault for j in jobs), "lane_cycles": lane_cycles, "gate_evals": gate_evals,
-           "lanes": "log-uniform 32-65536", "cycles": "log-uniform 10-5000 (C4 range / 10)",
+           "lanes": "log-uniform 32-65536", "cycles": f"log-uniform {cycles[0]}-{cycles[1]}",
            "persistent": {"value": lane_cycles / persist_s, "unit": "lane-cycles/s", "wall_s": persist_s,
-                          "device_ms": persist_dev_ms, "gate_evals_per_s": gate_evals / persist_s,
-                          "tile_words": widths, "launches": 1},
+                          "device_ms": persist_dev_ms, "device_value": lane_cycles / (persist_dev_ms / 1e3),
+                          "gate_evals_per_s": gate_evals / persist_s, "tile_words": widths, "launches": 1},
+           "fault_coverage": {"faulted_lanes": fl, "detected": fd, "frac": fd / max(fl, 1),
+                              "fault_free_lanes_quiet": bool(fault_free_quiet),
+                              "protocol": "one stuck-at fault per lane, lane-uniform random inputs, detection = first "
+                                          "cycle a lane's outputs differ from the fault-free lane 0 of its word"},
            "setup_s": setup_s}
-    if plain:
-        same = True
+    if plain and plain_jobs:
+        step = max(1, len(jobs) // plain_jobs)
+        idx = list(range(0, len(jobs), step))[:plain_jobs]
+        sub = [jobs[i] for i in idx]
+        sub_lc = sum(j.lanes * j.cycles for j in sub)
+        q_s, q_ms, q_out, _ = queue_run(sub)
+        same = all(np.array_equal(q_out[k]["hash"], results[i]["hash"]) and
+                   (q_out[k]["detect"] is None or np.array_equal(q_out[k]["detect"], results[i]["detect"]))
+                   for k, i in enumerate(idx))
         per_job = {}
-        for name, path, n in (("plain", sim.PATH_PLAIN, len(jobs)), ("plain_graph", sim.PATH_PLAIN_GRAPH, graph_jobs)):
+        for name, path, n in (("plain", sim.PATH_PLAIN, len(sub)), ("plain_graph", sim.PATH_PLAIN_GRAPH, graph_jobs)):
             times = []
-            sub = jobs[:n]
-            for j, ref in zip(sub, results):
+            for j, i in zip(sub[:n], idx[:n]):
                 g = make(j, path)
+                stim, rec, mode = spec(j)
                 ctx.synchronize()
-                t0 = time.perf_counter()
-                r = g.run(j.cycles, seed=j.seed, stim=cds[j.design][2], record=cds[j.design][3], mode=mode(j))
-                times.append(time.perf_counter() - t0)
-                same = same and np.array_equal(r["hash"], ref["hash"]) and (
-                    r["detect"] is None or np.array_equal(r["detect"], ref["detect"]))
+                t = time.perf_counter()
+                r = g.run(j.cycles, seed=j.seed, stim=stim, record=rec, mode=mode)
+                times.append(time.perf_counter() - t)
+                same = same and np.array_equal(r["hash"], results[i]["hash"]) and (
+                    r["detect"] is None or np.array_equal(r["detect"], results[i]["detect"]))
                 del g
             per_job[name] = times
-            tot = sum(times)
-            sub_lc = sum(j.lanes * j.cycles for j in sub)
-            out[name] = {"value": sub_lc / tot, "unit": "lane-cycles/s", "wall_s": tot, "jobs": len(sub),
-                         "launches": sum(j.cycles + 1 for j in sub) if path == sim.PATH_PLAIN else len(sub)}
-        out["speedup_vs_plain"] = out["persistent"]["value"] / out["plain"]["value"]
-        # graph capture against the plain launches on the same jobs (capture and instantiation included)
-        out["plain_graph"]["speedup_vs_plain_same_jobs"] = sum(per_job["plain"][:graph_jobs]) / sum(per_job["plain_graph"])
+        tot = sum(per_job["plain"])
+        rates = sorted(j.lanes * j.cycles / t for j, t in zip(sub, per_job["plain"]))
+        out["subset"] = {"jobs": len(sub), "indices": f"every {step}th job from 0", "lane_cycles": sub_lc,
+                         "persistent": {"value": sub_lc / q_s, "wall_s": q_s, "device_ms": q_ms},
+                         "plain": {"value": sub_lc / tot, "wall_s": tot, "launches": sum(j.cycles + 1 for j in sub),
+                                   "per_job_rate_min": rates[0], "per_job_rate_median": rates[len(rates) // 2],
+                                   "per_job_rate_max": rates[-1]},
+                         "unit": "lane-cycles/s"}
+        out["speedup_vs_plain"] = out["subset"]["persistent"]["value"] / out["subset"]["plain"]["value"]
+        gsum = sum(per_job["plain_graph"])
+        out["subset"]["plain_graph"] = {"jobs": graph_jobs, "wall_s": gsum,
+                                        "speedup_vs_plain_same_jobs": sum(per_job["plain"][:graph_jobs]) / gsum}
         out["bitexact_across_paths"] = bool(same)
     return out
 
@@ -487,33 +585,53 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
     return out
 
 
-def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True):
+def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True, parity_lanes=16384):
     """The word-engine configs: the README Counter (1,024 lanes x 10,000
     cycles, full output trace recorded) and the 8-stage pipelined CPU
     (16,384 lanes x 20,000 cycles, per-lane hashed ROMs). The fused path runs
     the design's compiled kernel; each config is also timed on the
     interpreted word kernel (whole run, one launch) and on the plain
-    one-launch-per-cycle path (200 cycles of the same batch shape), and the
-    CPU's per-cycle hashes are compared across the three."""
+    one-launch-per-cycle path (200 cycles of the same batch shape). Parity at
+    the stated sizes: the Counter's full trace, and the CPU's per-cycle hash
+    over all 20,000 cycles plus the final register file, PC, pipeline
+    registers and data memory of the first `parity_lanes` lanes (all of them
+    by default; 0 skips it), against the SIMD-shaped packed engine (oracle)
+    on every host thread. The CPU run is timed three ways: CUDA events inside
+    the library around its kernels, CUDA events on the stream around the
+    whole call (table uploads and output copies included), and the host
+    clock."""
+    from oracle import binding as ob
     from rrtl_gb300.workloads import counter as counter_design, cpu_rom_hashed, pipelined_cpu
 
     out = {}
-    cd = sim.CompiledDesign(counter_design(), "Counter", ctx)
-    jit, jit_ms, why = cd.word_jit()
-    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 1)]
-    for path, cyc, key in ((sim.PATH_FUSED, 10_000, "value"), (sim.PATH_WORD_INTERP, 10_000, "interpreted"),
-                           (sim.PATH_PLAIN, 200, "plain"))[:3 if counter else 0]:
-        g = sim.GpuBatchSimulator(cd, lanes=1024)
-        g.set_path(path)
-        g.run(cyc, seed=1, stim=stim, record=["out"], mode=sim.REC_TRACE)
-        v = 1024 * cyc / (g.last_kernel_ms / 1e3)
-        if key == "value":
-            out["counter"] = {"lanes": 1024, "cycles": cyc, "value": v, "unit": "lane-cycles/s",
-                              "kernel_ms": g.last_kernel_ms, "trace_bytes": 1024 * cyc * 4, "compiled": jit,
-                              "compile_ms": jit_ms}
-        else:
-            out["counter"][key] = v
-    cd = sim.CompiledDesign(pipelined_cpu(), "Cpu8", ctx)
+    if counter:
+        cjs = counter_design()
+        cd = sim.CompiledDesign(cjs, "Counter", ctx)
+        jit, jit_ms, why = cd.word_jit()
+        stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 1)]
+        for path, cyc, key in ((sim.PATH_FUSED, 10_000, "value"), (sim.PATH_WORD_INTERP, 10_000, "interpreted"),
+                               (sim.PATH_PLAIN, 200, "plain")):
+            g = sim.GpuBatchSimulator(cd, lanes=1024)
+            g.set_path(path)
+            r = g.run(cyc, seed=1, stim=stim, record=["out"], mode=sim.REC_TRACE)
+            v = 1024 * cyc / (g.last_kernel_ms / 1e3)
+            if key == "value":
+                out["counter"] = {"lanes": 1024, "cycles": cyc, "value": v, "unit": "lane-cycles/s",
+                                  "kernel_ms": g.last_kernel_ms, "trace_bytes": 1024 * cyc * 4, "compiled": jit,
+                                  "compile_ms": jit_ms}
+                if parity_lanes:
+                    od = ob.OracleDesign(cjs, "Counter")
+                    ps = ob.SimdSim(od, 1024)
+                    tr = np.zeros((cyc, 1, 1024), dtype=np.uint32)
+                    ps.run(ob.make_run(cyc, 1, [(od.signal(n), k, p) for n, k, p in stim], [od.signal("out")], 1,
+                                       out_trace=tr))
+                    out["counter"]["parity"] = {"equal": bool(np.array_equal(tr, r["trace"])),
+                                                "checked": "full out trace, 1,024 lanes x 10,000 cycles",
+                                                "oracle": "SIMD-shaped packed engine"}
+            else:
+                out["counter"][key] = v
+    cjs = pipelined_cpu()
+    cd = sim.CompiledDesign(cjs, "Cpu8", ctx)
     jit, jit_ms, why = cd.word_jit()
     stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]
     rom = cpu_rom_hashed(16384, seed=3)
@@ -528,12 +646,52 @@ def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True):
     n = min(2000, cpu8_cycles)
     same = bool(np.array_equal(h[:200], res[sim.PATH_PLAIN][1][:200]) and
                 np.array_equal(h[:n], res[sim.PATH_WORD_INTERP][1][:n]))
+    gf = res[sim.PATH_FUSED][2]
+    # the same run again on a fresh batch, timed three ways
+    g2 = sim.GpuBatchSimulator(cd, lanes=16384)
+    g2.set_memory_limbs("rom", rom)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    ctx.record(6)
+    g2.run(cpu8_cycles, stim=stim, record=["out_pc", "out_acc"], mode=sim.REC_HASH)
+    ctx.record(7)
+    stream_ms = ctx.elapsed_ms(6, 7)
+    wall_ms = (time.perf_counter() - t0) * 1e3
+    kernel_ms = g2.last_kernel_ms
+    del g2
+    timing = {"kernel_events_ms": kernel_ms, "stream_events_ms": stream_ms, "wall_ms": wall_ms,
+              "kernel_events_value": 16384 * cpu8_cycles / (kernel_ms / 1e3),
+              "stream_events_value": 16384 * cpu8_cycles / (stream_ms / 1e3),
+              "wall_value": 16384 * cpu8_cycles / (wall_ms / 1e3)}
     out["cpu8"] = {"lanes": 16384, "cycles": cpu8_cycles, "value": res[sim.PATH_FUSED][0], "unit": "lane-cycles/s",
                    "interpreted": res[sim.PATH_WORD_INTERP][0], "interpreted_cycles": 2_000,
                    "plain": res[sim.PATH_PLAIN][0], "hash_prefix_equal_all_paths": same, "compiled": jit,
-                   "compile_ms": jit_ms,
+                   "compile_ms": jit_ms, "timing": timing,
                    "note": "one thread per lane: 16,384 lanes are 512 warps, under one per warp scheduler, so "
                            "the run is bound by one warp's dependent-instruction latency"}
+    if parity_lanes:
+        # parity against the SIMD-shaped packed engine at the stated size
+        od = ob.OracleDesign(cjs, "Cpu8")
+        pl = min(parity_lanes, 16384)
+        t = time.perf_counter()
+        h_or, v_or, m_or = ob.simd_run_parallel(od, pl, cpu8_cycles, 0, [(od.signal(nm), k, p) for nm, k, p in stim],
+                                                [od.signal("out_pc"), od.signal("out_acc")], 2,
+                                                memories={od.memory("rom"): rom[:, :, :pl]}, snapshot=True)
+        odt = time.perf_counter() - t
+        v_gpu, m_gpu = gf.snapshot_storage()
+        tsw, tmw = od.total_signal_words, od.total_memory_words
+        v_gpu = v_gpu.reshape(tsw, 16384)[:, :pl].reshape(-1)
+        m_gpu = m_gpu.reshape(16384, tmw)[:pl].reshape(-1)
+        parity = {"state_equal": bool(np.array_equal(v_gpu, v_or) and np.array_equal(m_gpu, m_or)),
+                  "lanes": pl, "cycles": cpu8_cycles,
+                  "oracle": f"SIMD-shaped packed engine, {os.cpu_count()} host threads", "oracle_s": round(odt, 2),
+                  "checked": "final signal words (register-file read ports, PC, pipeline registers, accumulator) and "
+                             "all memory words (register file, data memory, ROM) of every checked lane"}
+        if pl == 16384:
+            parity["hash_equal"] = bool(np.array_equal(h, h_or))
+            parity["checked"] += f", and the per-cycle hash of out_pc/out_acc over all {cpu8_cycles} cycles"
+        parity["equal"] = parity["state_equal"] and parity.get("hash_equal", True)
+        out["cpu8"]["parity"] = parity
     return out
 
 
@@ -651,8 +809,9 @@ def instance_fold_leg(ctx, sim, cycles=2000):
 
 def run_reference(args, ws, rank):
     """The reference's CPU implementation of the path on the host cores: the
-    AOT bit-parallel engine restated (see cpu_baseline), each step a bounded
-    sample of the same workload."""
+    AOT bit-parallel engine restated (see cpu_baseline: the same emitted C,
+    flags and threads), each step a bounded sample of the same workload long
+    enough (at least half a second) that thread start-up is noise."""
     if rank != 0:
         return
     d, meta, js, stim, rec = build_workload()
@@ -662,9 +821,12 @@ def run_reference(args, ws, rank):
     stim_idx = [(od.signal(n), k, p) for n, k, p in stim]
     rec_idx = [od.signal(r) for r in rec]
     threads = os.cpu_count() or 1
-    aot = ob.BitParallelAot(od, stim_idx, rec_idx, opt="-O2")
+    aot, _ = aot_engine(od, stim_idx, rec_idx)
     lanes = 64 * threads * 8
-    cycles = 16
+    t = time.perf_counter()
+    aot.run(lanes, 8, SEED)
+    per_cycle = max(time.perf_counter() - t, 1e-4) / 8
+    cycles = max(16, int(0.6 / per_cycle))
     vals = []
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
@@ -683,7 +845,7 @@ def run_reference(args, ws, rank):
                    "lanes_per_step": lanes, "cycles_per_step": cycles, "parallelism": f"{threads} host threads"},
         "cpu_baseline": {"value": value, "unit": "lane-cycles/s", "cores": threads, "kind": "port",
                          "sample": f"{lanes} lanes x {cycles} cycles per step (bit-parallel AOT restated from "
-                                   f"crates/rrtl-sim-ir/src/bitparallel.rs:348-528, gcc -O2)"},
+                                   f"crates/rrtl-sim-ir/src/bitparallel.rs:348-528, gcc {' '.join(aot.flags)})"},
         "e2e": {"value": value, "unit": "lane-cycles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -700,8 +862,12 @@ def main():
     ap.add_argument("--lanes", type=int, default=LANES, help="lanes per GPU (profiling cases)")
     ap.add_argument("--cycles", type=int, default=CYCLES, help="cycles per step (profiling cases)")
     ap.add_argument("--tile-words", type=int, default=0, help="fused tile width in 32-lane words (0 = automatic)")
-    ap.add_argument("--jobs", type=int, default=96, help="jobs in the uneven job-stream leg (0 = skip it)")
-    ap.add_argument("--job-designs", type=int, default=8, help="distinct netlists in the job stream")
+    ap.add_argument("--jobs", type=int, default=2048, help="jobs in the uneven job-stream leg (0 = skip it)")
+    ap.add_argument("--job-designs", type=int, default=16, help="netlists of distinct seeds in the job stream's pool")
+    ap.add_argument("--plain-jobs", type=int, default=24, help="job stream: jobs of the subset timed on the plain path")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the benchmarked runs")
+    ap.add_argument("--cpu8-parity-lanes", type=int, default=16384,
+                    help="pipelined CPU: lanes checked against the oracle after the full run")
     ap.add_argument("--no-plain-jobs", action="store_true", help="job stream: skip the plain-path comparison")
     ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
     ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
@@ -754,9 +920,13 @@ def main():
     dev = torch.device("cuda", local)
     hash_dev = [torch.zeros(CYCLES, dtype=torch.int64, device=dev) for _ in range(args.steps + args.warmup)]
 
+    # rank r simulates global lanes [r*L, (r+1)*L) of one run: stimulus and
+    # hashes follow global lanes, so the ranks' shards compose into one job
+    lane_base = rank * LANES
+
     def device_run(i, path=sim.PATH_FUSED, cycles=CYCLES):
         g.set_path(path)
-        r = g.make_run(cycles, seed=SEED + i + 1000 * rank, stim=stim, record=rec, mode=sim.REC_HASH)
+        r = g.make_run(cycles, seed=SEED + i, stim=stim, record=rec, mode=sim.REC_HASH, lane_base=lane_base)
         r.out_hash = ctypes_u64(hash_dev[i].data_ptr())
         sim.check(sim.lib().rrtl_batch_run_device(g.h, sim.byref(r)))
 
@@ -792,7 +962,7 @@ def main():
     ctx.record(2)
     for i in range(args.steps):
         g.set_path(sim.PATH_FUSED)
-        r = g.make_run(CYCLES, seed=SEED + i + 1000 * rank, stim=stim, record=rec, mode=sim.REC_HASH)
+        r = g.make_run(CYCLES, seed=SEED + i, stim=stim, record=rec, mode=sim.REC_HASH, lane_base=lane_base)
         r.out_hash = ctypes_u64(hash_host.data_ptr())
         sim.check(sim.lib().rrtl_batch_run(g.h, sim.byref(r)))
         sim.check(sim.lib().rrtl_batch_get_signals_bits(g.h, reg_idx.ctypes.data_as(sim.POINTER(sim.c_uint32)),
@@ -815,10 +985,29 @@ def main():
         plain = {"value": LANES * pc / (pms / 1000.0) * ws, "unit": "lane-cycles/s", "cycles_timed": pc,
                  "launches": pc + 1}
 
+    del g
+    clock_summary = clocks.summary()
+    # the headline run at its full size against the oracle (rank 0's shard)
+    parity = {}
+    aot = aot_compile_s = od = None
+    if rank == 0 and not args.no_parity:
+        from oracle import binding as ob
+
+        od = ob.OracleDesign(js, meta.top)
+        aot, aot_compile_s = aot_engine(od, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec])
+        parity["c2"] = c2_parity(sim, cd, meta, stim, rec, aot, od, LANES, CYCLES, lane_base)
+
     peak, peak_kind = load_peaks()
     bpl = net_stream_bytes_per_lane_cycle(gate_fanins(js), FFS, PIS, POS)
     algo_bytes = bpl * LANES * CYCLES
     achieved = algo_bytes / (ms_step / 1000.0) / 1e9
+    # the roof that binds: every cell-word evaluation reads its fanin rows and
+    # writes its output row in shared memory, so the net-streaming bytes are
+    # the kernel's shared-memory traffic; the nominal shared-memory bandwidth
+    # is 128 bytes per clock per SM
+    sm_mhz = clock_summary.get("sm_mhz") or 2070.0
+    smem_peak = ctx.sm_count * 128.0 * sm_mhz * 1e6 / 1e9
+    issue = profiled_issue("gate_fused_kernel_c2.md")
     # DRAM traffic of one launch grows with lanes (closing write-back of every
     # net), not with cycles (per-cycle work stays in shared memory and L2)
     traffic, tlanes = profiled_traffic("gate_fused_kernel_c2.md")
@@ -830,16 +1019,22 @@ def main():
                 "model": "net-streaming bytes per lane-cycle (fanin reads + output write per gate, D read + Q write "
                          "per flop, inputs and outputs), 4 bytes per 32 lanes",
                 "note": "nets stay in shared memory for all cycles of a tile, so measured DRAM traffic per launch "
-                        "(traffic) is far below the streamed bytes (achieved*time); the kernel is bound by SM issue "
-                        "and the shared-memory pipe, not HBM"}
+                        "(traffic) is far below the streamed bytes (achieved*time): HBM does not bind this kernel; "
+                        "the shared-memory roof below does",
+                "smem": {"bound": "smem", "achieved": achieved, "peak": smem_peak, "unit": "GB/s",
+                         "frac": achieved / smem_peak,
+                         "peak_kind": f"nominal: {ctx.sm_count} SMs x 128 B/clock x {sm_mhz:.0f} MHz (sampled SM clock)",
+                         "model": "the net-streaming bytes are the cell evaluations' shared-memory row reads and "
+                                  "writes"},
+                "issue": issue}
     out = {
         "metric": METRIC, "value": value, "unit": "lane-cycles/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 bit-sliced (32 lanes per word)", "data": "synthetic (seeded netlist and stimulus)",
         "config": {"workload": f"gate netlist {GATES} gates / {FFS} FF / {PIS} PI / {POS} PO / depth {DEPTH} / "
                                f"window {WINDOW}", "lanes_per_gpu": LANES, "cycles_per_step": CYCLES,
-                   "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective; rank r simulates lanes "
-                                                     f"{lane_shard(LANES * ws, rank, ws)} of the job, seed offset by r)",
+                   "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective; rank r simulates "
+                                                     f"global lanes [r*{LANES}, (r+1)*{LANES}) of one run)",
                    "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": "fused persistent kernel",
                    "tile_words": tile_words},
         "gate_evals_per_s": value * info.n_gates,
@@ -849,10 +1044,17 @@ def main():
         "plain_path": plain,
         "roofline": roofline,
         "gpu_launches": args.steps,
-        "clocks": clocks.summary(),
+        "clocks": clock_summary,
+        "parity": parity,
     }
     if not args.no_word_configs:
-        out["word_configs"] = word_configs_leg(ctx, sim, args.cpu8_cycles)
+        out["word_configs"] = word_configs_leg(ctx, sim, args.cpu8_cycles,
+                                               parity_lanes=0 if rank != 0 or args.no_parity else args.cpu8_parity_lanes)
+        wc = out["word_configs"]
+        if "counter" in wc and "parity" in wc["counter"]:
+            parity["c1"] = wc["counter"]["parity"]
+        if "parity" in wc["cpu8"]:
+            parity["c3"] = wc["cpu8"]["parity"]
     if not args.no_fold:
         out["instance_fold"] = instance_fold_leg(ctx, sim)
     if not args.no_crc32:
@@ -860,7 +1062,8 @@ def main():
     if not args.no_bitslice:
         out["bitslice"] = bitslice_leg(ctx, sim)
     if args.jobs > 0:
-        out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs)
+        out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs,
+                                           plain_jobs=args.plain_jobs)
     if args.serve_rates:
         rates = [float(x) for x in args.serve_rates.split(",") if x]
         out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), rates, args.serve_seconds,
@@ -868,9 +1071,11 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import binding as ob
 
-        od = ob.OracleDesign(js, meta.top)
-        out["cpu_baseline"] = cpu_baseline(js, meta.top, [(od.signal(n), k, p) for n, k, p in stim],
-                                           [od.signal(r) for r in rec])
+        od = od or ob.OracleDesign(js, meta.top)
+        si, ri = [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec]
+        if aot is None:
+            aot, aot_compile_s = aot_engine(od, si, ri)
+        out["cpu_baseline"] = cpu_baseline(od, aot, aot_compile_s, si, ri)
     if rank == 0:
         print(json.dumps(out))
     if dist:
