@@ -605,7 +605,7 @@ def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True, parity_lanes=16
 
     out = {}
     if counter:
-        cjs = counter_design()
+        cjs = counter_design().to_json()
         cd = sim.CompiledDesign(cjs, "Counter", ctx)
         jit, jit_ms, why = cd.word_jit()
         stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1), ("en", sim.STIM_RANDOM, 1)]
@@ -630,7 +630,7 @@ def word_configs_leg(ctx, sim, cpu8_cycles=20_000, counter=True, parity_lanes=16
                                                 "oracle": "SIMD-shaped packed engine"}
             else:
                 out["counter"][key] = v
-    cjs = pipelined_cpu()
+    cjs = pipelined_cpu().to_json()
     cd = sim.CompiledDesign(cjs, "Cpu8", ctx)
     jit, jit_ms, why = cd.word_jit()
     stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 1)]

@@ -2,6 +2,7 @@
 #include "gateprog.h"
 
 #include <algorithm>
+#include <array>
 #include <map>
 #include <tuple>
 #include <unordered_map>
@@ -252,6 +253,147 @@ struct Builder {
 
 }  // namespace
 
+// Input symmetries of a truth table: the input orders that map it to itself
+// (a cell may read its inputs in any of them without changing its table).
+struct LutSymmetry {
+  std::vector<std::array<int, 3>> perms;  // automorphisms, identity first
+};
+
+const LutSymmetry& lut_symmetry(uint8_t lut) {
+  static const std::vector<LutSymmetry> table = [] {
+    static const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    std::vector<LutSymmetry> t(256);
+    for (int l = 0; l < 256; ++l)
+      for (int k = 0; k < 6; ++k)
+        if (permute_lut((uint8_t)l, perms[k]) == (uint8_t)l) t[l].perms.push_back({perms[k][0], perms[k][1], perms[k][2]});
+    return t;
+  }();
+  return table[lut];
+}
+
+// Shared-memory wavefronts of a group's operand reads with the given input
+// orders: per position, the largest number of distinct rows that share a
+// bank residue (rows read twice are one broadcast).
+uint32_t group_wavefronts(const GateProgram& gp, const std::vector<uint32_t>& grp, const bool use[3], uint32_t G,
+                          const int* choice, const LutSymmetry& sym) {
+  uint32_t total = 0;
+  const size_t n = grp.size();
+  uint32_t rows[32];
+  for (int p = 0; p < 3; ++p) {
+    if (!use[p]) continue;
+    uint32_t per[32] = {0}, mx = 0;
+    for (size_t k = 0; k < n; ++k) {
+      const GateCell& c = gp.cells[grp[k]];
+      const uint32_t r = (uint32_t)gp.net_slot[c.in[sym.perms[choice ? choice[k] : 0][p]]];
+      bool seen = false;
+      for (size_t q = 0; q < k && !seen; ++q) seen = rows[q] == r;
+      rows[k] = r;
+      if (!seen) mx = std::max(mx, ++per[r % G]);
+    }
+    total += mx;
+  }
+  return total;
+}
+
+// The fewest wavefronts a group reaches over its cells' input orders, and
+// the orders that reach it: every combination for small groups of tables
+// with two orders, else a local search from the identity.
+uint32_t best_orientation(const GateProgram& gp, const std::vector<uint32_t>& grp, const LutSymmetry& sym,
+                          const bool use[3], uint32_t G, std::vector<int>* out) {
+  std::vector<int> choice(grp.size(), 0);
+  uint32_t best = group_wavefronts(gp, grp, use, G, choice.data(), sym);
+  if (sym.perms.size() >= 2) {
+    if (sym.perms.size() == 2 && grp.size() <= 4) {
+      std::vector<int> c(grp.size(), 0), bc = choice;
+      for (uint32_t m = 1; m < (1u << grp.size()) && best > 0; ++m) {
+        for (size_t k = 0; k < grp.size(); ++k) c[k] = (m >> k) & 1;
+        const uint32_t w = group_wavefronts(gp, grp, use, G, c.data(), sym);
+        if (w < best) {
+          best = w;
+          bc = c;
+        }
+      }
+      choice = bc;
+    } else {
+      for (int pass = 0; pass < 2; ++pass) {
+        bool improved = false;
+        for (size_t k = 0; k < grp.size(); ++k) {
+          const int keep = choice[k];
+          for (int q = 0; q < (int)sym.perms.size(); ++q) {
+            if (q == keep) continue;
+            choice[k] = q;
+            const uint32_t w = group_wavefronts(gp, grp, use, G, choice.data(), sym);
+            if (w < best) {
+              best = w;
+              improved = true;
+              break;
+            }
+            choice[k] = keep;
+          }
+        }
+        if (!improved) break;
+      }
+    }
+  }
+  if (out) *out = choice;
+  return best;
+}
+
+// Apply the best input orders to a group's cells.
+void orient_group(GateProgram& gp, const std::vector<uint32_t>& grp, const LutSymmetry& sym, const bool use[3],
+                  uint32_t G) {
+  if (sym.perms.size() < 2) return;
+  std::vector<int> choice;
+  best_orientation(gp, grp, sym, use, G, &choice);
+  for (size_t k = 0; k < grp.size(); ++k) {
+    if (!choice[k]) continue;
+    GateCell& c = gp.cells[grp[k]];
+    const uint32_t in[3] = {c.in[0], c.in[1], c.in[2]};
+    for (int p = 0; p < 3; ++p) c.in[p] = in[sym.perms[choice[k]][p]];
+  }
+}
+
+// Move cells between the groups of one truth-table run to cut bank
+// conflicts: random swaps of two cells of two groups, kept when the pair's
+// wavefronts (each at its best input orders) do not grow. The greedy
+// grouping fills groups from a bounded look-ahead, so later groups take what
+// is left; swapping evens them out.
+void refine_groups(const GateProgram& gp, std::vector<std::vector<uint32_t>>& groups, const LutSymmetry& sym,
+                   const bool use[3], uint32_t G, uint64_t& rng) {
+  const size_t ng = groups.size();
+  if (ng < 2) return;
+  std::vector<uint32_t> cost(ng);
+  size_t cells = 0;
+  for (size_t g = 0; g < ng; ++g) {
+    cost[g] = best_orientation(gp, groups[g], sym, use, G, nullptr);
+    cells += groups[g].size();
+  }
+  uint32_t floor = 0;  // a group reads each used position at least once
+  for (int p = 0; p < 3; ++p) floor += use[p] ? 1 : 0;
+  auto next = [&]() {
+    rng ^= rng << 13;
+    rng ^= rng >> 7;
+    rng ^= rng << 17;
+    return rng;
+  };
+  const size_t tries = cells * (G <= 4 ? 12 : G <= 8 ? 4 : 0);
+  for (size_t t = 0; t < tries; ++t) {
+    const size_t a = next() % ng, b = next() % ng;
+    if (a == b || (cost[a] <= floor && cost[b] <= floor)) continue;
+    const size_t i = next() % groups[a].size(), j = next() % groups[b].size();
+    std::swap(groups[a][i], groups[b][j]);
+    const uint32_t ca = best_orientation(gp, groups[a], sym, use, G, nullptr);
+    const uint32_t cb = best_orientation(gp, groups[b], sym, use, G, nullptr);
+    if (ca + cb <= cost[a] + cost[b]) {
+      cost[a] = ca;
+      cost[b] = cb;
+    } else {
+      std::swap(groups[a][i], groups[b][j]);
+    }
+  }
+}
+
+
 GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   const PackedProgram& P = mp.source;
   GateProgram gp;
@@ -447,6 +589,7 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   std::vector<uint32_t> cnt(3 * G);
   std::vector<uint32_t> stamp(3 * (size_t)65536, 0);
   uint32_t group_id = 0;
+  uint64_t refine_rng = 0x243F6A8885A308D3ull;  // fixed seed: the lowering is deterministic
   for (uint32_t L = 0; L < gp.n_levels; ++L) {
     for (uint32_t s : q_free_after[L]) release(s);
     if (L > 0)
@@ -461,6 +604,7 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
       const bool use[3] = {(lut & 0x0F) != ((lut >> 4) & 0x0F), (lut & 0x33) != ((lut >> 2) & 0x33),
                            (lut & 0x55) != ((lut >> 1) & 0x55)};
       std::vector<uint32_t> rem(cs.begin() + i, cs.begin() + j);
+      std::vector<std::vector<uint32_t>> run_groups;
       size_t head = 0;
       std::vector<uint8_t> taken(rem.size(), 0);
       auto slot_in = [&](uint32_t cell, int p) { return (uint32_t)gp.net_slot[gp.cells[cell].in[p]]; };
@@ -508,6 +652,12 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
           taken[best] = 1;
           add(rem[best]);
         }
+        run_groups.push_back(std::move(grp));
+      }
+      const LutSymmetry& sym = lut_symmetry(lut);
+      refine_groups(gp, run_groups, sym, use, G, refine_rng);
+      for (std::vector<uint32_t>& grp : run_groups) {
+        orient_group(gp, grp, sym, use, G);
         // outputs: distinct residues; residue 0 last when padding (scratch slot 0) shares the group
         const bool padded = grp.size() < G;
         for (size_t k = 0; k < grp.size(); ++k) {
