@@ -447,7 +447,8 @@ rrtl_status rrtl_design_word_jit(rrtl_design* design, uint32_t* active, float* c
  * be NULL); *source_len its length. *cubin_bytes the compiled image's size
  * (0 when not compiled); log (may be NULL) the compiler's messages.
  * RRTL_E_UNSUPPORTED when the design is outside the word engine's scope
- * (values over 64 bits) or the compiler fails. */
+ * (values over 128 bits) or the compiler fails. Values of 65 to 128 bits
+ * compute on 128-bit integers in pairs of value slots. */
 rrtl_status rrtl_word_jit_emit(const char* json, size_t len, const char* top, const rrtl_run* run, const char* arch,
                                char* source, size_t source_cap, size_t* source_len, uint32_t* cubin_bytes, char* log,
                                size_t log_cap, uint32_t flags);

@@ -24,7 +24,14 @@ enum WOp : uint8_t {
   W_MEMWR,     // if (a & 1) and b < depth: mem[aux][b] = c
 };
 
-// flags: bit0 two limbs (signal/memory access), bit1 has reset, bit2 active-low reset
+// flags: bit0 two limbs (signal/memory access), bit1 has reset, bit2 active-low reset.
+// Values of 65 to 128 bits take a pair of value slots (s: bits 0-63, s+1: bits
+// 64-127). An instruction with kWWide set computes on 128 bits: kWPairD says
+// its result is a pair, kWPairA/B/C which operands are pairs (a single slot
+// reads as a value below 2^64). Wide signal accesses
+// (W_SIG, W_STORE, W_ASTORE, W_CAPTURE) carry their limb count in `c`; wide
+// literals and capture reset values are two consecutive `lits` entries.
+enum : uint8_t { kWWide = 8, kWPairA = 16, kWPairB = 32, kWPairC = 64, kWPairD = 128 };
 struct WInstr {
   uint8_t op;
   uint8_t flags;

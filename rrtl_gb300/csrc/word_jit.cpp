@@ -98,8 +98,9 @@ struct Emitter {
       case W_MEMRD: w = std::min<uint32_t>(I.width, wp.mems[I.aux].width); break;
       default: w = I.width; break;
     }
-    if (I.dst >= vw.size()) vw.resize(I.dst + 1, 64u);
+    if (I.dst + 1u >= vw.size()) vw.resize(I.dst + 2u, 64u);
     vw[I.dst] = std::min<uint32_t>(w, 64u);
+    if (I.flags & kWPairD) vw[I.dst + 1u] = 64u;
   }
 
   // 32-bit form of an instruction whose result (and every operand bit it
@@ -155,8 +156,112 @@ struct Emitter {
     }
   }
 
+  // Statement for one wide instruction (kWWide): the same semantics on
+  // 128-bit integers; a pair slot s holds bits 0-63 and s+1 bits 64-127.
+  std::string wide_stmt(const WInstr& I) const {
+    auto P = [&](uint32_t s, uint8_t bit) {
+      return (I.flags & bit) ? "(((u128)" + V(s + 1) + " << 64) | (u128)" + V(s) + ")" : "(u128)" + V(s);
+    };
+    auto M2 = [](uint32_t w) {
+      return w >= 128u ? std::string("(~(u128)0)") : "((((u128)1) << " + u(w) + ") - (u128)1)";
+    };
+    const std::string a = P(I.a, kWPairA), b = P(I.b, kWPairB), c = P(I.c, kWPairC), m = M2(I.width);
+    auto set = [&](const std::string& e) {
+      if (I.flags & kWPairD)
+        return "{ const u128 t = " + e + "; " + V(I.dst) + " = (u64)t; " + V(I.dst + 1) + " = (u64)(t >> 64); }";
+      return V(I.dst) + " = (u64)(" + e + ");";
+    };
+    auto load_sig = [&](uint32_t off, uint32_t limbs) {
+      std::string s = "((u128)0";
+      for (uint32_t l = 0; l < limbs; ++l) s += " | ((u128)" + sig(off + l) + " << " + u(32 * l) + ")";
+      return s + ")";
+    };
+    auto store_sig = [&](uint32_t off, uint32_t limbs, const std::string& t) {
+      std::string s;
+      for (uint32_t l = 0; l < limbs; ++l) s += sig(off + l) + " = (uint32_t)(" + t + " >> " + u(32 * l) + "); ";
+      return s;
+    };
+    // decode_usize: an address past 64 bits saturates
+    auto addr = [](const std::string& x) { return "(((" + x + ") >> 64) != 0 ? ~0ull : (u64)(" + x + "))"; };
+    switch (I.op) {
+      case W_LIT: {
+        char buf[96];
+        snprintf(buf, sizeof buf, "((((u128)0x%llxull) << 64) | (u128)0x%llxull)", wp.lits[I.aux + 1], wp.lits[I.aux]);
+        return set(std::string(buf) + " & " + m);
+      }
+      case W_SIG: return set(load_sig(I.aux, I.c) + " & " + m);
+      case W_NOT: return set("~" + a + " & " + m);
+      case W_AND: return set("(" + a + " & " + b + ") & " + m);
+      case W_OR: return set("(" + a + " | " + b + ") & " + m);
+      case W_XOR: return set("(" + a + " ^ " + b + ") & " + m);
+      case W_ADD: return set("(" + a + " + " + b + ") & " + m);
+      case W_SUB: return set("(" + a + " - " + b + ") & " + m);
+      case W_MUL: return set("(" + a + " * " + b + ") & " + m);
+      case W_EQ: return set("(u128)(" + a + " == " + b + ")");
+      case W_NE: return set("(u128)(" + a + " != " + b + ")");
+      case W_LT: return set("(u128)((" + a + " & " + M2(I.aux) + ") < (" + b + " & " + M2(I.aux) + "))");
+      case W_LTS: {
+        if (I.aux == 0) return set("(u128)0");
+        const std::string om = M2(I.aux), sb = "(((u128)1) << " + u(I.aux - 1u) + ")";
+        return "{ const u128 x = " + a + " & " + om + ", y = " + b + " & " + om + "; const bool xs = (x & " + sb +
+               ") != 0, ys = (y & " + sb + ") != 0; " + set("(xs != ys) ? (u128)xs : (u128)(x < y)") + " }";
+      }
+      case W_MUX: return set("(((u64)" + a + " & 1ull) ? " + b + " : " + c + ") & " + m);
+      case W_SLICE:
+        if (I.aux >= 128u) return set("(u128)0");
+        return set("(" + a + " >> " + u(I.aux) + ") & " + m);
+      case W_MASK: return set(a + " & " + m);
+      case W_SEXT: {
+        if (I.aux == 0) return set("(u128)0");
+        const std::string wm = M2(I.aux);
+        return "{ const u128 x = " + a + " & " + wm + "; " +
+               set("((((x >> " + u(I.aux - 1u) + ") & (u128)1) != 0) ? (x | ~" + wm + ") : x) & " + m) + " }";
+      }
+      case W_CAT:
+        if (I.aux >= 128u) return set(b + " & " + m);
+        return set("((" + a + " << " + u(I.aux) + ") | " + b + ") & " + m);
+      case W_MEMRD: {
+        const WMemDev& Md = wp.mems[I.aux];
+        std::string s = "{ const u64 ad = " + addr(a) + "; u128 r = 0; if (ad < " + hex(Md.depth) +
+                        ") { const size_t w0 = (size_t)ad * " + u(Md.limbs) + ";";
+        for (uint32_t l = 0; l < Md.limbs; ++l)
+          s += " r |= (u128)" + mem(I.aux, "w0 + " + u(l)) + " << " + u(32 * l) + ";";
+        s += " r &= " + M2(Md.width) + " & " + m + "; } " + set("r") + " }";
+        return s;
+      }
+      case W_STORE: return "{ const u128 t = " + a + " & " + m + "; " + store_sig(I.aux, I.c, "t") + "}";
+      case W_ASTORE:
+        return "if (" + reset(I.aux2, I.flags & 4) + ") { const u128 t = " + a + " & " + m + "; " +
+               store_sig(I.aux, I.c, "t") + "}";
+      case W_CAPTURE: {
+        std::string t = a;
+        if (I.flags & 2) {
+          char buf[96];
+          snprintf(buf, sizeof buf, "((((u128)0x%llxull) << 64) | (u128)0x%llxull)", wp.lits[I.aux3 + 1],
+                   wp.lits[I.aux3]);
+          t = "(" + reset(I.aux2, I.flags & 4) + " ? " + std::string(buf) + " : " + a + ")";
+        }
+        std::string s = "{ const u128 t = " + t + " & " + m + ";";
+        for (uint32_t l = 0; l < I.c; ++l)
+          s += " c" + std::to_string(I.aux + l) + " = (uint32_t)(t >> " + u(32 * l) + ");";
+        return s + " }";
+      }
+      case W_MEMWR: {
+        const WMemDev& Md = wp.mems[I.aux];
+        std::string s = "if ((u64)" + a + " & 1ull) { const u64 ad = " + addr(b) + "; if (ad < " + hex(Md.depth) +
+                        ") { const u128 t = " + c + " & " + M2(Md.width) + "; const size_t w0 = (size_t)ad * " +
+                        u(Md.limbs) + ";";
+        for (uint32_t l = 0; l < Md.limbs; ++l)
+          s += " " + mem(I.aux, "w0 + " + u(l)) + " = (uint32_t)(t >> " + u(32 * l) + ");";
+        return s + " } }";
+      }
+      default: return "";
+    }
+  }
+
   // Statement for one instruction (empty for opcodes the interpreter skips).
   std::string stmt(const WInstr& I) const {
+    if (I.flags & kWWide) return wide_stmt(I);
     {
       std::string s = narrow(I);
       if (!s.empty()) return s;
@@ -241,6 +346,22 @@ struct Emitter {
   }
 
   static void uses(const WInstr& I, std::set<uint32_t>& s) {
+    if (I.flags & kWWide) {
+      // wide instructions: the slots the opcode uses, and the second slot of every pair
+      switch (I.op) {
+        case W_LIT: case W_SIG: break;
+        case W_NOT: case W_SLICE: case W_MASK: case W_SEXT: case W_MEMRD: s.insert(I.a); break;
+        case W_MUX: case W_MEMWR: s.insert(I.a); s.insert(I.b); s.insert(I.c); break;
+        case W_STORE: case W_ASTORE: case W_CAPTURE: s.insert(I.a); break;
+        default: s.insert(I.a); s.insert(I.b); break;
+      }
+      if (I.op != W_STORE && I.op != W_ASTORE && I.op != W_CAPTURE && I.op != W_MEMWR) s.insert(I.dst);
+      if (I.flags & kWPairA) s.insert(I.a + 1u);
+      if (I.flags & kWPairB) s.insert(I.b + 1u);
+      if (I.flags & kWPairC) s.insert(I.c + 1u);
+      if (I.flags & kWPairD) s.insert(I.dst + 1u);
+      return;
+    }
     switch (I.op) {
       case W_LIT:
       case W_SIG: s.insert(I.dst); break;
@@ -292,6 +413,7 @@ struct Emitter {
     o += "#include \"word_lane.h\"\n";
     o += "namespace rrtl {\n";
     o += "typedef unsigned long long u64;\n";
+    o += "typedef unsigned __int128 u128;\n";
     o += "struct JitLane : JitLaneBase {\n";
     if (regs && wp.n_sig_words) {
       const uint32_t n = wp.n_sig_words;
@@ -486,6 +608,8 @@ bool word_split_plan(const WordProgram& wp, const WordRunTables& run, WordSplitP
   };
   if (wp.async_b != wp.async_e) return no("asynchronous resets");
   if (wp.n_sig_words > kJitRegSignals || wp.code.size() > kJitMaxInstrs) return no("too large");
+  for (const WInstr& I : wp.code)
+    if (I.flags & kWWide) return no("values wider than 64 bits");
   const size_t N = wp.code.size();
   std::vector<std::vector<uint32_t>> dep(N);
   std::unordered_map<uint32_t, uint32_t> sig_def;  // signal word -> the comb store that defines it this cycle
@@ -664,8 +788,9 @@ std::vector<char> word_jit_compile(const std::string& src, const std::string& ar
   }
   const std::string arch_opt = "--gpu-architecture=" + arch;
   // -default-device: the C ABI header's host prototypes become inert device declarations
-  const char* opts[] = {arch_opt.c_str(), "-std=c++17", "-default-device"};
-  r = N.compile(prog, 3, opts);
+  // --device-int128: values of 65 to 128 bits compute on unsigned __int128
+  const char* opts[] = {arch_opt.c_str(), "-std=c++17", "-default-device", "--device-int128"};
+  r = N.compile(prog, 4, opts);
   size_t ls = 0;
   N.log_size(prog, &ls);
   std::string lg(ls, '\0');

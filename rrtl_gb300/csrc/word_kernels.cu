@@ -7,8 +7,9 @@
 // design needs more slots than fit, in a spill array in HBM.
 //
 // Operation semantics follow eval_machine_instr_lane and its limb helpers
-// (crates/rrtl-sim-ir/src/lib.rs:9796-9907, 12942-13196) specialised to
-// values of at most 64 bits: every result is masked to its width.
+// (crates/rrtl-sim-ir/src/lib.rs:9796-9907, 12942-13196) for values of at
+// most 128 bits (those past 64 bits in slot pairs, computed on 128-bit
+// integers): every result is masked to its width.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -53,9 +54,115 @@ struct WordLane {
     return active_low ? !b : b;
   }
 
+  // ---- values of 65 to 128 bits (slot pairs, see kWWide)
+  typedef unsigned __int128 u128;
+  __device__ static u128 wmask2(uint32_t w) { return w >= 128u ? ~(u128)0 : (((u128)1 << w) - 1u); }
+  __device__ u128 W2(uint16_t s, bool pair) const {
+    return pair ? (((u128)V(s + 1u) << 64) | (u128)V(s)) : (u128)V(s);
+  }
+  __device__ void set2(uint16_t s, bool pair, u128 x) const {
+    V(s) = (unsigned long long)x;
+    if (pair) V(s + 1u) = (unsigned long long)(x >> 64);
+  }
+  __device__ u128 load_limbs(uint32_t off, uint32_t limbs) const {
+    u128 v = 0;
+    for (uint32_t l = 0; l < limbs; ++l) v |= (u128)SV(off + l) << (32u * l);
+    return v;
+  }
+  __device__ void store_limbs(uint32_t off, uint32_t limbs, u128 v) const {
+    for (uint32_t l = 0; l < limbs; ++l) SV(off + l) = (uint32_t)(v >> (32u * l));
+  }
+  // decode_usize (crates/rrtl-sim-ir/src/lib.rs:12989-13008): an address past 64 bits saturates
+  __device__ static unsigned long long addr_of(u128 a) { return (a >> 64) ? ~0ull : (unsigned long long)a; }
+  __device__ u128 mem_load(const WMemDev& M, unsigned long long addr) const {
+    u128 r = 0;
+    const size_t w0 = (size_t)M.offset + (size_t)addr * M.limbs;
+    for (uint32_t l = 0; l < M.limbs; ++l) r |= (u128)R.mems[(w0 + l) * LP + lane] << (32u * l);
+    return r & wmask2(M.width);
+  }
+
+  // One wide instruction: the narrow semantics below on 128-bit values.
+  __device__ void run_wide(const WInstr& I) const {
+    const u128 m = wmask2(I.width);
+    const u128 a = W2(I.a, I.flags & kWPairA), b = W2(I.b, I.flags & kWPairB);
+    u128 r = 0;
+    switch (I.op) {
+      case W_LIT: r = (((u128)__ldg(P.lits + I.aux + 1u) << 64) | __ldg(P.lits + I.aux)) & m; break;
+      case W_SIG: r = load_limbs(I.aux, I.c) & m; break;
+      case W_NOT: r = ~a & m; break;
+      case W_AND: r = (a & b) & m; break;
+      case W_OR: r = (a | b) & m; break;
+      case W_XOR: r = (a ^ b) & m; break;
+      case W_ADD: r = (a + b) & m; break;
+      case W_SUB: r = (a - b) & m; break;
+      case W_MUL: r = (a * b) & m; break;
+      case W_EQ: r = a == b; break;
+      case W_NE: r = a != b; break;
+      case W_LT: {
+        const u128 om = wmask2(I.aux);
+        r = (a & om) < (b & om);
+        break;
+      }
+      case W_LTS: {
+        if (I.aux == 0u) break;
+        const u128 om = wmask2(I.aux), sb = (u128)1 << (I.aux - 1u);
+        const u128 x = a & om, y = b & om;
+        const bool xs = (x & sb) != 0, ys = (y & sb) != 0;
+        r = (xs != ys) ? (u128)xs : (u128)(x < y);
+        break;
+      }
+      case W_MUX: r = (((unsigned long long)a & 1ull) ? b : W2(I.c, I.flags & kWPairC)) & m; break;
+      case W_SLICE: r = I.aux >= 128u ? (u128)0 : ((a >> I.aux) & m); break;
+      case W_MASK: r = a & m; break;
+      case W_SEXT: {
+        if (I.aux == 0u) break;
+        const u128 x = a & wmask2(I.aux);
+        r = ((((x >> (I.aux - 1u)) & 1u) != 0) ? (x | ~wmask2(I.aux)) : x) & m;
+        break;
+      }
+      case W_CAT: r = ((I.aux >= 128u ? (u128)0 : (a << I.aux)) | b) & m; break;
+      case W_MEMRD: {
+        const WMemDev M = P.mems[I.aux];
+        const unsigned long long addr = addr_of(a);
+        if (addr < M.depth) r = mem_load(M, addr) & m;
+        break;
+      }
+      case W_STORE: store_limbs(I.aux, I.c, a & m); return;
+      case W_ASTORE:
+        if (reset_asserted(I.aux2, I.flags & 4)) store_limbs(I.aux, I.c, a & m);
+        return;
+      case W_CAPTURE: {
+        u128 v = a;
+        if ((I.flags & 2) && reset_asserted(I.aux2, I.flags & 4))
+          v = ((u128)__ldg(P.lits + I.aux3 + 1u) << 64) | __ldg(P.lits + I.aux3);
+        v &= m;
+        for (uint32_t l = 0; l < I.c; ++l) R.caps[(size_t)(I.aux + l) * LP + lane] = (uint32_t)(v >> (32u * l));
+        return;
+      }
+      case W_MEMWR: {
+        if ((unsigned long long)a & 1ull) {
+          const WMemDev M = P.mems[I.aux];
+          const unsigned long long addr = addr_of(b);
+          if (addr < M.depth) {
+            const u128 v = W2(I.c, I.flags & kWPairC) & wmask2(M.width);
+            const size_t w0 = (size_t)M.offset + (size_t)addr * M.limbs;
+            for (uint32_t l = 0; l < M.limbs; ++l) R.mems[(w0 + l) * LP + lane] = (uint32_t)(v >> (32u * l));
+          }
+        }
+        return;
+      }
+      default: return;
+    }
+    set2(I.dst, I.flags & kWPairD, r);
+  }
+
   __device__ void run(uint32_t b, uint32_t e) const {
     for (uint32_t pc = b; pc < e; ++pc) {
       const WInstr I = P.code[pc];
+      if (I.flags & kWWide) {
+        run_wide(I);
+        continue;
+      }
       const unsigned long long m = wmask(I.width);
       unsigned long long r = 0;
       switch (I.op) {

@@ -23,9 +23,11 @@ struct Emitter {
   uint32_t cap_words = 0;
 
   // per block
-  std::unordered_map<uint32_t, uint32_t> slot_of;  // value -> slot
+  const Block* blk_ = nullptr;
+  std::unordered_map<uint32_t, uint32_t> slot_of;  // value -> slot (the first of a pair)
   std::unordered_map<uint32_t, size_t> last_use;   // value -> item index of last use
-  std::vector<uint32_t> free_slots;
+  std::unordered_set<uint32_t> pair_val;           // values held in a slot pair (wider than 64 bits)
+  std::vector<uint32_t> free_slots, free_pairs;
   uint32_t next_slot = 0;
   uint32_t temp_base = 0x80000000u;  // synthetic value ids for concat temporaries
 
@@ -40,40 +42,58 @@ struct Emitter {
     return i;
   }
 
-  static unsigned long long limbs_to_u64(const std::vector<uint32_t>& l) {
+  static unsigned long long limbs_to_u64(const std::vector<uint32_t>& l, size_t first = 0) {
     unsigned long long v = 0;
-    if (l.size() > 0) v |= l[0];
-    if (l.size() > 1) v |= (unsigned long long)l[1] << 32;
+    if (l.size() > first) v |= l[first];
+    if (l.size() > first + 1) v |= (unsigned long long)l[first + 1] << 32;
     return v;
   }
+  // two consecutive literal entries (bits 0-63, 64-127) of a wide value
+  uint32_t lit_pair(const std::vector<uint32_t>& l) {
+    uint32_t i = (uint32_t)wp.lits.size();
+    wp.lits.push_back(limbs_to_u64(l, 0));
+    wp.lits.push_back(limbs_to_u64(l, 2));
+    return i;
+  }
 
-  uint32_t alloc() {
-    if (!free_slots.empty()) {
-      uint32_t s = free_slots.back();
-      free_slots.pop_back();
+  uint32_t alloc(bool pair = false) {
+    std::vector<uint32_t>& fl = pair ? free_pairs : free_slots;
+    if (!fl.empty()) {
+      uint32_t s = fl.back();
+      fl.pop_back();
       return s;
     }
-    uint32_t s = next_slot++;
+    uint32_t s = next_slot;
+    next_slot += pair ? 2 : 1;
     if (next_slot > 0xFFFF) throw RrtlError("E_WORD_SCOPE", "too many live values");
     return s;
   }
   void release_if_last(uint32_t v, size_t at) {
     auto it = last_use.find(v);
     if (it != last_use.end() && it->second == at) {
-      free_slots.push_back(slot_of.at(v));
+      (pair_val.count(v) ? free_pairs : free_slots).push_back(slot_of.at(v));
       last_use.erase(it);
     }
   }
+  // Slot of value v as an operand; sets `pair_flag` in *flags when v is a pair.
+  uint16_t opnd(uint32_t v, uint8_t pair_flag, uint8_t* flags) {
+    if (pair_val.count(v)) *flags |= pair_flag;
+    return (uint16_t)slot_of.at(v);
+  }
+  uint32_t vwidth(uint32_t v) const { return blk_->value_width[v]; }
 
   void check_width(uint32_t w) {
-    if (w > 64) throw RrtlError("E_WORD_SCOPE", "values wider than 64 bits are outside the word engine");
+    if (w > 128) throw RrtlError("E_WORD_SCOPE", "values wider than 128 bits are outside the word engine");
   }
 
   // Emit a block's items (already ordered) with slot allocation.
   void emit_items(const std::vector<Item>& items, const Block& blk) {
+    blk_ = &blk;
     slot_of.clear();
     last_use.clear();
+    pair_val.clear();
     free_slots.clear();
+    free_pairs.clear();
     next_slot = 0;
     // last uses
     for (size_t i = 0; i < items.size(); ++i) {
@@ -105,26 +125,47 @@ struct Emitter {
 
   void emit_instr(const Instr& in, const Block& blk, size_t at) {
     check_width(in.ty.width);
-    auto S = [&](uint32_t v) { return (uint16_t)slot_of.at(v); };
     WInstr w = base(0, in.ty.width);
+    // a value wider than 64 bits, or any operand that is, makes the instruction wide
+    bool wide = in.ty.width > 64;
+    for (uint32_t v : instr_deps(in)) wide = wide || blk.value_width[v] > 64;
     std::vector<uint16_t> ops;
-    for (uint32_t v : instr_deps(in)) ops.push_back(S(v));
+    const uint8_t pair_bits[3] = {kWPairA, kWPairB, kWPairC};
+    size_t k = 0;
+    for (uint32_t v : instr_deps(in)) {
+      ops.push_back(opnd(v, k < 3 ? pair_bits[k] : 0, &w.flags));
+      ++k;
+    }
     auto finish = [&](WInstr x) {
       for (uint32_t v : instr_deps(in)) release_if_last(v, at);
-      x.dst = (uint16_t)alloc();
+      const bool pair = in.ty.width > 64;
+      if (wide) x.flags |= kWWide;
+      if (pair) {
+        x.flags |= kWPairD;
+        pair_val.insert(in.dst);
+      }
+      x.dst = (uint16_t)alloc(pair);
       slot_of[in.dst] = x.dst;
       wp.code.push_back(x);
       release_if_last(in.dst, at);
     };
     switch (in.kind) {
-      case IK::Lit: w.op = W_LIT; w.aux = lit(limbs_to_u64(in.lit)); break;
+      case IK::Lit:
+        w.op = W_LIT;
+        w.aux = wide ? lit_pair(in.lit) : lit(limbs_to_u64(in.lit));
+        break;
       case IK::Signal: {
         const ValueLayout& L = mp.source.signals[in.index].layout;
         check_width(L.width);
         w.op = W_SIG;
         w.aux = L.offset;
-        w.flags = L.limbs == 2 ? 1 : 0;
         w.width = (uint16_t)std::min(in.ty.width, L.width);
+        if (wide || L.width > 64) {
+          wide = true;
+          w.c = (uint16_t)L.limbs;
+        } else {
+          w.flags = L.limbs == 2 ? 1 : 0;
+        }
         break;
       }
       case IK::Not: w.op = W_NOT; w.a = ops[0]; break;
@@ -147,33 +188,48 @@ struct Emitter {
       case IK::Slice: w.op = W_SLICE; w.a = ops[0]; w.aux = in.lsb; check_width(blk.value_width[in.ops[0]]); break;
       case IK::Zext: case IK::Trunc: case IK::Cast: w.op = W_MASK; w.a = ops[0]; break;
       case IK::Sext: w.op = W_SEXT; w.a = ops[0]; w.aux = blk.value_width[in.ops[0]]; break;
-      case IK::MemRead: w.op = W_MEMRD; w.a = ops[0]; w.aux = in.index; break;
+      case IK::MemRead: {
+        w.op = W_MEMRD;
+        w.a = ops[0];
+        w.aux = in.index;
+        wide = wide || mp.source.memories[in.index].data_layout.width > 64;
+        break;
+      }
       case IK::Concat: {
-        // t0 = p0; t_i = (t_{i-1} << w_i) | p_i
+        // t0 = p0; t_i = (t_{i-1} << w_i) | p_i, in one accumulator (a pair
+        // when the result is wider than 64 bits)
+        const bool pair = in.ty.width > 64;
         uint32_t acc_w = blk.value_width[in.ops[0]];
         check_width(acc_w);
         WInstr m = base(W_MASK, std::min<uint32_t>(acc_w, in.ty.width));
+        m.flags = w.flags & kWPairA;
         m.a = ops[0];
         if (in.ops.size() == 1) {
           finish(m);
           return;
         }
         // the accumulator gets its own slot, kept until the last part is merged
-        uint32_t acc_slot = alloc();
+        const uint32_t acc_slot = alloc(pair);
         m.dst = (uint16_t)acc_slot;
+        if (wide) m.flags |= kWWide | (pair ? kWPairD : 0);
         wp.code.push_back(m);
-        for (size_t k = 1; k < in.ops.size(); ++k) {
-          uint32_t pw = blk.value_width[in.ops[k]];
+        for (size_t k2 = 1; k2 < in.ops.size(); ++k2) {
+          uint32_t pw = blk.value_width[in.ops[k2]];
           acc_w += pw;
           WInstr c = base(W_CAT, std::min<uint32_t>(acc_w, in.ty.width));
           c.a = (uint16_t)acc_slot;
-          c.b = ops[k];
+          c.b = ops[k2];
           c.aux = pw;
           c.dst = (uint16_t)acc_slot;
-          if (k + 1 == in.ops.size()) {
+          if (wide) {
+            c.flags = kWWide | (pair ? kWPairA | kWPairD : 0);
+            if (pair_val.count(in.ops[k2])) c.flags |= kWPairB;
+          }
+          if (k2 + 1 == in.ops.size()) {
             c.width = (uint16_t)in.ty.width;
             for (uint32_t v : instr_deps(in)) release_if_last(v, at);
             slot_of[in.dst] = acc_slot;
+            if (pair) pair_val.insert(in.dst);
             wp.code.push_back(c);
             release_if_last(in.dst, at);
             return;
@@ -188,34 +244,50 @@ struct Emitter {
 
   void emit_effect(const Effect& e, size_t at) {
     const PackedProgram& P = mp.source;
-    auto S = [&](uint32_t v) { return (uint16_t)slot_of.at(v); };
     if (e.kind == EffK::StoreSignal) {
       const ValueLayout& L = P.signals[e.dst].layout;
       check_width(L.width);
       WInstr w = base(W_STORE, L.width);
-      w.a = S(e.value);
+      w.a = opnd(e.value, kWPairA, &w.flags);
       w.aux = L.offset;
-      w.flags = L.limbs == 2 ? 1 : 0;
+      if (L.width > 64 || vwidth(e.value) > 64) {
+        w.flags |= kWWide;
+        w.c = (uint16_t)L.limbs;
+      } else {
+        w.flags = L.limbs == 2 ? 1 : 0;
+      }
       wp.code.push_back(w);
       release_if_last(e.value, at);
     } else if (e.kind == EffK::CaptureReg) {
       const ValueLayout& L = P.signals[e.dst].layout;
       check_width(L.width);
+      const bool wide = L.width > 64 || vwidth(e.value) > 64;
       bool async_block = cur_block_async;
       if (async_block) {
         if (e.has_reset && e.reset.async) {
           WInstr w = base(W_ASTORE, L.width);
-          w.a = S(e.value);
+          w.a = opnd(e.value, kWPairA, &w.flags);
           w.aux = L.offset;
           w.aux2 = P.signals[e.reset.signal].layout.offset;
-          w.flags = (uint8_t)((L.limbs == 2 ? 1 : 0) | 2 | (e.reset.active_low ? 4 : 0));
+          w.flags |= (uint8_t)(2 | (e.reset.active_low ? 4 : 0));
+          if (wide) {
+            w.flags |= kWWide;
+            w.c = (uint16_t)L.limbs;
+          } else if (L.limbs == 2) {
+            w.flags |= 1;
+          }
           wp.code.push_back(w);
         }
       } else {
         WInstr w = base(W_CAPTURE, L.width);
-        w.a = S(e.value);
+        w.a = opnd(e.value, kWPairA, &w.flags);
         w.aux = cap_words;
-        w.flags = (uint8_t)(L.limbs == 2 ? 1 : 0);
+        if (wide) {
+          w.flags |= kWWide;
+          w.c = (uint16_t)L.limbs;
+        } else if (L.limbs == 2) {
+          w.flags |= 1;
+        }
         if (e.has_reset) {
           w.flags |= 2;
           if (e.reset.active_low) w.flags |= 4;
@@ -223,7 +295,7 @@ struct Emitter {
           std::vector<uint32_t> rv = e.reset.value;
           rv.resize(L.limbs, 0);
           rv.back() &= final_limb_mask(L.width);
-          w.aux3 = lit(limbs_to_u64(rv));
+          w.aux3 = wide ? lit_pair(rv) : lit(limbs_to_u64(rv));
         }
         wp.code.push_back(w);
         wp.commits.push_back(WCommitDev{cap_words, L.offset, L.limbs, 0});
@@ -233,10 +305,11 @@ struct Emitter {
     } else {
       const PackedMemory& M = P.memories[e.dst];
       WInstr w = base(W_MEMWR, M.data_layout.width);
-      w.a = S(e.enable);
-      w.b = S(e.addr);
-      w.c = S(e.value);
+      w.a = opnd(e.enable, kWPairA, &w.flags);
+      w.b = opnd(e.addr, kWPairB, &w.flags);
+      w.c = opnd(e.value, kWPairC, &w.flags);
       w.aux = e.dst;
+      if (M.data_layout.width > 64 || w.flags) w.flags |= kWWide;
       wp.code.push_back(w);
       release_if_last(e.enable, at);
       release_if_last(e.addr, at);
@@ -323,9 +396,9 @@ WordProgram build_word_program(const MachineProgram& mp) {
   WordProgram wp;
   const PackedProgram& P = mp.source;
   for (auto& s : P.signals)
-    if (s.layout.width > 64) throw RrtlError("E_WORD_SCOPE", "signal `" + s.name + "` is wider than 64 bits");
+    if (s.layout.width > 128) throw RrtlError("E_WORD_SCOPE", "signal `" + s.name + "` is wider than 128 bits");
   for (auto& m : P.memories) {
-    if (m.data_layout.width > 64) throw RrtlError("E_WORD_SCOPE", "memory `" + m.name + "` is wider than 64 bits");
+    if (m.data_layout.width > 128) throw RrtlError("E_WORD_SCOPE", "memory `" + m.name + "` is wider than 128 bits");
     if (m.depth > 0xFFFFFFFFull || m.offset + m.depth * m.data_layout.limbs > 0xFFFFFFFFull)
       throw RrtlError("E_WORD_SCOPE", "memory `" + m.name + "` is too deep");
     wp.mems.push_back(WMemDev{(uint32_t)m.offset, (uint32_t)m.depth, m.data_layout.limbs, m.data_layout.width});

@@ -1,6 +1,7 @@
 // Word program: lowering of a machine program for the lane-per-thread engine.
 //
-// Values of up to 64 bits live in 64-bit value slots; signals and memories
+// Values of up to 64 bits live in 64-bit value slots, values of 65 to 128
+// bits in slot pairs (see kWWide in word_dev.h); signals and memories
 // stay in their packed u32-limb layout (crates/rrtl-sim-ir/src/lib.rs:12698-12722),
 // stored word-major [word][lane] so a warp's accesses coalesce.
 //
@@ -35,7 +36,7 @@ struct WordProgram {
   uint64_t source_instrs = 0;
 };
 
-// Throws RrtlError("E_WORD_SCOPE", ...) for values wider than 64 bits.
+// Throws RrtlError("E_WORD_SCOPE", ...) for values wider than 128 bits.
 WordProgram build_word_program(const MachineProgram& mp);
 
 }  // namespace rrtl

@@ -149,3 +149,57 @@ def random_word_design(seed, n_inputs=4, n_regs=5, n_wires=14, n_mems=1, max_wid
         outs.append((f"out{i}", w))
     return d, {"inputs": inputs, "outputs": outs, "regs": [(f"r{i}", w) for i, (_, w) in enumerate(regs)],
                "mems": [(f"mem{i}", aw, dw, (1 << aw)) for i, (_, aw, dw) in enumerate(mems)], "top": top}
+
+
+def wide_ops_design(w, top="WideOps"):
+    """Registers of every operation class at width `w` (up to 128 bits):
+    add, sub, mul, unsigned and signed lt, eq, sext, concat, slice, trunc,
+    zext, mux, an accumulator and a 16-entry memory written and read each
+    cycle. Inputs a, b, din (w bits), sel, we (1 bit), addr (4 bits)."""
+    from rrtl_gb300.builder import sint
+
+    d = Design()
+    m = d.module(top)
+    clk = m.input("clk", uint(1))
+    rst = m.input("rst", uint(1))
+    a = m.input("a", uint(w))
+    b = m.input("b", uint(w))
+    din = m.input("din", uint(w))
+    sel = m.input("sel", uint(1))
+    we = m.input("we", uint(1))
+    addr = m.input("addr", uint(4))
+    mem = m.mem("mem", 4, uint(w), 16)
+    m.mem_write(mem, clk, we, addr, din)
+    ext = min(128, w + 37)
+    half = w // 2
+    exprs = {
+        "r_add": (a + b, w),
+        "r_sub": (a - b, w),
+        "r_mul": (a * b, w),
+        "r_ltu": (a.lt_expr(b), 1),
+        "r_lts": (a.as_sint().lt_expr(b.as_sint()), 1),
+        "r_eq": (a.eq_expr(b), 1),
+        "r_sext": (a.sext(ext).as_uint(), ext),
+        "r_zext": (b.slice(0, min(w, 40)).zext(ext), ext),
+        "r_cat": (concat([a.slice(0, half), sel, b.slice(w - (w - half - 1), w - half - 1)]), w),
+        "r_slice": (a.slice(w // 3, w - w // 3), w - w // 3),
+        "r_trunc": (b.trunc(max(1, w - 70)), max(1, w - 70)),
+        "r_mux": (mux(sel, a, b), w),
+        "r_mem": (mem_read(mem, addr), w),
+    }
+    regs = []
+    for name, (e, ew) in exprs.items():
+        r = m.reg(name, uint(ew))
+        m.clock(r, clk)
+        m.reset(r, rst, (1 << ew) - 3 if ew > 2 else 0)
+        m.next(r, e)
+        regs.append((name, ew))
+    acc = m.reg("r_acc", uint(w))
+    m.clock(acc, clk)
+    m.reset(acc, rst, 0)
+    m.next(acc, (acc + (a ^ b)) * lit_u(3, w))
+    regs.append(("r_acc", w))
+    o = m.output("o", uint(w))
+    m.assign(o, acc.value() ^ mem_read(mem, addr))
+    inputs = [("a", w), ("b", w), ("din", w), ("sel", 1), ("we", 1), ("addr", 4)]
+    return d, {"top": top, "inputs": inputs, "regs": regs, "outputs": [("o", w)]}

@@ -45,17 +45,28 @@ def test_sources_compile_for_sm103a(which):
     assert "error" not in log.lower()
 
 
-def test_wide_values_are_outside_the_word_engine():
+@pytest.mark.parametrize("w", [65, 96, 128])
+def test_wide_value_sources_compile_for_sm103a(w):
+    """Values of 65 to 128 bits run on 128-bit integers in slot pairs."""
+    from .designs import wide_ops_design
+
+    d, meta = wide_ops_design(w)
+    src, cub, log = _compile(d, meta["top"])
+    assert cub > 0, log
+    assert "u128" in src
+
+
+def test_values_past_128_bits_are_outside_the_word_engine():
     from rrtl_gb300.builder import Design, uint
 
     d = Design()
     m = d.module("Wide")
     clk = m.input("clk", uint(1))
-    a = m.input("a", uint(100))
-    r = m.reg("r", uint(100))
+    a = m.input("a", uint(130))
+    r = m.reg("r", uint(130))
     m.clock(r, clk)
     m.next(r, a)
-    o = m.output("o", uint(100))
+    o = m.output("o", uint(130))
     m.assign(o, r)
     with pytest.raises(sim.RrtlError) as e:
         sim.word_jit_emit(d, "Wide")
