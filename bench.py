@@ -498,17 +498,22 @@ def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, plain_jobs=24, graph
     return out
 
 
-def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000), round_us=5_000):
-    """Serving loop (the C5 shape): Poisson arrivals over three resident
-    designs (the 50k-gate netlist, the 8-stage CPU, a 500k-gate / 20k-FF
-    netlist of the same family); lanes log-uniform 64-16,384, cycles
+def serving_leg(ctx, sim, c2, loads, rates, duration_s, cycle_div=50, chunk=128, big=(500_000, 20_000),
+                round_us=5_000, policy=None, burst=64):
+    """Serving loop (C5): Poisson arrivals over three resident designs (the
+    50k-gate netlist, the 8-stage CPU on the word engine, a 500k-gate /
+    20k-FF netlist of the same family); lanes log-uniform 64-16,384, cycles
     log-uniform 1,000-50,000 divided by `cycle_div`, stimulus from a
     per-request seed (CPU requests: a per-request window of a hashed ROM).
-    Reports throughput and p50/p99 latency per arrival rate; a sample of
-    requests is re-run alone and must match bit for bit."""
-    from rrtl_gb300.workloads import (Rng, cpu_rom_hashed, gate_netlist, log_uniform_int, netlist_run_spec,
-                                      pipelined_cpu)
+    First the capacity: a burst of `burst` requests submitted at once, in
+    requests/s and lane-cycles/s; then arrivals at each fraction of that
+    capacity in `loads` and at each absolute rate in `rates`, each for
+    `duration_s` seconds of arrivals. Reports throughput and p50/p99 latency
+    overall and per design; a sample of requests is re-run alone and must
+    match bit for bit."""
+    from rrtl_gb300.workloads import Rng, cpu_rom_hashed, gate_netlist, log_uniform_int, netlist_run_spec, pipelined_cpu
 
+    policy = sim.SERVE_SHORTEST_FIRST if policy is None else policy
     t0 = time.perf_counter()
     d_big, m_big = gate_netlist(n_gates=big[0], n_ff=big[1], depth=40, seed=5)
     s_big, r_big = netlist_run_spec(m_big)
@@ -522,7 +527,9 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
     setup_s = time.perf_counter() - t0
     out = {"designs": {"c2": cd_c2.info.n_gates, "cpu": "8-stage CPU (word engine)", "big": cd_big.info.n_gates},
            "lanes": "log-uniform 64-16384", "cycles": f"log-uniform 1000-50000 / {cycle_div}",
-           "chunk_cycles": chunk, "round_us": round_us, "duration_s": duration_s, "setup_s": setup_s, "rates": []}
+           "chunk_cycles": chunk, "round_us": round_us,
+           "policy": "shortest remaining first" if policy == sim.SERVE_SHORTEST_FIRST else "fair share",
+           "duration_s": duration_s, "setup_s": setup_s, "rates": []}
 
     def spec(rng, i):
         k = rng.below(3)
@@ -538,8 +545,56 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
             mems = {"rom": rom_pool[:, :, off:off + lanes]}
         return server.submit(cd, lanes, cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH, memories=mems)
 
-    for rate in rates:
-        server = sim.Server(ctx, chunk_cycles=chunk, round_us=round_us)
+    def summarize(handles, t_start, t_end, server, check_sample):
+        infos = [h.info() for _, h in handles]
+        lat = np.array([(x["done_ns"] - x["submit_ns"]) / 1e6 for x in infos])
+        queue = np.array([(x["admit_ns"] - x["submit_ns"]) / 1e6 for x in infos])
+        lc = sum(sp[1] * sp[2] for sp, _ in handles)
+        st = server.stats
+        per = {}
+        for k, (name, _, _, _) in enumerate(designs):
+            l = np.array([lat[i] for i, (sp, _) in enumerate(handles) if sp[0] == k])
+            if len(l):
+                per[name] = {"requests": len(l), "p50_ms": float(np.percentile(l, 50)),
+                             "p99_ms": float(np.percentile(l, 99))}
+        same = True
+        if check_sample:
+            for sp, h in handles[:: max(1, len(handles) // 4)][:4]:
+                k, lanes, cycles, seed = sp
+                name, cd, stim, rec = designs[k]
+                g = sim.GpuBatchSimulator(cd, lanes=lanes)
+                if name == "cpu":
+                    off = seed % (rom_pool.shape[2] - lanes + 1)
+                    g.set_memory_limbs("rom", rom_pool[:, :, off:off + lanes])
+                ref = g.run(cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH)
+                same = same and np.array_equal(ref["hash"], h.outputs["hash"])
+                del g
+        return {"requests": len(handles), "failed": st["failed"], "throughput": lc / (t_end - t_start),
+                "unit": "lane-cycles/s", "wall_s": t_end - t_start,
+                "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                "p50_queue_ms": float(np.percentile(queue, 50)) if len(queue) else None,
+                "per_design": per, "rounds": st["rounds"], "gpu_busy_frac": st["busy_ns"] / 1e9 / (t_end - t_start),
+                "bitexact_sample": bool(same)}
+
+    # capacity: a burst of requests submitted at once
+    server = sim.Server(ctx, chunk_cycles=chunk, round_us=round_us, policy=policy)
+    rng = Rng(424242)
+    handles = []
+    t_start = time.perf_counter()
+    for i in range(burst):
+        sp = spec(rng, i)
+        handles.append((sp, submit(server, *sp)))
+    server.drain()
+    t_end = time.perf_counter()
+    cap = summarize(handles, t_start, t_end, server, False)
+    server.close()
+    capacity = burst / (t_end - t_start)
+    out["capacity"] = {"requests_per_s": capacity, "lane_cycles_per_s": cap["throughput"], "burst": burst,
+                       "wall_s": cap["wall_s"], "p99_ms": cap["p99_ms"], "per_design": cap["per_design"]}
+    plan = [("load", f, f * capacity) for f in loads] + [("rate", r, r) for r in rates]
+    for kind, tag, rate in plan:
+        server = sim.Server(ctx, chunk_cycles=chunk, round_us=round_us, policy=policy)
         rng = Rng(int(rate * 1000) + 1)
         handles = []
         t_start = time.perf_counter()
@@ -549,39 +604,20 @@ def serving_leg(ctx, sim, c2, rates, duration_s, cycle_div=50, chunk=128, big=(5
             t_next += -math.log(1.0 - rng.uniform()) / rate
             if t_next - t_start > duration_s:
                 break
-            k, lanes, cycles, seed = spec(rng, i)
+            sp = spec(rng, i)
             i += 1
             wait = t_next - time.perf_counter()
             if wait > 0:
                 time.sleep(wait)
-            handles.append(((k, lanes, cycles, seed), submit(server, k, lanes, cycles, seed)))
+            handles.append((sp, submit(server, *sp)))
         server.drain()
         t_end = time.perf_counter()
-        infos = [h.info() for _, h in handles]
-        lat = np.array([(x["done_ns"] - x["submit_ns"]) / 1e6 for x in infos])
-        queue = np.array([(x["admit_ns"] - x["submit_ns"]) / 1e6 for x in infos])
-        lc = sum(sp[1] * sp[2] for sp, _ in handles)
-        st = server.stats
-        # bit-exact: a sample of requests re-run alone on fresh batches
-        same = True
-        for sp, h in handles[:: max(1, len(handles) // 4)][:4]:
-            k, lanes, cycles, seed = sp
-            name, cd, stim, rec = designs[k]
-            g = sim.GpuBatchSimulator(cd, lanes=lanes)
-            if name == "cpu":
-                off = seed % (rom_pool.shape[2] - lanes + 1)
-                g.set_memory_limbs("rom", rom_pool[:, :, off:off + lanes])
-            ref = g.run(cycles, seed=seed, stim=stim, record=rec, mode=sim.REC_HASH)
-            same = same and np.array_equal(ref["hash"], h.outputs["hash"])
-            del g
+        row = summarize(handles, t_start, t_end, server, True)
+        row["rate_per_s"] = rate
+        if kind == "load":
+            row["load_of_capacity"] = tag
+        out["rates"].append(row)
         server.close()
-        out["rates"].append({"rate_per_s": rate, "requests": len(handles), "failed": st["failed"],
-                             "throughput": lc / (t_end - t_start), "unit": "lane-cycles/s",
-                             "wall_s": t_end - t_start, "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
-                             "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
-                             "p50_queue_ms": float(np.percentile(queue, 50)) if len(queue) else None,
-                             "rounds": st["rounds"], "gpu_busy_frac": st["busy_ns"] / 1e9 / (t_end - t_start),
-                             "bitexact_sample": bool(same)})
     return out
 
 
@@ -869,7 +905,11 @@ def main():
     ap.add_argument("--cpu8-parity-lanes", type=int, default=16384,
                     help="pipelined CPU: lanes checked against the oracle after the full run")
     ap.add_argument("--no-plain-jobs", action="store_true", help="job stream: skip the plain-path comparison")
-    ap.add_argument("--serve-rates", default="50,200", help="serving leg arrival rates per second ('' = skip it)")
+    ap.add_argument("--serve-loads", default="0.5,0.9",
+                    help="serving leg: arrival rates as fractions of the measured capacity ('' = none)")
+    ap.add_argument("--serve-rates", default="50,2000", help="serving leg: absolute arrival rates per second ('' = none)")
+    ap.add_argument("--serve-cycle-div", type=int, default=50, help="serving leg: request cycles divided by this")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-word-configs", action="store_true", help="skip the Counter and pipelined-CPU legs")
     ap.add_argument("--serve-seconds", type=float, default=5.0, help="serving leg arrival window per rate")
     ap.add_argument("--serve-round-us", type=int, default=5_000, help="serving loop target round time")
@@ -1064,10 +1104,11 @@ def main():
     if args.jobs > 0:
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs,
                                            plain_jobs=args.plain_jobs)
-    if args.serve_rates:
+    if not args.no_serving:
+        loads = [float(x) for x in args.serve_loads.split(",") if x]
         rates = [float(x) for x in args.serve_rates.split(",") if x]
-        out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), rates, args.serve_seconds,
-                                     round_us=args.serve_round_us)
+        out["serving"] = serving_leg(ctx, sim, (cd, stim, rec), loads, rates, args.serve_seconds,
+                                     cycle_div=args.serve_cycle_div, round_us=args.serve_round_us)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import binding as ob
 

@@ -345,8 +345,13 @@ typedef struct {
   uint32_t max_active;    /* requests on the device at once; 0 = no limit */
   uint32_t round_us;      /* target round time: gate-engine chunks are sized per request from its
                              program's cost so a round lasts about this long; 0 = fixed chunks */
-  uint32_t pad;
+  uint32_t policy;        /* RRTL_SERVE_FAIR: every active request shares each round;
+                             RRTL_SERVE_SHORTEST_FIRST: the gate-engine requests with the least work left
+                             (as many as fill the SMs twice) share the round, the others advance by a minimum
+                             chunk, so short requests are not held to the pace of long ones */
 } rrtl_server_opts;
+
+enum { RRTL_SERVE_FAIR = 0, RRTL_SERVE_SHORTEST_FIRST = 1 };
 
 typedef struct {
   uint32_t memory;        /* memory index (rrtl_design_memory) */

@@ -26,6 +26,7 @@
 #include <mutex>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 
 #include "runtime.h"
 
@@ -91,6 +92,7 @@ struct rrtl_server {
   uint32_t chunk = 256;
   uint32_t max_active = 0;
   double round_ms = 0;      // target round time (0: fixed chunks)
+  uint32_t policy = RRTL_SERVE_FAIR;
   double ms_per_cost = 0;   // calibrated device time of one unit of tile-cycle cost
   double ms_per_wcycle = 0; // calibrated device time of one cycle of a compiled word kernel
   std::mutex mu;
@@ -189,10 +191,31 @@ void rrtl_server::round() {
   // round, with c chosen so the round (its longest tile, or all tiles spread
   // over the SMs) lasts about round_ms
   double cost_per_tile_round = 0;
+  // shortest remaining first: the gate-engine requests with the least work
+  // left, as many as fill the SMs twice, share the round; the others advance
+  // by the minimum chunk only, so short requests are not held to the pace of
+  // long ones
+  std::unordered_set<const Request*> front;
+  if (policy == RRTL_SERVE_SHORTEST_FIRST) {
+    std::vector<std::pair<double, const Request*>> rem;
+    for (auto& rp : active)
+      if (rp->gate && rp->fused)
+        rem.push_back({(double)(rp->run.cycles - rp->done_cycles) * rp->gp.v->tile_cycle_cost * rp->gp.R.n_tiles,
+                       rp.get()});
+    std::sort(rem.begin(), rem.end(), [](const std::pair<double, const Request*>& x,
+                                         const std::pair<double, const Request*>& y) { return x.first < y.first; });
+    double tiles = 0;
+    for (auto& x : rem) {
+      if (tiles >= 2.0 * ctx->sm_count) break;
+      front.insert(x.second);
+      tiles += x.second->gp.R.n_tiles;
+    }
+  }
+  auto in_front = [&](const Request* r) { return policy != RRTL_SERVE_SHORTEST_FIRST || front.count(r) > 0; };
   if (round_ms > 0 && ms_per_cost > 0) {
     double tiles = 0;
     for (auto& rp : active)
-      if (rp->gate && rp->fused) tiles += rp->gp.R.n_tiles;
+      if (rp->gate && rp->fused && in_front(rp.get())) tiles += rp->gp.R.n_tiles;
     cost_per_tile_round = round_ms / ms_per_cost / std::max(1.0, tiles / std::max<uint32_t>(1, ctx->sm_count));
   }
   for (auto& rp : active) {
@@ -205,7 +228,9 @@ void rrtl_server::round() {
       continue;
     }
     r.chunk = std::min<uint64_t>(left, chunk);
-    if (r.gate && cost_per_tile_round > 0) {
+    if (r.gate && !in_front(&r)) {
+      r.chunk = std::min<uint64_t>(left, kMinChunk);
+    } else if (r.gate && cost_per_tile_round > 0) {
       const uint64_t want = (uint64_t)std::max((double)kMinChunk, cost_per_tile_round / std::max(r.gp.v->tile_cycle_cost, 1e-9));
       r.chunk = std::min<uint64_t>(left, want);
     }
@@ -439,6 +464,8 @@ rrtl_status rrtl_server_create(rrtl_ctx* ctx, const rrtl_server_opts* opts, rrtl
     s->chunk = opts && opts->chunk_cycles ? opts->chunk_cycles : 256;
     s->max_active = opts ? opts->max_active : 0;
     s->round_ms = opts ? opts->round_us / 1000.0 : 0.0;
+    s->policy = opts ? opts->policy : RRTL_SERVE_FAIR;
+    if (s->policy > RRTL_SERVE_SHORTEST_FIRST) fail(RRTL_E_ARG, "E_ARG: unknown serving policy");
     // the first NVRTC compile of a process pays for loading the compiler;
     // pay it here rather than in the first word request's admission
     jit_warm();

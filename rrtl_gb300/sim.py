@@ -26,6 +26,7 @@ REC_TRACE, REC_HASH, REC_DETECT, REC_CHECK = 1, 2, 4, 8
 PATH_FUSED, PATH_PLAIN, PATH_PLAIN_GRAPH, PATH_WORD_INTERP = 0, 1, 2, 3
 JOB_QUEUED, JOB_RUNNING, JOB_DONE, JOB_FAILED = 0, 1, 2, 3
 ENGINE_GATE, ENGINE_WORD = 1, 2
+SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 _STATUS = {
     1: "RRTL_E_ARG",
@@ -733,7 +734,7 @@ class ServerStats(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget", c_uint64), ("chunk_cycles", c_uint32), ("max_active", c_uint32),
-                ("round_us", c_uint32), ("pad", c_uint32)]
+                ("round_us", c_uint32), ("policy", c_uint32)]
 
 
 class _RunShape:
@@ -765,9 +766,11 @@ class Server:
     """The serving loop (rrtl_server_*): continuous batching of requests on one GPU."""
 
     def __init__(self, ctx: Optional[Context] = None, hbm_budget: int = 0, chunk_cycles: int = 0, max_active: int = 0,
-                 round_us: int = 0):
+                 round_us: int = 0, policy: int = 0):
+        """policy: SERVE_FAIR (every active request shares each round) or
+        SERVE_SHORTEST_FIRST (requests with the least work left go first)."""
         self.ctx = ctx or default_context()
-        o = ServerOpts(hbm_budget, chunk_cycles, max_active, round_us, 0)
+        o = ServerOpts(hbm_budget, chunk_cycles, max_active, round_us, policy)
         self.h = c_void_p()
         check(lib().rrtl_server_create(self.ctx.h, byref(o), byref(self.h)))
 

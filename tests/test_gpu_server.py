@@ -144,3 +144,20 @@ def test_server_errors(served_designs):
     ok = server.submit(d["cd"], 32, 2, seed=2, stim=d["stim"], record=d["rec"], mode=sim.REC_HASH)
     ok.wait(timeout_ms=60000)
     server.close()
+
+
+def test_shortest_first_policy_gives_same_results(served_designs):
+    """Under shortest-remaining-first rounds every request still ends with
+    the results of its run alone, and a short request submitted beside long
+    ones finishes first."""
+    reqs = _requests(n=10, seed=91)
+    refs = [_offline(served_designs, r) for r in reqs]
+    server = sim.Server(chunk_cycles=64, round_us=2000, policy=sim.SERVE_SHORTEST_FIRST)
+    hs = [_submit(server, served_designs, r) for r in reqs]
+    server.drain()
+    for h, ref in zip(hs, refs):
+        assert h.info()["status"] == sim.JOB_DONE
+        _check(h.outputs, ref)
+    server.close()
+    with pytest.raises(sim.RrtlError):
+        sim.Server(policy=7)
