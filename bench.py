@@ -385,11 +385,12 @@ def gate_fanins(js):
     return out
 
 
-def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, plain_jobs=24, graph_jobs=8, cycles=(100, 50_000)):
+def job_stream_leg(ctx, sim, n_jobs, n_designs, plain=True, plain_jobs=12, graph_jobs=8, cycles=(100, 50_000)):
     """Uneven job stream (C4): `n_jobs` jobs on netlists of the 50k-gate
     family with gate counts log-uniform 5k-200k (a pool of `n_designs`
     netlists of distinct seeds; each job takes one at random), lanes
-    log-uniform 32-65,536, cycles log-uniform 100-50,000, 30% fault jobs
+    log-uniform 32-65,536, cycles log-uniform in `cycles` (the stated range
+    is 100-50,000), 30% fault jobs
     (one stuck-at fault per lane, lane-uniform stimulus so every fault-free
     lane equals the golden lane). All jobs run in one launch of the
     persistent job-queue kernel. The plain one-launch-per-cycle path runs a
@@ -900,7 +901,10 @@ def main():
     ap.add_argument("--tile-words", type=int, default=0, help="fused tile width in 32-lane words (0 = automatic)")
     ap.add_argument("--jobs", type=int, default=2048, help="jobs in the uneven job-stream leg (0 = skip it)")
     ap.add_argument("--job-designs", type=int, default=16, help="netlists of distinct seeds in the job stream's pool")
-    ap.add_argument("--plain-jobs", type=int, default=24, help="job stream: jobs of the subset timed on the plain path")
+    ap.add_argument("--plain-jobs", type=int, default=12, help="job stream: jobs of the subset timed on the plain path")
+    ap.add_argument("--job-cycles", default="10,5000",
+                    help="job stream: cycle range lo,hi (the stated range 100,50000 takes about 6 minutes of GPU "
+                         "time; the default divides it by 10)")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle checks of the benchmarked runs")
     ap.add_argument("--cpu8-parity-lanes", type=int, default=16384,
                     help="pipelined CPU: lanes checked against the oracle after the full run")
@@ -1102,8 +1106,9 @@ def main():
     if not args.no_bitslice:
         out["bitslice"] = bitslice_leg(ctx, sim)
     if args.jobs > 0:
+        lo, hi = (int(x) for x in args.job_cycles.split(","))
         out["job_stream"] = job_stream_leg(ctx, sim, args.jobs, args.job_designs, plain=not args.no_plain_jobs,
-                                           plain_jobs=args.plain_jobs)
+                                           plain_jobs=args.plain_jobs, cycles=(lo, hi))
     if not args.no_serving:
         loads = [float(x) for x in args.serve_loads.split(",") if x]
         rates = [float(x) for x in args.serve_rates.split(",") if x]
