@@ -326,6 +326,38 @@ rrtl_status rrtl_queue_poll(rrtl_ctx* ctx, uint64_t id, uint32_t* status);
 /* Device time of the last launch (ms), valid after rrtl_queue_wait. */
 rrtl_status rrtl_queue_last_ms(rrtl_ctx* ctx, float* ms);
 
+/* ---- lane-shard runtime ------------------------------------------------------
+ * The reference's DistributedRuntime splits a run's lanes into contiguous
+ * shards (RuntimeShardInfo{worker, start_lane, lanes},
+ * crates/rrtl-runtime/src/lib.rs:168-175) and runs each on a worker engine
+ * (:6785-7760); RuntimeEngine::Gpu holds its GPU engine (:7785-7792). Here a
+ * runtime holds one lane batch per shard of one design on one GPU: a run goes
+ * to every shard with lane_base = the run's lane_base + the shard's first
+ * lane (so stimulus and hashes follow global lanes); gate-engine shards run
+ * as the jobs of one device job-queue launch, word-engine shards one after
+ * another. Outputs are in global-lane order: out_hash is the wrapping sum of
+ * the shards' hashes (the hash of the whole run), detect and out_trace hold
+ * every shard's lanes at their global positions, and input_trace columns are
+ * cut per shard. Shards start on multiples of 32 lanes. */
+typedef struct {
+  uint32_t worker;      /* shard index */
+  uint32_t lanes;
+  uint64_t start_lane;  /* global index of the shard's lane 0 */
+} rrtl_shard_info;
+
+typedef struct rrtl_runtime rrtl_runtime;
+
+/* Contiguous shards of total_lanes lanes over n shards (out: n entries). */
+rrtl_status rrtl_shard_plan(uint64_t total_lanes, uint32_t n, rrtl_shard_info* out);
+rrtl_status rrtl_runtime_create(rrtl_design* design, uint64_t total_lanes, uint32_t shards, rrtl_runtime** out);
+rrtl_status rrtl_runtime_destroy(rrtl_runtime* rt);
+/* Shard k's plan entry and lane batch (the batch belongs to the runtime). */
+rrtl_status rrtl_runtime_shard(rrtl_runtime* rt, uint32_t k, rrtl_shard_info* info, rrtl_batch** batch);
+/* Stuck-at faults on global lanes, handed to the shards that hold them (gate engine). */
+rrtl_status rrtl_runtime_set_faults(rrtl_runtime* rt, const rrtl_fault* faults, size_t n);
+/* One run over every shard; host buffers as for rrtl_batch_run, sized for all lanes. */
+rrtl_status rrtl_runtime_run(rrtl_runtime* rt, const rrtl_run* run);
+
 /* ---- serving loop ----------------------------------------------------------
  * Continuous batching of simulation requests on one GPU. Producer threads
  * submit requests (a design, a lane count, a run and optional faults); a

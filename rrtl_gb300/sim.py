@@ -93,6 +93,10 @@ class Fault(ctypes.Structure):
     _fields_ = [("lane", c_uint32), ("signal", c_uint32), ("value", c_uint32)]
 
 
+class ShardInfo(ctypes.Structure):
+    _fields_ = [("worker", c_uint32), ("lanes", c_uint32), ("start_lane", c_uint64)]
+
+
 class DesignInfo(ctypes.Structure):
     _fields_ = [
         ("n_signals", c_uint32),
@@ -169,6 +173,12 @@ EXPORTS = (
     "rrtl_gate_jit_emit",
     "rrtl_design_load_bitslice",
     "rrtl_bitslice_json",
+    "rrtl_shard_plan",
+    "rrtl_runtime_create",
+    "rrtl_runtime_destroy",
+    "rrtl_runtime_shard",
+    "rrtl_runtime_set_faults",
+    "rrtl_runtime_run",
 )
 
 _lib = None
@@ -244,6 +254,12 @@ def lib():
         "rrtl_bitslice_json": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
         "rrtl_gate_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
+        "rrtl_shard_plan": [c_uint64, c_uint32, P(ShardInfo)],
+        "rrtl_runtime_create": [c_void_p, c_uint64, c_uint32, P(c_void_p)],
+        "rrtl_runtime_destroy": [c_void_p],
+        "rrtl_runtime_shard": [c_void_p, c_uint32, P(ShardInfo), P(c_void_p)],
+        "rrtl_runtime_set_faults": [c_void_p, P(Fault), c_size_t],
+        "rrtl_runtime_run": [c_void_p, P(Run)],
     }
     for name, args in sigs.items():
         fn = getattr(L, name)
@@ -988,3 +1004,53 @@ class BitSliceSimulator:
 
     def tick_many(self, steps: int):
         self.sim.tick_many(steps)
+
+
+def shard_plan(total_lanes: int, shards: int) -> list:
+    """Contiguous lane shards [(worker, start_lane, lanes)], each starting on a 32-lane word."""
+    arr = (ShardInfo * shards)()
+    check(lib().rrtl_shard_plan(total_lanes, shards, arr))
+    return [(x.worker, x.start_lane, x.lanes) for x in arr]
+
+
+class Runtime:
+    """Lane-shard runtime (rrtl_runtime_*): the reference's DistributedRuntime
+    shard plan on one GPU, one lane batch per shard; runs and outputs use
+    global lanes."""
+
+    def __init__(self, design: "CompiledDesign", total_lanes: int, shards: int):
+        self.design = design
+        self.lanes = total_lanes
+        self.h = c_void_p()
+        check(lib().rrtl_runtime_create(design.h, total_lanes, shards, byref(self.h)))
+        self.n = shards
+        self._shape = _RunShape(design, total_lanes)
+
+    def shard(self, k: int):
+        info = ShardInfo()
+        check(lib().rrtl_runtime_shard(self.h, k, byref(info), None))
+        return info.worker, info.start_lane, info.lanes
+
+    def set_faults(self, faults: Sequence[tuple]):
+        arr = (Fault * max(1, len(faults)))(*[Fault(l, self._shape._sig(s), v) for l, s, v in faults])
+        check(lib().rrtl_runtime_set_faults(self.h, arr, len(faults)))
+
+    def run(self, cycles: int, seed: int = 0, stim: Iterable = (), record: Iterable = (), mode: int = 0,
+            input_trace: Optional[np.ndarray] = None, lane_base: int = 0):
+        record = list(record)
+        out = self._shape.alloc_outputs(cycles, record, mode)
+        r = self._shape.make_run(cycles, seed, stim, record, mode, input_trace, out["trace"], out["hash"],
+                                 out["detect"], lane_base)
+        check(lib().rrtl_runtime_run(self.h, byref(r)))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().rrtl_runtime_destroy(self.h)
+            self.h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
