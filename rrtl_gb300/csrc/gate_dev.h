@@ -23,7 +23,10 @@ __host__ __device__
 constexpr uint32_t gate_fused_vec(uint32_t W) {
   return (uint32_t)RRTL_FUSED_V <= W ? (uint32_t)RRTL_FUSED_V : (W >= 2 ? 2u : 1u);
 }
-constexpr uint32_t kGateFusedCtasPerSm = 32 / kGateFusedWarps;
+#ifndef RRTL_FUSED_CTAS_PER_SM
+#define RRTL_FUSED_CTAS_PER_SM (32 / RRTL_FUSED_WARPS)
+#endif
+constexpr uint32_t kGateFusedCtasPerSm = RRTL_FUSED_CTAS_PER_SM;
 
 struct GateStimDev {
   uint32_t slot;  // on-chip slot (fused path)
