@@ -376,7 +376,7 @@ void refine_groups(const GateProgram& gp, std::vector<std::vector<uint32_t>>& gr
     rng ^= rng << 17;
     return rng;
   };
-  const size_t tries = cells * (G <= 4 ? 12 : G <= 8 ? 4 : 0);
+  const size_t tries = cells * (G <= 4 ? 40 : G <= 8 ? 4 : 0);
   for (size_t t = 0; t < tries; ++t) {
     const size_t a = next() % ng, b = next() % ng;
     if (a == b || (cost[a] <= floor && cost[b] <= floor)) continue;
@@ -393,6 +393,109 @@ void refine_groups(const GateProgram& gp, std::vector<std::vector<uint32_t>>& gr
   }
 }
 
+// Residue bookkeeping for placing rows: per consumer bucket (level, truth
+// table, operand position) the number of operand rows placed at each bank
+// residue so far. A net's cost at residue r is the count at r summed over its
+// consumers' buckets.
+struct ResidueBalance {
+  uint32_t G;
+  std::vector<uint32_t> cons_off, cons_bucket;  // per net: buckets of its consumer inputs
+  std::vector<uint32_t> cnt;                    // bucket * G + residue
+  std::vector<uint32_t> placed;                 // rows placed per residue (tie-break: even packing)
+
+  ResidueBalance(const GateProgram& gp, uint32_t g) : G(g), placed(g, 0) {
+    std::vector<uint64_t> keys;
+    std::vector<std::pair<uint32_t, uint64_t>> uses;  // (net, key)
+    for (const GateCell& c : gp.cells) {
+      const bool use[3] = {(c.lut & 0x0F) != ((c.lut >> 4) & 0x0F), (c.lut & 0x33) != ((c.lut >> 2) & 0x33),
+                           (c.lut & 0x55) != ((c.lut >> 1) & 0x55)};
+      for (int p = 0; p < 3; ++p) {
+        if (!use[p]) continue;
+        const uint64_t key = ((uint64_t)(uint32_t)c.level << 10) | ((uint64_t)c.lut << 2) | (uint64_t)p;
+        uses.push_back({c.in[p], key});
+        keys.push_back(key);
+      }
+    }
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    cons_off.assign(gp.n_nets + 1, 0);
+    for (auto& u : uses) ++cons_off[u.first + 1];
+    for (size_t n = 0; n < gp.n_nets; ++n) cons_off[n + 1] += cons_off[n];
+    cons_bucket.resize(uses.size());
+    std::vector<uint32_t> fill(cons_off.begin(), cons_off.end() - 1);
+    for (auto& u : uses)
+      cons_bucket[fill[u.first]++] =
+          (uint32_t)(std::lower_bound(keys.begin(), keys.end(), u.second) - keys.begin());
+    cnt.assign(keys.size() * G, 0);
+  }
+  uint64_t cost(uint32_t n, uint32_t r) const {
+    uint64_t c = 0;
+    for (uint32_t i = cons_off[n]; i < cons_off[n + 1]; ++i) c += cnt[(size_t)cons_bucket[i] * G + r];
+    return c;
+  }
+  void place(uint32_t n, uint32_t r) {
+    for (uint32_t i = cons_off[n]; i < cons_off[n + 1]; ++i) ++cnt[(size_t)cons_bucket[i] * G + r];
+    ++placed[r];
+  }
+  // One net, any residue.
+  uint32_t pick(uint32_t n) {
+    uint32_t best = 0;
+    uint64_t bc = ~0ull;
+    for (uint32_t r = 0; r < G; ++r) {
+      const uint64_t c = cost(n, r) * 65536u + placed[r];
+      if (c < bc) {
+        bc = c;
+        best = r;
+      }
+    }
+    place(n, best);
+    return best;
+  }
+  // The outputs of one group: distinct residues (not 0 when `padded`), the
+  // cheapest assignment (every permutation for four cells, greedy beyond).
+  std::vector<uint32_t> assign(const std::vector<uint32_t>& outs, bool padded) {
+    const size_t k = outs.size();
+    std::vector<uint32_t> res(k);
+    const uint32_t r0 = padded ? 1u : 0u;
+    std::vector<std::vector<uint64_t>> c(k, std::vector<uint64_t>(G));
+    for (size_t i = 0; i < k; ++i)
+      for (uint32_t r = r0; r < G; ++r) c[i][r] = cost(outs[i], r);
+    if (G <= 4) {
+      std::vector<uint32_t> perm;
+      for (uint32_t r = r0; r < G; ++r) perm.push_back(r);
+      uint64_t best = ~0ull;
+      do {
+        uint64_t t = 0;
+        for (size_t i = 0; i < k; ++i) t += c[i][perm[i]];
+        if (t < best) {
+          best = t;
+          std::copy(perm.begin(), perm.begin() + (long)k, res.begin());
+        }
+      } while (std::next_permutation(perm.begin(), perm.end()));
+    } else {
+      std::vector<uint8_t> used_r(G, 0), done(k, 0);
+      for (size_t step = 0; step < k; ++step) {
+        uint64_t best = ~0ull;
+        size_t bi = 0;
+        uint32_t br = r0;
+        for (size_t i = 0; i < k; ++i) {
+          if (done[i]) continue;
+          for (uint32_t r = r0; r < G; ++r)
+            if (!used_r[r] && c[i][r] < best) {
+              best = c[i][r];
+              bi = i;
+              br = r;
+            }
+        }
+        done[bi] = 1;
+        used_r[br] = 1;
+        res[bi] = br;
+      }
+    }
+    for (size_t i = 0; i < k; ++i) place(outs[i], res[i]);
+    return res;
+  }
+};
 
 GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   const PackedProgram& P = mp.source;
@@ -478,39 +581,41 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
       r.reset_value = e.has_reset && !e.reset.value.empty() && (e.reset.value[0] & 1);
       gp.regs.push_back(r);
     }
-  gp.n_real_cells = (uint32_t)gp.cells.size();
 
   // ---- levelize
-  gp.net_level.assign(gp.n_nets, -1);
-  std::vector<int32_t> cell_of_net(gp.n_nets, -1);
-  for (size_t i = 0; i < gp.cells.size(); ++i) cell_of_net[gp.cells[i].out] = (int32_t)i;
-  std::vector<int32_t> memo(gp.cells.size(), -2);
   // cells were created in dependency order except for signal reads of later
   // stores (rejected above), so one forward pass suffices; iterate to a fixpoint
   // to be robust to creation order.
-  bool changed = true;
-  for (auto& c : gp.cells) c.level = 0;
-  while (changed) {
-    changed = false;
-    for (auto& c : gp.cells) {
-      int32_t lv = 0;
-      for (int k = 0; k < 3; ++k) {
-        int32_t pc = cell_of_net[c.in[k]];
-        if (pc >= 0) lv = std::max(lv, gp.cells[pc].level + 1);
-      }
-      if (lv != c.level) {
-        if (lv > (int32_t)gp.cells.size()) throw RrtlError("E_GATE_SCOPE", "combinational cycle between cells");
-        c.level = lv;
-        changed = true;
+  auto levelize = [&]() {
+    gp.net_level.assign(gp.n_nets, -1);
+    std::vector<int32_t> cell_of_net(gp.n_nets, -1);
+    for (size_t i = 0; i < gp.cells.size(); ++i) cell_of_net[gp.cells[i].out] = (int32_t)i;
+    bool changed = true;
+    for (auto& c : gp.cells) c.level = 0;
+    while (changed) {
+      changed = false;
+      for (auto& c : gp.cells) {
+        int32_t lv = 0;
+        for (int k = 0; k < 3; ++k) {
+          int32_t pc = cell_of_net[c.in[k]];
+          if (pc >= 0) lv = std::max(lv, gp.cells[pc].level + 1);
+        }
+        if (lv != c.level) {
+          if (lv > (int32_t)gp.cells.size()) throw RrtlError("E_GATE_SCOPE", "combinational cycle between cells");
+          c.level = lv;
+          changed = true;
+        }
       }
     }
-  }
-  int32_t max_level = -1;
-  for (auto& c : gp.cells) {
-    max_level = std::max(max_level, c.level);
-    gp.net_level[c.out] = c.level;
-  }
-  gp.n_levels = (uint32_t)(max_level + 1);
+    int32_t max_level = -1;
+    for (auto& c : gp.cells) {
+      max_level = std::max(max_level, c.level);
+      gp.net_level[c.out] = c.level;
+    }
+    gp.n_levels = (uint32_t)(max_level + 1);
+  };
+  levelize();
+  gp.n_real_cells = (uint32_t)gp.cells.size();
 
   // ---- liveness: consumer level; D nets, reset nets and output-port nets live to the end
   const int32_t kEnd = (int32_t)gp.n_levels;
@@ -535,17 +640,36 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   // read in the settle and the commit its slot can host nets that die before
   // the end of the cycle. End-live nets (D, reset, outputs) never take such a
   // slot, so every register slot is free again when the commit writes it.
+  //
+  // A group's cells read their operand rows in one access per position, so
+  // what decides the conflicts of a truth-table run is how evenly the
+  // residues of its operand rows spread: with c cells per residue among n
+  // groups, max(c) - n groups must take a residue twice. Each net's residue is
+  // chosen where its row is placed (sources up front, cell outputs as their
+  // group is placed) to even out the residues seen by the (level, table,
+  // position) buckets of its consumers.
+  ResidueBalance bal(gp, G);
   gp.net_slot.assign(gp.n_nets, -1);
   std::vector<uint8_t> is_reg_q(gp.n_nets, 0);
   for (auto& r : gp.regs) is_reg_q[r.q_net] = 1;
   uint32_t next_slot = 1;  // slot 0 is the scratch slot for padding cells
   std::vector<std::vector<uint32_t>> q_free_after(gp.n_levels + 1);  // register slots released before level L
   std::vector<uint8_t> slot_is_q;
+  std::vector<uint32_t> src_next(G);  // next unused source slot of each residue
+  for (uint32_t r = 0; r < G; ++r) src_next[r] = r == 0 ? G : r;
   for (uint32_t n = 0; n < gp.n_nets; ++n)
     if (gp.net_is_source[n]) {
-      gp.net_slot[n] = (int32_t)next_slot++;
+      const uint32_t r = bal.pick(n);
+      gp.net_slot[n] = (int32_t)src_next[r];
+      src_next[r] += G;
+      next_slot = std::max(next_slot, (uint32_t)gp.net_slot[n] + 1);
       if (n != kNetConst0 && n != kNetConst1) gp.source_nets.push_back(n);
-      slot_is_q.resize(next_slot, 0);
+    }
+  slot_is_q.assign(next_slot, 0);
+  std::vector<uint8_t> src_used(next_slot, 0);
+  for (uint32_t n = 0; n < gp.n_nets; ++n)
+    if (gp.net_is_source[n]) {
+      src_used[gp.net_slot[n]] = 1;
       if (is_reg_q[n]) {
         slot_is_q[gp.net_slot[n]] = 1;
         if (last_use[n] < kEnd) q_free_after[std::max<int32_t>(last_use[n], -1) + 1].push_back((uint32_t)gp.net_slot[n]);
@@ -562,6 +686,9 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
     bool q = s < slot_is_q.size() && slot_is_q[s];
     (q ? free_q : free_general)[s % G].push_back(s);
   };
+  // source slots skipped by the residue choice are free from the start
+  for (uint32_t s2 = next_slot; s2-- > 1;)
+    if (!src_used[s2]) free_general[s2 % G].push_back(s2);
   auto take = [&](bool live_to_end, uint32_t res) -> uint32_t {
     if (!live_to_end && !free_q[res].empty()) {
       uint32_t s = free_q[res].back();
@@ -584,7 +711,7 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
   for (uint32_t i = 0; i < gp.cells.size(); ++i) cells_at[gp.cells[i].level].push_back(i);
   std::vector<GateCell> grouped;
   gp.level_group_begin.assign(gp.n_levels + 1, 0);
-  const int kLook = 48;
+  const int kLook = 200;
   // per operand position: distinct rows per residue in the group being built
   std::vector<uint32_t> cnt(3 * G);
   std::vector<uint32_t> stamp(3 * (size_t)65536, 0);
@@ -658,12 +785,15 @@ GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words) {
       refine_groups(gp, run_groups, sym, use, G, refine_rng);
       for (std::vector<uint32_t>& grp : run_groups) {
         orient_group(gp, grp, sym, use, G);
-        // outputs: distinct residues; residue 0 last when padding (scratch slot 0) shares the group
+        // outputs: distinct residues, residue 0 left to the padding (scratch
+        // slot 0) when the group is short, assigned to even out the consumers
         const bool padded = grp.size() < G;
+        std::vector<uint32_t> outs(grp.size());
+        for (size_t k = 0; k < grp.size(); ++k) outs[k] = gp.cells[grp[k]].out;
+        const std::vector<uint32_t> res_of = bal.assign(outs, padded);
         for (size_t k = 0; k < grp.size(); ++k) {
           GateCell c = gp.cells[grp[k]];
-          const uint32_t res = (uint32_t)((k + (padded ? 1 : 0)) % G);
-          gp.net_slot[c.out] = (int32_t)take(end_live(c.out), res);
+          gp.net_slot[c.out] = (int32_t)take(end_live(c.out), res_of[k]);
           if (slot_is_q.size() <= (size_t)gp.net_slot[c.out]) slot_is_q.resize(gp.net_slot[c.out] + 1, 0);
           grouped.push_back(c);
         }
