@@ -222,6 +222,20 @@ __device__ __forceinline__ uint4 lut_v(uint32_t t, uint4 a, uint4 b, uint4 c) {
   return make_uint4(lut_eval(t, a.x, b.x, c.x), lut_eval(t, a.y, b.y, c.y), lut_eval(t, a.z, b.z, c.z),
                     lut_eval(t, a.w, b.w, c.w));
 }
+// Synchronous reset on commit: where the reset net is active (flags: 2
+// active low), the register takes its reset value (flags: 4 one) instead of D.
+__device__ __forceinline__ uint32_t reset_select(uint32_t d, uint32_t m, uint32_t flags) {
+  if (flags & 2u) m = ~m;
+  const uint32_t rv = (flags & 4u) ? 0xFFFFFFFFu : 0u;
+  return (m & rv) | (~m & d);
+}
+__device__ __forceinline__ uint2 reset_select(uint2 d, uint2 m, uint32_t flags) {
+  return make_uint2(reset_select(d.x, m.x, flags), reset_select(d.y, m.y, flags));
+}
+__device__ __forceinline__ uint4 reset_select(uint4 d, uint4 m, uint32_t flags) {
+  return make_uint4(reset_select(d.x, m.x, flags), reset_select(d.y, m.y, flags), reset_select(d.z, m.z, flags),
+                    reset_select(d.w, m.w, flags));
+}
 __device__ __forceinline__ void store_net(uint32_t* p, uint32_t v) { p[0] = v; }
 __device__ __forceinline__ void store_net(uint32_t* p, uint2 v) {
   p[0] = v.x;
@@ -500,20 +514,21 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
         }
       }
     }
-    // commit (D and reset nets are never register nets, so one pass is safe)
+    // commit (D and reset nets are never register nets, so one pass is
+    // safe): a thread moves V words of one register with one vector access
+    // per row; the list is ordered so the registers of one wavefront have
+    // distinct D and Q residues
+    {
+      constexpr uint32_t RV = W / Sh::V;
+      T* const Sb = reinterpret_cast<T*>(S);
 #pragma unroll 4
-    for (uint32_t i = tid; i < P.n_regs * W; i += blockDim.x) {
-      const uint4 rr = __ldg(reinterpret_cast<const uint4*>(P.sregs) + i / W);
-      const GateRegDev r{rr.x, rr.y, rr.z, rr.w};
-      uint32_t ww = i % W;
-      uint32_t d = S[r.d * W + ww];
-      if (r.flags & 1u) {
-        uint32_t m = S[r.rst * W + ww];
-        if (r.flags & 2u) m = ~m;
-        uint32_t rv = (r.flags & 4u) ? 0xFFFFFFFFu : 0u;
-        d = (m & rv) | (~m & d);
+      for (uint32_t j = tid; j < P.n_regs * RV; j += blockDim.x) {
+        const uint4 rr = __ldg(reinterpret_cast<const uint4*>(P.sregs) + j / RV);
+        const uint32_t part = j % RV;
+        T d = Sb[rr.y * RV + part];
+        if (rr.w & 1u) d = reset_select(d, Sb[rr.z * RV + part], rr.w);
+        Sb[rr.x * RV + part] = d;
       }
-      S[r.q * W + ww] = d;
     }
     __syncthreads();
     if (R.has_forces) {

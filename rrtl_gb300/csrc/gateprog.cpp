@@ -897,6 +897,47 @@ static std::vector<std::vector<uint32_t>> split_piece(const GateProgram& gp, con
   return out;
 }
 
+std::vector<uint32_t> commit_order(const GateProgram& gp) {
+  const uint32_t G = gp.group;
+  const size_t n = gp.regs.size();
+  std::vector<uint32_t> out;
+  out.reserve(n);
+  std::vector<uint8_t> taken(n, 0);
+  const size_t kLook = 256;
+  size_t head = 0;
+  std::vector<uint8_t> used_d(G), used_q(G);
+  auto res = [&](uint32_t net) { return (uint32_t)gp.net_slot[net] % G; };
+  while (out.size() < n) {
+    while (taken[head]) ++head;
+    std::fill(used_d.begin(), used_d.end(), 0);
+    std::fill(used_q.begin(), used_q.end(), 0);
+    auto add = [&](size_t k) {
+      taken[k] = 1;
+      out.push_back((uint32_t)k);
+      used_d[res(gp.regs[k].d_net)] = 1;
+      used_q[res(gp.regs[k].q_net)] = 1;
+    };
+    add(head);
+    for (uint32_t pick = 1; pick < G && out.size() < n; ++pick) {
+      size_t best = n, seen = 0;
+      uint32_t best_cost = ~0u;
+      for (size_t k = head + 1; k < n && seen < kLook; ++k) {
+        if (taken[k]) continue;
+        ++seen;
+        const uint32_t cost = used_d[res(gp.regs[k].d_net)] + used_q[res(gp.regs[k].q_net)];
+        if (cost < best_cost) {
+          best_cost = cost;
+          best = k;
+          if (cost == 0) break;
+        }
+      }
+      if (best == n) break;
+      add(best);
+    }
+  }
+  return out;
+}
+
 PieceBlob build_piece_blob(const GateProgram& gp, uint32_t warps, double lead_weight, uint32_t steps_per,
                            double run_cost) {
   PieceBlob pb;

@@ -100,6 +100,11 @@ bool lut_is_canonical(uint8_t lut);
 // Throws RrtlError("E_GATE_SCOPE", ...) when the program is outside the gate engine's scope.
 GateProgram build_gate_program(const MachineProgram& mp, uint32_t tile_words = 8);
 
+// The registers in commit order: groups of G (one shared-memory wavefront of
+// the fused kernel's vector commit) whose D rows, and whose Q rows, fall in
+// distinct bank residues where the residues allow it.
+std::vector<uint32_t> commit_order(const GateProgram& gp);
+
 // Split every level into nearly equal pieces of at most `piece_groups` groups
 // and record the truth-table runs of each piece.
 void build_pieces(GateProgram& gp, uint32_t piece_groups);

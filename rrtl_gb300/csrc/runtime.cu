@@ -186,7 +186,8 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
     }
     std::vector<uint32_t> src_slot;
     for (uint32_t n : gp.source_nets) src_slot.push_back((uint32_t)gp.net_slot[n]);
-    for (auto& r : gp.regs) {
+    for (uint32_t k : commit_order(gp)) {
+      const GateReg& r = gp.regs[k];
       uint32_t fl = (r.has_reset ? 1u : 0u) | (r.active_low ? 2u : 0u) | (r.reset_value ? 4u : 0u);
       sregs.push_back(GateRegDev{(uint32_t)gp.net_slot[r.q_net], (uint32_t)gp.net_slot[r.d_net],
                                  (uint32_t)gp.net_slot[r.rst_net], fl});
