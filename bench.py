@@ -1079,7 +1079,8 @@ def main():
                                f"window {WINDOW}", "lanes_per_gpu": LANES, "cycles_per_step": CYCLES,
                    "global_lanes": LANES * ws, "parallelism": f"lane shards x{ws} (no collective; rank r simulates "
                                                      f"global lanes [r*{LANES}, (r+1)*{LANES}) of one run)",
-                   "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": "fused persistent kernel",
+                   "l2": "lane state 428 MB > 129 MB L2 (no flush)", "path": ("fused persistent kernel (generic: RRTL_FUSED_JIT=0)" if os.environ.get("RRTL_FUSED_JIT", "1")[:1] == "0"
+                            else "fused persistent kernel compiled for the design's truth-table classes (NVRTC)"),
                    "tile_words": tile_words},
         "gate_evals_per_s": value * info.n_gates,
         "design": {"gates": info.n_gates, "levels": info.n_levels, "nets": info.n_nets, "slots": info.n_slots,

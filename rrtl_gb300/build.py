@@ -47,6 +47,8 @@ JIT_HEADERS = [
     ("check_log.h", "check_log.h"),
     ("gate_dev.h", "gate_dev.h"),
     ("gate_common.h", "gate_common.h"),
+    ("gate_fused.h", "gate_fused.h"),
+    ("lut_classes.h", "lut_classes.h"),
     ("../../include/rrtl_cuda.h", os.path.join("..", "..", "include", "rrtl_cuda.h")),
 ]
 JIT_STUBS = [

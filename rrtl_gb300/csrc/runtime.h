@@ -222,6 +222,7 @@ struct rrtl_design {
   // and one per run tables
   std::map<std::string, std::unique_ptr<rrtl::JitKernel>> wjit_runs;
   std::map<std::string, std::unique_ptr<rrtl::JitKernel>> gjit_runs;  // compiled gate kernels, per run tables
+  std::map<std::string, std::unique_ptr<rrtl::JitKernel>> gfused_jit;  // compiled fused kernels, per tile width
 };
 
 struct rrtl_batch {

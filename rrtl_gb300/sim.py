@@ -171,6 +171,7 @@ EXPORTS = (
     "rrtl_word_jit_emit",
     "rrtl_instance_fold_plan",
     "rrtl_gate_jit_emit",
+    "rrtl_gate_fused_jit_emit",
     "rrtl_design_load_bitslice",
     "rrtl_bitslice_json",
     "rrtl_shard_plan",
@@ -254,6 +255,8 @@ def lib():
         "rrtl_bitslice_json": [c_char_p, c_size_t, c_char_p, c_char_p, c_size_t, P(c_size_t)],
         "rrtl_gate_jit_emit": [c_char_p, c_size_t, c_char_p, c_void_p, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                P(c_uint32), c_char_p, c_size_t],
+        "rrtl_gate_fused_jit_emit": [c_char_p, c_size_t, c_char_p, c_uint32, c_char_p, c_char_p, c_size_t, P(c_size_t),
+                                     P(c_uint32), c_char_p, c_size_t],
         "rrtl_shard_plan": [c_uint64, c_uint32, P(ShardInfo)],
         "rrtl_runtime_create": [c_void_p, c_uint64, c_uint32, P(c_void_p)],
         "rrtl_runtime_destroy": [c_void_p],
@@ -409,6 +412,23 @@ def gate_jit_emit(design: Union[_b.Design, str], top: str, run: "Run", arch: Opt
     cub = c_uint32()
     check(lib().rrtl_gate_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
                                    n.value + 1, byref(n), byref(cub), logb, len(logb)))
+    return src.value.decode(), cub.value, logb.value.decode()
+
+
+def gate_fused_jit_emit(design: Union[_b.Design, str], top: str, tile_words: int = 8, arch: Optional[str] = None):
+    """CUDA source of the fused gate kernel compiled for the design's
+    truth-table classes at `tile_words`, and with `arch` its NVRTC compile (no
+    device needed): (source, cubin bytes, compiler log)."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    n = c_size_t()
+    check(lib().rrtl_gate_fused_jit_emit(raw, len(raw), top.encode(), tile_words, None, None, 0, byref(n), None, None,
+                                         0))
+    src = ctypes.create_string_buffer(n.value + 1)
+    logb = ctypes.create_string_buffer(1 << 16)
+    cub = c_uint32()
+    check(lib().rrtl_gate_fused_jit_emit(raw, len(raw), top.encode(), tile_words, arch.encode() if arch else None, src,
+                                         n.value + 1, byref(n), byref(cub), logb, len(logb)))
     return src.value.decode(), cub.value, logb.value.decode()
 
 

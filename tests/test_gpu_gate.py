@@ -193,6 +193,27 @@ def test_netlist_faults_tile_widths_match_oracle(small_netlist, words):
     assert 0 < n_det < len(faults)  # detected faults and latent ones, not stimulus noise
 
 
+@pytest.mark.parametrize("words", [8, 4, 2, 1])
+def test_design_compiled_fused_kernel_equals_generic(small_netlist, monkeypatch, words):
+    """The fused kernel compiled for the design's truth-table classes (the
+    default) and the generic fused kernel (RRTL_FUSED_JIT=0) give the same
+    traces, hashes and final state."""
+    d, meta, cd, od = small_netlist
+    lanes, cycles = 1000, 30
+    stim, rec = netlist_run_spec(meta)
+    out = {}
+    for jit in ("1", "0"):
+        monkeypatch.setenv("RRTL_FUSED_JIT", jit)
+        g = sim.GpuBatchSimulator(cd, lanes=lanes)
+        g.set_tile_words(words)
+        res = g.run(cycles, seed=77, stim=stim, record=rec, mode=sim.REC_TRACE | sim.REC_HASH)
+        out[jit] = (res["trace"], res["hash"], [g.get_signal_bits(n) for n in meta.regs[::11] + meta.gate_names[::53]])
+    assert np.array_equal(out["1"][0], out["0"][0])
+    assert np.array_equal(out["1"][1], out["0"][1])
+    for a, b in zip(out["1"][2], out["0"][2]):
+        assert np.array_equal(a, b)
+
+
 def test_auto_tile_width_is_a_valid_width(small_netlist):
     d, meta, cd, od = small_netlist
     stim, rec = netlist_run_spec(meta)

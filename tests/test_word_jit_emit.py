@@ -246,3 +246,33 @@ def test_compiled_gate_kernel_of_a_plane_design_compiles():
         raise
     assert cub > 0, log
     assert src.count("lop3<") >= 2 * 500
+
+
+@pytest.mark.parametrize("which,w", [("netlist", 8), ("netlist", 4), ("crc32", 2), ("plane", 1)])
+def test_fused_kernel_compiled_for_a_design(which, w):
+    """The fused gate kernel compiled for a design's truth-table classes: its
+    dispatch lists exactly those classes (and 0, an empty run), and it
+    compiles for sm_103a at every tile width."""
+    from rrtl_gb300.workloads import gate_netlist, narrow_alu
+
+    from .helpers import crc32_netlist_json
+
+    if which == "netlist":
+        d, meta = gate_netlist(n_gates=3000, n_ff=64, n_pi=16, n_po=16, depth=12, seed=5)
+        js, top = d.to_json(), meta.top
+    elif which == "crc32":
+        js, top = crc32_netlist_json(), "crc32"
+    else:
+        js, top = sim.bitslice_json(narrow_alu(16), "Alu"), "Alu"
+    src, _, _ = sim.gate_fused_jit_emit(js, top, w)
+    line = next(l for l in src.splitlines() if l.startswith("#define RRTL_LUT_CLASSES(X)"))
+    listed = [int(t[2:-1]) for t in line.split()[2:]]
+    assert listed[0] == 0 and listed == sorted(set(listed)) and len(listed) < 80
+    assert f"fused_kernel_body<{w}>" in src
+    try:
+        src, cub, log = sim.gate_fused_jit_emit(js, top, w, "sm_103a")
+    except sim.RrtlError as e:
+        if "NVRTC not found" in str(e):
+            pytest.skip("NVRTC is not installed")
+        raise
+    assert cub > 0, log
