@@ -509,7 +509,10 @@ def serving_leg(ctx, sim, c2, loads, rates, duration_s, cycle_div=50, chunk=128,
     First the capacity: a burst of `burst` requests submitted at once, in
     requests/s and lane-cycles/s; then arrivals at each fraction of that
     capacity in `loads` and at each absolute rate in `rates`, each for
-    `duration_s` seconds of arrivals. Reports throughput and p50/p99 latency
+    `duration_s` seconds of arrivals (shorter above twice the capacity, so
+    the backlog stays at twice what the capacity serves in `duration_s`:
+    such a rate measures the overloaded loop, not the length of its queue).
+    Reports throughput and p50/p99 latency
     overall and per design; a sample of requests is re-run alone and must
     match bit for bit."""
     from rrtl_gb300.workloads import Rng, cpu_rom_hashed, gate_netlist, log_uniform_int, netlist_run_spec, pipelined_cpu
@@ -598,12 +601,15 @@ def serving_leg(ctx, sim, c2, loads, rates, duration_s, cycle_div=50, chunk=128,
         server = sim.Server(ctx, chunk_cycles=chunk, round_us=round_us, policy=policy)
         rng = Rng(int(rate * 1000) + 1)
         handles = []
+        # above twice the capacity the backlog grows without bound: arrivals
+        # stop once they hold twice what the capacity serves in `duration_s`
+        window = min(duration_s, duration_s * 2.0 * capacity / rate)
         t_start = time.perf_counter()
         t_next = t_start
         i = 0
         while True:
             t_next += -math.log(1.0 - rng.uniform()) / rate
-            if t_next - t_start > duration_s:
+            if t_next - t_start > window:
                 break
             sp = spec(rng, i)
             i += 1
@@ -615,6 +621,7 @@ def serving_leg(ctx, sim, c2, loads, rates, duration_s, cycle_div=50, chunk=128,
         t_end = time.perf_counter()
         row = summarize(handles, t_start, t_end, server, True)
         row["rate_per_s"] = rate
+        row["arrival_window_s"] = round(window, 3)
         if kind == "load":
             row["load_of_capacity"] = tag
         out["rates"].append(row)
