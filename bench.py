@@ -867,10 +867,17 @@ def run_reference(args, ws, rank):
     threads = os.cpu_count() or 1
     aot, _ = aot_engine(od, stim_idx, rec_idx)
     lanes = 64 * threads * 8
-    t = time.perf_counter()
-    aot.run(lanes, 8, SEED)
-    per_cycle = max(time.perf_counter() - t, 1e-4) / 8
-    cycles = max(16, int(0.6 / per_cycle))
+    # step length: at least 0.6 s of simulation, so thread start-up is noise
+    # (the probe's per-cycle time includes that start-up, so grow until a
+    # probe of the chosen length itself lasts long enough)
+    cycles = 32
+    for _ in range(6):
+        t = time.perf_counter()
+        aot.run(lanes, cycles, SEED)
+        dt = time.perf_counter() - t
+        if dt >= 0.6:
+            break
+        cycles = max(cycles + 1, int(cycles * 0.7 / max(dt, 1e-4)))
     vals = []
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
