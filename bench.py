@@ -910,6 +910,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e-trace", action="store_true", help="skip the e2e leg with a host-resident input trace")
     ap.add_argument("--lanes", type=int, default=LANES, help="lanes per GPU (profiling cases)")
     ap.add_argument("--cycles", type=int, default=CYCLES, help="cycles per step (profiling cases)")
     ap.add_argument("--tile-words", type=int, default=0, help="fused tile width in 32-lane words (0 = automatic)")
@@ -1030,6 +1031,42 @@ def main():
     e2e_ms = reduce_max(dist, e2e_ms)
     e2e_value = throughput(ws, LANES, CYCLES, args.steps, e2e_ms)
 
+    # e2e with host stimulus: the primary inputs as a host-resident (pinned)
+    # input trace, copied to the device inside every step, as a caller with
+    # its own stimulus would drive the batch. The trace holds the bits the
+    # on-device generator gives for seed SEED, so the run's per-cycle hash
+    # must equal the first warm-up step's from cycle 1 on (cycle 0's outputs
+    # depend on the state the previous run left; the reset pulse clears
+    # every register at the end of cycle 0).
+    e2e_trace = None
+    if not args.no_e2e_trace:
+        pis = [n for n, k, p in stim if k == sim.STIM_RANDOM]
+        tr = torch.empty((CYCLES, len(pis), words), dtype=torch.int32, pin_memory=True)
+        trn = tr.numpy().view(np.uint32)
+        g.set_path(sim.PATH_FUSED)
+        r = g.make_run(CYCLES, seed=SEED, stim=stim, record=pis, mode=sim.REC_TRACE, out_trace=trn, lane_base=lane_base)
+        sim.check(sim.lib().rrtl_batch_run(g.h, sim.byref(r)))
+        tstim = [(n, k, p) for n, k, p in stim if k != sim.STIM_RANDOM] + [(n, sim.STIM_TRACE, i) for i, n in enumerate(pis)]
+        ctx.synchronize()
+        if dist:
+            dist.barrier()
+        ctx.record(2)
+        for i in range(args.steps):
+            r = g.make_run(CYCLES, seed=SEED, stim=tstim, record=rec, mode=sim.REC_HASH, input_trace=trn,
+                           lane_base=lane_base)
+            r.out_hash = ctypes_u64(hash_host.data_ptr())
+            sim.check(sim.lib().rrtl_batch_run(g.h, sim.byref(r)))
+            sim.check(sim.lib().rrtl_batch_get_signals_bits(g.h, reg_idx.ctypes.data_as(sim.POINTER(sim.c_uint32)),
+                                                            len(reg_idx), ctypes_u32(regs_host.data_ptr()), FFS * words))
+        ctx.record(3)
+        t_ms = reduce_max(dist, ctx.elapsed_ms(2, 3))
+        same = bool(torch.equal(hash_host[1:], hash_dev[0].cpu()[1:]))
+        e2e_trace = {"value": throughput(ws, LANES, CYCLES, args.steps, t_ms), "unit": "lane-cycles/s",
+                     "h2d_bytes_per_step": int(trn.nbytes) + len(tstim) * 16 + len(rec) * 4, "d2h_bytes_per_step": d2h,
+                     "input_trace": f"{len(pis)} inputs x {words} words x {CYCLES} cycles, pinned host memory",
+                     "hash_equal_to_device_stimulus": same, "hash_cycles_compared": f"1-{CYCLES - 1}"}
+        del tr, trn
+
     # plain one-launch-per-cycle path on the same workload (fewer cycles; same per-cycle work)
     plain = None
     if not args.no_plain:
@@ -1100,6 +1137,7 @@ def main():
         "design": {"gates": info.n_gates, "levels": info.n_levels, "nets": info.n_nets, "slots": info.n_slots,
                    "flops": info.n_regs},
         "e2e": {"value": e2e_value, "unit": "lane-cycles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e_host_trace": e2e_trace,
         "plain_path": plain,
         "roofline": roofline,
         "gpu_launches": args.steps,
