@@ -29,7 +29,7 @@ constexpr uint32_t kFusedHeader = 128;     // bytes between the ring and the slo
 #if !RRTL_PAIR_STEPS
 constexpr int kUnroll = RRTL_FUSED_UNROLL;
 #endif
-static_assert(kRing * 8 + 8 + 16 * 4 <= kFusedHeader, "fused kernel header overflows");
+static_assert(kRing * 8 + 8 + 16 * 4 + 8 <= kFusedHeader, "fused kernel header overflows");
 static_assert(kRing == 4, "ring parity arithmetic assumes four buffers");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -175,6 +175,53 @@ __device__ __forceinline__ void run_seg(const uint2* __restrict__ rb, typename W
 #endif
 }
 
+// One warp step of a run: the cells of record r.
+template <int W, int L>
+__device__ __forceinline__ void cell_step(typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv, uint2 r) {
+  using Sh = FusedShape<W>;
+  using T = typename WordVec<Sh::V>::T;
+  constexpr int R = W / Sh::V;
+  constexpr bool kUseA = (L & 0x0F) != ((L >> 4) & 0x0F);
+  constexpr bool kUseB = (L & 0x33) != ((L >> 2) & 0x33);
+  constexpr bool kUseC = (L & 0x55) != ((L >> 1) & 0x55);
+  const T zero{};
+  const T va = kUseA ? Sv[(r.x & 0xFFFFu) * R] : zero;
+  const T vb = kUseB ? Sv[(r.x >> 16) * R] : zero;
+  const T vc = kUseC ? Sv[(r.y & 0xFFFFu) * R] : zero;
+  Sv[(r.y >> 16) * R] = lopv<L>(va, vb, vc);
+}
+
+// A warp's first run of a piece under the split barrier: wait until every
+// warp finished the previous piece (its outputs are this piece's operands),
+// then the first step from the record read before the wait, then the rest.
+template <int W, int L>
+__device__ __forceinline__ void run_seg_first(const uint2* __restrict__ rb,
+                                              typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv, int g, int e,
+                                              uint2 rf, uint64_t* pbar, uint32_t parity, int& abort_flag) {
+  if (!mbar_wait(pbar, parity)) abort_flag = 1;
+  if (g < e) {
+    cell_step<W, L>(Sv, rf);
+    g += FusedShape<W>::kSteps;
+  }
+  run_seg<W, L>(rb, Sv, g, e);
+}
+
+#define RRTL_CASE_FIRST(n) \
+  case n: run_seg_first<W, n>(rb, Sv, b + h, e, rf, pbar, parity, abort_flag); break;
+
+template <int W>
+__device__ __forceinline__ void eval_run_first(const uint2* __restrict__ rb,
+                                               typename WordVec<FusedShape<W>::V>::T* __restrict__ Sv, uint32_t run, int h,
+                                               uint2 rf, uint64_t* pbar, uint32_t parity, int& abort_flag) {
+  const int b = (int)((run >> 8) & 0xFFFu), e = (int)(run >> 20);
+  switch (run & 0xFFu) {
+    RRTL_LUT_CLASSES(RRTL_CASE_FIRST)
+    default:
+      if (!mbar_wait(pbar, parity)) abort_flag = 1;
+      break;
+  }
+}
+
 #define RRTL_CASE(n) \
   case n: run_seg<W, n>(rb, Sv, b + h, e); break;
 
@@ -282,6 +329,8 @@ __device__ __forceinline__ void apply_forces(const GateRunDev& R, uint32_t* S, u
 // a 16-byte boundary (ring buffers are bulk-copy destinations).
 struct FusedCta {
   uint64_t* bars;
+  uint64_t* pbar;    // split piece barrier: one arrival per warp
+  uint32_t pphase;   // its phases started (every thread)
   unsigned long long* hacc;
   uint32_t* dstate;  // diff[8], detected[8]
   uint8_t* dyn;
@@ -295,12 +344,15 @@ __device__ __forceinline__ void fused_cta_init(FusedCta& cta, uint8_t* smem) {
   cta.hacc = reinterpret_cast<unsigned long long*>(smem + kRing * 8);
   cta.dstate = reinterpret_cast<uint32_t*>(smem + kRing * 8 + 8);
   cta.dyn = smem + kFusedHeader;
+  cta.pbar = reinterpret_cast<uint64_t*>(smem + kRing * 8 + 8 + 16 * 4);
+  cta.pphase = 0;
   cta.q = 0;
   cta.issued = 0;
   cta.aborted = false;
   if (threadIdx.x == 0) {
     *cta.hacc = 0ull;
     for (int i = 0; i < kRing; ++i) mbar_init(&cta.bars[i], 1);
+    mbar_init(cta.pbar, (uint32_t)kFusedWarps);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -321,7 +373,13 @@ __device__ __forceinline__ void fused_cta_drain(const FusedCta& cta, uint32_t* e
 // Cycles [c0, c0 + ncyc) of one tile (W words) of a run, then the closing
 // settle if `final_settle`. Net state is read from and written back to the
 // run's global net rows, so a run may be split into consecutive calls.
-template <int W>
+// kSplit: cycles without forces separate pieces by the split piece barrier
+// (the fused kernel compiled for a design's few truth-table classes);
+// without it every piece ends at a CTA barrier (the generic fused kernel and
+// the job queue, whose loops cover all 80 classes: with the split form's
+// second copy of each, the generic kernel measured 3x slower on the 50k-gate
+// netlist and the job queue 1.8x).
+template <int W, bool kSplit>
 __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDev& R, uint32_t tile, uint64_t c0,
                                            uint64_t ncyc, bool final_settle, FusedCta& cta) {
   constexpr uint32_t G = 32 / W;
@@ -380,9 +438,16 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
   // thread. A program of at most kRing pieces is loaded once per tile and
   // stays resident. A wait that runs out sets the error word, and the
   // barrier's OR ends the CTA's work.
+  //
+  // Cycles without stuck-at forces separate pieces by the split piece
+  // barrier instead (cta.pbar, one arrival per warp): thread 0 refills the
+  // buffer of piece q-1 once its own wait has seen every warp finish piece
+  // q-1, and every thread waits for piece q+1 to land itself before it reads
+  // that piece's header and first record. A thread whose wait runs out reads
+  // nothing more, and the CTA barrier that ends the cycle ORs the error.
   uint32_t next_piece = 0;                // piece index of the next copy (thread 0)
   uint32_t next_off = 0, next_bytes = 0;  // its blob offset and size, loaded one copy ahead
-  int abort_flag = 0;                     // thread 0: a bounded wait ran out
+  int abort_flag = 0;                     // this thread: a bounded wait ran out
   auto load_next = [&]() {
     next_off = pieces[next_piece].off_words;
     next_bytes = pieces[next_piece].bytes;
@@ -432,6 +497,58 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
       }
     }
     __syncthreads();
+    if (kSplit && !final_pass && !R.has_forces && P.n_pieces > 1) {
+      // Split piece barrier: a warp that finished piece p arrives, reads the
+      // next piece's header word and its first record, and waits for the
+      // other warps only right before its first operand load of piece p+1,
+      // so a piece's start latency overlaps the slowest warp's tail. The
+      // last piece of a cycle ends at the CTA barrier below.
+      uint2 hw_n = make_uint2(0u, 0u), rf_n = make_uint2(0u, 0u);
+      for (uint32_t p = 0; p < P.n_pieces; ++p) {
+        const uint32_t buf = (uint32_t)(resident ? q0 + p : q) & (kRing - 1u);
+        const uint8_t* pb = ring + buf * ring_bytes;
+        const uint2* rb = reinterpret_cast<const uint2*>(pb + hdr_bytes) + cidx;
+        const uint32_t* extra = reinterpret_cast<const uint32_t*>(pb) + 2 * kFusedWarps;
+        if (p == 0) {
+          if (!resident && tid == 0 && q > q0 && cta.issued < q_end) issue_next();
+          const uint2 hw = reinterpret_cast<const uint2*>(pb)[warp];
+          eval_piece<W>(rb, Sv, hw.x, extra, hw.y & 0xFFFFu, hw.y >> 16, (int)h);
+        } else {
+          eval_run_first<W>(rb, Sv, hw_n.x, (int)h, rf_n, cta.pbar, (cta.pphase - 1u) & 1u, abort_flag);
+          for (uint32_t k = hw_n.y & 0xFFFFu; k < (hw_n.y >> 16); ++k) eval_run<W>(rb, Sv, extra[k], (int)h);
+          // every warp finished piece p-1: the ring buffer it used is free
+          if (!resident && tid == 0 && cta.issued < q_end) issue_next();
+        }
+        if (p + 1 < P.n_pieces) {
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(cta.pbar)) : "memory");
+          ++cta.pphase;
+          const uint64_t qn = resident ? q0 + p + 1 : q + 1;
+          bool landed = true;
+          if (!resident && !mbar_wait(&bars[(uint32_t)qn & (kRing - 1u)], ((uint32_t)qn >> 2) & 1u)) {
+            timed_out();
+            landed = false;
+          }
+          hw_n = make_uint2(0u, 0u);
+          if (landed) {
+            const uint8_t* pbn = ring + ((uint32_t)qn & (kRing - 1u)) * ring_bytes;
+            hw_n = reinterpret_cast<const uint2*>(pbn)[warp];
+            const int bn = (int)((hw_n.x >> 8) & 0xFFFu) + (int)h, en = (int)(hw_n.x >> 20);
+            if (bn < en) rf_n = (reinterpret_cast<const uint2*>(pbn + hdr_bytes) + cidx)[bn * Sh::G];
+          }
+        }
+        if (!resident) ++q;
+      }
+      if (!resident && tid == 0) {
+        const uint64_t qn = q;
+        if (qn < q_end && !mbar_wait(&bars[(uint32_t)qn & (kRing - 1u)], ((uint32_t)qn >> 2) & 1u)) timed_out();
+      }
+      if (__syncthreads_or(abort_flag)) {
+        cta.q = q;
+        cta.aborted = true;
+        return;
+      }
+    } else
     for (uint32_t p = 0; p < P.n_pieces; ++p) {
       const uint32_t buf = (uint32_t)(resident ? q0 + p : q) & (kRing - 1u);
       if (!resident && tid == 0 && q > q0 && cta.issued < q_end) issue_next();
@@ -532,13 +649,13 @@ __device__ __forceinline__ void fused_tile(const GateProgDev& P, const GateRunDe
 }
 
 // The whole fused kernel: tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-template <int W>
+template <int W, bool kSplit>
 __device__ __forceinline__ void fused_kernel_body(const GateProgDev& P, const GateRunDev& R) {
   extern __shared__ __align__(128) uint8_t smem[];
   FusedCta cta;
   fused_cta_init(cta, smem);
   for (uint32_t tile = blockIdx.x; tile < R.n_tiles && !cta.aborted; tile += gridDim.x)
-    fused_tile<W>(P, R, tile, R.cycle_base, R.cycles, R.final_settle != 0, cta);
+    fused_tile<W, kSplit>(P, R, tile, R.cycle_base, R.cycles, R.final_settle != 0, cta);
   fused_cta_drain(cta, R.err);
 }
 

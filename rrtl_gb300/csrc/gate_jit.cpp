@@ -173,7 +173,7 @@ std::string gate_fused_jit_source(const GateProgram& gp) {
   o += "\n#include \"gate_fused.h\"\n";
   o += "extern \"C\" __global__ void __launch_bounds__(rrtl::kFusedThreads, rrtl::kGateFusedCtasPerSm)\n";
   o += "rrtl_gate_fused_jit(rrtl::GateProgDev P, rrtl::GateRunDev R) {\n";
-  o += "  rrtl::fused_kernel_body<" + std::to_string(gp.tile_words) + ">(P, R);\n}\n";
+  o += "  rrtl::fused_kernel_body<" + std::to_string(gp.tile_words) + ", true>(P, R);\n}\n";
   return o;
 }
 

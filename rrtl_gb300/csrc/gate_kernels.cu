@@ -33,7 +33,7 @@ constexpr int kPlainThreads = 256;
 
 template <int W>
 __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_fused_kernel(GateProgDev P, GateRunDev R) {
-  fused_kernel_body<W>(P, R);
+  fused_kernel_body<W, false>(P, R);
 }
 
 // Persistent job-queue kernel: CTAs take (job, tile, cycle range) items from
@@ -59,10 +59,10 @@ __global__ void __launch_bounds__(kFusedThreads, kGateFusedCtasPerSm) gate_queue
     const uint64_t c0 = item.c0;
     const bool fin = (item.flags & 1u) != 0;
     switch (s_job.P.group) {
-      case 4: fused_tile<8>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
-      case 8: fused_tile<4>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
-      case 16: fused_tile<2>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
-      default: fused_tile<1>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      case 4: fused_tile<8, false>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      case 8: fused_tile<4, false>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      case 16: fused_tile<2, false>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
+      default: fused_tile<1, false>(s_job.P, s_job.R, item.tile, c0, item.ncyc, fin, cta); break;
     }
     if (cta.aborted) break;
   }
