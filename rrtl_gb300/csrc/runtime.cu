@@ -112,6 +112,19 @@ constexpr double kLeadWarpWeight = RRTL_LEAD_WARP_WEIGHT;
 #define RRTL_RUN_COST 4.0
 #endif
 constexpr double kRunCost = RRTL_RUN_COST;
+// The same two weights for the blob of the per-design compiled kernel,
+// whose split piece barrier lets a warp that arrives late start its next
+// piece late: lighter lead-warp relief and a cheaper run balance best there
+// (50k-gate netlist, 65,536 lanes: 83.7 ms per step at 0.7 / 4 steps, 78.8
+// at 0.85 / 2; the CTA-barrier kernels lose 2% at 0.85).
+#ifndef RRTL_LEAD_WARP_WEIGHT_SPLIT
+#define RRTL_LEAD_WARP_WEIGHT_SPLIT 0.85
+#endif
+#ifndef RRTL_RUN_COST_SPLIT
+#define RRTL_RUN_COST_SPLIT 2.0
+#endif
+constexpr double kLeadWarpWeightSplit = RRTL_LEAD_WARP_WEIGHT_SPLIT;
+constexpr double kRunCostSplit = RRTL_RUN_COST_SPLIT;
 
 uint32_t log2_words(uint32_t W) { return W == 8 ? 3u : W == 4 ? 2u : W == 2 ? 1u : 0u; }
 
@@ -229,6 +242,29 @@ GateVariant* gate_variant(rrtl_design* d, uint32_t W) {
       // every design's variant of this width can launch
       cuda_check(gate_fused_prepare(P, d->ctx->max_smem), "gate_fused_prepare");
       v->fused_ctas = (uint32_t)gate_fused_ctas_per_sm(P, v->fused_smem);
+    }
+  }
+  v->gdev_split = v->gdev;
+  v->fused_smem_split = v->fused_smem;
+  if (v->fused_ok) {
+    PieceBlob bs = build_piece_blob(gp, kGateFusedWarps, kLeadWarpWeightSplit, gate_fused_vec(W), kRunCostSplit);
+    GateProgDev Ps = v->gdev;
+    Ps.ring_bytes = bs.max_bytes;
+    Ps.hdr_bytes = bs.hdr_bytes;
+    const size_t need = gate_fused_smem_bytes(Ps);
+    if (need <= max_smem) {
+      std::vector<GatePieceDev> pieces;
+      for (size_t i = 0; i < gp.pieces.size(); ++i) {
+        const GatePiece& pc = gp.pieces[i];
+        pieces.push_back(GatePieceDev{pc.group_begin, pc.n_groups, pc.level, pc.last_of_level ? 1u : 0u,
+                                      bs.off_words[i], bs.bytes[i], 0, 0});
+      }
+      upload(v->d_srecs_split, bs.words);
+      upload(v->d_pieces_split, pieces);
+      Ps.blob = v->d_srecs_split.as<uint32_t>();
+      Ps.pieces = v->d_pieces_split.as<GatePieceDev>();
+      v->gdev_split = Ps;
+      v->fused_smem_split = need;
     }
   }
   // nets that hold their end-of-cycle value in a slot (recordable on the fused path)
@@ -619,7 +655,8 @@ void gate_run(rrtl_batch* b, const rrtl_run& run, bool device_ptrs, const CheckT
   } else if (g.fused) {
     uint32_t grid = std::min<uint32_t>(g.R.n_tiles, d->ctx->sm_count * g.v->fused_ctas);
     if (F)
-      cuda_check(launch_gate_fused_jit(*F, g.v->gdev, g.R, grid, g.v->fused_smem, st), "rrtl_gate_fused_jit");
+      cuda_check(launch_gate_fused_jit(*F, g.v->gdev_split, g.R, grid, g.v->fused_smem_split, st),
+                 "rrtl_gate_fused_jit");
     else
       cuda_check(launch_gate_fused(g.v->gdev, g.R, grid, g.v->fused_smem, st), "gate_fused_kernel");
   } else {

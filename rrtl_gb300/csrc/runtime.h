@@ -57,6 +57,11 @@ struct GateVariant {
   GateProgDev gdev{};
   bool fused_ok = false;
   size_t fused_smem = 0;
+  // the same pieces with warp shares balanced for the split piece barrier of
+  // the per-design compiled kernel (gdev when they would not fit)
+  GateProgDev gdev_split{};
+  size_t fused_smem_split = 0;
+  DevBuf d_srecs_split, d_pieces_split;
   uint32_t fused_ctas = 1;  // resident fused CTAs per SM
   double tile_cycle_cost = 0;  // estimated warp steps of one tile-cycle (job ordering)
   DevBuf d_srecs, d_pieces, d_src_net, d_src_slot, d_sregs, d_wb, d_grecs, d_lgb, d_gregs;
