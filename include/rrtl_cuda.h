@@ -519,7 +519,7 @@ rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, co
  * rrtl_batch_run on the gate engine): the generic kernel's code with a run
  * dispatch over only the truth-table classes the design's cells use, which
  * leaves room for a split barrier between pieces in runs without stuck-at
- * forces (about 4.5% faster on a 50k-gate netlist: 11 of 80 classes). Built on the first such run of a tile width and cached with the
+ * forces (about 10% faster on a 50k-gate netlist: 11 of 80 classes). Built on the first such run of a tile width and cached with the
  * design; RRTL_FUSED_JIT=0 in the environment keeps the generic kernel. This
  * call emits (and with arch compiles) it for tile width tile_words (1, 2, 4
  * or 8) without a device. RRTL_E_UNSUPPORTED when the design is outside the

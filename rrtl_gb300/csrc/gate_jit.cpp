@@ -166,8 +166,12 @@ std::string gate_fused_jit_source(const GateProgram& gp) {
   std::vector<uint8_t> used(256, 0);
   used[0] = 1;  // an empty run (header word 0) dispatches to class 0
   for (const GateCell& c : gp.cells) used[c.lut] = 1;
+  // the kernel's shape as the host library was built with it (launch size, shares)
   std::string o = "// rrtl_gate_fused_jit: gate_fused_kernel<" + std::to_string(gp.tile_words) +
-                  "> for one design's truth-table classes\n#define RRTL_LUT_CLASSES(X)";
+                  "> for one design's truth-table classes\n#define RRTL_FUSED_WARPS " +
+                  std::to_string(kGateFusedWarps) + "\n#define RRTL_FUSED_CTAS_PER_SM " +
+                  std::to_string(kGateFusedCtasPerSm) + "\n#define RRTL_FUSED_V " + std::to_string(RRTL_FUSED_V) +
+                  "\n#define RRTL_LUT_CLASSES(X)";
   for (int l = 0; l < 256; ++l)
     if (used[l]) o += " X(" + std::to_string(l) + ")";
   o += "\n#include \"gate_fused.h\"\n";

@@ -48,8 +48,9 @@ cudaError_t launch_gate_jit(const JitKernel& J, const GateRunDev& R, cudaStream_
 // the design's cells use, so the dispatch and the code it jumps into stay
 // small enough for the split piece barrier (fused_tile's kSplit), whose
 // second copy of every loop the 80-class generic kernel cannot afford.
-// Measured on the 50k-gate netlist (11 of the 80 classes): 83.7 ms per
-// 1,000-cycle step at 65,536 lanes against 87.5 for the generic kernel.
+// Measured on the 50k-gate netlist (11 of the 80 classes): 78.5 ms per
+// 1,000-cycle step at 65,536 lanes, with its own piece blob balanced for the
+// split barrier, against 87.5 for the generic kernel.
 std::string gate_fused_jit_source(const GateProgram& gp);
 void gate_fused_jit_build(const GateProgram& gp, int device, JitKernel* J);
 cudaError_t launch_gate_fused_jit(const JitKernel& J, const GateProgDev& P, const GateRunDev& R, uint32_t grid,

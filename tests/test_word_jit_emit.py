@@ -268,7 +268,7 @@ def test_fused_kernel_compiled_for_a_design(which, w):
     line = next(l for l in src.splitlines() if l.startswith("#define RRTL_LUT_CLASSES(X)"))
     listed = [int(t[2:-1]) for t in line.split()[2:]]
     assert listed[0] == 0 and listed == sorted(set(listed)) and len(listed) < 80
-    assert f"fused_kernel_body<{w}, true>" in src
+    assert f"fused_kernel_body<{w}, true>" in src and "#define RRTL_FUSED_WARPS 16" in src
     try:
         src, cub, log = sim.gate_fused_jit_emit(js, top, w, "sm_103a")
     except sim.RrtlError as e:
