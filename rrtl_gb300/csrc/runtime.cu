@@ -294,8 +294,8 @@ void build_gate_variants(rrtl_design* d) {
 
 // Fused tile width for a run over `words` 32-lane words. Cost model per SM:
 // every tile runs every level; a warp evaluates one group of G = 32/W cells
-// per step, 32 warps share a level, and each level piece ends in a CTA
-// barrier worth about kBarrierSteps group steps. A step costs more at small
+// per step, the CTA's warps (kGateFusedWarps) share a level, and each level
+// piece ends in a barrier worth about kBarrierSteps group steps. A step costs more at small
 // W because G cells rarely find their inputs in G distinct shared-memory
 // banks (kStepCost, by log2 W). Tiles are spread over the SMs in whole rounds.
 uint32_t lane_bucket(uint32_t words) {
