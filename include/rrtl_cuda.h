@@ -528,6 +528,25 @@ rrtl_status rrtl_gate_fused_jit_emit(const char* json, size_t len, const char* t
                                      const char* arch, char* source, size_t source_cap, size_t* source_len,
                                      uint32_t* cubin_bytes, char* log, size_t log_cap);
 
+/* The gate lowering of a design at one fused tile width, without a device
+ * (no reference counterpart: the reference's interpreter encodes one record
+ * per gate and has no shared-memory layout). Shared-memory accounting per
+ * cycle of one tile: every group of G = 32/W cells reads each used input
+ * position in one access per quarter-warp, which takes as many wavefronts as
+ * the largest number of distinct slot rows sharing a bank residue
+ * (operand_wavefronts) against one per distinct row set (operand_rows, the
+ * conflict-free floor); the vector commit reads the D rows of G registers
+ * per wavefront in commit order (commit_wavefronts against commit_groups).
+ * RRTL_E_UNSUPPORTED when the design is outside the gate engine. */
+typedef struct {
+  uint32_t tile_words, group;  /* W and G = 32 / W */
+  uint32_t cells, pad_cells, groups, levels, slots, classes;
+  uint64_t operand_rows, operand_wavefronts;
+  uint64_t commit_groups, commit_wavefronts;
+} rrtl_gate_program_info;
+rrtl_status rrtl_gate_program_info_get(const char* json, size_t len, const char* top, uint32_t tile_words,
+                                       rrtl_gate_program_info* out);
+
 /* ---- bit-sliced multi-bit designs --------------------------------------------
  * The reference's BitSliceSimulator (crates/rrtl-sim-ir/src/bitslice.rs:1-402)
  * keeps a W-bit signal as W bit-planes across lanes. rrtl_design_load_bitslice

@@ -1516,6 +1516,71 @@ rrtl_status rrtl_gate_jit_emit(const char* json, size_t len, const char* top, co
   });
 }
 
+rrtl_status rrtl_gate_program_info_get(const char* json, size_t len, const char* top, uint32_t tile_words,
+                                       rrtl_gate_program_info* out) {
+  return guard([&] {
+    REQUIRE(json && top && out, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(tile_words == 1 || tile_words == 2 || tile_words == 4 || tile_words == 8, RRTL_E_ARG,
+            "E_ARG: tile width must be 1, 2, 4 or 8 words");
+    Design dz = design_from_json(json, len);
+    MachineProgram mp = lower_to_machine_program(lower_to_packed_program(dz, top));
+    GateProgram gp;
+    try {
+      gp = build_gate_program(mp, tile_words);
+    } catch (const RrtlError& e) {
+      fail(RRTL_E_UNSUPPORTED, e.what());
+    }
+    rrtl_gate_program_info I{};
+    const uint32_t G = gp.group;
+    I.tile_words = tile_words;
+    I.group = G;
+    I.levels = gp.n_levels;
+    I.slots = gp.n_slots;
+    std::vector<uint8_t> seen(256, 0);
+    // largest number of distinct rows that share a bank residue among `rows`
+    auto wavefronts = [&](std::vector<uint32_t>& rows) {
+      std::sort(rows.begin(), rows.end());
+      rows.erase(std::unique(rows.begin(), rows.end()), rows.end());
+      std::vector<uint32_t> per(G, 0);
+      uint32_t mx = 0;
+      for (uint32_t r : rows) mx = std::max(mx, ++per[r % G]);
+      return mx;
+    };
+    std::vector<uint32_t> rows;
+    const int32_t c0 = gp.net_slot[kNetConst0];
+    for (size_t g = 0; g + G <= gp.cells.size(); g += G) {
+      const uint8_t lut = gp.cells[g].lut;
+      seen[lut] = 1;
+      ++I.groups;
+      const bool use[3] = {(lut & 0x0F) != ((lut >> 4) & 0x0F), (lut & 0x33) != ((lut >> 2) & 0x33),
+                           (lut & 0x55) != ((lut >> 1) & 0x55)};
+      for (int p = 0; p < 3; ++p) {
+        if (!use[p]) continue;
+        rows.clear();
+        for (uint32_t k = 0; k < G; ++k) {
+          const GateCell& c = gp.cells[g + k];
+          rows.push_back((uint32_t)(c.pad ? c0 : gp.net_slot[c.in[p]]));
+        }
+        I.operand_wavefronts += wavefronts(rows);
+        I.operand_rows += 1;
+      }
+      for (uint32_t k = 0; k < G; ++k) {
+        if (gp.cells[g + k].pad) ++I.pad_cells;
+        else ++I.cells;
+      }
+    }
+    for (int l = 0; l < 256; ++l) I.classes += seen[l];
+    const std::vector<uint32_t> ord = commit_order(gp);
+    for (size_t i = 0; i < ord.size(); i += G) {
+      rows.clear();
+      for (size_t k = i; k < std::min(ord.size(), i + G); ++k) rows.push_back((uint32_t)gp.net_slot[gp.regs[ord[k]].d_net]);
+      I.commit_wavefronts += wavefronts(rows);
+      ++I.commit_groups;
+    }
+    *out = I;
+  });
+}
+
 rrtl_status rrtl_gate_fused_jit_emit(const char* json, size_t len, const char* top, uint32_t tile_words,
                                      const char* arch, char* source, size_t source_cap, size_t* source_len,
                                      uint32_t* cubin_bytes, char* log, size_t log_cap) {

@@ -93,6 +93,13 @@ class Fault(ctypes.Structure):
     _fields_ = [("lane", c_uint32), ("signal", c_uint32), ("value", c_uint32)]
 
 
+class GateProgramInfo(ctypes.Structure):
+    _fields_ = [("tile_words", c_uint32), ("group", c_uint32), ("cells", c_uint32), ("pad_cells", c_uint32),
+                ("groups", c_uint32), ("levels", c_uint32), ("slots", c_uint32), ("classes", c_uint32),
+                ("operand_rows", c_uint64), ("operand_wavefronts", c_uint64), ("commit_groups", c_uint64),
+                ("commit_wavefronts", c_uint64)]
+
+
 class ShardInfo(ctypes.Structure):
     _fields_ = [("worker", c_uint32), ("lanes", c_uint32), ("start_lane", c_uint64)]
 
@@ -172,6 +179,7 @@ EXPORTS = (
     "rrtl_instance_fold_plan",
     "rrtl_gate_jit_emit",
     "rrtl_gate_fused_jit_emit",
+    "rrtl_gate_program_info_get",
     "rrtl_design_load_bitslice",
     "rrtl_bitslice_json",
     "rrtl_shard_plan",
@@ -257,6 +265,7 @@ def lib():
                                P(c_uint32), c_char_p, c_size_t],
         "rrtl_gate_fused_jit_emit": [c_char_p, c_size_t, c_char_p, c_uint32, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                      P(c_uint32), c_char_p, c_size_t],
+        "rrtl_gate_program_info_get": [c_char_p, c_size_t, c_char_p, c_uint32, P(GateProgramInfo)],
         "rrtl_shard_plan": [c_uint64, c_uint32, P(ShardInfo)],
         "rrtl_runtime_create": [c_void_p, c_uint64, c_uint32, P(c_void_p)],
         "rrtl_runtime_destroy": [c_void_p],
@@ -413,6 +422,18 @@ def gate_jit_emit(design: Union[_b.Design, str], top: str, run: "Run", arch: Opt
     check(lib().rrtl_gate_jit_emit(raw, len(raw), top.encode(), rp, arch.encode() if arch else None, src,
                                    n.value + 1, byref(n), byref(cub), logb, len(logb)))
     return src.value.decode(), cub.value, logb.value.decode()
+
+
+def gate_program_info(design: Union[_b.Design, str], top: str, tile_words: int = 8) -> dict:
+    """The gate lowering at one fused tile width (rrtl_gate_program_info_get):
+    cell, group, level, slot and class counts and the shared-memory
+    wavefronts of its operand reads and register commit against their
+    conflict-free floors."""
+    text = design.to_json() if isinstance(design, _b.Design) else design
+    raw = text.encode()
+    info = GateProgramInfo()
+    check(lib().rrtl_gate_program_info_get(raw, len(raw), top.encode(), tile_words, byref(info)))
+    return {name: getattr(info, name) for name, _ in GateProgramInfo._fields_}
 
 
 def gate_fused_jit_emit(design: Union[_b.Design, str], top: str, tile_words: int = 8, arch: Optional[str] = None):
