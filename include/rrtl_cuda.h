@@ -294,6 +294,41 @@ rrtl_status rrtl_design_autotune(rrtl_design* design, uint32_t lanes, uint32_t c
                                  float* best_ms);
 rrtl_status rrtl_batch_tile_words(rrtl_batch* b, uint32_t* words);
 
+/* Autotune recommendation table (the reference's GpuAutotuneRecommendation
+ * records, crates/rrtl-gpu-sim/src/lib.rs:58-189): a JSON array of objects
+ * {"case": string, "lanes": n, "steps": n, "tile_words": 8|4|2|1|0,
+ *  "autotune_metric": string, "autotune_metric_ns": n or null}, tile_words 0
+ * meaning the compiled gate kernel. The table is the caller's to keep (a
+ * file); the library writes one record and reads a table.
+ *
+ * rrtl_design_autotune_recommend runs rrtl_design_autotune for `lanes` lanes
+ * and `steps` cycles and writes that record for `case_name` (JSON text, NUL
+ * terminated; *len is its length, also when cap is too small).
+ *
+ * rrtl_autotune_find picks a record as the reference does
+ * (find_gpu_autotune_recommendation_with_mode, :123-144): mode
+ * RRTL_AUTOTUNE_EXACT needs case, lanes and steps equal; RRTL_AUTOTUNE_NEAREST
+ * takes the record of the same case with the smallest lane distance, then
+ * step distance, then metric, lanes and steps (autotune_match_key,
+ * :175-189). No device. RRTL_E_ARG with E_GPU_AUTOTUNE_JSON for a table that
+ * does not parse; RRTL_E_ARG with E_GPU_AUTOTUNE_RECOMMENDATION when no
+ * record matches (:160-170).
+ *
+ * rrtl_design_autotune_apply finds the record the same way and makes its
+ * choice the design's for batches of `lanes` lanes (the power-of-two bucket
+ * rrtl_design_autotune fills); *tile_words gets the choice. RRTL_E_ARG with
+ * E_GPU_AUTOTUNE_RECOMMENDATION when the record's choice does not fit this
+ * design (a width whose slots do not fit, or the compiled kernel for a
+ * design past its size limit). */
+enum { RRTL_AUTOTUNE_EXACT = 0, RRTL_AUTOTUNE_NEAREST = 1 };
+rrtl_status rrtl_design_autotune_recommend(rrtl_design* design, const char* case_name, uint32_t lanes,
+                                           uint32_t steps, char* json, size_t cap, size_t* len);
+rrtl_status rrtl_autotune_find(const char* table, size_t table_len, const char* case_name, uint64_t lanes,
+                               uint64_t steps, uint32_t mode, uint32_t* index);
+rrtl_status rrtl_design_autotune_apply(rrtl_design* design, const char* table, size_t table_len,
+                                       const char* case_name, uint32_t lanes, uint64_t steps, uint32_t mode,
+                                       uint32_t* tile_words);
+
 /* Device time of the last run/tick_many in milliseconds (CUDA events on the
  * context stream around the kernels of that call). */
 rrtl_status rrtl_batch_last_kernel_ms(rrtl_batch* b, float* ms);

@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 
 namespace rrtl {
 
@@ -2250,6 +2251,140 @@ rrtl_status rrtl_design_autotune(rrtl_design* d, uint32_t lanes, uint32_t cycles
     d->tuned_w[lane_bucket(words)] = best;
     if (best_words) *best_words = best == kTunedCompiled ? 0u : best;
     if (best_ms) *best_ms = best_t;
+  });
+}
+
+// ---- autotune recommendation table
+namespace {
+
+struct TuneRecord {
+  std::string case_name;
+  uint64_t lanes = 0, steps = 0;
+  uint32_t tile_words = 0;
+  bool has_metric = false;
+  uint64_t metric_ns = 0;
+};
+
+std::vector<TuneRecord> parse_tune_table(const char* table, size_t len) {
+  std::vector<TuneRecord> out;
+  try {
+    const json::Value v = json::Parser(table, len).parse();
+    if (!v.is_arr()) throw std::runtime_error("expected an array of records");
+    for (const json::Value& r : v.arr) {
+      TuneRecord t;
+      t.case_name = r.at("case").str();
+      t.lanes = r.at("lanes").u64();
+      t.steps = r.at("steps").u64();
+      t.tile_words = r.at("tile_words").u32();
+      if (t.tile_words != 0 && t.tile_words != 1 && t.tile_words != 2 && t.tile_words != 4 && t.tile_words != 8)
+        throw std::runtime_error("tile_words must be 0, 1, 2, 4 or 8");
+      const json::Value* m = r.find("autotune_metric_ns");
+      if (m && !m->is_null()) {
+        t.has_metric = true;
+        t.metric_ns = m->u64();
+      }
+      out.push_back(std::move(t));
+    }
+  } catch (const std::exception& e) {
+    fail(RRTL_E_ARG, std::string("E_GPU_AUTOTUNE_JSON: failed to load GPU autotune recommendations: ") + e.what());
+  }
+  return out;
+}
+
+// The reference's match rule: exact (case, lanes, steps), or the record of the
+// same case with the smallest (|lane difference|, |step difference|, metric
+// (absent last), lanes, steps).
+uint32_t find_tune_record(const std::vector<TuneRecord>& items, const std::string& case_name, uint64_t lanes,
+                          uint64_t steps, uint32_t mode) {
+  REQUIRE(mode == RRTL_AUTOTUNE_EXACT || mode == RRTL_AUTOTUNE_NEAREST, RRTL_E_ARG, "E_ARG: unknown match mode");
+  auto diff = [](uint64_t a, uint64_t b) { return a > b ? a - b : b - a; };
+  int best = -1;
+  for (size_t i = 0; i < items.size(); ++i) {
+    const TuneRecord& r = items[i];
+    if (r.case_name != case_name) continue;
+    if (mode == RRTL_AUTOTUNE_EXACT) {
+      if (r.lanes == lanes && r.steps == steps) {
+        best = (int)i;
+        break;
+      }
+      continue;
+    }
+    if (best < 0) {
+      best = (int)i;
+      continue;
+    }
+    const TuneRecord& b = items[best];
+    auto key = [&](const TuneRecord& x) {
+      return std::make_tuple(diff(x.lanes, lanes), diff(x.steps, steps), x.has_metric ? x.metric_ns : ~0ull, x.lanes,
+                             x.steps);
+    };
+    if (key(r) < key(b)) best = (int)i;
+  }
+  if (best < 0)
+    fail(RRTL_E_ARG, "E_GPU_AUTOTUNE_RECOMMENDATION: no GPU autotune recommendation for case `" + case_name +
+                         "` lanes=" + std::to_string(lanes) + " steps=" + std::to_string(steps));
+  return (uint32_t)best;
+}
+
+}  // namespace
+
+rrtl_status rrtl_autotune_find(const char* table, size_t table_len, const char* case_name, uint64_t lanes,
+                               uint64_t steps, uint32_t mode, uint32_t* index) {
+  return guard([&] {
+    REQUIRE(table && case_name && index, RRTL_E_ARG, "E_ARG: null argument");
+    *index = find_tune_record(parse_tune_table(table, table_len), case_name, lanes, steps, mode);
+  });
+}
+
+rrtl_status rrtl_design_autotune_recommend(rrtl_design* d, const char* case_name, uint32_t lanes, uint32_t steps,
+                                           char* out, size_t cap, size_t* len) {
+  return guard([&] {
+    REQUIRE(d && case_name, RRTL_E_ARG, "E_ARG: null argument");
+    uint32_t w = 0;
+    float ms = 0.f;
+    const rrtl_status st = rrtl_design_autotune(d, lanes, steps, &w, &ms);
+    if (st) fail(st, g_last_error);
+    std::string name;
+    for (const char* p = case_name; *p; ++p) {
+      if (*p == '"' || *p == '\\') name += '\\';
+      if ((unsigned char)*p >= 0x20) name += *p;
+    }
+    const bool measured = d->engine == RRTL_ENGINE_GATE && d->gate_w_max;
+    const std::string js = "{\"case\": \"" + name + "\", \"lanes\": " + std::to_string(lanes) +
+                           ", \"steps\": " + std::to_string(steps) + ", \"tile_words\": " + std::to_string(w) +
+                           ", \"autotune_metric\": \"kernel_ms\", \"autotune_metric_ns\": " +
+                           (measured ? std::to_string((uint64_t)((double)ms * 1e6)) : std::string("null")) + "}";
+    if (len) *len = js.size();
+    if (out && cap) {
+      const size_t n = std::min(cap - 1, js.size());
+      memcpy(out, js.data(), n);
+      out[n] = 0;
+    }
+  });
+}
+
+rrtl_status rrtl_design_autotune_apply(rrtl_design* d, const char* table, size_t table_len, const char* case_name,
+                                       uint32_t lanes, uint64_t steps, uint32_t mode, uint32_t* tile_words) {
+  return guard([&] {
+    REQUIRE(d && table && case_name, RRTL_E_ARG, "E_ARG: null argument");
+    REQUIRE(lanes > 0, RRTL_E_LANES, "E_GPU_AUTOTUNE_LANES: a recommendation applies to at least one lane");
+    const std::vector<TuneRecord> items = parse_tune_table(table, table_len);
+    const TuneRecord& r = items[find_tune_record(items, case_name, lanes, steps, mode)];
+    REQUIRE(d->engine == RRTL_ENGINE_GATE && d->gate_w_max, RRTL_E_UNSUPPORTED,
+            "E_GPU_AUTOTUNE_RECOMMENDATION: tile widths apply to gate-engine designs on the fused path");
+    set_device(d->ctx);
+    uint32_t choice = r.tile_words;
+    if (choice == 0) {
+      REQUIRE(d->gp().n_real_cells <= kGateJitMaxCells, RRTL_E_ARG,
+              "E_GPU_AUTOTUNE_RECOMMENDATION: the compiled gate kernel does not take a design of this size");
+      choice = kTunedCompiled;
+    } else {
+      REQUIRE(choice <= d->gate_w_max && gate_variant(d, choice)->fused_ok, RRTL_E_ARG,
+              "E_GPU_AUTOTUNE_RECOMMENDATION: tile width " + std::to_string(choice) +
+                  " does not fit this design's slots");
+    }
+    d->tuned_w[lane_bucket((lanes + 31) / 32)] = choice;
+    if (tile_words) *tile_words = r.tile_words;
   });
 }
 

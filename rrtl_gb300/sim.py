@@ -180,6 +180,9 @@ EXPORTS = (
     "rrtl_gate_jit_emit",
     "rrtl_gate_fused_jit_emit",
     "rrtl_gate_program_info_get",
+    "rrtl_design_autotune_recommend",
+    "rrtl_autotune_find",
+    "rrtl_design_autotune_apply",
     "rrtl_design_load_bitslice",
     "rrtl_bitslice_json",
     "rrtl_shard_plan",
@@ -266,6 +269,10 @@ def lib():
         "rrtl_gate_fused_jit_emit": [c_char_p, c_size_t, c_char_p, c_uint32, c_char_p, c_char_p, c_size_t, P(c_size_t),
                                      P(c_uint32), c_char_p, c_size_t],
         "rrtl_gate_program_info_get": [c_char_p, c_size_t, c_char_p, c_uint32, P(GateProgramInfo)],
+        "rrtl_design_autotune_recommend": [c_void_p, c_char_p, c_uint32, c_uint32, c_char_p, c_size_t, P(c_size_t)],
+        "rrtl_autotune_find": [c_char_p, c_size_t, c_char_p, c_uint64, c_uint64, c_uint32, P(c_uint32)],
+        "rrtl_design_autotune_apply": [c_void_p, c_char_p, c_size_t, c_char_p, c_uint32, c_uint64, c_uint32,
+                                       P(c_uint32)],
         "rrtl_shard_plan": [c_uint64, c_uint32, P(ShardInfo)],
         "rrtl_runtime_create": [c_void_p, c_uint64, c_uint32, P(c_void_p)],
         "rrtl_runtime_destroy": [c_void_p],
@@ -424,6 +431,23 @@ def gate_jit_emit(design: Union[_b.Design, str], top: str, run: "Run", arch: Opt
     return src.value.decode(), cub.value, logb.value.decode()
 
 
+AUTOTUNE_EXACT, AUTOTUNE_NEAREST = 0, 1
+
+
+def autotune_find(table, case: str, lanes: int, steps: int, nearest: bool = False) -> int:
+    """Index of the recommendation for (case, lanes, steps) in `table` (a list
+    of records or its JSON text), by the reference's exact or nearest rule
+    (rrtl_autotune_find; no device)."""
+    import json as _json
+
+    text = table if isinstance(table, str) else _json.dumps(table)
+    raw = text.encode()
+    i = c_uint32()
+    check(lib().rrtl_autotune_find(raw, len(raw), case.encode(), lanes, steps,
+                                   AUTOTUNE_NEAREST if nearest else AUTOTUNE_EXACT, byref(i)))
+    return i.value
+
+
 def gate_program_info(design: Union[_b.Design, str], top: str, tile_words: int = 8) -> dict:
     """The gate lowering at one fused tile width (rrtl_gate_program_info_get):
     cell, group, level, slot and class counts and the shared-memory
@@ -486,6 +510,29 @@ class CompiledDesign:
         w, ms = c_uint32(), c_float()
         check(lib().rrtl_design_autotune(self.h, lanes, cycles, byref(w), byref(ms)))
         return w.value, ms.value
+
+    def autotune_recommend(self, case: str, lanes: int, steps: int = 32) -> dict:
+        """Autotune for `lanes` lanes and `steps` cycles and return the
+        recommendation record for `case` (rrtl_design_autotune_recommend)."""
+        import json as _json
+
+        n = c_size_t()
+        buf = ctypes.create_string_buffer(2 * len(case.encode()) + 512)  # the record is the case name and five numbers
+        check(lib().rrtl_design_autotune_recommend(self.h, case.encode(), lanes, steps, buf, len(buf), byref(n)))
+        return _json.loads(buf.value.decode())
+
+    def autotune_apply(self, table, case: str, lanes: int, steps: int, nearest: bool = False) -> int:
+        """Make the recommendation for (case, lanes, steps) in `table` (a list
+        of records or its JSON text) this design's choice for batches of
+        `lanes` lanes; returns its tile width (0: the compiled gate kernel)."""
+        import json as _json
+
+        text = table if isinstance(table, str) else _json.dumps(table)
+        raw = text.encode()
+        w = c_uint32()
+        check(lib().rrtl_design_autotune_apply(self.h, raw, len(raw), case.encode(), lanes, steps,
+                                               AUTOTUNE_NEAREST if nearest else AUTOTUNE_EXACT, byref(w)))
+        return w.value
 
     def word_jit(self):
         """Compile the design's word kernel if not yet tried: (active, compile ms, reason if inactive)."""

@@ -240,6 +240,31 @@ def test_autotune_picks_a_measured_width(small_netlist):
     assert np.array_equal(res["hash"], ref["hash"])
 
 
+def test_autotune_recommendation_round_trip(small_netlist):
+    """A recommendation record written by the autotuner, and one written by
+    hand, become another design instance's choice for their lane bucket
+    without timing anything; runs at that choice match the oracle."""
+    d, meta, cd, od = small_netlist
+    stim, rec = netlist_run_spec(meta)
+    r = cd.autotune_recommend("small", 4096, 8)
+    assert (r["case"], r["lanes"], r["steps"]) == ("small", 4096, 8) and r["tile_words"] in (0, 1, 2, 4, 8)
+    assert r["autotune_metric_ns"] > 0
+    cd2 = sim.CompiledDesign(d.to_json(), meta.top)
+    assert cd2.autotune_apply([r], "small", 4096, 8) == r["tile_words"]
+    hand = {"case": "small", "lanes": 20000, "steps": 8, "tile_words": 2, "autotune_metric": "kernel_ms",
+            "autotune_metric_ns": None}
+    assert cd2.autotune_apply([r, hand], "small", 20000, 30, nearest=True) == 2
+    for lanes, want in ((4000, r["tile_words"]), (20000, 2)):
+        g = sim.GpuBatchSimulator(cd2, lanes=lanes)
+        res = g.run(9, seed=5, stim=stim, record=rec, mode=sim.REC_HASH)
+        assert g.tile_words == want, lanes
+        ref = oracle_bp_run(od, lanes, 9, 5, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(x) for x in rec], 2)
+        assert np.array_equal(res["hash"], ref["hash"]), lanes
+    with pytest.raises(sim.RrtlError) as e:
+        cd2.autotune_apply([hand], "small", 20000, 9)  # exact: no record for 9 steps
+    assert e.value.code == "E_GPU_AUTOTUNE_RECOMMENDATION"
+
+
 def test_large_netlist_runs_fused_at_narrow_tiles(engine):
     """100k gates and 4,096 flops: the slots need more shared memory than one
     CTA has at 8 words per tile, so the fused path runs narrower tiles; it
