@@ -98,3 +98,53 @@ def test_emulated_crc32_and_lane_base(emu):
         ref = oracle_bp_run(od, 100, 20, 7, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in rec],
                             2, lane_base=lane_base)
         assert np.array_equal(h, ref["hash"]), lane_base
+
+
+def _register_mix():
+    """1-bit registers with every commit form: reset high/low to 0/1, no
+    reset, D taken straight from another register (a copy cell keeps D and Q
+    apart), an output driven by a register, a constant-driven register."""
+    from rrtl_gb300.builder import Design, lit_u, mux, uint
+
+    d = Design()
+    m = d.module("Mix")
+    clk, rst, rstn = m.input("clk", uint(1)), m.input("rst", uint(1)), m.input("rstn", uint(1))
+    a, b, c = m.input("a", uint(1)), m.input("b", uint(1)), m.input("c", uint(1))
+    regs = [m.reg(f"r{i}", uint(1)) for i in range(8)]
+    for r in regs:
+        m.clock(r, clk)
+    m.next(regs[0], a ^ regs[7])
+    m.reset(regs[0], rst, 1)
+    m.next(regs[1], regs[0])  # D is another register
+    m.reset_low(regs[1], rstn, 0)
+    m.next(regs[2], mux(b, regs[1], ~regs[2]))
+    m.reset_low(regs[2], rstn, 1)
+    m.next(regs[3], (regs[2] & c) | regs[0])
+    m.next(regs[4], regs[3] ^ regs[1] ^ a)
+    m.reset(regs[4], rst, 0)
+    m.next(regs[5], lit_u(1, 1))  # constant D
+    m.next(regs[6], regs[5] & ~regs[4])
+    m.next(regs[7], regs[6] | (b & c))
+    outs = []
+    for i, r in enumerate((regs[1], regs[4], regs[7])):
+        o = m.output(f"o{i}", uint(1))
+        m.assign(o, r)
+        outs.append(f"o{i}")
+    w = m.wire("w", uint(1))
+    m.assign(w, regs[2] ^ regs[6])
+    o = m.output("o3", uint(1))
+    m.assign(o, w & a)
+    outs.append("o3")
+    return d, "Mix", outs
+
+
+@pytest.mark.parametrize("W", [8, 4, 1])
+def test_emulated_register_commit_forms(emu, W):
+    d, top, outs = _register_mix()
+    js = d.to_json()
+    od = ob.OracleDesign(js, top)
+    stim = [("clk", sim.STIM_CONST, 1), ("rst", sim.STIM_PULSE, 3), ("rstn", sim.STIM_RANDOM, 9),
+            ("a", sim.STIM_RANDOM, 1), ("b", sim.STIM_RANDOM, 2), ("c", sim.STIM_RANDOM, 3)]
+    h = _emulate(emu, js, top, od, stim, outs, 70, 40, 13, W, 8, 0.85, 2.0)
+    ref = oracle_bp_run(od, 70, 40, 13, [(od.signal(n), k, p) for n, k, p in stim], [od.signal(r) for r in outs], 2)
+    assert np.array_equal(h, ref["hash"])
